@@ -1,0 +1,202 @@
+"""ORACLE — test infrastructure, not the product.
+
+ctypes bindings for the plain-C restatement of Puck's Puck-Flat search path
+(oracle/puck_oracle.c) and, where it has been built, for the reference's own
+code compiled from its sources (oracle/_ref/, see oracle/ref/Makefile).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this package, and only as the checker or the timed CPU baseline.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libpuck_oracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libpuckref.so")
+REF_NATIVE_LIB_PATH = os.path.join(HERE, "_ref", "libpuckref_native.so")
+
+
+def build_oracle(force=False):
+    """Compile the C restatement (seconds). No FMA contraction, no fast-math."""
+    src = os.path.join(HERE, "puck_oracle.c")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB_PATH + ".tmp"
+    subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+                           "-fno-fast-math", "-pthread", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_reference(native=False):
+    """Compile the reference's own sources from /root/reference (x86 only)."""
+    ref = "/root/reference"
+    if not os.path.isdir(ref):
+        return None
+    target = "native" if native else "all"
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref}", "-j8",
+                           target])
+    return REF_NATIVE_LIB_PATH if native else REF_LIB_PATH
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("search_coarse_count", ctypes.c_uint32), ("filter_topk", ctypes.c_uint32),
+                ("topk", ctypes.c_uint32), ("radius_rate", ctypes.c_double)]
+
+
+class _Trace(ctypes.Structure):
+    _fields_ = [("coarse_tag", ctypes.c_void_p), ("coarse_dist", ctypes.c_void_p),
+                ("filter_tag", ctypes.c_void_p), ("filter_dist", ctypes.c_void_p),
+                ("filter_cnt", ctypes.c_uint32), ("lut", ctypes.c_void_p),
+                ("scanned_points", ctypes.c_uint64), ("scanned_cells", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        lib = ctypes.CDLL(build_oracle())
+        lib.po_load.restype = ctypes.c_void_p
+        lib.po_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+        lib.po_free.argtypes = [ctypes.c_void_p]
+        lib.po_info.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_uint32)] * 6 + [
+            ctypes.POINTER(ctypes.c_int)]
+        lib.po_memory_to_local.restype = ctypes.c_void_p
+        lib.po_memory_to_local.argtypes = [ctypes.c_void_p]
+        lib.po_stationary.restype = ctypes.c_void_p
+        lib.po_stationary.argtypes = [ctypes.c_void_p]
+        lib.po_cell_start.restype = ctypes.c_void_p
+        lib.po_cell_start.argtypes = [ctypes.c_void_p]
+        lib.po_search.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Params), ctypes.c_void_p,
+                                  ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_Trace)]
+        lib.po_search_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Params), ctypes.c_uint32,
+                                        ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.po_nearest_center.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
+                                          ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                          ctypes.c_void_p]
+        lib.po_nearest_cell_assign.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                                               ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                               ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+class OracleIndex:
+    """The C restatement loaded on one Puck-Flat index directory."""
+
+    def __init__(self, index_dir):
+        lib = _load()
+        err = ctypes.c_int(0)
+        self._h = lib.po_load(index_dir.encode(), ctypes.byref(err))
+        if not self._h:
+            raise RuntimeError(f"oracle could not load {index_dir} (error {err.value})")
+        vals = [ctypes.c_uint32() for _ in range(6)]
+        wn = ctypes.c_int()
+        lib.po_info(self._h, *[ctypes.byref(v) for v in vals], ctypes.byref(wn))
+        self.d, self.n, self.C, self.F, self.nsq, self.lsq = [v.value for v in vals]
+        self.whether_norm = bool(wn.value)
+
+    def close(self):
+        if self._h:
+            _load().po_free(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def memory_to_local(self):
+        p = _load().po_memory_to_local(self._h)
+        return np.ctypeslib.as_array((ctypes.c_uint32 * self.n).from_address(p)).copy()
+
+    def stationary(self):
+        p = _load().po_stationary(self._h)
+        return np.ctypeslib.as_array((ctypes.c_float * (self.C * self.F)).from_address(p)).copy()
+
+    def cell_start(self):
+        p = _load().po_cell_start(self._h)
+        return np.ctypeslib.as_array(
+            (ctypes.c_uint32 * (self.C * self.F + 1)).from_address(p)).copy()
+
+    def params(self, search_coarse_count, filter_topk, topk_max=100, radius_rate=1.0):
+        return _Params(search_coarse_count, filter_topk, topk_max, radius_rate)
+
+    def search_one(self, q, topk, search_coarse_count, filter_topk, topk_max=None,
+                   radius_rate=1.0, trace=False):
+        """Returns (rc, dist[topk], ids[topk], result_num, trace dict or None)."""
+        lib = _load()
+        P = min(search_coarse_count, self.C)
+        p = _Params(search_coarse_count, filter_topk, topk_max or max(topk, 100), radius_rate)
+        q = np.ascontiguousarray(q, np.float32)
+        dist = np.zeros(topk, np.float32)
+        ids = np.full(topk, 0xFFFFFFFF, np.uint32)
+        rn = ctypes.c_uint32(0)
+        tr = None
+        arrs = None
+        if trace:
+            arrs = dict(coarse_tag=np.zeros(P, np.uint32), coarse_dist=np.zeros(P, np.float32),
+                        filter_tag=np.zeros(filter_topk, np.uint32),
+                        filter_dist=np.zeros(filter_topk, np.float32),
+                        lut=np.zeros(self.nsq * 256, np.float32))
+            tr = _Trace(_ptr(arrs["coarse_tag"]), _ptr(arrs["coarse_dist"]),
+                        _ptr(arrs["filter_tag"]), _ptr(arrs["filter_dist"]), 0, _ptr(arrs["lut"]),
+                        0, 0)
+        rc = lib.po_search(self._h, ctypes.byref(p), q.ctypes.data, topk, dist.ctypes.data,
+                           ids.ctypes.data, ctypes.byref(rn),
+                           ctypes.byref(tr) if tr is not None else None)
+        if trace:
+            arrs["filter_cnt"] = tr.filter_cnt
+            arrs["scanned_points"] = tr.scanned_points
+            arrs["scanned_cells"] = tr.scanned_cells
+        return rc, dist, ids, rn.value, arrs
+
+    def search_batch(self, q, topk, search_coarse_count, filter_topk, topk_max=None,
+                     radius_rate=1.0, nthreads=None):
+        lib = _load()
+        q = np.ascontiguousarray(q, np.float32)
+        n = q.shape[0]
+        p = _Params(search_coarse_count, filter_topk, topk_max or max(topk, 100), radius_rate)
+        dist = np.zeros((n, topk), np.float32)
+        ids = np.full((n, topk), 0xFFFFFFFF, np.uint32)
+        status = np.zeros(n, np.int32)
+        lib.po_search_batch(self._h, ctypes.byref(p), n, q.ctypes.data, topk, dist.ctypes.data,
+                            ids.ctypes.data, status.ctypes.data, nthreads or os.cpu_count())
+        return dist, ids, status
+
+
+def nearest_center(centroids, x):
+    lib = _load()
+    centroids = np.ascontiguousarray(centroids, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    n = x.shape[0]
+    assign = np.zeros(n, np.int32)
+    dis = np.zeros(n, np.float32)
+    lib.po_nearest_center(x.shape[1], centroids.ctypes.data, centroids.shape[0], x.ctypes.data, n,
+                          assign.ctypes.data, dis.ctypes.data)
+    return assign, dis
+
+
+def nearest_cell_assign(coarse, fine, x):
+    lib = _load()
+    coarse = np.ascontiguousarray(coarse, np.float32)
+    fine = np.ascontiguousarray(fine, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    n = x.shape[0]
+    cell = np.zeros(n, np.uint32)
+    dist = np.zeros(n, np.float32)
+    lib.po_nearest_cell_assign(x.shape[1], coarse.ctypes.data, coarse.shape[0], fine.ctypes.data,
+                               fine.shape[0], x.ctypes.data, n, cell.ctypes.data,
+                               dist.ctypes.data)
+    return cell, dist

@@ -1,0 +1,726 @@
+/*
+ * ORACLE — test infrastructure, not the product. See puck_oracle.h.
+ *
+ * Restates, in plain C and in the reference's float operation order:
+ *   load    : HierarchicalClusterIndex::read_coodbooks
+ *             (puck/hierarchical_cluster/hierarchical_cluster_index.cpp:257-324),
+ *             PuckIndex::convert_local_to_memory_idx (puck/puck/puck_index.cpp:229-309),
+ *             read_feature_index (puck_index.cpp:198-227, hierarchical_cluster_index.cpp:367-406)
+ *   search  : PuckIndex::search (puck_index.cpp:559-600) and the stages it calls
+ *   assign  : nearest_center (puck/hierarchical_cluster/kmeans.cpp:221-258),
+ *             nearest_cell_assign (hierarchical_cluster_index.cpp:1042-1085)
+ * Build with -O2 -ffp-contract=off (no FMA contraction, no fast-math).
+ */
+#include "puck_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct po_index {
+    uint32_t d, n, C, F, nsq, lsq;
+    int whether_norm, ip2cos;
+    float* coarse;          /* C*d */
+    float* fine;            /* F*d */
+    float* coarse_norms;    /* C: 0.5*|c|^2 */
+    float* stationary;      /* C*F: 0.5*|f|^2 + f.c, sqrt(FLT_MAX) for empty cells */
+    uint32_t* cell_start;   /* C*F + 1 */
+    float* min_dist_offset; /* C */
+    uint32_t* mem2local;    /* n */
+    float* offsets;         /* n, memory order */
+    uint8_t* codes;         /* n*nsq, memory order */
+    float* feat;            /* n*d, memory order */
+    float* codebook;        /* nsq*256*lsq */
+};
+
+/* ---------------------------------------------------------------- BLAS order */
+
+/* Sequential dot product: the deterministic BLAS the oracle build of the
+ * reference links (oracle/ref/shim_blas.c). */
+static float dotf(const float* x, const float* y, uint32_t n) {
+    float s = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        float p = x[i] * y[i];
+        s = s + p;
+    }
+    return s;
+}
+
+/* ------------------------------------------------------------------ MaxHeap */
+/* Bounded max-heap of puck/hierarchical_cluster/max_heap.cpp:28-102: 1-based
+ * arrays, 0x7f7f7f7f sentinel fill, a new value is rejected if >= top, the
+ * first `size` inserts sift down from the last empty slot, reorder() is an
+ * in-place heap sort to ascending order. */
+typedef struct {
+    float* val; /* 1-based view */
+    uint32_t* tag;
+    uint32_t size;
+    uint32_t dpc; /* slots not yet filled */
+} po_heap;
+
+static void heap_init(po_heap* h, uint32_t size, float* val, uint32_t* tag) {
+    memset(val, 0x7f, sizeof(float) * size);
+    h->val = val - 1;
+    h->tag = tag - 1;
+    h->size = size;
+    h->dpc = size;
+}
+
+static void heap_insert(po_heap* h, uint32_t heap_size, uint32_t father, float v, uint32_t t) {
+    for (;;) {
+        uint32_t left = father << 1;
+        if (left > heap_size) break;
+        uint32_t right = left + 1;
+        if (right > heap_size || h->val[left] > h->val[right]) {
+            if (h->val[left] < v) break;
+            h->val[father] = h->val[left];
+            h->tag[father] = h->tag[left];
+            father = left;
+        } else {
+            if (h->val[right] < v) break;
+            h->val[father] = h->val[right];
+            h->tag[father] = h->tag[right];
+            father = right;
+        }
+    }
+    h->val[father] = v;
+    h->tag[father] = t;
+}
+
+static int heap_update(po_heap* h, float v, uint32_t t) {
+    uint32_t father = 1;
+    if (v >= h->val[1]) return 0;
+    if (h->dpc > 0) father = h->dpc--;
+    heap_insert(h, h->size, father, v, t);
+    return 1;
+}
+
+static void heap_reorder(po_heap* h) {
+    for (uint32_t i = 0; i < h->size; ++i) {
+        float vb = h->val[1];
+        uint32_t tb = h->tag[1];
+        uint32_t hs = h->size - i;
+        heap_insert(h, hs - 1, 1, h->val[hs], h->tag[hs]);
+        h->val[hs] = vb;
+        h->tag[hs] = tb;
+    }
+}
+
+static uint32_t heap_count(const po_heap* h) { return h->size - h->dpc; }
+
+/* --------------------------------------------------------------- file input */
+
+static int read_file(const char* dir, const char* name, void** out, size_t* len) {
+    char path[4096];
+    snprintf(path, sizeof(path), "%s/%s", dir, name);
+    FILE* f = fopen(path, "rb");
+    if (!f) return -1;
+    fseek(f, 0, SEEK_END);
+    long sz = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    void* buf = malloc(sz > 0 ? (size_t)sz : 1);
+    if (!buf || (sz > 0 && fread(buf, 1, (size_t)sz, f) != (size_t)sz)) {
+        fclose(f);
+        free(buf);
+        return -1;
+    }
+    fclose(f);
+    *out = buf;
+    *len = (size_t)sz;
+    return 0;
+}
+
+/* fvecs: per row an int32 dim then dim floats. */
+static float* read_fvecs(const char* dir, const char* name, uint32_t dim, uint64_t rows) {
+    void* raw;
+    size_t len;
+    if (read_file(dir, name, &raw, &len) != 0) return NULL;
+    if (len != rows * (4 + 4ull * dim)) {
+        free(raw);
+        return NULL;
+    }
+    float* out = (float*)malloc(sizeof(float) * dim * rows + 4);
+    const uint8_t* p = (const uint8_t*)raw;
+    for (uint64_t i = 0; i < rows; ++i) {
+        int32_t dd;
+        memcpy(&dd, p, 4);
+        if ((uint32_t)dd != dim) {
+            free(raw);
+            free(out);
+            return NULL;
+        }
+        memcpy(out + i * dim, p + 4, 4ull * dim);
+        p += 4 + 4ull * dim;
+    }
+    free(raw);
+    return out;
+}
+
+typedef struct {
+    uint32_t cell;
+    float offset;
+    uint32_t local;
+} mem_order;
+
+/* std::pair<uint32_t, std::pair<float, uint32_t>> ordering (puck_index.cpp:248-268);
+ * the local id makes the key unique, so any sort reproduces std::stable_sort. */
+static int cmp_mem_order(const void* a, const void* b) {
+    const mem_order* x = (const mem_order*)a;
+    const mem_order* y = (const mem_order*)b;
+    if (x->cell != y->cell) return x->cell < y->cell ? -1 : 1;
+    if (x->offset < y->offset) return -1;
+    if (y->offset < x->offset) return 1;
+    if (x->local != y->local) return x->local < y->local ? -1 : 1;
+    return 0;
+}
+
+void po_free(po_index* ix) {
+    if (!ix) return;
+    free(ix->coarse);
+    free(ix->fine);
+    free(ix->coarse_norms);
+    free(ix->stationary);
+    free(ix->cell_start);
+    free(ix->min_dist_offset);
+    free(ix->mem2local);
+    free(ix->offsets);
+    free(ix->codes);
+    free(ix->feat);
+    free(ix->codebook);
+    free(ix);
+}
+
+po_index* po_load(const char* dir, int* err) {
+    int e = 0;
+    po_index* ix = (po_index*)calloc(1, sizeof(po_index));
+    void* raw = NULL;
+    size_t len = 0;
+    uint32_t* cell_assign = NULL;
+    mem_order* order = NULL;
+    uint8_t* rec = NULL;
+    float* feat_local = NULL;
+
+    /* index.dat: size_t length + packed config (hierarchical_cluster_index.cpp:551-567) */
+    if (read_file(dir, "index.dat", &raw, &len) != 0 || len < 8 + 43) { e = -1; goto fail; }
+    {
+        const uint8_t* p = (const uint8_t*)raw + 8;
+        int32_t itype;
+        uint32_t u;
+        memcpy(&itype, p, 4); p += 4;
+        if (itype != 1) { e = -2; goto fail; } /* PUCK */
+        memcpy(&ix->d, p, 4); p += 4;
+        ix->whether_norm = *p; p += 1;
+        memcpy(&ix->n, p, 4); p += 4;
+        uint8_t whether_filter = *p; p += 1;
+        memcpy(&ix->nsq, p, 4); p += 4;
+        memcpy(&u, p, 4); p += 4; /* ks */
+        if (u != 256 || !whether_filter) { e = -3; goto fail; }
+        uint8_t whether_pq = *p; p += 1;
+        if (whether_pq) { e = -4; goto fail; } /* Puck-Flat only */
+        p += 4; /* nsq */
+        p += 4; /* ks */
+        memcpy(&u, p, 4); p += 4;
+        ix->ip2cos = (int)u;
+        if (ix->ip2cos != 0) { e = -5; goto fail; }
+        memcpy(&ix->C, p, 4); p += 4;
+        memcpy(&ix->F, p, 4); p += 4;
+    }
+    free(raw);
+    raw = NULL;
+    if (ix->nsq == 0 || ix->nsq > ix->d) { e = -6; goto fail; }
+    ix->lsq = (ix->d + ix->nsq - 1) / ix->nsq;
+    if (ix->lsq * ix->nsq != ix->d) { e = -7; goto fail; } /* reference reads past d otherwise */
+
+    const uint32_t d = ix->d, n = ix->n, C = ix->C, F = ix->F, nsq = ix->nsq;
+    const uint64_t cells = (uint64_t)C * F;
+    ix->coarse = read_fvecs(dir, "coarse.dat", d, C);
+    ix->fine = read_fvecs(dir, "fine.dat", d, F);
+    if (!ix->coarse || !ix->fine) { e = -8; goto fail; }
+
+    /* read_coodbooks: coarse norms, fine norms, F x C products (sgemm "TN"). */
+    ix->coarse_norms = (float*)malloc(sizeof(float) * C);
+    for (uint32_t c = 0; c < C; ++c)
+        ix->coarse_norms[c] = dotf(ix->coarse + (uint64_t)c * d, ix->coarse + (uint64_t)c * d, d) / 2;
+    float* fine_norms = (float*)malloc(sizeof(float) * F);
+    for (uint32_t f = 0; f < F; ++f)
+        fine_norms[f] = dotf(ix->fine + (uint64_t)f * d, ix->fine + (uint64_t)f * d, d) / 2;
+    ix->stationary = (float*)malloc(sizeof(float) * cells);
+    for (uint32_t c = 0; c < C; ++c)
+        for (uint32_t f = 0; f < F; ++f) {
+            float prod = dotf(ix->fine + (uint64_t)f * d, ix->coarse + (uint64_t)c * d, d);
+            ix->stationary[(uint64_t)c * F + f] = fine_norms[f] + prod;
+        }
+    free(fine_norms);
+
+    /* convert_local_to_memory_idx */
+    if (read_file(dir, "cell_assign.dat", &raw, &len) != 0 || len != 4ull * n) { e = -9; goto fail; }
+    cell_assign = (uint32_t*)raw;
+    raw = NULL;
+    const uint32_t rb = 4 + nsq;
+    if (read_file(dir, "filter_data.dat", &raw, &len) != 0 || len != (uint64_t)rb * n) { e = -10; goto fail; }
+    rec = (uint8_t*)raw;
+    raw = NULL;
+    order = (mem_order*)malloc(sizeof(mem_order) * (n ? n : 1));
+    for (uint32_t i = 0; i < n; ++i) {
+        if (cell_assign[i] >= cells) { e = -11; goto fail; }
+        order[i].cell = cell_assign[i];
+        memcpy(&order[i].offset, rec + (uint64_t)i * rb, 4);
+        order[i].local = i;
+    }
+    qsort(order, n, sizeof(mem_order), cmp_mem_order);
+    ix->cell_start = (uint32_t*)malloc(sizeof(uint32_t) * (cells + 1));
+    for (uint64_t i = 0; i <= cells; ++i) ix->cell_start[i] = n;
+    ix->mem2local = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    {
+        uint32_t cellcount = 0;
+        ix->cell_start[0] = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            ix->mem2local[i] = order[i].local;
+            while (cellcount + 1 <= order[i].cell) {
+                ++cellcount;
+                ix->cell_start[cellcount] = i;
+            }
+        }
+    }
+    ix->min_dist_offset = (float*)malloc(sizeof(float) * C);
+    for (uint32_t c = 0; c < C; ++c) ix->min_dist_offset[c] = FLT_MAX;
+    for (uint64_t i = 0; i < cells; ++i) {
+        uint32_t s = ix->cell_start[i], t = ix->cell_start[i + 1];
+        uint32_t c = (uint32_t)(i / F);
+        if (s > t) { e = -12; goto fail; }
+        if (s == t) ix->stationary[i] = sqrtf(FLT_MAX);
+        float st = ix->stationary[i];
+        if (st < ix->min_dist_offset[c]) ix->min_dist_offset[c] = st;
+    }
+
+    /* read_feature_index: filter records and original vectors in memory order. */
+    ix->offsets = (float*)malloc(sizeof(float) * (n ? n : 1));
+    ix->codes = (uint8_t*)malloc((uint64_t)nsq * (n ? n : 1));
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint8_t* r = rec + (uint64_t)ix->mem2local[i] * rb;
+        memcpy(&ix->offsets[i], r, 4);
+        memcpy(ix->codes + (uint64_t)i * nsq, r + 4, nsq);
+    }
+    feat_local = read_fvecs(dir, "all_data.feat.bin", d, n);
+    if (!feat_local) { e = -13; goto fail; }
+    ix->feat = (float*)malloc(sizeof(float) * (uint64_t)d * (n ? n : 1));
+    for (uint32_t i = 0; i < n; ++i)
+        memcpy(ix->feat + (uint64_t)i * d, feat_local + (uint64_t)ix->mem2local[i] * d, 4ull * d);
+    ix->codebook = read_fvecs(dir, "filter_codebook.dat", ix->lsq, (uint64_t)nsq * 256);
+    if (!ix->codebook) { e = -14; goto fail; }
+
+    free(cell_assign);
+    free(order);
+    free(rec);
+    free(feat_local);
+    if (err) *err = 0;
+    return ix;
+fail:
+    free(raw);
+    free(cell_assign);
+    free(order);
+    free(rec);
+    free(feat_local);
+    po_free(ix);
+    if (err) *err = e;
+    return NULL;
+}
+
+int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,
+            uint32_t* filter_nsq, uint32_t* lsq, int* whether_norm) {
+    *d = ix->d;
+    *n = ix->n;
+    *coarse = ix->C;
+    *fine = ix->F;
+    *filter_nsq = ix->nsq;
+    *lsq = ix->lsq;
+    *whether_norm = ix->whether_norm;
+    return 0;
+}
+
+const uint32_t* po_memory_to_local(const po_index* ix) { return ix->mem2local; }
+const float* po_stationary(const po_index* ix) { return ix->stationary; }
+const uint32_t* po_cell_start(const po_index* ix) { return ix->cell_start; }
+
+/* ------------------------------------------------------------ distance kernels */
+
+/* fvec_L2sqr SSE order (puck/puck/distances_simd.cpp:120-133, 210-236): four lane
+ * accumulators over chunks of 4 (masked zero tail), then (l0+l1)+(l2+l3). */
+static float l2sqr_sse(const float* x, const float* y, uint32_t d) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t i = 0;
+    for (; i + 4 <= d; i += 4)
+        for (int j = 0; j < 4; ++j) {
+            float t = x[i + j] - y[i + j];
+            float sq = t * t;
+            acc[j] = acc[j] + sq;
+        }
+    if (i < d) {
+        for (int j = 0; j < 4; ++j) {
+            float t = (i + j < d) ? x[i + j] - y[i + j] : 0.0f;
+            float sq = t * t;
+            acc[j] = acc[j] + sq;
+        }
+    }
+    float h0 = acc[0] + acc[1];
+    float h1 = acc[2] + acc[3];
+    return h0 + h1;
+}
+
+/* lookup_dist_table (puck_index.cpp:75-113): lane j sums subspaces m = j mod 4 in
+ * increasing m; final (l0+l1)+(l2+l3). */
+static float lookup_lut(const uint8_t* code, const float* lut, uint32_t nsq) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint32_t m = 0; m < nsq; ++m) {
+        float v = lut[(uint64_t)m * 256 + code[m]];
+        acc[m & 3] = acc[m & 3] + v;
+    }
+    float h0 = acc[0] + acc[1];
+    float h1 = acc[2] + acc[3];
+    return h0 + h1;
+}
+
+/* L2Sqr16Ext, AVX build (puck/tinker/method/hnsw_distfunc_opt_impl_inline.h:41-69):
+ * lanes i<8 hold d_i^2 + d_{i+8}^2; lanes summed left to right. */
+static float l2sqr16(const float* x, const float* q) {
+    float lane[8];
+    for (int i = 0; i < 8; ++i) {
+        float a = x[i] - q[i];
+        float b = x[i + 8] - q[i + 8];
+        float a2 = a * a, b2 = b * b;
+        lane[i] = a2 + b2;
+    }
+    float s = lane[0];
+    for (int i = 1; i < 8; ++i) s = s + lane[i];
+    return s;
+}
+
+/* L2SqrExt with fewer than 16 dims (hnsw_distfunc_opt_impl_inline.h:71-122): 4-lane
+ * chunks, lanes summed left to right, then a scalar tail. */
+static float l2sqr_ext(const float* x, const float* q, uint32_t qty) {
+    float lane[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t i = 0;
+    for (; i + 4 <= qty; i += 4)
+        for (int j = 0; j < 4; ++j) {
+            float t = x[i + j] - q[i + j];
+            float sq = t * t;
+            lane[j] = lane[j] + sq;
+        }
+    float s = ((lane[0] + lane[1]) + lane[2]) + lane[3];
+    for (; i < qty; ++i) {
+        float t = x[i] - q[i];
+        float sq = t * t;
+        s = s + sq;
+    }
+    return s;
+}
+
+/* -------------------------------------------------------------------- search */
+
+typedef struct {
+    float* q;
+    float* ip;
+    float* cd;
+    uint32_t* ctag;
+    float* fd;
+    uint32_t* ftag;
+    float* lut;
+    float* rdist;
+    uint32_t* rtag;
+} po_scratch;
+
+static void scratch_alloc(po_scratch* s, const po_index* ix, const po_params* p) {
+    uint32_t cmax = ix->C > ix->F ? ix->C : ix->F;
+    s->q = (float*)malloc(sizeof(float) * ix->d);
+    s->ip = (float*)malloc(sizeof(float) * cmax);
+    s->cd = (float*)malloc(sizeof(float) * (p->search_coarse_count + 1));
+    s->ctag = (uint32_t*)malloc(sizeof(uint32_t) * (p->search_coarse_count + 1));
+    s->fd = (float*)malloc(sizeof(float) * ix->F);
+    s->ftag = (uint32_t*)malloc(sizeof(uint32_t) * ix->F);
+    s->lut = (float*)malloc(sizeof(float) * ix->nsq * 256);
+    s->rdist = (float*)malloc(sizeof(float) * (p->filter_topk + 1));
+    s->rtag = (uint32_t*)malloc(sizeof(uint32_t) * (p->filter_topk + 1));
+}
+
+static void scratch_free(po_scratch* s) {
+    free(s->q);
+    free(s->ip);
+    free(s->cd);
+    free(s->ctag);
+    free(s->fd);
+    free(s->ftag);
+    free(s->lut);
+    free(s->rdist);
+    free(s->rtag);
+}
+
+/* compute_quantized_distance (puck_index.cpp:346-390) */
+static uint32_t scan_cell(const po_index* ix, uint64_t cell, float cell_dist, const float* lut,
+                          po_heap* heap, uint64_t* scanned) {
+    uint32_t start = ix->cell_start[cell];
+    uint32_t cnt = ix->cell_start[cell + 1] - start;
+    uint32_t updated = 0;
+    for (uint32_t i = 0; i < cnt; ++i) {
+        uint32_t mi = start + i;
+        float t = (float)(2.0 * (double)cell_dist + (double)ix->offsets[mi]);
+        if (t >= heap->val[1]) break;
+        ++*scanned;
+        t = t + lookup_lut(ix->codes + (uint64_t)mi * ix->nsq, lut, ix->nsq);
+        if (t < heap->val[1]) {
+            heap_update(heap, t, mi);
+            ++updated;
+        }
+    }
+    return updated;
+}
+
+static int search_one(const po_index* ix, const po_params* p, po_scratch* s, const float* query,
+                      uint32_t topk, float* dist, uint32_t* ids, uint32_t* result_num,
+                      po_trace* trace) {
+    const uint32_t d = ix->d, C = ix->C, F = ix->F, nsq = ix->nsq;
+    uint32_t P = p->search_coarse_count < C ? p->search_coarse_count : C;
+    const uint32_t T = p->filter_topk;
+    if (topk > p->topk || query == NULL || P == 0 || T == 0 || topk == 0) return -1;
+
+    /* normalization (hierarchical_cluster_index.cpp:1513-1536) */
+    memcpy(s->q, query, sizeof(float) * d);
+    if (ix->whether_norm) {
+        float norm = sqrtf(dotf(s->q, s->q, d));
+        if ((double)norm < 1e-6) return -2; /* the reference dereferences nullptr here */
+        float alpha = (float)(1.0 / (double)norm);
+        for (uint32_t i = 0; i < d; ++i) s->q[i] = alpha * s->q[i];
+    }
+    const float* q = s->q;
+
+    /* search_nearest_coarse_cluster (hierarchical_cluster_index.cpp:700-727) */
+    po_heap ch;
+    heap_init(&ch, P, s->cd, s->ctag);
+    for (uint32_t c = 0; c < C; ++c) {
+        float ipc = dotf(ix->coarse + (uint64_t)c * d, q, d);
+        float cdv = ix->coarse_norms[c] - ipc;
+        if (cdv < ch.val[1]) heap_update(&ch, cdv, c);
+    }
+    heap_reorder(&ch);
+
+    /* pre_filter_search -> get_dist_table (quantization.cpp:260-270) */
+    for (uint32_t m = 0; m < nsq; ++m)
+        for (uint32_t j = 0; j < 256; ++j)
+            s->lut[m * 256 + j] = l2sqr_sse(q + (uint64_t)m * ix->lsq,
+                                            ix->codebook + ((uint64_t)m * 256 + j) * ix->lsq, ix->lsq);
+
+    /* fine stage (puck_index.cpp:494-504): full heap sort of -q.f */
+    po_heap fh;
+    heap_init(&fh, F, s->fd, s->ftag);
+    for (uint32_t f = 0; f < F; ++f) {
+        float ipf = dotf(ix->fine + (uint64_t)f * d, q, d);
+        heap_update(&fh, -ipf, f);
+    }
+    heap_reorder(&fh);
+
+    /* walk (puck_index.cpp:513-556) */
+    po_heap rh;
+    heap_init(&rh, T, s->rdist, s->rtag);
+    const float qnorm = dotf(q, q, d);
+    const double rr = p->radius_rate;
+    float pivot = (float)((double)(rh.val[1] - qnorm) / rr / 2.0);
+    uint64_t scanned = 0, cells_scanned = 0;
+    for (uint32_t l = 0; l < P; ++l) {
+        const uint32_t c = s->ctag[l];
+        const float cdl = s->cd[l];
+        const float* stat = ix->stationary + (uint64_t)c * F;
+        const float min_dist = ix->min_dist_offset[c] + cdl;
+        float max_stat = (pivot - cdl) - s->fd[0];
+        for (uint32_t idx = 0; idx < F; ++idx) {
+            if (s->fd[idx] + min_dist >= pivot) break;
+            const uint32_t k = s->ftag[idx];
+            if (stat[k] >= max_stat) continue;
+            const float cell_dist = (cdl + stat[k]) + s->fd[idx];
+            ++cells_scanned;
+            uint32_t upd = scan_cell(ix, (uint64_t)c * F + k, cell_dist, s->lut, &rh, &scanned);
+            if (upd > 0) pivot = (float)((double)(rh.val[1] - qnorm) / rr / 2.0);
+            float cand = (pivot - cdl) - s->fd[idx];
+            if (cand < max_stat) max_stat = cand;
+        }
+    }
+    if (heap_count(&rh) < T) heap_reorder(&rh);
+    const uint32_t cnt = heap_count(&rh);
+
+    if (trace) {
+        if (trace->coarse_tag) memcpy(trace->coarse_tag, s->ctag, sizeof(uint32_t) * P);
+        if (trace->coarse_dist) memcpy(trace->coarse_dist, s->cd, sizeof(float) * P);
+        if (trace->filter_tag) memcpy(trace->filter_tag, s->rtag, sizeof(uint32_t) * T);
+        if (trace->filter_dist) memcpy(trace->filter_dist, s->rdist, sizeof(float) * T);
+        if (trace->lut) memcpy(trace->lut, s->lut, sizeof(float) * nsq * 256);
+        trace->filter_cnt = cnt;
+        trace->scanned_points = scanned;
+        trace->scanned_cells = cells_scanned;
+    }
+
+    /* rank_topN_points, Puck-Flat branch (puck_index.cpp:428-457) */
+    po_heap fin;
+    heap_init(&fin, topk, dist, ids);
+    for (uint32_t idx = 0; idx < cnt; ++idx) {
+        const float* x = ix->feat + (uint64_t)s->rtag[idx] * d;
+        float t = 0.0f;
+        uint32_t m = 0;
+        for (; m + 16 <= d && t < fin.val[1]; m += 16) t = t + l2sqr16(x + m, q + m);
+        if (t < fin.val[1]) {
+            if (d - m > 0) t = t + l2sqr_ext(x + m, q + m, d - m);
+            heap_update(&fin, t, ix->mem2local[s->rtag[idx]]);
+        }
+    }
+    heap_reorder(&fin);
+    *result_num = heap_count(&fin);
+    return 0;
+}
+
+int po_search(const po_index* ix, const po_params* p, const float* q, uint32_t topk, float* dist,
+              uint32_t* ids, uint32_t* result_num, po_trace* trace) {
+    po_scratch s;
+    scratch_alloc(&s, ix, p);
+    int rc = search_one(ix, p, &s, q, topk, dist, ids, result_num, trace);
+    scratch_free(&s);
+    return rc;
+}
+
+typedef struct {
+    const po_index* ix;
+    const po_params* p;
+    uint32_t n, topk;
+    const float* q;
+    float* dist;
+    uint32_t* ids;
+    int32_t* status;
+    atomic_uint_fast64_t next;
+} batch_job;
+
+static void* batch_worker(void* arg) {
+    batch_job* job = (batch_job*)arg;
+    po_scratch s;
+    scratch_alloc(&s, job->ix, job->p);
+    for (;;) {
+        uint64_t i = atomic_fetch_add(&job->next, 1);
+        if (i >= job->n) break;
+        uint32_t rn = 0;
+        int rc = search_one(job->ix, job->p, &s, job->q + i * job->ix->d, job->topk,
+                            job->dist + i * job->topk, job->ids + i * job->topk, &rn, NULL);
+        if (job->status) job->status[i] = rc;
+    }
+    scratch_free(&s);
+    return NULL;
+}
+
+int po_search_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
+                    uint32_t topk, float* dist, uint32_t* ids, int32_t* status, int nthreads) {
+    batch_job job;
+    job.ix = ix;
+    job.p = p;
+    job.n = n;
+    job.topk = topk;
+    job.q = q;
+    job.dist = dist;
+    job.ids = ids;
+    job.status = status;
+    atomic_init(&job.next, 0);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, batch_worker, &job);
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(th);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ assign */
+
+void po_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* x,
+                       uint64_t n, int32_t* assign, float* dis) {
+    float* cn = (float*)malloc(sizeof(float) * (k ? k : 1));
+    for (uint64_t c = 0; c < k; ++c) cn[c] = dotf(centroids + c * dim, centroids + c * dim, dim);
+    for (uint64_t j = 0; j < n; ++j) {
+        const float* xj = x + j * dim;
+        float pn = dotf(xj, xj, dim);
+        float best = FLT_MAX;
+        uint32_t bi = 0;
+        for (uint64_t c = 0; c < k; ++c) {
+            float s = pn + cn[c];
+            float cur = (float)((double)s - 2.0 * (double)dotf(xj, centroids + c * dim, dim));
+            if (cur < best) {
+                best = cur;
+                bi = (uint32_t)c;
+            }
+        }
+        assign[j] = (int32_t)bi;
+        dis[j] = best;
+    }
+    free(cn);
+}
+
+typedef struct {
+    float v;
+    int32_t id;
+} pair_fi;
+
+static int cmp_pair_fi(const void* a, const void* b) {
+    const pair_fi* x = (const pair_fi*)a;
+    const pair_fi* y = (const pair_fi*)b;
+    if (x->v < y->v) return -1;
+    if (y->v < x->v) return 1;
+    return (x->id > y->id) - (x->id < y->id);
+}
+
+void po_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C, const float* fine,
+                            uint32_t F, const float* x, uint64_t n, uint32_t* cell,
+                            float* cell_dist) {
+    float* cnorm = (float*)malloc(sizeof(float) * C);
+    float* fneg = (float*)malloc(sizeof(float) * F);
+    float* fn = (float*)malloc(sizeof(float) * F);
+    float* stat = (float*)malloc(sizeof(float) * (uint64_t)C * F);
+    float* fip = (float*)malloc(sizeof(float) * F);
+    pair_fi* list = (pair_fi*)malloc(sizeof(pair_fi) * C);
+    for (uint32_t c = 0; c < C; ++c) cnorm[c] = dotf(coarse + (uint64_t)c * dim, coarse + (uint64_t)c * dim, dim) / 2;
+    for (uint32_t f = 0; f < F; ++f) {
+        fn[f] = dotf(fine + (uint64_t)f * dim, fine + (uint64_t)f * dim, dim) / 2;
+        fneg[f] = 0 - sqrtf(fn[f]);
+    }
+    for (uint32_t c = 0; c < C; ++c)
+        for (uint32_t f = 0; f < F; ++f)
+            stat[(uint64_t)c * F + f] =
+                fn[f] + dotf(fine + (uint64_t)f * dim, coarse + (uint64_t)c * dim, dim);
+    for (uint64_t j = 0; j < n; ++j) {
+        const float* xj = x + j * dim;
+        float qn = dotf(xj, xj, dim) / 2;
+        for (uint32_t c = 0; c < C; ++c) {
+            float ipc = dotf(coarse + (uint64_t)c * dim, xj, dim);
+            list[c].id = (int32_t)c;
+            list[c].v = (cnorm[c] - ipc) + qn;
+        }
+        for (uint32_t f = 0; f < F; ++f) fip[f] = dotf(fine + (uint64_t)f * dim, xj, dim);
+        qsort(list, C, sizeof(pair_fi), cmp_pair_fi);
+        float best = FLT_MAX;
+        int32_t best_id = -1;
+        for (uint32_t i = 0; i < C; ++i) {
+            const int32_t cc = list[i].id;
+            const float term = list[i].v;
+            for (uint32_t f = 0; f < F; ++f) {
+                if (sqrtf(best) - fneg[f] < sqrtf(term)) break;
+                float score = (term - fip[f]) + stat[(uint64_t)cc * F + f];
+                if (score < best) {
+                    best = score;
+                    best_id = cc * (int32_t)F + (int32_t)f;
+                }
+            }
+        }
+        cell[j] = (uint32_t)best_id;
+        cell_dist[j] = best;
+    }
+    free(cnorm);
+    free(fneg);
+    free(fn);
+    free(stat);
+    free(fip);
+    free(list);
+}

@@ -1,0 +1,71 @@
+/*
+ * ORACLE — test infrastructure, not the product.
+ *
+ * A plain-C restatement of Puck's Puck-Flat batched search path (index load,
+ * normalisation, coarse/fine stage, filter-PQ ADC walk, exact rerank) and of
+ * the k-means assignment step, following the reference's float operation order
+ * exactly (every product and sum rounded separately, BLAS dot products summed
+ * sequentially). Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it, and only as the checker. Pinned against golden
+ * vectors produced by the reference itself (tests/golden/make_golden.py).
+ */
+#ifndef PUCK_ORACLE_H
+#define PUCK_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct po_index po_index;
+
+typedef struct {
+    uint32_t search_coarse_count; /* clamped to the index's coarse_cluster_count */
+    uint32_t filter_topk;
+    uint32_t topk;                /* the configured maximum top-k (FLAGS_topk) */
+    double radius_rate;
+} po_params;
+
+/* Per-query intermediates, all optional (NULL = not wanted). */
+typedef struct {
+    uint32_t* coarse_tag; /* [search_coarse_count] */
+    float* coarse_dist;   /* [search_coarse_count] */
+    uint32_t* filter_tag; /* [filter_topk] memory idx, heap layout as the reference leaves it */
+    float* filter_dist;   /* [filter_topk] */
+    uint32_t filter_cnt;
+    float* lut;           /* [filter_nsq * 256] */
+    uint64_t scanned_points;
+    uint64_t scanned_cells;
+} po_trace;
+
+po_index* po_load(const char* index_dir, int* err);
+void po_free(po_index* ix);
+int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,
+            uint32_t* filter_nsq, uint32_t* lsq, int* whether_norm);
+/* Memory-order arrays built at load (memory_to_local, stationary, cell starts). */
+const uint32_t* po_memory_to_local(const po_index* ix);
+const float* po_stationary(const po_index* ix);
+const uint32_t* po_cell_start(const po_index* ix);
+
+/* One query, PuckIndex::search semantics. Returns 0, or <0 on error. */
+int po_search(const po_index* ix, const po_params* p, const float* q, uint32_t topk, float* dist,
+              uint32_t* ids, uint32_t* result_num, po_trace* trace);
+
+/* PySearcher::search semantics: queries fanned out over nthreads threads. */
+int po_search_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
+                    uint32_t topk, float* dist, uint32_t* ids, int32_t* status, int nthreads);
+
+/* k-means assignment step: nearest_center (kmeans.cpp:221-258). */
+void po_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* x,
+                       uint64_t n, int32_t* assign, float* dis);
+
+/* Exact nearest-cell assignment of build (hierarchical_cluster_index.cpp:1042-1138),
+ * given coarse/fine vocab with fine rows already in the trained (norm-sorted) order. */
+void po_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C, const float* fine,
+                            uint32_t F, const float* x, uint64_t n, uint32_t* cell,
+                            float* cell_dist);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,176 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+For each small case below this script
+  1. writes a seeded synthetic base set and query set (same mixture families as
+     the benchmark workloads, at test sizes),
+  2. runs the reference's own ``PuckIndex::train()`` and ``build()``
+     (puck/puck/puck_index.cpp:764-874, hierarchical_cluster_index.cpp:987-1017)
+     to produce a Puck-Flat index (whether_pq=false) in the reference's file
+     formats,
+  3. runs the reference's batch entry point ``PySearcher::search``
+     (pyapi_wrapper/py_api_wrapper.cpp:154-170) over the queries, and probes
+     the per-query intermediates with the reference's own stage functions
+     (coarse list, filter heap, LUT),
+  4. stores index files + queries + outputs in ``<case>.npz``.
+
+The reference is the copy compiled from its sources by oracle/ref/Makefile
+(parity build: -O2, AVX2 without FMA, no FP contraction, deterministic BLAS).
+Its training is seeded from time(0) (puck/hierarchical_cluster/kmeans.h:47-48),
+so the index files themselves are committed rather than regenerated.
+
+Usage: python tests/golden/make_golden.py [case ...]
+"""
+import ctypes
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from puck_gb300 import index_io  # noqa: E402
+
+REF_LIB = os.path.join(REPO, "oracle", "_ref", "libpuckref.so")
+
+# name: (n, d, C, F, whether_norm, mixture, P, T, topk, nq, extra flags)
+CASES = {
+    # L2 on integer-valued data (ties in exact distances are common), d=32,
+    # filter_nsq = 8 (lsq = 4). Includes exact duplicate base rows.
+    "l2_int_d32": dict(n=6000, d=32, C=16, F=16, norm=False, mix="int", P=8, T=64, topk=10,
+                       nq=64, dup=200),
+    # Cosine on L2-normalised data, d=24, filter_nsq = 6; P = C probes all.
+    "cos_d24": dict(n=8000, d=24, C=24, F=24, norm=True, mix="gauss", P=12, T=100, topk=20,
+                    nq=64, dup=0),
+    # d=30 -> the reference picks lsq=5, filter_nsq=6 (index_conf.cpp:123-131):
+    # exercises the generic LUT path and the scalar tail of the rerank.
+    "l2_d30_lsq5": dict(n=4000, d=30, C=12, F=12, norm=False, mix="gauss", P=5, T=48, topk=10,
+                        nq=48, dup=0),
+    # Filter heap larger than the scanned set -> the not-full reorder path,
+    # and topk > candidates for some queries.
+    "l2_small_heap": dict(n=1500, d=16, C=8, F=8, norm=False, mix="int", P=2, T=400, topk=100,
+                          nq=32, dup=50),
+}
+
+
+def make_data(case, seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n, d = case["n"], case["d"]
+    ncomp = 64
+    if case["mix"] == "int":
+        centers = rng.uniform(0, 128, size=(ncomp, d))
+        def draw(m):
+            comp = rng.integers(0, ncomp, size=m)
+            x = centers[comp] + rng.normal(0, 12, size=(m, d))
+            return np.rint(np.clip(x, 0, 255)).astype(np.float32)
+    else:
+        centers = rng.normal(0, 1, size=(ncomp, d))
+        def draw(m):
+            comp = rng.integers(0, ncomp, size=m)
+            x = (centers[comp] + rng.normal(0, 0.3, size=(m, d))).astype(np.float32)
+            x /= np.linalg.norm(x, axis=1, keepdims=True)
+            return x.astype(np.float32)
+    base = draw(n)
+    if case["dup"]:
+        src = rng.integers(0, n, size=case["dup"])
+        dst = rng.integers(0, n, size=case["dup"])
+        base[dst] = base[src]
+    queries = draw(case["nq"])
+    return base, queries
+
+
+def run_case(name):
+    case = CASES[name]
+    base, queries = make_data(case)
+    lib = ctypes.CDLL(REF_LIB)
+    lib.ref_set_flag.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    lib.ref_open_searcher.restype = ctypes.c_void_p
+    lib.ref_open_probe.restype = ctypes.c_void_p
+    lib.ref_search.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                               ctypes.c_void_p, ctypes.c_void_p]
+    lib.ref_probe.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
+    lib.ref_memory_to_local.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+
+    def flag(k, v):
+        assert lib.ref_set_flag(k.encode(), str(v).encode()) == 0, k
+
+    with tempfile.TemporaryDirectory() as tmp:
+        idx = os.path.join(tmp, "index")
+        os.makedirs(idx)
+        index_io.write_fvecs(os.path.join(idx, "all_data.feat.bin"), base)
+        flag("index_path", idx)
+        flag("feature_dim", case["d"])
+        flag("coarse_cluster_count", case["C"])
+        flag("fine_cluster_count", case["F"])
+        flag("whether_norm", "true" if case["norm"] else "false")
+        flag("whether_pq", "false")
+        flag("kmeans_iterations_count", 2)
+        flag("train_points_count", case["n"])
+        flag("pq_train_points_count", case["n"])
+        flag("threads_count", 4)
+        flag("train_fea_file_name", os.path.join(tmp, "train_clusters.dat"))
+        flag("train_pq_file_name", os.path.join(tmp, "train_pq.dat"))
+        assert lib.ref_train_build() == 0, "reference train/build failed"
+
+        flag("search_coarse_count", case["P"])
+        flag("filter_topk", case["T"])
+        flag("topk", case["topk"])
+        flag("context_initial_pool_size", 4)
+
+        searcher = lib.ref_open_searcher()
+        assert searcher, "reference init failed"
+        nq, k = queries.shape[0], case["topk"]
+        dist = np.zeros((nq, k), np.float32)
+        labels = np.full((nq, k), 0xFFFFFFFF, np.uint32)
+        q = np.ascontiguousarray(queries)
+        lib.ref_search(searcher, nq, q.ctypes.data, k, dist.ctypes.data, labels.ctypes.data)
+
+        probe = lib.ref_open_probe()
+        assert probe
+        P, T = case["P"], case["T"]
+        nsq = index_io.read_index_conf(os.path.join(idx, "index.dat"))["filter_nsq"]
+        ctag = np.zeros((nq, P), np.uint32)
+        cdist = np.zeros((nq, P), np.float32)
+        ftag = np.zeros((nq, T), np.uint32)
+        fdist = np.zeros((nq, T), np.float32)
+        fcnt = np.zeros(nq, np.uint32)
+        nlut = min(nq, 8)
+        lut = np.zeros((nlut, nsq * 256), np.float32)
+        for i in range(nq):
+            lp = lut[i].ctypes.data if i < nlut else None
+            rc = lib.ref_probe(probe, q[i].ctypes.data, ctag[i].ctypes.data, cdist[i].ctypes.data,
+                               ftag[i].ctypes.data, fdist[i].ctypes.data,
+                               fcnt[i:i + 1].ctypes.data, lp)
+            assert rc == 0, rc
+        m2l = np.zeros(case["n"], np.uint32)
+        lib.ref_memory_to_local(probe, m2l.ctypes.data)
+
+        files = {}
+        for fn in sorted(os.listdir(idx)):
+            with open(os.path.join(idx, fn), "rb") as f:
+                files["file:" + fn] = np.frombuffer(f.read(), np.uint8)
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(
+            out, queries=queries, dist=dist, labels=labels, coarse_tag=ctag, coarse_dist=cdist,
+            filter_tag=ftag, filter_dist=fdist, filter_cnt=fcnt, lut=lut, memory_to_local=m2l,
+            params=np.array([case["P"], case["T"], case["topk"]], np.int64), **files)
+        print(f"{name}: wrote {out} ({os.path.getsize(out)} bytes)")
+
+
+def main():
+    names = sys.argv[1:] or list(CASES)
+    if not os.path.exists(REF_LIB):
+        subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"])
+    for name in names:
+        # One process per case: the reference keeps its flags in globals.
+        if len(names) > 1:
+            subprocess.check_call([sys.executable, os.path.abspath(__file__), name])
+        else:
+            run_case(name)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,84 @@
+"""Pins the oracle (the C restatement) to the reference's own outputs.
+
+The golden fixtures hold index files built by the reference's train()/build()
+and the outputs of its PySearcher::search plus per-query intermediates. The
+oracle must reproduce every one bit for bit: memory order, probed coarse list,
+LUT, filter-heap layout (the reference leaves a full heap unsorted and the
+rerank walks it in that order), final distances and ids.
+"""
+import numpy as np
+
+import oracle
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def test_oracle_matches_reference(golden):
+    name, z, index_dir = golden
+    P, T, k = [int(v) for v in z["params"]]
+    ix = oracle.OracleIndex(index_dir)
+    assert np.array_equal(ix.memory_to_local(), z["memory_to_local"])
+    nq = z["queries"].shape[0]
+    for i in range(nq):
+        rc, dist, ids, rn, tr = ix.search_one(z["queries"][i], k, P, T, topk_max=k, trace=True)
+        assert rc == 0
+        assert np.array_equal(tr["coarse_tag"], z["coarse_tag"][i])
+        assert np.array_equal(_bits(tr["coarse_dist"]), _bits(z["coarse_dist"][i]))
+        cnt = tr["filter_cnt"]
+        assert cnt == z["filter_cnt"][i]
+        assert np.array_equal(tr["filter_tag"][:cnt], z["filter_tag"][i, :cnt])
+        assert np.array_equal(_bits(tr["filter_dist"][:cnt]), _bits(z["filter_dist"][i, :cnt]))
+        if i < z["lut"].shape[0]:
+            assert np.array_equal(_bits(tr["lut"]), _bits(z["lut"][i]))
+        assert np.array_equal(_bits(dist[:rn]), _bits(z["dist"][i, :rn]))
+        assert np.array_equal(ids[:rn], z["labels"][i, :rn])
+
+
+def test_oracle_batch_equals_single(golden):
+    name, z, index_dir = golden
+    P, T, k = [int(v) for v in z["params"]]
+    ix = oracle.OracleIndex(index_dir)
+    dist, ids, status = ix.search_batch(z["queries"], k, P, T, topk_max=k, nthreads=4)
+    assert (status == 0).all()
+    for i in range(z["queries"].shape[0]):
+        _, d1, i1, rn, _ = ix.search_one(z["queries"][i], k, P, T, topk_max=k)
+        assert np.array_equal(_bits(dist[i, :rn]), _bits(d1[:rn]))
+        assert np.array_equal(ids[i, :rn], i1[:rn])
+
+
+def test_oracle_rejects_bad_requests(golden):
+    name, z, index_dir = golden
+    P, T, k = [int(v) for v in z["params"]]
+    ix = oracle.OracleIndex(index_dir)
+    # topk above the configured maximum is an error (puck_index.cpp:560-563)
+    rc, *_ = ix.search_one(z["queries"][0], k + 1, P, T, topk_max=k)
+    assert rc == -1
+    if ix.whether_norm:
+        rc, *_ = ix.search_one(np.zeros(ix.d, np.float32), k, P, T, topk_max=k)
+        assert rc == -2
+
+
+def test_nearest_center_known_answer():
+    # kmeans.cpp:221-258: argmin of |x|^2 + |c|^2 - 2 x.c, first index wins ties.
+    cents = np.array([[0, 0], [2, 0], [0, 2], [2, 0]], np.float32)
+    x = np.array([[0.1, 0.1], [1.9, 0.2], [1.0, 0.0], [0.0, 3.0]], np.float32)
+    assign, dis = oracle.nearest_center(cents, x)
+    assert assign.tolist() == [0, 1, 0, 2]  # [1,0] ties between 0 and 1 -> 0
+    np.testing.assert_allclose(dis, [0.02, 0.05, 1.0, 1.0], rtol=1e-5, atol=1e-6)
+
+
+def test_nearest_cell_assign_is_exact_argmin():
+    rng = np.random.default_rng(3)
+    coarse = rng.normal(size=(6, 8)).astype(np.float32)
+    fine = (0.3 * rng.normal(size=(5, 8))).astype(np.float32)
+    # the reference sorts fine rows by descending norm at train time
+    fine = fine[np.argsort(-np.linalg.norm(fine, axis=1), kind="stable")]
+    x = rng.normal(size=(200, 8)).astype(np.float32)
+    cell, dist = oracle.nearest_cell_assign(coarse, fine, x)
+    cent = (coarse[:, None, :] + fine[None, :, :]).reshape(-1, 8).astype(np.float64)
+    full = ((x[:, None, :].astype(np.float64) - cent[None]) ** 2).sum(-1) / 2
+    best = full.min(1)
+    # the pruned walk must land on an exact minimiser (up to float rounding)
+    assert np.all(full[np.arange(len(x)), cell] <= best + 1e-4)
