@@ -1,0 +1,141 @@
+/*
+ * puck_gb300 — GB300-native batched search for Puck (Puck-Flat) indexes.
+ *
+ * C ABI: plain pointers and sizes, no C++ or torch types. Every entry point
+ * returns 0 on success and a negative PGPU_E* code on failure; the message of
+ * the last failure on the calling thread is available from pgpu_last_error().
+ *
+ * The index is the reference's on-disk Puck index (index.dat, coarse.dat,
+ * fine.dat, cell_assign.dat, filter_codebook.dat, filter_data.dat,
+ * all_data.feat.bin) with whether_pq = false ("Puck-Flat"): filter-PQ ADC scan
+ * followed by an exact FP32 rerank against the original vectors. The search
+ * runs on one GPU; there is no CPU fallback.
+ */
+#ifndef PUCK_GB300_H
+#define PUCK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGPU_OK 0
+#define PGPU_E_INVALID (-1)     /* bad argument: topk > configured topk, null feature, ... */
+#define PGPU_E_ZERO_NORM (-2)   /* whether_norm index and a query with norm < 1e-6 */
+#define PGPU_E_IO (-3)          /* index file missing, short or inconsistent */
+#define PGPU_E_UNSUPPORTED (-4) /* index feature outside Puck-Flat (whether_pq, ip2cos, ks != 256) */
+#define PGPU_E_CUDA (-5)        /* CUDA runtime error, or no usable GPU */
+#define PGPU_E_NOMEM (-6)       /* device allocation failed */
+#define PGPU_E_LIMIT (-7)       /* size beyond a documented limit of a kernel */
+
+/* Search modes. */
+#define PGPU_MODE_EXACT 0      /* reference-exact: the same cells, heap and ties as PuckIndex::search */
+
+/* Search parameters. Field names and meanings follow Puck's gflags
+ * (puck/gflags/puck_gflags.cpp:68-78): search_coarse_count (default 200),
+ * topk (default 100, the largest request topk allowed), filter_topk
+ * (default 11 * topk, puck/index_conf.cpp:178-180), radius_rate (default 1.0). */
+typedef struct {
+    uint32_t search_coarse_count;
+    uint32_t topk;
+    uint32_t filter_topk;
+    double radius_rate;
+    int32_t device;     /* CUDA device ordinal */
+    uint32_t max_batch; /* queries per device pass; sizes the per-pass scratch */
+    int32_t mode;       /* PGPU_MODE_* */
+} pgpu_params;
+
+typedef struct pgpu_index pgpu_index;
+
+typedef struct {
+    uint32_t feature_dim;
+    uint32_t total_point_count;
+    uint32_t coarse_cluster_count;
+    uint32_t fine_cluster_count;
+    uint32_t filter_nsq;
+    uint32_t lsq;
+    int32_t whether_norm;
+    uint64_t device_bytes; /* HBM held by the resident index */
+} pgpu_index_info;
+
+/* Host arrays of a Puck-Flat index, in the reference's input ("local") order,
+ * i.e. exactly what the index files hold. Used by pgpu_open_arrays. */
+typedef struct {
+    uint32_t feature_dim, total_point_count, coarse_cluster_count, fine_cluster_count;
+    uint32_t filter_nsq;
+    int32_t whether_norm;
+    const float* coarse;          /* [coarse_cluster_count][feature_dim] */
+    const float* fine;            /* [fine_cluster_count][feature_dim] */
+    const float* base;            /* [total_point_count][feature_dim] */
+    const uint32_t* cell_assign;  /* [total_point_count], coarse * fine_cluster_count + fine */
+    const float* filter_codebook; /* [filter_nsq][256][feature_dim / filter_nsq] */
+    const float* filter_offsets;  /* [total_point_count] */
+    const uint8_t* filter_codes;  /* [total_point_count][filter_nsq] */
+} pgpu_index_arrays;
+
+/* Fills the reference's flag defaults (search_coarse_count 200, topk 100,
+ * filter_topk 1100, radius_rate 1.0, device 0, max_batch 8192, exact mode). */
+void pgpu_params_default(pgpu_params* params);
+
+/* Replaces Index::init() (puck/hierarchical_cluster/hierarchical_cluster_index.cpp:220-255,
+ * PuckIndex overrides puck/puck/puck_index.cpp:173-344): reads the index files under
+ * index_path, builds the memory order (stable by cell, filter offset, input id),
+ * the per-cell constants, and uploads the device-resident layout. */
+int pgpu_open(const char* index_path, const pgpu_params* params, pgpu_index** out);
+
+/* Same as pgpu_open, from host arrays instead of files. */
+int pgpu_open_arrays(const pgpu_index_arrays* arrays, const pgpu_params* params,
+                     pgpu_index** out);
+
+/* Replaces the search-parameter part of update_gflag() + init()
+ * (pyapi_wrapper/py_api_wrapper.cpp:33-35, 78-108) without reloading the index.
+ * feature/structure come from the index; only search_coarse_count, topk,
+ * filter_topk, radius_rate, max_batch and mode are taken. */
+int pgpu_set_search_params(pgpu_index* index, const pgpu_params* params);
+
+/* Replaces PySearcher::search (pyapi_wrapper/py_api_wrapper.cpp:154-170): n queries
+ * of feature_dim floats, row-major, HOST memory; writes n*topk distances
+ * (squared L2 in the searched space, ascending) and labels (input-order ids) per
+ * query. Slots past a query's result count hold distance 0x7f7f7f7f (3.3961514e38)
+ * and label 0xFFFFFFFF. status (optional, n entries) receives each query's
+ * PuckIndex::search return code (0, or PGPU_E_INVALID / PGPU_E_ZERO_NORM). */
+int pgpu_search_batch(pgpu_index* index, uint32_t n, const float* query, uint32_t topk,
+                      float* distance, uint32_t* labels, int32_t* status);
+
+/* Replaces virtual int puck::Index::search(const Request*, Response*)
+ * (puck/index.h:46, implemented by puck/puck/puck_index.cpp:559-600) for one query:
+ * Request{topk, feature} -> Response{distance, local_idx, result_num}. */
+int pgpu_search(pgpu_index* index, const float* feature, uint32_t topk, float* distance,
+                uint32_t* local_idx, uint32_t* result_num);
+
+/* Device-memory variant of pgpu_search_batch: query, distance, labels and status
+ * are DEVICE pointers on the index's GPU; work is enqueued on `stream`
+ * (a cudaStream_t, NULL = the legacy default stream) and the call returns
+ * without synchronising. */
+int pgpu_search_batch_device(pgpu_index* index, uint32_t n, const float* query, uint32_t topk,
+                             float* distance, uint32_t* labels, int32_t* status, void* stream);
+
+int pgpu_index_info_get(const pgpu_index* index, pgpu_index_info* info);
+
+/* Launch statistics of the last search call on this index: kernels launched and
+ * the number of filter records the ADC scan evaluated. */
+int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
+                    uint64_t* records_scanned, uint64_t* cells_scanned);
+
+int pgpu_close(pgpu_index* index);
+
+/* k-means assignment step used by train (kmeans.cpp:221-258 nearest_center):
+ * for each of n points (DEVICE pointer, [n][dim]) the id of the nearest of k
+ * centroids (DEVICE pointer, [k][dim]) and its distance
+ * |x|^2 + |c|^2 - 2 x.c, first centroid wins ties. Enqueued on `stream`. */
+int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* points,
+                        uint64_t n, int32_t* assign, float* distance, void* stream);
+
+const char* pgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,401 @@
+// extern "C" entry points of libpuck_gb300 (declared in include/puck_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pgpu_internal.h"
+
+struct pgpu_index {
+    int device = 0;
+    pgpu::DeviceIndex ix;
+    pgpu::Scratch s;
+    pgpu::SearchConfig cfg;
+    uint32_t max_batch = 8192;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    // staging for host-buffer searches
+    float* d_qin = nullptr;
+    float* d_dist = nullptr;
+    uint32_t* d_ids = nullptr;
+    int32_t* d_status = nullptr;
+    uint32_t stage_topk = 0;
+    uint64_t kernels = 0, records = 0, cells = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void free_scratch(pgpu::Scratch* s) {
+    void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
+                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    *s = pgpu::Scratch();
+}
+
+void free_staging(pgpu_index* h) {
+    void* ptrs[] = {h->d_qin, h->d_dist, h->d_ids, h->d_status};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    h->d_qin = nullptr;
+    h->d_dist = nullptr;
+    h->d_ids = nullptr;
+    h->d_status = nullptr;
+    h->stage_topk = 0;
+}
+
+template <class T>
+cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
+    const size_t sz = sizeof(T) * (count ? count : 1);
+    cudaError_t e = cudaMalloc((void**)p, sz);
+    if (e == cudaSuccess) *bytes += sz;
+    return e;
+}
+
+int alloc_scratch(pgpu_index* h) {
+    free_scratch(&h->s);
+    pgpu::Scratch& s = h->s;
+    const uint64_t B = h->max_batch;
+    const auto& ix = h->ix;
+    s.P = std::min(h->cfg.P, ix.C);
+    s.T = h->cfg.T;
+    uint64_t b = 0;
+    cudaError_t e;
+#define PGPU_ALLOC(ptr, cnt)                                   \
+    e = alloc(&(ptr), (cnt), &b);                              \
+    if (e != cudaSuccess) {                                    \
+        free_scratch(&s);                                      \
+        return cuda_fail(e, "scratch allocation");             \
+    }
+    PGPU_ALLOC(s.q, B * ix.d);
+    PGPU_ALLOC(s.qnorm, B);
+    PGPU_ALLOC(s.status, B);
+    PGPU_ALLOC(s.dots, B * std::max(ix.C, ix.F));
+    PGPU_ALLOC(s.cdist, B * s.P);
+    PGPU_ALLOC(s.ctag, B * s.P);
+    PGPU_ALLOC(s.fdist, B * ix.F);
+    PGPU_ALLOC(s.ftag, B * ix.F);
+    PGPU_ALLOC(s.hdist, B * s.T);
+    PGPU_ALLOC(s.htag, B * s.T);
+    PGPU_ALLOC(s.hcnt, B);
+    PGPU_ALLOC(s.counters, 4);
+#undef PGPU_ALLOC
+    s.cap = (uint32_t)B;
+    s.bytes = b;
+    return PGPU_OK;
+}
+
+int check_config(const pgpu_index* h, const pgpu_params* p) {
+    // IndexConf::adaptive_search_param (puck/index_conf.cpp:152-199)
+    if (p->radius_rate < 1.0) return fail(PGPU_E_INVALID, "radius_rate should >= 1.0");
+    if (p->filter_topk < p->topk) return fail(PGPU_E_INVALID, "filter_topk should >= topk");
+    if (p->search_coarse_count == 0 || p->filter_topk == 0)
+        return fail(PGPU_E_INVALID, "search_coarse_count and filter_topk must be positive");
+    if (p->filter_topk > pgpu::kMaxFilterTopk)
+        return fail(PGPU_E_LIMIT, "filter_topk above " + std::to_string(pgpu::kMaxFilterTopk));
+    if (p->topk > pgpu::kMaxFilterTopk)
+        return fail(PGPU_E_LIMIT, "topk above " + std::to_string(pgpu::kMaxFilterTopk));
+    if (p->max_batch == 0) return fail(PGPU_E_INVALID, "max_batch must be positive");
+    if (p->mode != PGPU_MODE_EXACT) return fail(PGPU_E_INVALID, "unknown search mode");
+    if (h != nullptr) {
+        if (pgpu::walk_smem_bytes(h->ix, p->filter_topk) > 220 * 1024 ||
+            pgpu::rerank_smem_bytes(h->ix, p->filter_topk, p->topk) > 220 * 1024)
+            return fail(PGPU_E_LIMIT, "filter_topk/topk/filter_nsq exceed the shared-memory budget");
+    }
+    return PGPU_OK;
+}
+
+void apply_config(pgpu_index* h, const pgpu_params* p) {
+    h->cfg.P = p->search_coarse_count;
+    h->cfg.T = p->filter_topk;
+    h->cfg.topk_max = p->topk;
+    h->cfg.radius_rate = p->radius_rate;
+    h->cfg.mode = p->mode;
+    h->max_batch = p->max_batch;
+}
+
+int ensure_staging(pgpu_index* h, uint32_t topk) {
+    if (h->d_qin != nullptr && h->stage_topk >= topk) return PGPU_OK;
+    free_staging(h);
+    const uint64_t B = h->max_batch;
+    uint64_t b = 0;
+    cudaError_t e = alloc(&h->d_qin, B * h->ix.d, &b);
+    if (e == cudaSuccess) e = alloc(&h->d_dist, B * std::max(1u, topk), &b);
+    if (e == cudaSuccess) e = alloc(&h->d_ids, B * std::max(1u, topk), &b);
+    if (e == cudaSuccess) e = alloc(&h->d_status, B, &b);
+    if (e != cudaSuccess) {
+        free_staging(h);
+        return cuda_fail(e, "staging allocation");
+    }
+    h->stage_topk = topk;
+    return PGPU_OK;
+}
+
+// One pass of <= max_batch queries, all buffers on the device.
+int run_pass(pgpu_index* h, uint32_t n, const float* d_q, uint32_t topk, float* d_dist,
+             uint32_t* d_ids, int32_t* d_status, cudaStream_t st) {
+    auto& ix = h->ix;
+    auto& s = h->s;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 4, st)) != cudaSuccess)
+        return cuda_fail(e, "memset");
+    if ((e = pgpu::launch_prep_queries(ix, d_q, n, s, st)) != cudaSuccess)
+        return cuda_fail(e, "prep_queries");
+    if ((e = pgpu::launch_centroid_scores(s.q, n, ix.coarse, ix.C, ix.d, ix.coarse_norms, false,
+                                          s.dots, ix.C, st)) != cudaSuccess)
+        return cuda_fail(e, "coarse scores");
+    if ((e = pgpu::launch_topsort_status(s.dots, n, ix.C, ix.C, s.P, s.cdist, s.ctag, s.status,
+                                         st)) != cudaSuccess)
+        return cuda_fail(e, "coarse select");
+    if ((e = pgpu::launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F,
+                                          st)) != cudaSuccess)
+        return cuda_fail(e, "fine scores");
+    if ((e = pgpu::launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status,
+                                         st)) != cudaSuccess)
+        return cuda_fail(e, "fine order");
+    if ((e = pgpu::launch_walk_scan(ix, h->cfg, n, s, st)) != cudaSuccess)
+        return cuda_fail(e, "walk_scan");
+    if ((e = pgpu::launch_rerank(ix, h->cfg, n, topk, s, d_dist, d_ids, d_status, st)) !=
+        cudaSuccess)
+        return cuda_fail(e, "rerank");
+    h->kernels += 7;
+    return PGPU_OK;
+}
+
+int open_common(const pgpu_index_arrays& a, const pgpu_params* params, pgpu_index** out) {
+    pgpu_params p;
+    if (params) p = *params;
+    else pgpu_params_default(&p);
+    if (int rc = check_config(nullptr, &p)) return rc;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(PGPU_E_CUDA, "no CUDA device available");
+    if (p.device < 0 || p.device >= ndev) return fail(PGPU_E_INVALID, "device ordinal out of range");
+    if ((e = cudaSetDevice(p.device)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    pgpu::HostIndex hidx;
+    std::string err;
+    if (int rc = pgpu::build_host_index(a, &hidx, &err)) return fail(rc, err);
+    auto* h = new pgpu_index();
+    h->device = p.device;
+    if (int rc = pgpu::upload_index_with_base(hidx, a.base, &h->ix, &err)) {
+        delete h;
+        return fail(rc, err);
+    }
+    if (int rc = check_config(h, &p)) {
+        pgpu::free_device_index(&h->ix);
+        delete h;
+        return rc;
+    }
+    apply_config(h, &p);
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        pgpu::free_device_index(&h->ix);
+        delete h;
+        return cuda_fail(e, "stream create");
+    }
+    if (int rc = alloc_scratch(h)) {
+        cudaStreamDestroy(h->stream);
+        pgpu::free_device_index(&h->ix);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return PGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pgpu_params_default(pgpu_params* p) {
+    p->search_coarse_count = 200;
+    p->topk = 100;
+    p->filter_topk = 1100;
+    p->radius_rate = 1.0;
+    p->device = 0;
+    p->max_batch = 8192;
+    p->mode = PGPU_MODE_EXACT;
+}
+
+const char* pgpu_last_error(void) { return g_last_error.c_str(); }
+
+int pgpu_open_arrays(const pgpu_index_arrays* arrays, const pgpu_params* params,
+                     pgpu_index** out) {
+    if (arrays == nullptr || out == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    *out = nullptr;
+    return open_common(*arrays, params, out);
+}
+
+int pgpu_open(const char* index_path, const pgpu_params* params, pgpu_index** out) {
+    if (index_path == nullptr || out == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    *out = nullptr;
+    if (params != nullptr)
+        if (int rc = check_config(nullptr, params)) return rc;
+    pgpu_index_arrays a;
+    std::memset(&a, 0, sizeof(a));
+    std::vector<char> storage;
+    std::string err;
+    if (int rc = pgpu::read_index_files(index_path, &a, storage, &err)) return fail(rc, err);
+    return open_common(a, params, out);
+}
+
+int pgpu_set_search_params(pgpu_index* h, const pgpu_params* params) {
+    if (h == nullptr || params == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> g(h->mu);
+    if (int rc = check_config(h, params)) return rc;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    apply_config(h, params);
+    free_staging(h);
+    return alloc_scratch(h);
+}
+
+int pgpu_search_batch_device(pgpu_index* h, uint32_t n, const float* query, uint32_t topk,
+                             float* distance, uint32_t* labels, int32_t* status, void* stream) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    if (n == 0 || topk == 0) return PGPU_OK;
+    if (query == nullptr || distance == nullptr || labels == nullptr)
+        return fail(PGPU_E_INVALID, "feature is nullptr");
+    if (topk > h->cfg.topk_max)
+        return fail(PGPU_E_INVALID, "topk should <= topk, topk = " + std::to_string(h->cfg.topk_max));
+    std::lock_guard<std::mutex> g(h->mu);
+    cudaSetDevice(h->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    h->kernels = 0;
+    const uint32_t d = h->ix.d;
+    for (uint32_t off = 0; off < n; off += h->max_batch) {
+        const uint32_t m = std::min(h->max_batch, n - off);
+        if (int rc = run_pass(h, m, query + (uint64_t)off * d, topk, distance + (uint64_t)off * topk,
+                              labels + (uint64_t)off * topk, status ? status + off : nullptr, st))
+            return rc;
+    }
+    return PGPU_OK;
+}
+
+int pgpu_search_batch(pgpu_index* h, uint32_t n, const float* query, uint32_t topk,
+                      float* distance, uint32_t* labels, int32_t* status) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    if (n == 0 || topk == 0) return PGPU_OK;
+    if (query == nullptr || distance == nullptr || labels == nullptr)
+        return fail(PGPU_E_INVALID, "feature is nullptr");
+    if (topk > h->cfg.topk_max) {
+        if (status)
+            for (uint32_t i = 0; i < n; ++i) status[i] = PGPU_E_INVALID;
+        return fail(PGPU_E_INVALID, "topk should <= topk, topk = " + std::to_string(h->cfg.topk_max));
+    }
+    std::lock_guard<std::mutex> g(h->mu);
+    cudaSetDevice(h->device);
+    if (int rc = ensure_staging(h, topk)) return rc;
+    const uint32_t d = h->ix.d;
+    cudaStream_t st = h->stream;
+    h->kernels = 0;
+    h->records = 0;
+    h->cells = 0;
+    cudaError_t e;
+    for (uint32_t off = 0; off < n; off += h->max_batch) {
+        const uint32_t m = std::min(h->max_batch, n - off);
+        if ((e = cudaMemcpyAsync(h->d_qin, query + (uint64_t)off * d, sizeof(float) * m * d,
+                                 cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_fail(e, "query upload");
+        if (int rc = run_pass(h, m, h->d_qin, topk, h->d_dist, h->d_ids, h->d_status, st)) return rc;
+        if ((e = cudaMemcpyAsync(distance + (uint64_t)off * topk, h->d_dist,
+                                 sizeof(float) * m * topk, cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaMemcpyAsync(labels + (uint64_t)off * topk, h->d_ids,
+                                 sizeof(uint32_t) * m * topk, cudaMemcpyDeviceToHost, st)))
+            return cuda_fail(e, "result download");
+        if (status && (e = cudaMemcpyAsync(status + off, h->d_status, sizeof(int32_t) * m,
+                                           cudaMemcpyDeviceToHost, st)))
+            return cuda_fail(e, "status download");
+        unsigned long long cnt[4];
+        if ((e = cudaMemcpyAsync(cnt, h->s.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaStreamSynchronize(st)))
+            return cuda_fail(e, "search");
+        h->records += cnt[0];
+        h->cells += cnt[1];
+    }
+    return PGPU_OK;
+}
+
+int pgpu_search(pgpu_index* h, const float* feature, uint32_t topk, float* distance,
+                uint32_t* local_idx, uint32_t* result_num) {
+    if (h == nullptr || feature == nullptr) return fail(PGPU_E_INVALID, "feature is nullptr");
+    if (topk > h->cfg.topk_max)
+        return fail(PGPU_E_INVALID, "topk should <= topk, topk = " + std::to_string(h->cfg.topk_max));
+    if (topk == 0) {
+        if (result_num) *result_num = 0;
+        return PGPU_OK;
+    }
+    int32_t status = 0;
+    if (int rc = pgpu_search_batch(h, 1, feature, topk, distance, local_idx, &status)) return rc;
+    if (result_num) {
+        uint32_t rn = 0;
+        while (rn < topk && local_idx[rn] != pgpu::kNoLabel) ++rn;
+        *result_num = rn;
+    }
+    if (status != 0) return fail(status, "query rejected (zero norm)");
+    return PGPU_OK;
+}
+
+int pgpu_index_info_get(const pgpu_index* h, pgpu_index_info* info) {
+    if (h == nullptr || info == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    info->feature_dim = h->ix.d;
+    info->total_point_count = h->ix.n;
+    info->coarse_cluster_count = h->ix.C;
+    info->fine_cluster_count = h->ix.F;
+    info->filter_nsq = h->ix.nsq;
+    info->lsq = h->ix.lsq;
+    info->whether_norm = h->ix.whether_norm;
+    info->device_bytes = h->ix.bytes;
+    return PGPU_OK;
+}
+
+int pgpu_last_stats(const pgpu_index* h, uint64_t* kernels_launched, uint64_t* records_scanned,
+                    uint64_t* cells_scanned) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    if (kernels_launched) *kernels_launched = h->kernels;
+    if (records_scanned) *records_scanned = h->records;
+    if (cells_scanned) *cells_scanned = h->cells;
+    return PGPU_OK;
+}
+
+int pgpu_close(pgpu_index* h) {
+    if (h == nullptr) return PGPU_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    free_staging(h);
+    free_scratch(&h->s);
+    pgpu::free_device_index(&h->ix);
+    delete h;
+    return PGPU_OK;
+}
+
+int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* points,
+                        uint64_t n, int32_t* assign, float* distance, void* stream) {
+    if (dim == 0 || k == 0 || centroids == nullptr || points == nullptr || assign == nullptr ||
+        distance == nullptr)
+        return fail(PGPU_E_INVALID, "invalid argument");
+    if (n == 0) return PGPU_OK;
+    cudaError_t e = pgpu::launch_nearest_center(dim, centroids, k, points, n, assign, distance,
+                                                (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nearest_center");
+    return PGPU_OK;
+}
+
+}  // extern "C"

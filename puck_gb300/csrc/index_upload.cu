@@ -1,0 +1,107 @@
+// Device-resident index construction: copies the host layout to HBM, permutes
+// the original vectors into memory order on the GPU, and computes the per-cell
+// constants of HierarchicalClusterIndex::read_coodbooks
+// (puck/hierarchical_cluster/hierarchical_cluster_index.cpp:278-320) and
+// PuckIndex::convert_local_to_memory_idx (puck/puck/puck_index.cpp:284-305).
+#include <cfloat>
+#include <cmath>
+
+#include "pgpu_internal.h"
+
+namespace pgpu {
+namespace {
+
+__global__ void k_gather_rows(const float* __restrict__ src, const uint32_t* __restrict__ rows,
+                              uint64_t n, uint32_t d, float* __restrict__ dst) {
+    // one warp per destination row
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const float* s = src + (uint64_t)rows[w] * d;
+    float* t = dst + w * d;
+    for (uint32_t k = lane; k < d; k += 32) t[k] = s[k];
+}
+
+template <class T>
+cudaError_t dev_copy(T** dst, const T* src, uint64_t count, uint64_t* bytes) {
+    const size_t sz = sizeof(T) * (count ? count : 1);
+    cudaError_t e = cudaMalloc((void**)dst, sz);
+    if (e != cudaSuccess) return e;
+    *bytes += sz;
+    if (count) e = cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+    return e;
+}
+
+template <class T>
+cudaError_t dev_alloc(T** dst, uint64_t count, uint64_t* bytes) {
+    const size_t sz = sizeof(T) * (count ? count : 1);
+    cudaError_t e = cudaMalloc((void**)dst, sz);
+    if (e == cudaSuccess) *bytes += sz;
+    return e;
+}
+
+}  // namespace
+
+// base: the original vectors in input order (host).
+int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* ix,
+                           std::string* err) {
+    *ix = DeviceIndex();
+    ix->d = h.d;
+    ix->n = h.n;
+    ix->C = h.C;
+    ix->F = h.F;
+    ix->nsq = h.nsq;
+    ix->lsq = h.lsq;
+    ix->whether_norm = h.whether_norm;
+    ix->code_stride = h.code_stride;
+    uint64_t bytes = 0;
+    const uint64_t cells = (uint64_t)h.C * h.F;
+    cudaError_t e = cudaSuccess;
+    float* fine_half = nullptr;
+    float* base_dev = nullptr;
+#define PGPU_TRY(x)              \
+    do {                         \
+        e = (x);                 \
+        if (e != cudaSuccess) goto fail; \
+    } while (0)
+    PGPU_TRY(dev_copy(&ix->coarse, h.coarse.data(), h.coarse.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->fine, h.fine.data(), h.fine.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->codebook, h.codebook.data(), h.codebook.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->cell_start, h.cell_start.data(), h.cell_start.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->mem2local, h.mem2local.data(), h.mem2local.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->offsets, h.offsets_mem.data(), h.offsets_mem.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->codes, h.codes_mem.data(), h.codes_mem.size(), &bytes));
+    PGPU_TRY(dev_alloc(&ix->coarse_norms, h.C, &bytes));
+    PGPU_TRY(dev_alloc(&ix->stationary, cells, &bytes));
+    PGPU_TRY(dev_alloc(&ix->min_dist_offset, h.C, &bytes));
+    PGPU_TRY(dev_alloc(&ix->feat, (uint64_t)h.n * h.d, &bytes));
+    PGPU_TRY(cudaMalloc(&fine_half, sizeof(float) * h.F));
+    PGPU_TRY(cudaMalloc(&base_dev, sizeof(float) * ((uint64_t)h.n * h.d + 1)));
+    if (h.n) PGPU_TRY(cudaMemcpy(base_dev, base, sizeof(float) * (uint64_t)h.n * h.d,
+                                 cudaMemcpyHostToDevice));
+    if (h.n) {
+        const uint64_t threads = (uint64_t)h.n * 32;
+        k_gather_rows<<<(unsigned)((threads + 255) / 256), 256>>>(base_dev, ix->mem2local, h.n, h.d,
+                                                                  ix->feat);
+        PGPU_TRY(cudaGetLastError());
+    }
+    PGPU_TRY(launch_half_norms(ix->coarse, h.C, h.d, ix->coarse_norms, 0));
+    PGPU_TRY(launch_half_norms(ix->fine, h.F, h.d, fine_half, 0));
+    PGPU_TRY(launch_stationary(ix->coarse, h.C, ix->fine, h.F, h.d, fine_half, ix->stationary, 0));
+    PGPU_TRY(launch_cell_constants(ix->stationary, ix->cell_start, ix->min_dist_offset, h.C, h.F,
+                                   std::sqrt(FLT_MAX), 0));
+    PGPU_TRY(cudaDeviceSynchronize());
+    cudaFree(fine_half);
+    cudaFree(base_dev);
+    ix->bytes = bytes;
+    return PGPU_OK;
+fail:
+#undef PGPU_TRY
+    if (fine_half) cudaFree(fine_half);
+    if (base_dev) cudaFree(base_dev);
+    *err = std::string("CUDA error during index upload: ") + cudaGetErrorString(e);
+    free_device_index(ix);
+    return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
+}
+
+}  // namespace pgpu

@@ -1,0 +1,965 @@
+// Exact-mode search kernels for Puck-Flat indexes on sm_103a.
+//
+// Float semantics: every product and sum is rounded separately (__fmul_rn,
+// __fadd_rn: no FMA contraction) and every reduction runs in the order the
+// reference's code (built without FMA contraction, with a sequential BLAS)
+// uses, so distances, heap contents and tie resolution are bit-identical to
+// PuckIndex::search (puck/puck/puck_index.cpp:559-600).
+//
+// Pipeline per pass of B queries (one stream):
+//   k_prep_queries     normalisation + |q|^2          hierarchical_cluster_index.cpp:1513-1536
+//   k_centroid_scores  0.5|c|^2 - q.c  /  -q.f        hierarchical_cluster_index.cpp:700-727,
+//                                                     puck_index.cpp:494-501
+//   k_topsort          top-P coarse / full fine order max_heap.cpp (exact heap on ties)
+//   k_walk_scan        cell walk + filter-PQ ADC      puck_index.cpp:346-390, 485-557
+//   k_rerank           exact L2 of the survivors      puck_index.cpp:392-457
+#include <cfloat>
+#include <cstdint>
+
+#include "pgpu_internal.h"
+
+namespace pgpu {
+namespace {
+
+__device__ __forceinline__ float sentinel_f() { return __uint_as_float(kHeapSentinelBits); }
+
+// Sequential dot product, each product and partial sum rounded (BLAS order of
+// the oracle build: s = 0; s += x[i]*y[i]).
+__device__ __forceinline__ float dot_seq(const float* x, const float* y, uint32_t n) {
+    float s = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) s = __fadd_rn(s, __fmul_rn(x[i], y[i]));
+    return s;
+}
+
+// ------------------------------------------------------------------ MaxHeap
+// Puck's bounded max-heap (puck/hierarchical_cluster/max_heap.cpp:28-102) on
+// 1-based arrays: reject v >= top; the first `size` inserts sift down from the
+// last unfilled slot; reorder() heap-sorts to ascending order. Single thread.
+__device__ __forceinline__ void heap_insert(float* hv, uint32_t* ht, uint32_t heap_size,
+                                            uint32_t father, float v, uint32_t t) {
+    for (;;) {
+        uint32_t left = father << 1;
+        if (left > heap_size) break;
+        uint32_t right = left + 1;
+        float lv = hv[left];
+        if (right > heap_size || lv > hv[right]) {
+            if (lv < v) break;
+            hv[father] = lv;
+            ht[father] = ht[left];
+            father = left;
+        } else {
+            float rv = hv[right];
+            if (rv < v) break;
+            hv[father] = rv;
+            ht[father] = ht[right];
+            father = right;
+        }
+    }
+    hv[father] = v;
+    ht[father] = t;
+}
+
+__device__ __forceinline__ bool heap_update(float* hv, uint32_t* ht, uint32_t size,
+                                            uint32_t& dpc, float v, uint32_t t) {
+    if (v >= hv[1]) return false;
+    uint32_t father = 1;
+    if (dpc > 0) father = dpc--;
+    heap_insert(hv, ht, size, father, v, t);
+    return true;
+}
+
+__device__ void heap_reorder(float* hv, uint32_t* ht, uint32_t size) {
+    for (uint32_t i = 0; i < size; ++i) {
+        float vb = hv[1];
+        uint32_t tb = ht[1];
+        uint32_t hs = size - i;
+        heap_insert(hv, ht, hs - 1, 1, hv[hs], ht[hs]);
+        hv[hs] = vb;
+        ht[hs] = tb;
+    }
+}
+
+// ------------------------------------------------------------- block scans
+constexpr int kWalkThreads = 128;  // also the number of fine cells per speculation chunk
+constexpr int kPointBuf = 1024;    // points whose ADC is precomputed per chunk
+
+// Inclusive scan over a 128-thread block; `warp_tot` needs 4 slots.
+__device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* warp_tot,
+                                                   uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) warp_tot[warp] = v;
+    __syncthreads();
+    uint32_t add = 0;
+    for (int w = 0; w < warp; ++w) add += warp_tot[w];
+    *total = warp_tot[0] + warp_tot[1] + warp_tot[2] + warp_tot[3];
+    __syncthreads();
+    return v + add;
+}
+
+// ---------------------------------------------------------------- kernels
+
+__global__ void k_prep_queries(const float* __restrict__ q_in, float* __restrict__ q_out,
+                               float* __restrict__ qnorm, int32_t* __restrict__ status,
+                               uint32_t n, uint32_t d, int whether_norm) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* x = q_in + (uint64_t)i * d;
+    float* y = q_out + (uint64_t)i * d;
+    int32_t st = 0;
+    // Non-finite input has no defined result in the reference; it is rejected so
+    // that no NaN reaches the sorts and the walk.
+    for (uint32_t k = 0; k < d; ++k)
+        if (!isfinite(x[k])) st = PGPU_E_INVALID;
+    if (st != 0) {
+        for (uint32_t k = 0; k < d; ++k) y[k] = 0.0f;
+    } else if (whether_norm) {
+        // cblas_snrm2 then cblas_sscal(1.0 / norm) (hierarchical_cluster_index.cpp:1524-1531)
+        const float norm = __fsqrt_rn(dot_seq(x, x, d));
+        if ((double)norm < 1e-6) {
+            st = PGPU_E_ZERO_NORM;
+            for (uint32_t k = 0; k < d; ++k) y[k] = 0.0f;
+        } else {
+            const float alpha = __double2float_rn(1.0 / (double)norm);
+            for (uint32_t k = 0; k < d; ++k) y[k] = __fmul_rn(alpha, x[k]);
+        }
+    } else {
+        for (uint32_t k = 0; k < d; ++k) y[k] = x[k];
+    }
+    qnorm[i] = dot_seq(y, y, d);
+    if (st == 0 && !isfinite(qnorm[i])) st = PGPU_E_INVALID;
+    status[i] = st;
+}
+
+// out[i][j] = bias[j] - a_i.b_j (MODE 0), -(a_i.b_j) (MODE 1), bias[j] + a_i.b_j (MODE 2).
+// 64x64 output tile per block, 4x4 per thread; the k loop runs in order for
+// every output, so each dot product is summed sequentially.
+constexpr int kTile = 64, kTileK = 32;
+template <int MODE>
+__global__ __launch_bounds__(256) void k_centroid_scores(const float* __restrict__ A, uint32_t na,
+                                                         const float* __restrict__ B, uint32_t nb,
+                                                         uint32_t d, const float* __restrict__ bias,
+                                                         float* __restrict__ out, uint32_t ld_out) {
+    __shared__ float As[kTileK][kTile + 1];
+    __shared__ float Bs[kTileK][kTile + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const uint32_t a0 = blockIdx.y * kTile, b0 = blockIdx.x * kTile;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+    for (uint32_t k0 = 0; k0 < d; k0 += kTileK) {
+        for (int e = threadIdx.x; e < kTile * kTileK; e += 256) {
+            const int r = e / kTileK, kk = e % kTileK;
+            const uint32_t k = k0 + kk;
+            As[kk][r] = (a0 + r < na && k < d) ? A[(uint64_t)(a0 + r) * d + k] : 0.0f;
+            Bs[kk][r] = (b0 + r < nb && k < d) ? B[(uint64_t)(b0 + r) * d + k] : 0.0f;
+        }
+        __syncthreads();
+        const uint32_t kmax = min((uint32_t)kTileK, d - k0);
+        for (uint32_t kk = 0; kk < kmax; ++kk) {
+            float av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(av[i], bv[j]));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t a = a0 + ty + 16 * i;
+        if (a >= na) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t b = b0 + tx + 16 * j;
+            if (b >= nb) continue;
+            float v;
+            if (MODE == 0) v = __fsub_rn(bias[b], acc[i][j]);
+            else if (MODE == 1) v = -acc[i][j];
+            else v = __fadd_rn(bias[b], acc[i][j]);
+            out[(uint64_t)a * ld_out + b] = v;
+        }
+    }
+}
+
+__global__ void k_half_norms(const float* __restrict__ X, uint32_t rows, uint32_t d,
+                             float* __restrict__ out) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const float* x = X + (uint64_t)r * d;
+    out[r] = dot_seq(x, x, d) / 2.0f;
+}
+
+// Empty cells get stationary = sqrt(FLT_MAX); min_dist_offset[c] = min over the
+// coarse cluster's cells (puck_index.cpp:284-305).
+__global__ void k_cell_constants(float* __restrict__ stationary, const uint32_t* __restrict__ cell_start,
+                                 float* __restrict__ mdo, uint32_t C, uint32_t F, float empty_value) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    float m = FLT_MAX;
+    for (uint32_t f = 0; f < F; ++f) {
+        const uint64_t cell = (uint64_t)c * F + f;
+        float s = stationary[cell];
+        if (cell_start[cell] == cell_start[cell + 1]) {
+            s = empty_value;
+            stationary[cell] = s;
+        }
+        if (s < m) m = s;
+    }
+    mdo[c] = m;
+}
+
+// Per row: ascending order of L values by (value, index); the first K are
+// written out. Equal to Puck's heap + reorder() whenever no two values among the
+// first K+1 are equal; otherwise one thread replays the heap exactly.
+__global__ void k_topsort(const float* __restrict__ vals, uint32_t L, uint32_t Lp, uint32_t ld,
+                          uint32_t K, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
+                          const int32_t* __restrict__ status) {
+    extern __shared__ unsigned char smem[];
+    float* sv = reinterpret_cast<float*>(smem);
+    uint32_t* si = reinterpret_cast<uint32_t*>(sv + Lp);
+    const uint32_t row = blockIdx.x;
+    const float* v = vals + (uint64_t)row * ld;
+    float* ov = out_val + (uint64_t)row * K;
+    uint32_t* oi = out_idx + (uint64_t)row * K;
+    if (status != nullptr && status[row] != 0) {
+        for (uint32_t i = threadIdx.x; i < K; i += blockDim.x) {
+            ov[i] = sentinel_f();
+            oi[i] = kNoLabel;
+        }
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < Lp; i += blockDim.x) {
+        sv[i] = i < L ? v[i] : __int_as_float(0x7f800000);
+        si[i] = i < L ? i : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= Lp; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = threadIdx.x; t < Lp / 2; t += blockDim.x) {
+                const uint32_t lo = 2 * t - (t & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const float a = sv[lo], b = sv[hi];
+                const uint32_t ia = si[lo], ib = si[hi];
+                const bool gt = (a > b) || (a == b && ia > ib);
+                if (gt == asc) {
+                    sv[lo] = b;
+                    sv[hi] = a;
+                    si[lo] = ib;
+                    si[hi] = ia;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    int tie = 0;
+    const uint32_t last = K < L ? K : L - 1;
+    for (uint32_t i = threadIdx.x; i < last; i += blockDim.x)
+        if (sv[i] == sv[i + 1]) tie = 1;
+    tie = __syncthreads_or(tie);
+    if (!tie) {
+        for (uint32_t i = threadIdx.x; i < K; i += blockDim.x) {
+            ov[i] = sv[i];
+            oi[i] = si[i];
+        }
+        return;
+    }
+    if (threadIdx.x == 0) {
+        // Exact replay of MaxHeap(K) fed in index order, then reorder().
+        float* hv = sv - 1;
+        uint32_t* ht = si - 1;
+        for (uint32_t i = 1; i <= K; ++i) hv[i] = sentinel_f();
+        uint32_t dpc = K;
+        for (uint32_t i = 0; i < L; ++i) heap_update(hv, ht, K, dpc, v[i], i);
+        heap_reorder(hv, ht, K);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < K; i += blockDim.x) {
+        ov[i] = sv[i];
+        oi[i] = si[i];
+    }
+}
+
+// fvec_L2sqr, SSE order (puck/puck/distances_simd.cpp:120-133, 210-236).
+__device__ __forceinline__ float l2sqr_sse(const float* x, const float* y, uint32_t d) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    uint32_t i = 0;
+    for (; i + 4 <= d; i += 4) {
+        float t0 = __fsub_rn(x[i], y[i]), t1 = __fsub_rn(x[i + 1], y[i + 1]);
+        float t2 = __fsub_rn(x[i + 2], y[i + 2]), t3 = __fsub_rn(x[i + 3], y[i + 3]);
+        a0 = __fadd_rn(a0, __fmul_rn(t0, t0));
+        a1 = __fadd_rn(a1, __fmul_rn(t1, t1));
+        a2 = __fadd_rn(a2, __fmul_rn(t2, t2));
+        a3 = __fadd_rn(a3, __fmul_rn(t3, t3));
+    }
+    if (i < d) {
+        float t0 = __fsub_rn(x[i], y[i]);
+        float t1 = (i + 1 < d) ? __fsub_rn(x[i + 1], y[i + 1]) : 0.0f;
+        float t2 = (i + 2 < d) ? __fsub_rn(x[i + 2], y[i + 2]) : 0.0f;
+        a0 = __fadd_rn(a0, __fmul_rn(t0, t0));
+        a1 = __fadd_rn(a1, __fmul_rn(t1, t1));
+        a2 = __fadd_rn(a2, __fmul_rn(t2, t2));
+        a3 = __fadd_rn(a3, 0.0f);
+    }
+    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+}
+
+// lookup_dist_table (puck_index.cpp:75-113): lane m%4 accumulates subspace m in
+// increasing m, then (l0+l1)+(l2+l3). `code` is 4-byte aligned.
+__device__ __forceinline__ float lut_sum(const uint8_t* __restrict__ code, const float* lut,
+                                         uint32_t nsq) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(code);
+    uint32_t m = 0;
+    for (; m + 4 <= nsq; m += 4) {
+        const uint32_t c = __ldg(w + (m >> 2));
+        a0 = __fadd_rn(a0, lut[(m + 0) * 256 + (c & 0xff)]);
+        a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
+        a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
+        a3 = __fadd_rn(a3, lut[(m + 3) * 256 + (c >> 24)]);
+    }
+    if (m < nsq) {
+        const uint32_t c = __ldg(w + (m >> 2));
+        a0 = __fadd_rn(a0, lut[m * 256 + (c & 0xff)]);
+        if (m + 1 < nsq) a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
+        if (m + 2 < nsq) a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
+    }
+    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+}
+
+// First half of compute_quantized_distance's per-point value
+// (float)(2.0 * cell_dist + offset) (puck_index.cpp:360). The reference adds in
+// double and rounds to float; for float operands double rounding of a sum is
+// innocuous (53 >= 2*24 + 2), so one float add of the exact 2*cell_dist gives
+// the same bits whenever 2*cell_dist is finite.
+__device__ __forceinline__ float adc_base(float cell_dist, float offset) {
+    return __fadd_rn(2.0f * cell_dist, offset);
+}
+
+struct WalkParams {
+    const float* q;
+    const float* qnorm;
+    const int32_t* status;
+    const float* cdist;
+    const uint32_t* ctag;
+    const float* fdist;
+    const uint32_t* ftag;
+    float* hdist;
+    uint32_t* htag;
+    uint32_t* hcnt;
+    const float* stationary;
+    const uint32_t* cell_start;
+    const float* mdo;
+    const float* offsets;
+    const uint8_t* codes;
+    const float* codebook;
+    unsigned long long* counters;
+    uint32_t d, C, F, nsq, lsq, code_stride, P, T;
+    double rr;
+};
+
+struct WalkState {
+    float pivot, max_stat, min_dist, cdl;
+    uint32_t c, base, broke, dpc;
+    uint32_t bpos, n_cand, n_used, big, npts;
+    uint32_t warp_tot[4];
+    unsigned long long scanned_pts, scanned_cells;
+};
+
+__device__ __forceinline__ float pivot_of(float top, float qn, double rr) {
+    // (top - query_norm) / radius_rate / 2.0 (puck_index.cpp:517, 544)
+    return __double2float_rn((double)__fsub_rn(top, qn) / rr / 2.0);
+}
+
+// One block per query. Reproduces search_nearest_filter_points exactly: cells
+// of each probed coarse cluster are visited in ascending fine-term order and
+// pruned with the evolving pivot. Per chunk of 128 fine cells, all threads
+// evaluate the pruning tests against the current (larger or equal) pivot and
+// precompute the ADC value of every point of the surviving cells; thread 0
+// then replays the walk in order with the exact pivot, max_stationary_dist and
+// heap, which only prunes further. Breaks and skips are monotone in the pivot,
+// so the replay sees exactly the cells the sequential walk scans.
+__global__ __launch_bounds__(kWalkThreads) void k_walk_scan(WalkParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ WalkState st;
+    const uint32_t qi = blockIdx.x;
+    const int tid = threadIdx.x;
+    const uint32_t nsq = p.nsq, T = p.T, F = p.F;
+    float* lut = reinterpret_cast<float*>(smem);
+    float* hv = lut + nsq * 256;               // 1-based [1..T]
+    uint32_t* ht = reinterpret_cast<uint32_t*>(hv + T + 1);
+    float* qv = reinterpret_cast<float*>(ht + T + 1);
+    uint32_t* c_idx = reinterpret_cast<uint32_t*>(qv + p.d);
+    float* c_dist = reinterpret_cast<float*>(c_idx + kWalkThreads);
+    uint32_t* c_start = reinterpret_cast<uint32_t*>(c_dist + kWalkThreads);
+    uint32_t* c_cnt = c_start + kWalkThreads;
+    float* c_stat = reinterpret_cast<float*>(c_cnt + kWalkThreads);
+    float* c_fd = c_stat + kWalkThreads;
+    uint32_t* c_pref = reinterpret_cast<uint32_t*>(c_fd + kWalkThreads);  // [kWalkThreads + 1]
+    float* pt0 = reinterpret_cast<float*>(c_pref + kWalkThreads + 1);
+    float* ptf = pt0 + kPointBuf;
+
+    if (p.status[qi] != 0) {
+        if (tid == 0) p.hcnt[qi] = 0;
+        return;
+    }
+    const float* fd = p.fdist + (uint64_t)qi * F;
+    const uint32_t* ftag = p.ftag + (uint64_t)qi * F;
+    for (uint32_t i = tid; i < p.d; i += kWalkThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    for (uint32_t i = tid; i <= T; i += kWalkThreads) hv[i] = sentinel_f();
+    __syncthreads();
+    // get_dist_table (quantization.cpp:260-270)
+    for (uint32_t e = tid; e < nsq * 256; e += kWalkThreads) {
+        const uint32_t m = e >> 8, j = e & 255;
+        lut[e] = l2sqr_sse(qv + m * p.lsq, p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
+    }
+    const float qn = p.qnorm[qi];
+    if (tid == 0) {
+        st.dpc = T;
+        st.pivot = pivot_of(sentinel_f(), qn, p.rr);
+        st.scanned_pts = 0;
+        st.scanned_cells = 0;
+    }
+    __syncthreads();
+
+    for (uint32_t l = 0; l < p.P; ++l) {
+        if (tid == 0) {
+            const uint32_t c = p.ctag[(uint64_t)qi * p.P + l];
+            const float cdl = p.cdist[(uint64_t)qi * p.P + l];
+            st.c = c < p.C ? c : 0u;
+            st.cdl = cdl;
+            st.min_dist = c < p.C ? __fadd_rn(p.mdo[c], cdl) : 0.0f;
+            st.max_stat = __fsub_rn(__fsub_rn(st.pivot, cdl), fd[0]);
+            st.base = 0;
+            st.broke = c < p.C ? 0u : 1u;  // never taken for finite queries
+        }
+        __syncthreads();
+        const uint32_t c = st.c;
+        const float cdl = st.cdl;
+        const float* statrow = p.stationary + (uint64_t)c * F;
+        const uint32_t* cs = p.cell_start + (uint64_t)c * F;
+        while (true) {
+            const uint32_t base = st.base;
+            if (st.broke || base >= F) break;
+            const float pv = st.pivot, ms = st.max_stat, md = st.min_dist;
+            __syncthreads();  // everyone has read the state before it changes
+            const uint32_t idx = base + tid;
+            const bool valid = idx < F;
+            const float fdv = valid ? fd[idx] : 0.0f;
+            const bool brk = !valid || (__fadd_rn(fdv, md) >= pv);
+            if (tid == 0) st.bpos = kWalkThreads;
+            __syncthreads();
+            if (brk) atomicMin(&st.bpos, (uint32_t)tid);
+            __syncthreads();
+            const uint32_t bpos = st.bpos;
+            bool cand = false;
+            float stv = 0.0f;
+            uint32_t k = 0, start = 0, cnt = 0;
+            if ((uint32_t)tid < bpos) {
+                k = ftag[idx];
+                if (k >= F) k = 0;  // never taken for finite queries
+                stv = statrow[k];
+                cand = !(stv >= ms);
+                if (cand) {
+                    start = cs[k];
+                    cnt = cs[k + 1] - start;
+                }
+            }
+            uint32_t n_cand, npts_total;
+            const uint32_t pos_incl = block_scan_incl(cand ? 1u : 0u, st.warp_tot, &n_cand);
+            const uint32_t pts_incl = block_scan_incl(cand ? cnt : 0u, st.warp_tot, &npts_total);
+            const uint32_t pos = pos_incl - 1, pts_excl = pts_incl - cnt;
+            if (cand) {
+                c_idx[pos] = idx;
+                c_dist[pos] = __fadd_rn(__fadd_rn(cdl, stv), fdv);
+                c_start[pos] = start;
+                c_cnt[pos] = cnt;
+                c_stat[pos] = stv;
+                c_fd[pos] = fdv;
+                c_pref[pos] = pts_excl;
+            }
+            uint32_t fits_total;
+            block_scan_incl((cand && pts_incl <= (uint32_t)kPointBuf) ? 1u : 0u, st.warp_tot,
+                            &fits_total);
+            if (tid == 0) {
+                uint32_t n_used = fits_total, big = 0;
+                if (n_used == 0 && n_cand > 0) {
+                    n_used = 1;
+                    big = 1;
+                }
+                st.n_cand = n_cand;
+                st.n_used = n_used;
+                st.big = big;
+                c_pref[n_cand] = npts_total;
+            }
+            __syncthreads();
+            const uint32_t n_used = st.n_used;
+            const uint32_t npts = st.big ? 0u : c_pref[n_used];
+            // Speculative ADC for every point of the used candidate cells.
+            for (uint32_t j = tid; j < npts; j += kWalkThreads) {
+                uint32_t lo = 0, hi = n_used;  // largest pos with c_pref[pos] <= j
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (c_pref[mid] <= j) lo = mid;
+                    else hi = mid;
+                }
+                const uint32_t mi = c_start[lo] + (j - c_pref[lo]);
+                const float t0 = adc_base(c_dist[lo], p.offsets[mi]);
+                pt0[j] = t0;
+                ptf[j] = __fadd_rn(t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
+            }
+            __syncthreads();
+            if (tid == 0) {
+                float pivot = st.pivot, max_stat = st.max_stat;
+                uint32_t dpc = st.dpc;
+                bool broke = false;
+                unsigned long long sp = 0, sc = 0;
+                for (uint32_t i = 0; i < n_used; ++i) {
+                    const float fdi = c_fd[i];
+                    if (__fadd_rn(fdi, md) >= pivot) {
+                        broke = true;
+                        break;
+                    }
+                    if (c_stat[i] >= max_stat) continue;
+                    uint32_t upd = 0;
+                    const uint32_t s0 = c_start[i], nc = c_cnt[i];
+                    ++sc;
+                    for (uint32_t pp = 0; pp < nc; ++pp) {
+                        float t0, tf;
+                        if (st.big) {
+                            t0 = adc_base(c_dist[i], p.offsets[s0 + pp]);
+                            if (t0 >= hv[1]) break;
+                            tf = __fadd_rn(t0, lut_sum(p.codes + (uint64_t)(s0 + pp) * p.code_stride,
+                                                       lut, nsq));
+                        } else {
+                            t0 = pt0[c_pref[i] + pp];
+                            if (t0 >= hv[1]) break;
+                            tf = ptf[c_pref[i] + pp];
+                        }
+                        ++sp;
+                        if (heap_update(hv, ht, T, dpc, tf, s0 + pp)) ++upd;
+                    }
+                    if (upd > 0) pivot = pivot_of(hv[1], qn, p.rr);
+                    const float cand_ms = __fsub_rn(__fsub_rn(pivot, cdl), fdi);
+                    if (cand_ms < max_stat) max_stat = cand_ms;
+                }
+                uint32_t next = base + kWalkThreads;
+                if (!broke) {
+                    if (n_used < st.n_cand) next = c_idx[n_used];
+                    else if (bpos < (uint32_t)kWalkThreads) broke = true;
+                }
+                st.pivot = pivot;
+                st.max_stat = max_stat;
+                st.dpc = dpc;
+                st.broke = broke ? 1u : 0u;
+                st.base = next;
+                st.scanned_pts += sp;
+                st.scanned_cells += sc;
+            }
+            __syncthreads();
+        }
+        __syncthreads();  // all threads have left the chunk loop before thread 0 resets the state
+    }
+    if (tid == 0) {
+        const uint32_t cnt = T - st.dpc;
+        if (cnt < T) heap_reorder(hv, ht, T);
+        p.hcnt[qi] = cnt;
+        if (p.counters) {
+            atomicAdd(p.counters + 0, st.scanned_pts);
+            atomicAdd(p.counters + 1, st.scanned_cells);
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < T; i += kWalkThreads) {
+        p.hdist[(uint64_t)qi * T + i] = hv[i + 1];
+        p.htag[(uint64_t)qi * T + i] = ht[i + 1];
+    }
+}
+
+// L2Sqr16Ext + L2SqrExt order of the AVX build
+// (puck/tinker/method/hnsw_distfunc_opt_impl_inline.h:41-122).
+__device__ __forceinline__ float l2_rerank(const float* __restrict__ x, const float* q, uint32_t d) {
+    float t = 0.0f;
+    uint32_t m = 0;
+    for (; m + 16 <= d; m += 16) {
+        float cs = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const float a = __fsub_rn(__ldg(x + m + i), q[m + i]);
+            const float b = __fsub_rn(__ldg(x + m + i + 8), q[m + i + 8]);
+            const float s = __fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b));
+            cs = (i == 0) ? s : __fadd_rn(cs, s);
+        }
+        t = __fadd_rn(t, cs);
+    }
+    if (m < d) {
+        const uint32_t qty = d - m;
+        float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f, l3 = 0.0f;
+        uint32_t i = 0;
+        for (; i + 4 <= qty; i += 4) {
+            const float a0 = __fsub_rn(__ldg(x + m + i), q[m + i]);
+            const float a1 = __fsub_rn(__ldg(x + m + i + 1), q[m + i + 1]);
+            const float a2 = __fsub_rn(__ldg(x + m + i + 2), q[m + i + 2]);
+            const float a3 = __fsub_rn(__ldg(x + m + i + 3), q[m + i + 3]);
+            l0 = __fadd_rn(l0, __fmul_rn(a0, a0));
+            l1 = __fadd_rn(l1, __fmul_rn(a1, a1));
+            l2 = __fadd_rn(l2, __fmul_rn(a2, a2));
+            l3 = __fadd_rn(l3, __fmul_rn(a3, a3));
+        }
+        float s = __fadd_rn(__fadd_rn(__fadd_rn(l0, l1), l2), l3);
+        for (; i < qty; ++i) {
+            const float a = __fsub_rn(__ldg(x + m + i), q[m + i]);
+            s = __fadd_rn(s, __fmul_rn(a, a));
+        }
+        t = __fadd_rn(t, s);
+    }
+    return t;
+}
+
+struct RerankParams {
+    const float* q;
+    const int32_t* status;
+    const float* hdist;
+    const uint32_t* htag;
+    const uint32_t* hcnt;
+    const float* feat;
+    const uint32_t* mem2local;
+    float* out_dist;
+    uint32_t* out_ids;
+    int32_t* out_status;
+    uint32_t d, T, topk;
+};
+
+constexpr int kRerankThreads = 128;
+
+// One block per query: exact distances of the filter survivors in the order the
+// reference walks them (heap layout when the filter heap is full, ascending
+// otherwise), then MaxHeap(topk) + reorder() on one thread.
+__global__ __launch_bounds__(kRerankThreads) void k_rerank(RerankParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* qv = reinterpret_cast<float*>(smem);
+    float* dist = qv + p.d;                         // [T]
+    float* hv = dist + p.T;                         // [topk + 1]
+    uint32_t* ht = reinterpret_cast<uint32_t*>(hv + p.topk + 1);
+    const uint32_t qi = blockIdx.x;
+    const uint32_t topk = p.topk;
+    float* od = p.out_dist + (uint64_t)qi * topk;
+    uint32_t* oi = p.out_ids + (uint64_t)qi * topk;
+    const int32_t stq = p.status[qi];
+    if (p.out_status && threadIdx.x == 0) p.out_status[qi] = stq;
+    if (stq != 0) {
+        for (uint32_t i = threadIdx.x; i < topk; i += kRerankThreads) {
+            od[i] = sentinel_f();
+            oi[i] = kNoLabel;
+        }
+        return;
+    }
+    const uint32_t cnt = p.hcnt[qi];
+    for (uint32_t i = threadIdx.x; i < p.d; i += kRerankThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    __syncthreads();
+    const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
+    for (uint32_t j = threadIdx.x; j < cnt; j += kRerankThreads)
+        dist[j] = l2_rerank(p.feat + (uint64_t)tags[j] * p.d, qv, p.d);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float* h1 = hv - 0;  // hv[0] unused, hv[1..topk]
+        for (uint32_t i = 1; i <= topk; ++i) h1[i] = sentinel_f();
+        uint32_t dpc = topk;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const float v = dist[j];
+            if (v < h1[1]) heap_update(h1, ht, topk, dpc, v, p.mem2local[tags[j]]);
+        }
+        heap_reorder(h1, ht, topk);
+        const uint32_t rn = topk - dpc;
+        for (uint32_t i = 0; i < topk; ++i) {
+            od[i] = h1[i + 1];
+            oi[i] = i < rn ? ht[i + 1] : kNoLabel;
+        }
+    }
+}
+
+// nearest_center (kmeans.cpp:221-258): argmin_c (|x|^2 + |c|^2) - 2 x.c, with the
+// double-precision subtraction of the reference done as one float subtraction
+// (exact 2*dot, innocuous double rounding), first centroid wins ties.
+__global__ __launch_bounds__(256) void k_nearest_center(const float* __restrict__ X, uint64_t n,
+                                                        const float* __restrict__ Cn, uint64_t k,
+                                                        uint32_t d, const float* __restrict__ xnorm,
+                                                        const float* __restrict__ cnorm,
+                                                        int32_t* __restrict__ assign,
+                                                        float* __restrict__ dis) {
+    __shared__ float As[kTileK][kTile + 1];
+    __shared__ float Bs[kTileK][kTile + 1];
+    __shared__ float red_v[16][kTile];
+    __shared__ uint32_t red_i[16][kTile];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const uint64_t a0 = (uint64_t)blockIdx.x * kTile;
+    float best[4];
+    uint32_t bidx[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        best[i] = FLT_MAX;
+        bidx[i] = 0;
+    }
+    for (uint64_t b0 = 0; b0 < k; b0 += kTile) {
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+        for (uint32_t k0 = 0; k0 < d; k0 += kTileK) {
+            for (int e = threadIdx.x; e < kTile * kTileK; e += 256) {
+                const int r = e / kTileK, kk = e % kTileK;
+                const uint32_t kd = k0 + kk;
+                As[kk][r] = (a0 + r < n && kd < d) ? X[(a0 + r) * d + kd] : 0.0f;
+                Bs[kk][r] = (b0 + r < k && kd < d) ? Cn[(b0 + r) * d + kd] : 0.0f;
+            }
+            __syncthreads();
+            const uint32_t kmax = min((uint32_t)kTileK, d - k0);
+            for (uint32_t kk = 0; kk < kmax; ++kk) {
+                float av[4], bv[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(av[i], bv[j]));
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint64_t a = a0 + ty + 16 * i;
+            if (a >= n) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint64_t b = b0 + tx + 16 * j;
+                if (b >= k) continue;
+                const float s = __fadd_rn(xnorm[a], cnorm[b]);
+                const float cur = __fsub_rn(s, 2.0f * acc[i][j]);
+                if (cur < best[i]) {  // j ascends within a thread, tiles ascend: first wins
+                    best[i] = cur;
+                    bidx[i] = (uint32_t)b;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        red_v[tx][ty + 16 * i] = best[i];
+        red_i[tx][ty + 16 * i] = bidx[i];
+    }
+    __syncthreads();
+    if (threadIdx.x < kTile) {
+        const int r = threadIdx.x;
+        // Per-thread results are either a strict improvement on FLT_MAX or
+        // (FLT_MAX, 0) for "none"; merge to the smallest value, lowest id.
+        float bv = FLT_MAX;
+        uint32_t bi = 0;
+        for (int t = 0; t < 16; ++t) {
+            const float v = red_v[t][r];
+            const uint32_t id = red_i[t][r];
+            if (v < bv || (v == bv && v < FLT_MAX && id < bi)) {
+                bv = v;
+                bi = id;
+            }
+        }
+        const uint64_t a = a0 + r;
+        if (a < n) {
+            assign[a] = (int32_t)bi;
+            dis[a] = bv;
+        }
+    }
+}
+
+__global__ void k_norms_full(const float* __restrict__ X, uint64_t rows, uint32_t d,
+                             float* __restrict__ out) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    out[r] = dot_seq(X + r * d, X + r * d, d);
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- launchers
+
+cudaError_t launch_prep_queries(const DeviceIndex& ix, const float* q_in, uint32_t n, Scratch& s,
+                                cudaStream_t stream) {
+    k_prep_queries<<<(n + 127) / 128, 128, 0, stream>>>(q_in, s.q, s.qnorm, s.status, n, ix.d,
+                                                       ix.whether_norm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_centroid_scores(const float* queries, uint32_t nq, const float* cents,
+                                   uint32_t nc, uint32_t d, const float* bias, bool negate,
+                                   float* out, uint32_t ld_out, cudaStream_t stream) {
+    dim3 grid((nc + kTile - 1) / kTile, (nq + kTile - 1) / kTile);
+    if (negate) {
+        k_centroid_scores<1><<<grid, 256, 0, stream>>>(queries, nq, cents, nc, d, bias, out, ld_out);
+    } else {
+        k_centroid_scores<0><<<grid, 256, 0, stream>>>(queries, nq, cents, nc, d, bias, out, ld_out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stationary(const float* coarse, uint32_t C, const float* fine, uint32_t F,
+                              uint32_t d, const float* fine_half_norms, float* stationary,
+                              cudaStream_t stream) {
+    // stationary[c][f] = 0.5|f|^2 + f.c (hierarchical_cluster_index.cpp:302-320)
+    dim3 grid((F + kTile - 1) / kTile, (C + kTile - 1) / kTile);
+    k_centroid_scores<2><<<grid, 256, 0, stream>>>(coarse, C, fine, F, d, fine_half_norms,
+                                                   stationary, F);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_half_norms(const float* X, uint32_t rows, uint32_t d, float* out,
+                              cudaStream_t stream) {
+    k_half_norms<<<(rows + 127) / 128, 128, 0, stream>>>(X, rows, d, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_constants(float* stationary, const uint32_t* cell_start, float* mdo,
+                                  uint32_t C, uint32_t F, float empty_value, cudaStream_t stream) {
+    k_cell_constants<<<(C + 127) / 128, 128, 0, stream>>>(stationary, cell_start, mdo, C, F,
+                                                         empty_value);
+    return cudaGetLastError();
+}
+
+static uint32_t next_pow2(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
+                                  uint32_t K, float* out_val, uint32_t* out_idx,
+                                  const int32_t* status, cudaStream_t stream) {
+    const uint32_t Lp = next_pow2(L < 2 ? 2 : L);
+    const size_t smem = (size_t)Lp * 8;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_topsort, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        attr_set = true;
+    }
+    k_topsort<<<nrows, 512, smem, stream>>>(vals, L, Lp, ld_vals, K, out_val, out_idx, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_topsort(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
+                           uint32_t K, float* out_val, uint32_t* out_idx, cudaStream_t stream) {
+    return launch_topsort_status(vals, nrows, L, ld_vals, K, out_val, out_idx, nullptr, stream);
+}
+
+size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T) {
+    return sizeof(float) * ix.nsq * 256 + (sizeof(float) + sizeof(uint32_t)) * (T + 1) +
+           sizeof(float) * ix.d + sizeof(uint32_t) * (7 * kWalkThreads + 1) +
+           sizeof(float) * 2 * kPointBuf;
+}
+
+cudaError_t launch_walk_scan(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
+                             Scratch& s, cudaStream_t stream) {
+    WalkParams p;
+    p.q = s.q;
+    p.qnorm = s.qnorm;
+    p.status = s.status;
+    p.cdist = s.cdist;
+    p.ctag = s.ctag;
+    p.fdist = s.fdist;
+    p.ftag = s.ftag;
+    p.hdist = s.hdist;
+    p.htag = s.htag;
+    p.hcnt = s.hcnt;
+    p.stationary = ix.stationary;
+    p.cell_start = ix.cell_start;
+    p.mdo = ix.min_dist_offset;
+    p.offsets = ix.offsets;
+    p.codes = ix.codes;
+    p.codebook = ix.codebook;
+    p.counters = s.counters;
+    p.d = ix.d;
+    p.C = ix.C;
+    p.F = ix.F;
+    p.nsq = ix.nsq;
+    p.lsq = ix.lsq;
+    p.code_stride = ix.code_stride;
+    p.P = s.P;
+    p.T = s.T;
+    p.rr = cfg.radius_rate;
+    const size_t smem = walk_smem_bytes(ix, s.T);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_walk_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        attr_set = true;
+    }
+    k_walk_scan<<<n, kWalkThreads, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
+    return sizeof(float) * (ix.d + T) + (sizeof(float) + sizeof(uint32_t)) * (topk + 1);
+}
+
+cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
+                          uint32_t topk, const Scratch& s, float* out_dist, uint32_t* out_ids,
+                          int32_t* out_status, cudaStream_t stream) {
+    (void)cfg;
+    RerankParams p;
+    p.q = s.q;
+    p.status = s.status;
+    p.hdist = s.hdist;
+    p.htag = s.htag;
+    p.hcnt = s.hcnt;
+    p.feat = ix.feat;
+    p.mem2local = ix.mem2local;
+    p.out_dist = out_dist;
+    p.out_ids = out_ids;
+    p.out_status = out_status;
+    p.d = ix.d;
+    p.T = s.T;
+    p.topk = topk;
+    const size_t smem = rerank_smem_bytes(ix, s.T, topk);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        attr_set = true;
+    }
+    k_rerank<<<n, kRerankThreads, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, const float* x,
+                                  uint64_t n, int32_t* assign, float* dis, cudaStream_t stream) {
+    float* xnorm = nullptr;
+    float* cnorm = nullptr;
+    cudaError_t e = cudaMallocAsync(&xnorm, sizeof(float) * (n ? n : 1), stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMallocAsync(&cnorm, sizeof(float) * (k ? k : 1), stream);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(xnorm, stream);
+        return e;
+    }
+    k_norms_full<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(x, n, dim, xnorm);
+    k_norms_full<<<(unsigned)((k + 255) / 256), 256, 0, stream>>>(cents, k, dim, cnorm);
+    k_nearest_center<<<(unsigned)((n + kTile - 1) / kTile), 256, 0, stream>>>(x, n, cents, k, dim,
+                                                                             xnorm, cnorm, assign,
+                                                                             dis);
+    e = cudaGetLastError();
+    cudaFreeAsync(xnorm, stream);
+    cudaFreeAsync(cnorm, stream);
+    return e;
+}
+
+}  // namespace pgpu

@@ -1,0 +1,117 @@
+// Internal types shared by the host loader, the C ABI and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/puck_gb300.h"
+
+namespace pgpu {
+
+// 0x7f7f7f7f: the fill value of Puck's MaxHeap (max_heap.cpp:32).
+constexpr uint32_t kHeapSentinelBits = 0x7f7f7f7fu;
+constexpr uint32_t kNoLabel = 0xFFFFFFFFu;
+
+// Limits of the exact-mode kernels (checked on the host; PGPU_E_LIMIT beyond).
+constexpr uint32_t kMaxClusters = 8192;   // coarse or fine count: sorted in shared memory
+constexpr uint32_t kMaxFilterNsq = 64;    // LUT of nsq*256 floats in shared memory
+constexpr uint32_t kMaxFilterTopk = 4096; // filter heap in shared memory
+constexpr uint32_t kMaxDim = 1024;
+
+// Device-resident index. Point arrays are in Puck's "memory order": sorted by
+// (cell id, filter offset, input id), so every coarse cluster is one
+// contiguous range and points inside a cell ascend by filter offset
+// (puck/puck/puck_index.cpp:248-282).
+struct DeviceIndex {
+    uint32_t d = 0, n = 0, C = 0, F = 0, nsq = 0, lsq = 0;
+    int whether_norm = 0;
+    uint32_t code_stride = 0;     // bytes per code row (nsq rounded up to 4)
+    float* coarse = nullptr;      // [C][d]
+    float* fine = nullptr;        // [F][d]
+    float* coarse_norms = nullptr;// [C]  0.5*|c|^2
+    float* stationary = nullptr;  // [C][F] 0.5*|f|^2 + f.c ; sqrt(FLT_MAX) for empty cells
+    uint32_t* cell_start = nullptr; // [C*F + 1]
+    float* min_dist_offset = nullptr; // [C]
+    uint32_t* mem2local = nullptr;  // [n]
+    float* offsets = nullptr;       // [n] filter offset per point
+    uint8_t* codes = nullptr;       // [n][code_stride]
+    float* feat = nullptr;          // [n][d] original vectors
+    float* codebook = nullptr;      // [nsq][256][lsq]
+    uint64_t bytes = 0;
+};
+
+// Per-pass scratch (sized for max_batch queries).
+struct Scratch {
+    uint32_t cap = 0;
+    float* q = nullptr;        // [B][d] normalised queries
+    float* qnorm = nullptr;    // [B]
+    int32_t* status = nullptr; // [B]
+    float* dots = nullptr;     // [B][max(C,F)]
+    float* cdist = nullptr;    // [B][P]
+    uint32_t* ctag = nullptr;  // [B][P]
+    float* fdist = nullptr;    // [B][F]
+    uint32_t* ftag = nullptr;  // [B][F]
+    float* hdist = nullptr;    // [B][T] filter heap values
+    uint32_t* htag = nullptr;  // [B][T] filter heap memory ids
+    uint32_t* hcnt = nullptr;  // [B]
+    unsigned long long* counters = nullptr; // [4] records scanned, cells scanned
+    uint32_t P = 0, T = 0;
+    uint64_t bytes = 0;
+};
+
+struct SearchConfig {
+    uint32_t P = 200, T = 1100, topk_max = 100;
+    double radius_rate = 1.0;
+    int mode = PGPU_MODE_EXACT;
+};
+
+// Kernel launchers (kernels_search.cu). All enqueue on `stream`.
+cudaError_t launch_prep_queries(const DeviceIndex& ix, const float* q_in, uint32_t n, Scratch& s,
+                                cudaStream_t stream);
+cudaError_t launch_centroid_scores(const float* queries, uint32_t nq, const float* cents,
+                                   uint32_t nc, uint32_t d, const float* bias, bool negate,
+                                   float* out, uint32_t ld_out, cudaStream_t stream);
+cudaError_t launch_topsort(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
+                           uint32_t K, float* out_val, uint32_t* out_idx, cudaStream_t stream);
+cudaError_t launch_walk_scan(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
+                             Scratch& s, cudaStream_t stream);
+cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
+                          uint32_t topk, const Scratch& s, float* out_dist, uint32_t* out_ids,
+                          int32_t* out_status, cudaStream_t stream);
+cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, const float* x,
+                                  uint64_t n, int32_t* assign, float* dis, cudaStream_t stream);
+cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
+                                  uint32_t K, float* out_val, uint32_t* out_idx,
+                                  const int32_t* status, cudaStream_t stream);
+cudaError_t launch_stationary(const float* coarse, uint32_t C, const float* fine, uint32_t F,
+                              uint32_t d, const float* fine_half_norms, float* stationary,
+                              cudaStream_t stream);
+cudaError_t launch_half_norms(const float* X, uint32_t rows, uint32_t d, float* out,
+                              cudaStream_t stream);
+cudaError_t launch_cell_constants(float* stationary, const uint32_t* cell_start, float* mdo,
+                                  uint32_t C, uint32_t F, float empty_value, cudaStream_t stream);
+size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T);
+size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
+
+// Host-side loader (index_host.cpp).
+struct HostIndex {
+    uint32_t d = 0, n = 0, C = 0, F = 0, nsq = 0, lsq = 0;
+    int whether_norm = 0;
+    std::vector<float> coarse, fine, codebook;
+    std::vector<uint32_t> cell_start, mem2local;
+    std::vector<float> offsets_mem;   // memory order
+    std::vector<uint8_t> codes_mem;   // memory order, code_stride bytes per row
+    std::vector<float> feat_mem;      // memory order
+    uint32_t code_stride = 0;
+};
+int read_index_files(const char* dir, pgpu_index_arrays* arrays, std::vector<char>& storage,
+                     std::string* err);
+int build_host_index(const pgpu_index_arrays& a, HostIndex* h, std::string* err);
+// base: original vectors in input order (host); permuted into memory order on the GPU.
+int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* ix,
+                           std::string* err);
+void free_device_index(DeviceIndex* ix);
+
+}  // namespace pgpu

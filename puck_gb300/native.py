@@ -1,0 +1,248 @@
+"""ctypes binding of libpuck_gb300.so (the C ABI in include/puck_gb300.h).
+
+The library is built in-tree by ``puck_gb300.build.build()``. There is no CPU
+fallback: if the shared library is missing or cannot be loaded, every entry
+point raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PGPU_OK = 0
+PGPU_E_INVALID = -1
+PGPU_E_ZERO_NORM = -2
+PGPU_E_IO = -3
+PGPU_E_UNSUPPORTED = -4
+PGPU_E_CUDA = -5
+PGPU_E_NOMEM = -6
+PGPU_E_LIMIT = -7
+PGPU_MODE_EXACT = 0
+
+HEAP_SENTINEL = np.uint32(0x7F7F7F7F).view(np.float32)
+NO_LABEL = 0xFFFFFFFF
+
+EXPORTED_SYMBOLS = (
+    "pgpu_params_default", "pgpu_open", "pgpu_open_arrays", "pgpu_set_search_params",
+    "pgpu_search_batch", "pgpu_search", "pgpu_search_batch_device", "pgpu_index_info_get",
+    "pgpu_last_stats", "pgpu_close", "pgpu_nearest_center", "pgpu_last_error",
+)
+
+
+class PuckGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"puck_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("search_coarse_count", ctypes.c_uint32), ("topk", ctypes.c_uint32),
+                ("filter_topk", ctypes.c_uint32), ("radius_rate", ctypes.c_double),
+                ("device", ctypes.c_int32), ("max_batch", ctypes.c_uint32),
+                ("mode", ctypes.c_int32)]
+
+
+class IndexInfo(ctypes.Structure):
+    _fields_ = [("feature_dim", ctypes.c_uint32), ("total_point_count", ctypes.c_uint32),
+                ("coarse_cluster_count", ctypes.c_uint32), ("fine_cluster_count", ctypes.c_uint32),
+                ("filter_nsq", ctypes.c_uint32), ("lsq", ctypes.c_uint32),
+                ("whether_norm", ctypes.c_int32), ("device_bytes", ctypes.c_uint64)]
+
+
+class IndexArrays(ctypes.Structure):
+    _fields_ = [("feature_dim", ctypes.c_uint32), ("total_point_count", ctypes.c_uint32),
+                ("coarse_cluster_count", ctypes.c_uint32), ("fine_cluster_count", ctypes.c_uint32),
+                ("filter_nsq", ctypes.c_uint32), ("whether_norm", ctypes.c_int32),
+                ("coarse", ctypes.c_void_p), ("fine", ctypes.c_void_p), ("base", ctypes.c_void_p),
+                ("cell_assign", ctypes.c_void_p), ("filter_codebook", ctypes.c_void_p),
+                ("filter_offsets", ctypes.c_void_p), ("filter_codes", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=False):
+    """Load the shared library (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise ImportError(f"{path} is not built; run puck_gb300.build.build() "
+                              "(there is no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    vp, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+    lib.pgpu_params_default.argtypes = [ctypes.POINTER(Params)]
+    lib.pgpu_params_default.restype = None
+    lib.pgpu_open.argtypes = [ctypes.c_char_p, ctypes.POINTER(Params), ctypes.POINTER(vp)]
+    lib.pgpu_open_arrays.argtypes = [ctypes.POINTER(IndexArrays), ctypes.POINTER(Params),
+                                     ctypes.POINTER(vp)]
+    lib.pgpu_set_search_params.argtypes = [vp, ctypes.POINTER(Params)]
+    lib.pgpu_search_batch.argtypes = [vp, u32, vp, u32, vp, vp, vp]
+    lib.pgpu_search.argtypes = [vp, vp, u32, vp, vp, ctypes.POINTER(u32)]
+    lib.pgpu_search_batch_device.argtypes = [vp, u32, vp, u32, vp, vp, vp, vp]
+    lib.pgpu_index_info_get.argtypes = [vp, ctypes.POINTER(IndexInfo)]
+    lib.pgpu_last_stats.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64),
+                                    ctypes.POINTER(u64)]
+    lib.pgpu_close.argtypes = [vp]
+    lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
+    lib.pgpu_last_error.restype = ctypes.c_char_p
+    lib.pgpu_last_error.argtypes = []
+    for name in EXPORTED_SYMBOLS:
+        getattr(lib, name)
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != PGPU_OK:
+        raise PuckGpuError(rc, load().pgpu_last_error().decode(errors="replace"))
+    return rc
+
+
+def default_params(**overrides):
+    p = Params()
+    load().pgpu_params_default(ctypes.byref(p))
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(x):
+    """Data pointer of a numpy array, a torch tensor, or an int."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError(f"cannot take a data pointer of {type(x)}")
+
+
+class GpuIndex:
+    """A Puck-Flat index resident on one GPU."""
+
+    def __init__(self, index_path=None, arrays=None, **params):
+        lib = load()
+        self._h = ctypes.c_void_p()
+        p = default_params(**params)
+        self._keep = None
+        if index_path is not None:
+            check(lib.pgpu_open(os.fsencode(index_path), ctypes.byref(p), ctypes.byref(self._h)))
+        elif arrays is not None:
+            a, keep = _arrays_struct(arrays)
+            self._keep = keep
+            check(lib.pgpu_open_arrays(ctypes.byref(a), ctypes.byref(p), ctypes.byref(self._h)))
+            self._keep = None
+        else:
+            raise ValueError("index_path or arrays is required")
+        self.params = p
+        info = IndexInfo()
+        check(lib.pgpu_index_info_get(self._h, ctypes.byref(info)))
+        self.info = info
+        self.d = info.feature_dim
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().pgpu_close(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_search_params(self, **params):
+        p = Params.from_buffer_copy(self.params)
+        for k, v in params.items():
+            setattr(p, k, v)
+        check(load().pgpu_set_search_params(self._h, ctypes.byref(p)))
+        self.params = p
+
+    def search(self, queries, topk, return_status=False):
+        """Host-buffer batch search (PySearcher::search semantics)."""
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self.d)
+        n = q.shape[0]
+        dist = np.empty((n, topk), np.float32)
+        ids = np.empty((n, topk), np.uint32)
+        status = np.empty(n, np.int32)
+        check(load().pgpu_search_batch(self._h, n, q.ctypes.data, topk, dist.ctypes.data,
+                                       ids.ctypes.data, status.ctypes.data))
+        return (dist, ids, status) if return_status else (dist, ids)
+
+    def search_into(self, n, query_ptr, topk, dist_ptr, ids_ptr, status_ptr=None):
+        return check(load().pgpu_search_batch(self._h, n, _ptr(query_ptr), topk, _ptr(dist_ptr),
+                                              _ptr(ids_ptr), _ptr(status_ptr)))
+
+    def search_device(self, n, query, topk, dist, ids, status=None, stream=None):
+        """Device-buffer batch search; enqueued on `stream` (int handle or torch stream)."""
+        s = stream
+        if s is not None and not isinstance(s, int):
+            s = s.cuda_stream
+        return check(load().pgpu_search_batch_device(self._h, n, _ptr(query), topk, _ptr(dist),
+                                                     _ptr(ids), _ptr(status), s))
+
+    def search_one(self, feature, topk):
+        """Index::search semantics: one query -> (distance, local_idx, result_num)."""
+        q = np.ascontiguousarray(feature, np.float32)
+        dist = np.empty(topk, np.float32)
+        ids = np.empty(topk, np.uint32)
+        rn = ctypes.c_uint32(0)
+        check(load().pgpu_search(self._h, q.ctypes.data, topk, dist.ctypes.data, ids.ctypes.data,
+                                 ctypes.byref(rn)))
+        return dist, ids, rn.value
+
+    def last_stats(self):
+        k, r, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(load().pgpu_last_stats(self._h, ctypes.byref(k), ctypes.byref(r), ctypes.byref(c)))
+        return dict(kernels=k.value, records_scanned=r.value, cells_scanned=c.value)
+
+
+def _arrays_struct(arr):
+    keep = {}
+
+    def c(name, dtype):
+        a = np.ascontiguousarray(arr[name], dtype=dtype)
+        keep[name] = a
+        return a.ctypes.data
+
+    coarse = np.asarray(arr["coarse"])
+    codes = np.asarray(arr["filter_codes"])
+    s = IndexArrays()
+    s.feature_dim = coarse.shape[1]
+    s.total_point_count = np.asarray(arr["base"]).shape[0]
+    s.coarse_cluster_count = coarse.shape[0]
+    s.fine_cluster_count = np.asarray(arr["fine"]).shape[0]
+    s.filter_nsq = codes.shape[1]
+    s.whether_norm = int(bool(arr.get("whether_norm", False)))
+    s.coarse = c("coarse", np.float32)
+    s.fine = c("fine", np.float32)
+    s.base = c("base", np.float32)
+    s.cell_assign = c("cell_assign", np.uint32)
+    s.filter_codebook = c("filter_codebook", np.float32)
+    s.filter_offsets = c("filter_offsets", np.float32)
+    s.filter_codes = c("filter_codes", np.uint8)
+    return s, keep
+
+
+def nearest_center(centroids, points, assign, distance, stream=None):
+    """k-means assignment on device tensors (torch CUDA tensors or raw pointers)."""
+    k, dim = centroids.shape
+    n = points.shape[0]
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    return check(load().pgpu_nearest_center(dim, _ptr(centroids), k, _ptr(points), n,
+                                            _ptr(assign), _ptr(distance), s))

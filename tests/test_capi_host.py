@@ -1,0 +1,98 @@
+"""Host-side checks of the C ABI library (no GPU compute).
+
+The shared library must build for sm_103a, load, and export every entry point
+include/puck_gb300.h declares. Calls that fail before touching a GPU (null
+arguments, bad parameters, no device) must return their documented codes.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from puck_gb300 import build, index_io, native, py_puck_api
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    src = open(os.path.join(REPO, "include", "puck_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(pgpu_[a-z_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    declared = _declared_symbols()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(declared) == set(native.EXPORTED_SYMBOLS)
+
+
+def test_params_default_matches_reference_flags(lib):
+    p = native.default_params()
+    # puck/gflags/puck_gflags.cpp:70-78 and index_conf.cpp:178-180
+    assert p.search_coarse_count == 200
+    assert p.topk == 100
+    assert p.filter_topk == 1100
+    assert p.radius_rate == 1.0
+    assert p.mode == native.PGPU_MODE_EXACT
+
+
+def test_null_arguments_rejected(lib):
+    h = ctypes.c_void_p()
+    assert lib.pgpu_open(None, None, ctypes.byref(h)) == native.PGPU_E_INVALID
+    assert lib.pgpu_search_batch(None, 1, None, 10, None, None, None) == native.PGPU_E_INVALID
+    assert lib.pgpu_close(None) == 0
+    assert b"null" in lib.pgpu_last_error()
+
+
+def test_bad_search_params_rejected_before_device(lib, tmp_path):
+    h = ctypes.c_void_p()
+    p = native.default_params(radius_rate=0.5)
+    assert lib.pgpu_open(str(tmp_path).encode(), ctypes.byref(p), ctypes.byref(h)) in (
+        native.PGPU_E_IO, native.PGPU_E_INVALID)
+    p = native.default_params(filter_topk=50, topk=100)
+    assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_INVALID
+    p = native.default_params(filter_topk=100000)
+    assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_LIMIT
+
+
+def test_missing_index_files(lib, tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("covered on the GPU")
+    h = ctypes.c_void_p()
+    rc = lib.pgpu_open(str(tmp_path).encode(), None, ctypes.byref(h))
+    assert rc == native.PGPU_E_IO
+
+
+def test_index_io_roundtrip(tmp_path, golden):
+    name, z, index_dir = golden
+    ix = index_io.read_index(index_dir)
+    out = str(tmp_path / "copy")
+    index_io.write_index(out, base=ix["base"], coarse=ix["coarse"], fine=ix["fine"],
+                         cell_assign=ix["cell_assign"], filter_codebook=ix["filter_codebook"],
+                         filter_offsets=ix["filter_offsets"], filter_codes=ix["filter_codes"],
+                         whether_norm=ix["conf"]["whether_norm"])
+    for fn in os.listdir(index_dir):
+        assert open(os.path.join(index_dir, fn), "rb").read() == \
+            open(os.path.join(out, fn), "rb").read(), fn
+
+
+def test_gflag_mirror_defaults():
+    py_puck_api.reset_gflags()
+    p = py_puck_api.current_params()
+    assert p["filter_topk"] == 1100 and p["search_coarse_count"] == 200
+    py_puck_api.update_gflag("topk", "10")
+    assert py_puck_api.current_params()["filter_topk"] == 110
+    py_puck_api.update_gflag("filter_topk", "500")
+    assert py_puck_api.current_params()["filter_topk"] == 500
+    assert py_puck_api.update_gflag("no_such_flag", "1") == ""
+    py_puck_api.reset_gflags()
