@@ -124,6 +124,15 @@ int pgpu_index_info_get(const pgpu_index* index, pgpu_index_info* info);
 int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
                     uint64_t* records_scanned, uint64_t* cells_scanned);
 
+/* Per-stage device timing (CUDA events recorded on the launching stream around
+ * each kernel). With profiling enabled, pgpu_stage_times returns, for the last
+ * search call, the milliseconds spent in each stage, summed over its passes:
+ * 0 query prep, 1 coarse scores, 2 coarse select, 3 fine scores, 4 fine order,
+ * 5 cell walk + ADC scan, 6 rerank. It waits for the call's work to finish. */
+#define PGPU_NUM_STAGES 7
+int pgpu_set_profiling(pgpu_index* index, int enable);
+int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
+
 int pgpu_close(pgpu_index* index);
 
 /* k-means assignment step used by train (kmeans.cpp:221-258 nearest_center):

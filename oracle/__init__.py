@@ -67,6 +67,9 @@ def _load():
         lib.po_load.restype = ctypes.c_void_p
         lib.po_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         lib.po_free.argtypes = [ctypes.c_void_p]
+        lib.po_load_arrays.restype = ctypes.c_void_p
+        lib.po_load_arrays.argtypes = [ctypes.c_uint32] * 5 + [ctypes.c_int] + [ctypes.c_void_p] * 7 + [
+            ctypes.POINTER(ctypes.c_int)]
         lib.po_info.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_uint32)] * 6 + [
             ctypes.POINTER(ctypes.c_int)]
         lib.po_memory_to_local.restype = ctypes.c_void_p
@@ -98,12 +101,25 @@ def _ptr(a):
 class OracleIndex:
     """The C restatement loaded on one Puck-Flat index directory."""
 
-    def __init__(self, index_dir):
+    def __init__(self, index_dir=None, arrays=None):
         lib = _load()
         err = ctypes.c_int(0)
-        self._h = lib.po_load(index_dir.encode(), ctypes.byref(err))
+        if index_dir is not None:
+            self._h = lib.po_load(index_dir.encode(), ctypes.byref(err))
+        else:
+            a = {k: np.ascontiguousarray(arrays[k], t) for k, t in (
+                ("coarse", np.float32), ("fine", np.float32), ("base", np.float32),
+                ("cell_assign", np.uint32), ("filter_codebook", np.float32),
+                ("filter_offsets", np.float32), ("filter_codes", np.uint8))}
+            n, d = a["base"].shape
+            self._h = lib.po_load_arrays(
+                d, n, a["coarse"].shape[0], a["fine"].shape[0], a["filter_codes"].shape[1],
+                int(bool(arrays.get("whether_norm", False))), a["coarse"].ctypes.data,
+                a["fine"].ctypes.data, a["base"].ctypes.data, a["cell_assign"].ctypes.data,
+                a["filter_codebook"].ctypes.data, a["filter_offsets"].ctypes.data,
+                a["filter_codes"].ctypes.data, ctypes.byref(err))
         if not self._h:
-            raise RuntimeError(f"oracle could not load {index_dir} (error {err.value})")
+            raise RuntimeError(f"oracle could not load the index (error {err.value})")
         vals = [ctypes.c_uint32() for _ in range(6)]
         wn = ctypes.c_int()
         lib.po_info(self._h, *[ctypes.byref(v) for v in vals], ctypes.byref(wn))

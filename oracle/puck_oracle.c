@@ -194,52 +194,26 @@ void po_free(po_index* ix) {
     free(ix);
 }
 
-po_index* po_load(const char* dir, int* err) {
+po_index* po_load_arrays(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_t nsq,
+                         int whether_norm, const float* coarse, const float* fine,
+                         const float* base, const uint32_t* cell_assign, const float* codebook,
+                         const float* offsets_local, const uint8_t* codes_local, int* err) {
     int e = 0;
-    po_index* ix = (po_index*)calloc(1, sizeof(po_index));
-    void* raw = NULL;
-    size_t len = 0;
-    uint32_t* cell_assign = NULL;
     mem_order* order = NULL;
-    uint8_t* rec = NULL;
-    float* feat_local = NULL;
-
-    /* index.dat: size_t length + packed config (hierarchical_cluster_index.cpp:551-567) */
-    if (read_file(dir, "index.dat", &raw, &len) != 0 || len < 8 + 43) { e = -1; goto fail; }
-    {
-        const uint8_t* p = (const uint8_t*)raw + 8;
-        int32_t itype;
-        uint32_t u;
-        memcpy(&itype, p, 4); p += 4;
-        if (itype != 1) { e = -2; goto fail; } /* PUCK */
-        memcpy(&ix->d, p, 4); p += 4;
-        ix->whether_norm = *p; p += 1;
-        memcpy(&ix->n, p, 4); p += 4;
-        uint8_t whether_filter = *p; p += 1;
-        memcpy(&ix->nsq, p, 4); p += 4;
-        memcpy(&u, p, 4); p += 4; /* ks */
-        if (u != 256 || !whether_filter) { e = -3; goto fail; }
-        uint8_t whether_pq = *p; p += 1;
-        if (whether_pq) { e = -4; goto fail; } /* Puck-Flat only */
-        p += 4; /* nsq */
-        p += 4; /* ks */
-        memcpy(&u, p, 4); p += 4;
-        ix->ip2cos = (int)u;
-        if (ix->ip2cos != 0) { e = -5; goto fail; }
-        memcpy(&ix->C, p, 4); p += 4;
-        memcpy(&ix->F, p, 4); p += 4;
-    }
-    free(raw);
-    raw = NULL;
-    if (ix->nsq == 0 || ix->nsq > ix->d) { e = -6; goto fail; }
-    ix->lsq = (ix->d + ix->nsq - 1) / ix->nsq;
-    if (ix->lsq * ix->nsq != ix->d) { e = -7; goto fail; } /* reference reads past d otherwise */
-
-    const uint32_t d = ix->d, n = ix->n, C = ix->C, F = ix->F, nsq = ix->nsq;
+    po_index* ix = (po_index*)calloc(1, sizeof(po_index));
+    ix->d = d;
+    ix->n = n;
+    ix->C = C;
+    ix->F = F;
+    ix->nsq = nsq;
+    ix->whether_norm = whether_norm;
+    if (nsq == 0 || nsq > d || d % nsq != 0 || C == 0 || F == 0) { e = -7; goto fail; }
+    ix->lsq = d / nsq;
     const uint64_t cells = (uint64_t)C * F;
-    ix->coarse = read_fvecs(dir, "coarse.dat", d, C);
-    ix->fine = read_fvecs(dir, "fine.dat", d, F);
-    if (!ix->coarse || !ix->fine) { e = -8; goto fail; }
+    ix->coarse = (float*)malloc(sizeof(float) * (uint64_t)C * d);
+    ix->fine = (float*)malloc(sizeof(float) * (uint64_t)F * d);
+    memcpy(ix->coarse, coarse, sizeof(float) * (uint64_t)C * d);
+    memcpy(ix->fine, fine, sizeof(float) * (uint64_t)F * d);
 
     /* read_coodbooks: coarse norms, fine norms, F x C products (sgemm "TN"). */
     ix->coarse_norms = (float*)malloc(sizeof(float) * C);
@@ -257,18 +231,11 @@ po_index* po_load(const char* dir, int* err) {
     free(fine_norms);
 
     /* convert_local_to_memory_idx */
-    if (read_file(dir, "cell_assign.dat", &raw, &len) != 0 || len != 4ull * n) { e = -9; goto fail; }
-    cell_assign = (uint32_t*)raw;
-    raw = NULL;
-    const uint32_t rb = 4 + nsq;
-    if (read_file(dir, "filter_data.dat", &raw, &len) != 0 || len != (uint64_t)rb * n) { e = -10; goto fail; }
-    rec = (uint8_t*)raw;
-    raw = NULL;
     order = (mem_order*)malloc(sizeof(mem_order) * (n ? n : 1));
     for (uint32_t i = 0; i < n; ++i) {
         if (cell_assign[i] >= cells) { e = -11; goto fail; }
         order[i].cell = cell_assign[i];
-        memcpy(&order[i].offset, rec + (uint64_t)i * rb, 4);
+        order[i].offset = offsets_local[i];
         order[i].local = i;
     }
     qsort(order, n, sizeof(mem_order), cmp_mem_order);
@@ -300,34 +267,99 @@ po_index* po_load(const char* dir, int* err) {
     /* read_feature_index: filter records and original vectors in memory order. */
     ix->offsets = (float*)malloc(sizeof(float) * (n ? n : 1));
     ix->codes = (uint8_t*)malloc((uint64_t)nsq * (n ? n : 1));
-    for (uint32_t i = 0; i < n; ++i) {
-        const uint8_t* r = rec + (uint64_t)ix->mem2local[i] * rb;
-        memcpy(&ix->offsets[i], r, 4);
-        memcpy(ix->codes + (uint64_t)i * nsq, r + 4, nsq);
-    }
-    feat_local = read_fvecs(dir, "all_data.feat.bin", d, n);
-    if (!feat_local) { e = -13; goto fail; }
     ix->feat = (float*)malloc(sizeof(float) * (uint64_t)d * (n ? n : 1));
-    for (uint32_t i = 0; i < n; ++i)
-        memcpy(ix->feat + (uint64_t)i * d, feat_local + (uint64_t)ix->mem2local[i] * d, 4ull * d);
-    ix->codebook = read_fvecs(dir, "filter_codebook.dat", ix->lsq, (uint64_t)nsq * 256);
-    if (!ix->codebook) { e = -14; goto fail; }
-
-    free(cell_assign);
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t l = ix->mem2local[i];
+        ix->offsets[i] = offsets_local[l];
+        memcpy(ix->codes + (uint64_t)i * nsq, codes_local + (uint64_t)l * nsq, nsq);
+        memcpy(ix->feat + (uint64_t)i * d, base + (uint64_t)l * d, 4ull * d);
+    }
+    ix->codebook = (float*)malloc(sizeof(float) * (uint64_t)nsq * 256 * ix->lsq);
+    memcpy(ix->codebook, codebook, sizeof(float) * (uint64_t)nsq * 256 * ix->lsq);
     free(order);
-    free(rec);
-    free(feat_local);
     if (err) *err = 0;
     return ix;
 fail:
-    free(raw);
-    free(cell_assign);
     free(order);
-    free(rec);
-    free(feat_local);
     po_free(ix);
     if (err) *err = e;
     return NULL;
+}
+
+po_index* po_load(const char* dir, int* err) {
+    int e = 0;
+    void* raw = NULL;
+    size_t len = 0;
+    uint32_t* cell_assign = NULL;
+    uint8_t* rec = NULL;
+    float *coarse = NULL, *fine = NULL, *feat = NULL, *codebook = NULL, *offsets = NULL;
+    uint8_t* codes = NULL;
+    po_index* ix = NULL;
+    uint32_t d, n, C, F, nsq;
+    int whether_norm;
+
+    /* index.dat: size_t length + packed config (hierarchical_cluster_index.cpp:551-567) */
+    if (read_file(dir, "index.dat", &raw, &len) != 0 || len < 8 + 43) { e = -1; goto done; }
+    {
+        const uint8_t* p = (const uint8_t*)raw + 8;
+        int32_t itype;
+        uint32_t u;
+        memcpy(&itype, p, 4); p += 4;
+        if (itype != 1) { e = -2; goto done; } /* PUCK */
+        memcpy(&d, p, 4); p += 4;
+        whether_norm = *p; p += 1;
+        memcpy(&n, p, 4); p += 4;
+        uint8_t whether_filter = *p; p += 1;
+        memcpy(&nsq, p, 4); p += 4;
+        memcpy(&u, p, 4); p += 4; /* ks */
+        if (u != 256 || !whether_filter) { e = -3; goto done; }
+        uint8_t whether_pq = *p; p += 1;
+        if (whether_pq) { e = -4; goto done; } /* Puck-Flat only */
+        p += 4; /* nsq */
+        p += 4; /* ks */
+        memcpy(&u, p, 4); p += 4;
+        if (u != 0) { e = -5; goto done; } /* ip2cos */
+        memcpy(&C, p, 4); p += 4;
+        memcpy(&F, p, 4); p += 4;
+    }
+    free(raw);
+    raw = NULL;
+    if (nsq == 0 || nsq > d || d % nsq != 0) { e = -7; goto done; } /* reference reads past d otherwise */
+    {
+        const uint32_t lsq = d / nsq;
+        coarse = read_fvecs(dir, "coarse.dat", d, C);
+        fine = read_fvecs(dir, "fine.dat", d, F);
+        feat = read_fvecs(dir, "all_data.feat.bin", d, n);
+        codebook = read_fvecs(dir, "filter_codebook.dat", lsq, (uint64_t)nsq * 256);
+        if (!coarse || !fine || !feat || !codebook) { e = -8; goto done; }
+        if (read_file(dir, "cell_assign.dat", &raw, &len) != 0 || len != 4ull * n) { e = -9; goto done; }
+        cell_assign = (uint32_t*)raw;
+        raw = NULL;
+        const uint32_t rb = 4 + nsq;
+        if (read_file(dir, "filter_data.dat", &raw, &len) != 0 || len != (uint64_t)rb * n) { e = -10; goto done; }
+        rec = (uint8_t*)raw;
+        raw = NULL;
+        offsets = (float*)malloc(sizeof(float) * (n ? n : 1));
+        codes = (uint8_t*)malloc((uint64_t)nsq * (n ? n : 1));
+        for (uint32_t i = 0; i < n; ++i) {
+            memcpy(&offsets[i], rec + (uint64_t)i * rb, 4);
+            memcpy(codes + (uint64_t)i * nsq, rec + (uint64_t)i * rb + 4, nsq);
+        }
+        ix = po_load_arrays(d, n, C, F, nsq, whether_norm, coarse, fine, feat, cell_assign, codebook,
+                            offsets, codes, &e);
+    }
+done:
+    free(raw);
+    free(cell_assign);
+    free(rec);
+    free(coarse);
+    free(fine);
+    free(feat);
+    free(codebook);
+    free(offsets);
+    free(codes);
+    if (err) *err = e;
+    return ix;
 }
 
 int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,

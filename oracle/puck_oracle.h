@@ -39,6 +39,11 @@ typedef struct {
 } po_trace;
 
 po_index* po_load(const char* index_dir, int* err);
+/* Same index from in-memory arrays in input order (the contents of the files). */
+po_index* po_load_arrays(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_t nsq,
+                         int whether_norm, const float* coarse, const float* fine,
+                         const float* base, const uint32_t* cell_assign, const float* codebook,
+                         const float* offsets_local, const uint8_t* codes_local, int* err);
 void po_free(po_index* ix);
 int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,
             uint32_t* filter_nsq, uint32_t* lsq, int* whether_norm);

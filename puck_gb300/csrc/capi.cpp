@@ -24,6 +24,11 @@ struct pgpu_index {
     int32_t* d_status = nullptr;
     uint32_t stage_topk = 0;
     uint64_t kernels = 0, records = 0, cells = 0;
+    // optional per-stage timing with CUDA events on the launching stream
+    bool profiling = false;
+    cudaEvent_t ev[PGPU_NUM_STAGES + 1] = {};
+    float stage_ms[PGPU_NUM_STAGES] = {};
+    bool stage_pending = false;
 };
 
 namespace {
@@ -146,33 +151,58 @@ int ensure_staging(pgpu_index* h, uint32_t topk) {
     return PGPU_OK;
 }
 
+// Accumulates the previous call's stage times once its events have completed.
+void collect_stage_times(pgpu_index* h) {
+    if (!h->stage_pending) return;
+    cudaEventSynchronize(h->ev[PGPU_NUM_STAGES]);
+    for (int i = 0; i < PGPU_NUM_STAGES; ++i) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]) == cudaSuccess) h->stage_ms[i] += ms;
+    }
+    h->stage_pending = false;
+}
+
 // One pass of <= max_batch queries, all buffers on the device.
 int run_pass(pgpu_index* h, uint32_t n, const float* d_q, uint32_t topk, float* d_dist,
              uint32_t* d_ids, int32_t* d_status, cudaStream_t st) {
     auto& ix = h->ix;
     auto& s = h->s;
     cudaError_t e;
+    const bool prof = h->profiling;
+    if (prof) collect_stage_times(h);
+    auto mark = [&](int i) {
+        if (prof) cudaEventRecord(h->ev[i], st);
+    };
     if ((e = cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 4, st)) != cudaSuccess)
         return cuda_fail(e, "memset");
+    mark(0);
     if ((e = pgpu::launch_prep_queries(ix, d_q, n, s, st)) != cudaSuccess)
         return cuda_fail(e, "prep_queries");
+    mark(1);
     if ((e = pgpu::launch_centroid_scores(s.q, n, ix.coarse, ix.C, ix.d, ix.coarse_norms, false,
                                           s.dots, ix.C, st)) != cudaSuccess)
         return cuda_fail(e, "coarse scores");
+    mark(2);
     if ((e = pgpu::launch_topsort_status(s.dots, n, ix.C, ix.C, s.P, s.cdist, s.ctag, s.status,
                                          st)) != cudaSuccess)
         return cuda_fail(e, "coarse select");
+    mark(3);
     if ((e = pgpu::launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F,
                                           st)) != cudaSuccess)
         return cuda_fail(e, "fine scores");
+    mark(4);
     if ((e = pgpu::launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status,
                                          st)) != cudaSuccess)
         return cuda_fail(e, "fine order");
+    mark(5);
     if ((e = pgpu::launch_walk_scan(ix, h->cfg, n, s, st)) != cudaSuccess)
         return cuda_fail(e, "walk_scan");
+    mark(6);
     if ((e = pgpu::launch_rerank(ix, h->cfg, n, topk, s, d_dist, d_ids, d_status, st)) !=
         cudaSuccess)
         return cuda_fail(e, "rerank");
+    mark(7);
+    if (prof) h->stage_pending = true;
     h->kernels += 7;
     return PGPU_OK;
 }
@@ -275,7 +305,9 @@ int pgpu_search_batch_device(pgpu_index* h, uint32_t n, const float* query, uint
     std::lock_guard<std::mutex> g(h->mu);
     cudaSetDevice(h->device);
     cudaStream_t st = (cudaStream_t)stream;
+    collect_stage_times(h);
     h->kernels = 0;
+    for (float& v : h->stage_ms) v = 0.0f;
     const uint32_t d = h->ix.d;
     for (uint32_t off = 0; off < n; off += h->max_batch) {
         const uint32_t m = std::min(h->max_batch, n - off);
@@ -302,7 +334,9 @@ int pgpu_search_batch(pgpu_index* h, uint32_t n, const float* query, uint32_t to
     if (int rc = ensure_staging(h, topk)) return rc;
     const uint32_t d = h->ix.d;
     cudaStream_t st = h->stream;
+    collect_stage_times(h);
     h->kernels = 0;
+    for (float& v : h->stage_ms) v = 0.0f;
     h->records = 0;
     h->cells = 0;
     cudaError_t e;
@@ -382,7 +416,35 @@ int pgpu_close(pgpu_index* h) {
     free_staging(h);
     free_scratch(&h->s);
     pgpu::free_device_index(&h->ix);
+    if (h->ev[0])
+        for (auto& e : h->ev) cudaEventDestroy(e);
     delete h;
+    return PGPU_OK;
+}
+
+int pgpu_set_profiling(pgpu_index* h, int enable) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    std::lock_guard<std::mutex> g(h->mu);
+    cudaSetDevice(h->device);
+    if (enable && h->ev[0] == nullptr) {
+        for (auto& e : h->ev) {
+            cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) return cuda_fail(r, "event create");
+        }
+    }
+    h->profiling = enable != 0;
+    h->stage_pending = false;
+    for (float& v : h->stage_ms) v = 0.0f;
+    return PGPU_OK;
+}
+
+int pgpu_stage_times(pgpu_index* h, float* ms, uint32_t n_stages) {
+    if (h == nullptr || ms == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> g(h->mu);
+    if (!h->profiling) return fail(PGPU_E_INVALID, "profiling is not enabled");
+    cudaSetDevice(h->device);
+    collect_stage_times(h);
+    for (uint32_t i = 0; i < n_stages && i < (uint32_t)PGPU_NUM_STAGES; ++i) ms[i] = h->stage_ms[i];
     return PGPU_OK;
 }
 

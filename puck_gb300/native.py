@@ -28,7 +28,10 @@ EXPORTED_SYMBOLS = (
     "pgpu_params_default", "pgpu_open", "pgpu_open_arrays", "pgpu_set_search_params",
     "pgpu_search_batch", "pgpu_search", "pgpu_search_batch_device", "pgpu_index_info_get",
     "pgpu_last_stats", "pgpu_close", "pgpu_nearest_center", "pgpu_last_error",
+    "pgpu_set_profiling", "pgpu_stage_times",
 )
+STAGES = ("prep", "coarse_scores", "coarse_select", "fine_scores", "fine_order", "walk_scan",
+          "rerank")
 
 
 class PuckGpuError(RuntimeError):
@@ -95,6 +98,8 @@ def load(build_if_missing=False):
                                     ctypes.POINTER(u64)]
     lib.pgpu_close.argtypes = [vp]
     lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
+    lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
+    lib.pgpu_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), u32]
     lib.pgpu_last_error.restype = ctypes.c_char_p
     lib.pgpu_last_error.argtypes = []
     for name in EXPORTED_SYMBOLS:
@@ -203,6 +208,15 @@ class GpuIndex:
         check(load().pgpu_search(self._h, q.ctypes.data, topk, dist.ctypes.data, ids.ctypes.data,
                                  ctypes.byref(rn)))
         return dist, ids, rn.value
+
+    def set_profiling(self, enable=True):
+        check(load().pgpu_set_profiling(self._h, int(bool(enable))))
+
+    def stage_times(self):
+        """Milliseconds per stage of the last search call (profiling must be on)."""
+        arr = (ctypes.c_float * len(STAGES))()
+        check(load().pgpu_stage_times(self._h, arr, len(STAGES)))
+        return dict(zip(STAGES, list(arr)))
 
     def last_stats(self):
         k, r, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
