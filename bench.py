@@ -221,7 +221,8 @@ def run_gpu(args, w, rank, ws):
     t0 = time.time()
     ix = native.GpuIndex(arrays=arrays, search_coarse_count=w["sweep"][0], filter_topk=w["T"],
                          topk=100, max_batch=nq, device=dev.index)
-    log(f"[bench] index resident ({ix.info.device_bytes / 1e9:.2f} GB) in {time.time() - t0:.1f}s")
+    ix_bytes = ix.info.device_bytes
+    log(f"[bench] index resident ({ix_bytes / 1e9:.2f} GB) in {time.time() - t0:.1f}s")
     q_dev = queries.contiguous()
     d_dev = torch.empty((nq, k), dtype=torch.float32, device=dev)
     i_dev = torch.empty((nq, k), dtype=torch.int32, device=dev)
@@ -302,6 +303,7 @@ def run_gpu(args, w, rank, ws):
     q_np = queries.cpu().numpy()
     ix.search(q_np, k)
     stats = ix.last_stats()
+    walk_counters = ix.walk_counters()
     recs, cells = stats["records_scanned"], stats["cells_scanned"]
     R = 4 + w["nsq"]
     walk_bytes = recs * R + cells * 12 + nq * w["F"] * 8
@@ -366,10 +368,11 @@ def run_gpu(args, w, rank, ws):
             "p50_ms": round(float(np.percentile(step_ms, 50)), 4),
             "p99_ms": round(float(np.percentile(step_ms, 99)), 4),
             "batch": nq,
-            "l2": "index (codes 280 MB + vectors 3.8 GB) larger than L2; no flush",
+            "l2": f"index ({ix_bytes / 1e9:.2f} GB resident) larger than L2 (129 MB); no flush",
             "stage_ms": {kk: round(v, 4) for kk, v in stage.items()},
             "walk_records_scanned": recs,
             "walk_cells_scanned": cells,
+            "walk_counters": walk_counters,
             "parallelism": f"replicas x{ws}",
         },
         "e2e": {"value": round(e2e_value, 1), "unit": "queries/s",

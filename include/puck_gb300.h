@@ -133,6 +133,13 @@ int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
 int pgpu_set_profiling(pgpu_index* index, int enable);
 int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
 
+/* Diagnostic counters of the cell walk for the last pgpu_search_batch call, summed
+ * over queries: 0 filter records scanned, 1 cells scanned, 2 fine-order chunks,
+ * 3 stationary-order enumerations, 4 coarse clusters walked in fine order, 5 heap
+ * inserts, then thread-0 clock cycles: 6 replay, 7 whole walk, 8 prologue (LUT),
+ * 9 candidate generation, 10 speculative ADC. Fills min(n, 11) values. */
+int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
+
 int pgpu_close(pgpu_index* index);
 
 /* k-means assignment step used by train (kmeans.cpp:221-258 nearest_center):

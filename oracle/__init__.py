@@ -54,7 +54,8 @@ class _Trace(ctypes.Structure):
     _fields_ = [("coarse_tag", ctypes.c_void_p), ("coarse_dist", ctypes.c_void_p),
                 ("filter_tag", ctypes.c_void_p), ("filter_dist", ctypes.c_void_p),
                 ("filter_cnt", ctypes.c_uint32), ("lut", ctypes.c_void_p),
-                ("scanned_points", ctypes.c_uint64), ("scanned_cells", ctypes.c_uint64)]
+                ("scanned_points", ctypes.c_uint64), ("scanned_cells", ctypes.c_uint64),
+                ("visited_cells", ctypes.c_uint64), ("low_stat_cells", ctypes.c_uint64)]
 
 
 _lib = None
@@ -168,7 +169,7 @@ class OracleIndex:
                         lut=np.zeros(self.nsq * 256, np.float32))
             tr = _Trace(_ptr(arrs["coarse_tag"]), _ptr(arrs["coarse_dist"]),
                         _ptr(arrs["filter_tag"]), _ptr(arrs["filter_dist"]), 0, _ptr(arrs["lut"]),
-                        0, 0)
+                        0, 0, 0, 0)
         rc = lib.po_search(self._h, ctypes.byref(p), q.ctypes.data, topk, dist.ctypes.data,
                            ids.ctypes.data, ctypes.byref(rn),
                            ctypes.byref(tr) if tr is not None else None)
@@ -176,6 +177,8 @@ class OracleIndex:
             arrs["filter_cnt"] = tr.filter_cnt
             arrs["scanned_points"] = tr.scanned_points
             arrs["scanned_cells"] = tr.scanned_cells
+            arrs["visited_cells"] = tr.visited_cells
+            arrs["low_stat_cells"] = tr.low_stat_cells
         return rc, dist, ids, rn.value, arrs
 
     def search_batch(self, q, topk, search_coarse_count, filter_topk, topk_max=None,

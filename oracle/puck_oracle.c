@@ -559,15 +559,18 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
     const float qnorm = dotf(q, q, d);
     const double rr = p->radius_rate;
     float pivot = (float)((double)(rh.val[1] - qnorm) / rr / 2.0);
-    uint64_t scanned = 0, cells_scanned = 0;
+    uint64_t scanned = 0, cells_scanned = 0, visited = 0, low_stat = 0;
     for (uint32_t l = 0; l < P; ++l) {
         const uint32_t c = s->ctag[l];
         const float cdl = s->cd[l];
         const float* stat = ix->stationary + (uint64_t)c * F;
         const float min_dist = ix->min_dist_offset[c] + cdl;
         float max_stat = (pivot - cdl) - s->fd[0];
+        if (trace)
+            for (uint32_t f = 0; f < F; ++f) low_stat += stat[f] < max_stat;
         for (uint32_t idx = 0; idx < F; ++idx) {
             if (s->fd[idx] + min_dist >= pivot) break;
+            ++visited;
             const uint32_t k = s->ftag[idx];
             if (stat[k] >= max_stat) continue;
             const float cell_dist = (cdl + stat[k]) + s->fd[idx];
@@ -590,6 +593,8 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
         trace->filter_cnt = cnt;
         trace->scanned_points = scanned;
         trace->scanned_cells = cells_scanned;
+        trace->visited_cells = visited;
+        trace->low_stat_cells = low_stat;
     }
 
     /* rank_topN_points, Puck-Flat branch (puck_index.cpp:428-457) */

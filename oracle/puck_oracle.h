@@ -36,6 +36,8 @@ typedef struct {
     float* lut;           /* [filter_nsq * 256] */
     uint64_t scanned_points;
     uint64_t scanned_cells;
+    uint64_t visited_cells;   /* fine-cell iterations of the walk before each break */
+    uint64_t low_stat_cells;  /* cells with stationary below each coarse cluster's initial bound */
 } po_trace;
 
 po_index* po_load(const char* index_dir, int* err);

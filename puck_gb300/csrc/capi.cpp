@@ -24,6 +24,7 @@ struct pgpu_index {
     int32_t* d_status = nullptr;
     uint32_t stage_topk = 0;
     uint64_t kernels = 0, records = 0, cells = 0;
+    uint64_t walk_counters[pgpu::kNumWalkCounters] = {};
     // optional per-stage timing with CUDA events on the launching stream
     bool profiling = false;
     cudaEvent_t ev[PGPU_NUM_STAGES + 1] = {};
@@ -98,7 +99,7 @@ int alloc_scratch(pgpu_index* h) {
     PGPU_ALLOC(s.hdist, B * s.T);
     PGPU_ALLOC(s.htag, B * s.T);
     PGPU_ALLOC(s.hcnt, B);
-    PGPU_ALLOC(s.counters, 4);
+    PGPU_ALLOC(s.counters, pgpu::kNumWalkCounters);
 #undef PGPU_ALLOC
     s.cap = (uint32_t)B;
     s.bytes = b;
@@ -173,7 +174,7 @@ int run_pass(pgpu_index* h, uint32_t n, const float* d_q, uint32_t topk, float* 
     auto mark = [&](int i) {
         if (prof) cudaEventRecord(h->ev[i], st);
     };
-    if ((e = cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * 4, st)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * pgpu::kNumWalkCounters, st)) != cudaSuccess)
         return cuda_fail(e, "memset");
     mark(0);
     if ((e = pgpu::launch_prep_queries(ix, d_q, n, s, st)) != cudaSuccess)
@@ -354,12 +355,13 @@ int pgpu_search_batch(pgpu_index* h, uint32_t n, const float* query, uint32_t to
         if (status && (e = cudaMemcpyAsync(status + off, h->d_status, sizeof(int32_t) * m,
                                            cudaMemcpyDeviceToHost, st)))
             return cuda_fail(e, "status download");
-        unsigned long long cnt[4];
+        unsigned long long cnt[pgpu::kNumWalkCounters];
         if ((e = cudaMemcpyAsync(cnt, h->s.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st)) ||
             (e = cudaStreamSynchronize(st)))
             return cuda_fail(e, "search");
         h->records += cnt[0];
         h->cells += cnt[1];
+        for (int i = 0; i < pgpu::kNumWalkCounters; ++i) h->walk_counters[i] += cnt[i];
     }
     return PGPU_OK;
 }
@@ -403,6 +405,12 @@ int pgpu_last_stats(const pgpu_index* h, uint64_t* kernels_launched, uint64_t* r
     if (kernels_launched) *kernels_launched = h->kernels;
     if (records_scanned) *records_scanned = h->records;
     if (cells_scanned) *cells_scanned = h->cells;
+    return PGPU_OK;
+}
+
+int pgpu_walk_counters(const pgpu_index* h, uint64_t* out, uint32_t n) {
+    if (h == nullptr || out == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    for (uint32_t i = 0; i < n && i < (uint32_t)pgpu::kNumWalkCounters; ++i) out[i] = h->walk_counters[i];
     return PGPU_OK;
 }
 

@@ -1,0 +1,153 @@
+// Device helpers shared by the search kernels: Puck's MaxHeap, the reference's
+// float operation orders (BLAS dot, SSE LUT build and lookup), block scans.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "pgpu_internal.h"
+
+namespace pgpu {
+
+__device__ __forceinline__ float sentinel_f() { return __uint_as_float(kHeapSentinelBits); }
+
+// Sequential dot product, each product and partial sum rounded (BLAS order of
+// the oracle build: s = 0; s += x[i]*y[i]).
+__device__ __forceinline__ float dot_seq(const float* x, const float* y, uint32_t n) {
+    float s = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) s = __fadd_rn(s, __fmul_rn(x[i], y[i]));
+    return s;
+}
+
+// ------------------------------------------------------------------ MaxHeap
+// Puck's bounded max-heap (puck/hierarchical_cluster/max_heap.cpp:28-102) on
+// 1-based arrays: reject v >= top; the first `size` inserts sift down from the
+// last unfilled slot; reorder() heap-sorts to ascending order. Single thread.
+__device__ __forceinline__ void heap_insert(float* hv, uint32_t* ht, uint32_t heap_size,
+                                            uint32_t father, float v, uint32_t t) {
+    for (;;) {
+        uint32_t left = father << 1;
+        if (left > heap_size) break;
+        uint32_t right = left + 1;
+        float lv = hv[left];
+        if (right > heap_size || lv > hv[right]) {
+            if (lv < v) break;
+            hv[father] = lv;
+            ht[father] = ht[left];
+            father = left;
+        } else {
+            float rv = hv[right];
+            if (rv < v) break;
+            hv[father] = rv;
+            ht[father] = ht[right];
+            father = right;
+        }
+    }
+    hv[father] = v;
+    ht[father] = t;
+}
+
+__device__ __forceinline__ bool heap_update(float* hv, uint32_t* ht, uint32_t size,
+                                            uint32_t& dpc, float v, uint32_t t) {
+    if (v >= hv[1]) return false;
+    uint32_t father = 1;
+    if (dpc > 0) father = dpc--;
+    heap_insert(hv, ht, size, father, v, t);
+    return true;
+}
+
+__device__ __forceinline__ void heap_reorder(float* hv, uint32_t* ht, uint32_t size) {
+    for (uint32_t i = 0; i < size; ++i) {
+        float vb = hv[1];
+        uint32_t tb = ht[1];
+        uint32_t hs = size - i;
+        heap_insert(hv, ht, hs - 1, 1, hv[hs], ht[hs]);
+        hv[hs] = vb;
+        ht[hs] = tb;
+    }
+}
+
+// ------------------------------------------------------------- block scans
+// Inclusive scan over a block of NW warps; `warp_tot` needs NW slots.
+template <int NW>
+__device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* warp_tot,
+                                                   uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) warp_tot[warp] = v;
+    __syncthreads();
+    uint32_t add = 0;
+    for (int w = 0; w < warp; ++w) add += warp_tot[w];
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) t += warp_tot[w];
+    *total = t;
+    __syncthreads();
+    return v + add;
+}
+
+// fvec_L2sqr, SSE order (puck/puck/distances_simd.cpp:120-133, 210-236).
+__device__ __forceinline__ float l2sqr_sse(const float* x, const float* y, uint32_t d) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    uint32_t i = 0;
+    for (; i + 4 <= d; i += 4) {
+        float t0 = __fsub_rn(x[i], y[i]), t1 = __fsub_rn(x[i + 1], y[i + 1]);
+        float t2 = __fsub_rn(x[i + 2], y[i + 2]), t3 = __fsub_rn(x[i + 3], y[i + 3]);
+        a0 = __fadd_rn(a0, __fmul_rn(t0, t0));
+        a1 = __fadd_rn(a1, __fmul_rn(t1, t1));
+        a2 = __fadd_rn(a2, __fmul_rn(t2, t2));
+        a3 = __fadd_rn(a3, __fmul_rn(t3, t3));
+    }
+    if (i < d) {
+        float t0 = __fsub_rn(x[i], y[i]);
+        float t1 = (i + 1 < d) ? __fsub_rn(x[i + 1], y[i + 1]) : 0.0f;
+        float t2 = (i + 2 < d) ? __fsub_rn(x[i + 2], y[i + 2]) : 0.0f;
+        a0 = __fadd_rn(a0, __fmul_rn(t0, t0));
+        a1 = __fadd_rn(a1, __fmul_rn(t1, t1));
+        a2 = __fadd_rn(a2, __fmul_rn(t2, t2));
+        a3 = __fadd_rn(a3, 0.0f);
+    }
+    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+}
+
+// lookup_dist_table (puck_index.cpp:75-113): lane m%4 accumulates subspace m in
+// increasing m, then (l0+l1)+(l2+l3). `code` is 4-byte aligned.
+__device__ __forceinline__ float lut_sum(const uint8_t* __restrict__ code, const float* lut,
+                                         uint32_t nsq) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(code);
+    uint32_t m = 0;
+    for (; m + 4 <= nsq; m += 4) {
+        const uint32_t c = __ldg(w + (m >> 2));
+        a0 = __fadd_rn(a0, lut[(m + 0) * 256 + (c & 0xff)]);
+        a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
+        a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
+        a3 = __fadd_rn(a3, lut[(m + 3) * 256 + (c >> 24)]);
+    }
+    if (m < nsq) {
+        const uint32_t c = __ldg(w + (m >> 2));
+        a0 = __fadd_rn(a0, lut[m * 256 + (c & 0xff)]);
+        if (m + 1 < nsq) a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
+        if (m + 2 < nsq) a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
+    }
+    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+}
+
+// First half of compute_quantized_distance's per-point value
+// (float)(2.0 * cell_dist + offset) (puck_index.cpp:360). The reference adds in
+// double and rounds to float; for float operands double rounding of a sum is
+// innocuous (53 >= 2*24 + 2), so one float add of the exact 2*cell_dist gives
+// the same bits whenever 2*cell_dist is finite.
+__device__ __forceinline__ float adc_base(float cell_dist, float offset) {
+    return __fadd_rn(2.0f * cell_dist, offset);
+}
+
+__device__ __forceinline__ float pivot_of(float top, float qn, double rr) {
+    // (top - query_norm) / radius_rate / 2.0 (puck_index.cpp:517, 544)
+    return __double2float_rn((double)__fsub_rn(top, qn) / rr / 2.0);
+}
+
+}  // namespace pgpu

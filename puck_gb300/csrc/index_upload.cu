@@ -73,6 +73,8 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     PGPU_TRY(dev_copy(&ix->codes, h.codes_mem.data(), h.codes_mem.size(), &bytes));
     PGPU_TRY(dev_alloc(&ix->coarse_norms, h.C, &bytes));
     PGPU_TRY(dev_alloc(&ix->stationary, cells, &bytes));
+    PGPU_TRY(dev_alloc(&ix->stat_sorted, cells, &bytes));
+    PGPU_TRY(dev_alloc(&ix->stat_fine, cells, &bytes));
     PGPU_TRY(dev_alloc(&ix->min_dist_offset, h.C, &bytes));
     PGPU_TRY(dev_alloc(&ix->feat, (uint64_t)h.n * h.d, &bytes));
     PGPU_TRY(cudaMalloc(&fine_half, sizeof(float) * h.F));
@@ -90,6 +92,9 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     PGPU_TRY(launch_stationary(ix->coarse, h.C, ix->fine, h.F, h.d, fine_half, ix->stationary, 0));
     PGPU_TRY(launch_cell_constants(ix->stationary, ix->cell_start, ix->min_dist_offset, h.C, h.F,
                                    std::sqrt(FLT_MAX), 0));
+    // per coarse cluster, its cells in ascending stationary order (after the
+    // empty-cell fix-up): the enumeration order of the walk kernel
+    PGPU_TRY(launch_topsort(ix->stationary, h.C, h.F, h.F, h.F, ix->stat_sorted, ix->stat_fine, 0));
     PGPU_TRY(cudaDeviceSynchronize());
     cudaFree(fine_half);
     cudaFree(base_dev);

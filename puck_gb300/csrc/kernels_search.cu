@@ -16,90 +16,11 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "device_common.cuh"
 #include "pgpu_internal.h"
 
 namespace pgpu {
 namespace {
-
-__device__ __forceinline__ float sentinel_f() { return __uint_as_float(kHeapSentinelBits); }
-
-// Sequential dot product, each product and partial sum rounded (BLAS order of
-// the oracle build: s = 0; s += x[i]*y[i]).
-__device__ __forceinline__ float dot_seq(const float* x, const float* y, uint32_t n) {
-    float s = 0.0f;
-    for (uint32_t i = 0; i < n; ++i) s = __fadd_rn(s, __fmul_rn(x[i], y[i]));
-    return s;
-}
-
-// ------------------------------------------------------------------ MaxHeap
-// Puck's bounded max-heap (puck/hierarchical_cluster/max_heap.cpp:28-102) on
-// 1-based arrays: reject v >= top; the first `size` inserts sift down from the
-// last unfilled slot; reorder() heap-sorts to ascending order. Single thread.
-__device__ __forceinline__ void heap_insert(float* hv, uint32_t* ht, uint32_t heap_size,
-                                            uint32_t father, float v, uint32_t t) {
-    for (;;) {
-        uint32_t left = father << 1;
-        if (left > heap_size) break;
-        uint32_t right = left + 1;
-        float lv = hv[left];
-        if (right > heap_size || lv > hv[right]) {
-            if (lv < v) break;
-            hv[father] = lv;
-            ht[father] = ht[left];
-            father = left;
-        } else {
-            float rv = hv[right];
-            if (rv < v) break;
-            hv[father] = rv;
-            ht[father] = ht[right];
-            father = right;
-        }
-    }
-    hv[father] = v;
-    ht[father] = t;
-}
-
-__device__ __forceinline__ bool heap_update(float* hv, uint32_t* ht, uint32_t size,
-                                            uint32_t& dpc, float v, uint32_t t) {
-    if (v >= hv[1]) return false;
-    uint32_t father = 1;
-    if (dpc > 0) father = dpc--;
-    heap_insert(hv, ht, size, father, v, t);
-    return true;
-}
-
-__device__ void heap_reorder(float* hv, uint32_t* ht, uint32_t size) {
-    for (uint32_t i = 0; i < size; ++i) {
-        float vb = hv[1];
-        uint32_t tb = ht[1];
-        uint32_t hs = size - i;
-        heap_insert(hv, ht, hs - 1, 1, hv[hs], ht[hs]);
-        hv[hs] = vb;
-        ht[hs] = tb;
-    }
-}
-
-// ------------------------------------------------------------- block scans
-constexpr int kWalkThreads = 128;  // also the number of fine cells per speculation chunk
-constexpr int kPointBuf = 1024;    // points whose ADC is precomputed per chunk
-
-// Inclusive scan over a 128-thread block; `warp_tot` needs 4 slots.
-__device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* warp_tot,
-                                                   uint32_t* total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += u;
-    }
-    if (lane == 31) warp_tot[warp] = v;
-    __syncthreads();
-    uint32_t add = 0;
-    for (int w = 0; w < warp; ++w) add += warp_tot[w];
-    *total = warp_tot[0] + warp_tot[1] + warp_tot[2] + warp_tot[3];
-    __syncthreads();
-    return v + add;
-}
 
 // ---------------------------------------------------------------- kernels
 
@@ -288,302 +209,6 @@ __global__ void k_topsort(const float* __restrict__ vals, uint32_t L, uint32_t L
     for (uint32_t i = threadIdx.x; i < K; i += blockDim.x) {
         ov[i] = sv[i];
         oi[i] = si[i];
-    }
-}
-
-// fvec_L2sqr, SSE order (puck/puck/distances_simd.cpp:120-133, 210-236).
-__device__ __forceinline__ float l2sqr_sse(const float* x, const float* y, uint32_t d) {
-    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-    uint32_t i = 0;
-    for (; i + 4 <= d; i += 4) {
-        float t0 = __fsub_rn(x[i], y[i]), t1 = __fsub_rn(x[i + 1], y[i + 1]);
-        float t2 = __fsub_rn(x[i + 2], y[i + 2]), t3 = __fsub_rn(x[i + 3], y[i + 3]);
-        a0 = __fadd_rn(a0, __fmul_rn(t0, t0));
-        a1 = __fadd_rn(a1, __fmul_rn(t1, t1));
-        a2 = __fadd_rn(a2, __fmul_rn(t2, t2));
-        a3 = __fadd_rn(a3, __fmul_rn(t3, t3));
-    }
-    if (i < d) {
-        float t0 = __fsub_rn(x[i], y[i]);
-        float t1 = (i + 1 < d) ? __fsub_rn(x[i + 1], y[i + 1]) : 0.0f;
-        float t2 = (i + 2 < d) ? __fsub_rn(x[i + 2], y[i + 2]) : 0.0f;
-        a0 = __fadd_rn(a0, __fmul_rn(t0, t0));
-        a1 = __fadd_rn(a1, __fmul_rn(t1, t1));
-        a2 = __fadd_rn(a2, __fmul_rn(t2, t2));
-        a3 = __fadd_rn(a3, 0.0f);
-    }
-    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
-}
-
-// lookup_dist_table (puck_index.cpp:75-113): lane m%4 accumulates subspace m in
-// increasing m, then (l0+l1)+(l2+l3). `code` is 4-byte aligned.
-__device__ __forceinline__ float lut_sum(const uint8_t* __restrict__ code, const float* lut,
-                                         uint32_t nsq) {
-    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-    const uint32_t* w = reinterpret_cast<const uint32_t*>(code);
-    uint32_t m = 0;
-    for (; m + 4 <= nsq; m += 4) {
-        const uint32_t c = __ldg(w + (m >> 2));
-        a0 = __fadd_rn(a0, lut[(m + 0) * 256 + (c & 0xff)]);
-        a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
-        a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
-        a3 = __fadd_rn(a3, lut[(m + 3) * 256 + (c >> 24)]);
-    }
-    if (m < nsq) {
-        const uint32_t c = __ldg(w + (m >> 2));
-        a0 = __fadd_rn(a0, lut[m * 256 + (c & 0xff)]);
-        if (m + 1 < nsq) a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
-        if (m + 2 < nsq) a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
-    }
-    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
-}
-
-// First half of compute_quantized_distance's per-point value
-// (float)(2.0 * cell_dist + offset) (puck_index.cpp:360). The reference adds in
-// double and rounds to float; for float operands double rounding of a sum is
-// innocuous (53 >= 2*24 + 2), so one float add of the exact 2*cell_dist gives
-// the same bits whenever 2*cell_dist is finite.
-__device__ __forceinline__ float adc_base(float cell_dist, float offset) {
-    return __fadd_rn(2.0f * cell_dist, offset);
-}
-
-struct WalkParams {
-    const float* q;
-    const float* qnorm;
-    const int32_t* status;
-    const float* cdist;
-    const uint32_t* ctag;
-    const float* fdist;
-    const uint32_t* ftag;
-    float* hdist;
-    uint32_t* htag;
-    uint32_t* hcnt;
-    const float* stationary;
-    const uint32_t* cell_start;
-    const float* mdo;
-    const float* offsets;
-    const uint8_t* codes;
-    const float* codebook;
-    unsigned long long* counters;
-    uint32_t d, C, F, nsq, lsq, code_stride, P, T;
-    double rr;
-};
-
-struct WalkState {
-    float pivot, max_stat, min_dist, cdl;
-    uint32_t c, base, broke, dpc;
-    uint32_t bpos, n_cand, n_used, big, npts;
-    uint32_t warp_tot[4];
-    unsigned long long scanned_pts, scanned_cells;
-};
-
-__device__ __forceinline__ float pivot_of(float top, float qn, double rr) {
-    // (top - query_norm) / radius_rate / 2.0 (puck_index.cpp:517, 544)
-    return __double2float_rn((double)__fsub_rn(top, qn) / rr / 2.0);
-}
-
-// One block per query. Reproduces search_nearest_filter_points exactly: cells
-// of each probed coarse cluster are visited in ascending fine-term order and
-// pruned with the evolving pivot. Per chunk of 128 fine cells, all threads
-// evaluate the pruning tests against the current (larger or equal) pivot and
-// precompute the ADC value of every point of the surviving cells; thread 0
-// then replays the walk in order with the exact pivot, max_stationary_dist and
-// heap, which only prunes further. Breaks and skips are monotone in the pivot,
-// so the replay sees exactly the cells the sequential walk scans.
-__global__ __launch_bounds__(kWalkThreads) void k_walk_scan(WalkParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ WalkState st;
-    const uint32_t qi = blockIdx.x;
-    const int tid = threadIdx.x;
-    const uint32_t nsq = p.nsq, T = p.T, F = p.F;
-    float* lut = reinterpret_cast<float*>(smem);
-    float* hv = lut + nsq * 256;               // 1-based [1..T]
-    uint32_t* ht = reinterpret_cast<uint32_t*>(hv + T + 1);
-    float* qv = reinterpret_cast<float*>(ht + T + 1);
-    uint32_t* c_idx = reinterpret_cast<uint32_t*>(qv + p.d);
-    float* c_dist = reinterpret_cast<float*>(c_idx + kWalkThreads);
-    uint32_t* c_start = reinterpret_cast<uint32_t*>(c_dist + kWalkThreads);
-    uint32_t* c_cnt = c_start + kWalkThreads;
-    float* c_stat = reinterpret_cast<float*>(c_cnt + kWalkThreads);
-    float* c_fd = c_stat + kWalkThreads;
-    uint32_t* c_pref = reinterpret_cast<uint32_t*>(c_fd + kWalkThreads);  // [kWalkThreads + 1]
-    float* pt0 = reinterpret_cast<float*>(c_pref + kWalkThreads + 1);
-    float* ptf = pt0 + kPointBuf;
-
-    if (p.status[qi] != 0) {
-        if (tid == 0) p.hcnt[qi] = 0;
-        return;
-    }
-    const float* fd = p.fdist + (uint64_t)qi * F;
-    const uint32_t* ftag = p.ftag + (uint64_t)qi * F;
-    for (uint32_t i = tid; i < p.d; i += kWalkThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
-    for (uint32_t i = tid; i <= T; i += kWalkThreads) hv[i] = sentinel_f();
-    __syncthreads();
-    // get_dist_table (quantization.cpp:260-270)
-    for (uint32_t e = tid; e < nsq * 256; e += kWalkThreads) {
-        const uint32_t m = e >> 8, j = e & 255;
-        lut[e] = l2sqr_sse(qv + m * p.lsq, p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
-    }
-    const float qn = p.qnorm[qi];
-    if (tid == 0) {
-        st.dpc = T;
-        st.pivot = pivot_of(sentinel_f(), qn, p.rr);
-        st.scanned_pts = 0;
-        st.scanned_cells = 0;
-    }
-    __syncthreads();
-
-    for (uint32_t l = 0; l < p.P; ++l) {
-        if (tid == 0) {
-            const uint32_t c = p.ctag[(uint64_t)qi * p.P + l];
-            const float cdl = p.cdist[(uint64_t)qi * p.P + l];
-            st.c = c < p.C ? c : 0u;
-            st.cdl = cdl;
-            st.min_dist = c < p.C ? __fadd_rn(p.mdo[c], cdl) : 0.0f;
-            st.max_stat = __fsub_rn(__fsub_rn(st.pivot, cdl), fd[0]);
-            st.base = 0;
-            st.broke = c < p.C ? 0u : 1u;  // never taken for finite queries
-        }
-        __syncthreads();
-        const uint32_t c = st.c;
-        const float cdl = st.cdl;
-        const float* statrow = p.stationary + (uint64_t)c * F;
-        const uint32_t* cs = p.cell_start + (uint64_t)c * F;
-        while (true) {
-            const uint32_t base = st.base;
-            if (st.broke || base >= F) break;
-            const float pv = st.pivot, ms = st.max_stat, md = st.min_dist;
-            __syncthreads();  // everyone has read the state before it changes
-            const uint32_t idx = base + tid;
-            const bool valid = idx < F;
-            const float fdv = valid ? fd[idx] : 0.0f;
-            const bool brk = !valid || (__fadd_rn(fdv, md) >= pv);
-            if (tid == 0) st.bpos = kWalkThreads;
-            __syncthreads();
-            if (brk) atomicMin(&st.bpos, (uint32_t)tid);
-            __syncthreads();
-            const uint32_t bpos = st.bpos;
-            bool cand = false;
-            float stv = 0.0f;
-            uint32_t k = 0, start = 0, cnt = 0;
-            if ((uint32_t)tid < bpos) {
-                k = ftag[idx];
-                if (k >= F) k = 0;  // never taken for finite queries
-                stv = statrow[k];
-                cand = !(stv >= ms);
-                if (cand) {
-                    start = cs[k];
-                    cnt = cs[k + 1] - start;
-                }
-            }
-            uint32_t n_cand, npts_total;
-            const uint32_t pos_incl = block_scan_incl(cand ? 1u : 0u, st.warp_tot, &n_cand);
-            const uint32_t pts_incl = block_scan_incl(cand ? cnt : 0u, st.warp_tot, &npts_total);
-            const uint32_t pos = pos_incl - 1, pts_excl = pts_incl - cnt;
-            if (cand) {
-                c_idx[pos] = idx;
-                c_dist[pos] = __fadd_rn(__fadd_rn(cdl, stv), fdv);
-                c_start[pos] = start;
-                c_cnt[pos] = cnt;
-                c_stat[pos] = stv;
-                c_fd[pos] = fdv;
-                c_pref[pos] = pts_excl;
-            }
-            uint32_t fits_total;
-            block_scan_incl((cand && pts_incl <= (uint32_t)kPointBuf) ? 1u : 0u, st.warp_tot,
-                            &fits_total);
-            if (tid == 0) {
-                uint32_t n_used = fits_total, big = 0;
-                if (n_used == 0 && n_cand > 0) {
-                    n_used = 1;
-                    big = 1;
-                }
-                st.n_cand = n_cand;
-                st.n_used = n_used;
-                st.big = big;
-                c_pref[n_cand] = npts_total;
-            }
-            __syncthreads();
-            const uint32_t n_used = st.n_used;
-            const uint32_t npts = st.big ? 0u : c_pref[n_used];
-            // Speculative ADC for every point of the used candidate cells.
-            for (uint32_t j = tid; j < npts; j += kWalkThreads) {
-                uint32_t lo = 0, hi = n_used;  // largest pos with c_pref[pos] <= j
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (c_pref[mid] <= j) lo = mid;
-                    else hi = mid;
-                }
-                const uint32_t mi = c_start[lo] + (j - c_pref[lo]);
-                const float t0 = adc_base(c_dist[lo], p.offsets[mi]);
-                pt0[j] = t0;
-                ptf[j] = __fadd_rn(t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
-            }
-            __syncthreads();
-            if (tid == 0) {
-                float pivot = st.pivot, max_stat = st.max_stat;
-                uint32_t dpc = st.dpc;
-                bool broke = false;
-                unsigned long long sp = 0, sc = 0;
-                for (uint32_t i = 0; i < n_used; ++i) {
-                    const float fdi = c_fd[i];
-                    if (__fadd_rn(fdi, md) >= pivot) {
-                        broke = true;
-                        break;
-                    }
-                    if (c_stat[i] >= max_stat) continue;
-                    uint32_t upd = 0;
-                    const uint32_t s0 = c_start[i], nc = c_cnt[i];
-                    ++sc;
-                    for (uint32_t pp = 0; pp < nc; ++pp) {
-                        float t0, tf;
-                        if (st.big) {
-                            t0 = adc_base(c_dist[i], p.offsets[s0 + pp]);
-                            if (t0 >= hv[1]) break;
-                            tf = __fadd_rn(t0, lut_sum(p.codes + (uint64_t)(s0 + pp) * p.code_stride,
-                                                       lut, nsq));
-                        } else {
-                            t0 = pt0[c_pref[i] + pp];
-                            if (t0 >= hv[1]) break;
-                            tf = ptf[c_pref[i] + pp];
-                        }
-                        ++sp;
-                        if (heap_update(hv, ht, T, dpc, tf, s0 + pp)) ++upd;
-                    }
-                    if (upd > 0) pivot = pivot_of(hv[1], qn, p.rr);
-                    const float cand_ms = __fsub_rn(__fsub_rn(pivot, cdl), fdi);
-                    if (cand_ms < max_stat) max_stat = cand_ms;
-                }
-                uint32_t next = base + kWalkThreads;
-                if (!broke) {
-                    if (n_used < st.n_cand) next = c_idx[n_used];
-                    else if (bpos < (uint32_t)kWalkThreads) broke = true;
-                }
-                st.pivot = pivot;
-                st.max_stat = max_stat;
-                st.dpc = dpc;
-                st.broke = broke ? 1u : 0u;
-                st.base = next;
-                st.scanned_pts += sp;
-                st.scanned_cells += sc;
-            }
-            __syncthreads();
-        }
-        __syncthreads();  // all threads have left the chunk loop before thread 0 resets the state
-    }
-    if (tid == 0) {
-        const uint32_t cnt = T - st.dpc;
-        if (cnt < T) heap_reorder(hv, ht, T);
-        p.hcnt[qi] = cnt;
-        if (p.counters) {
-            atomicAdd(p.counters + 0, st.scanned_pts);
-            atomicAdd(p.counters + 1, st.scanned_cells);
-        }
-    }
-    __syncthreads();
-    for (uint32_t i = tid; i < T; i += kWalkThreads) {
-        p.hdist[(uint64_t)qi * T + i] = hv[i + 1];
-        p.htag[(uint64_t)qi * T + i] = ht[i + 1];
     }
 }
 
@@ -861,51 +486,6 @@ cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L,
 cudaError_t launch_topsort(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
                            uint32_t K, float* out_val, uint32_t* out_idx, cudaStream_t stream) {
     return launch_topsort_status(vals, nrows, L, ld_vals, K, out_val, out_idx, nullptr, stream);
-}
-
-size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T) {
-    return sizeof(float) * ix.nsq * 256 + (sizeof(float) + sizeof(uint32_t)) * (T + 1) +
-           sizeof(float) * ix.d + sizeof(uint32_t) * (7 * kWalkThreads + 1) +
-           sizeof(float) * 2 * kPointBuf;
-}
-
-cudaError_t launch_walk_scan(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
-                             Scratch& s, cudaStream_t stream) {
-    WalkParams p;
-    p.q = s.q;
-    p.qnorm = s.qnorm;
-    p.status = s.status;
-    p.cdist = s.cdist;
-    p.ctag = s.ctag;
-    p.fdist = s.fdist;
-    p.ftag = s.ftag;
-    p.hdist = s.hdist;
-    p.htag = s.htag;
-    p.hcnt = s.hcnt;
-    p.stationary = ix.stationary;
-    p.cell_start = ix.cell_start;
-    p.mdo = ix.min_dist_offset;
-    p.offsets = ix.offsets;
-    p.codes = ix.codes;
-    p.codebook = ix.codebook;
-    p.counters = s.counters;
-    p.d = ix.d;
-    p.C = ix.C;
-    p.F = ix.F;
-    p.nsq = ix.nsq;
-    p.lsq = ix.lsq;
-    p.code_stride = ix.code_stride;
-    p.P = s.P;
-    p.T = s.T;
-    p.rr = cfg.radius_rate;
-    const size_t smem = walk_smem_bytes(ix, s.T);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_walk_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr_set = true;
-    }
-    k_walk_scan<<<n, kWalkThreads, smem, stream>>>(p);
-    return cudaGetLastError();
 }
 
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {

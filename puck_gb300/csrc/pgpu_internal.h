@@ -19,6 +19,7 @@ constexpr uint32_t kMaxClusters = 8192;   // coarse or fine count: sorted in sha
 constexpr uint32_t kMaxFilterNsq = 64;    // LUT of nsq*256 floats in shared memory
 constexpr uint32_t kMaxFilterTopk = 4096; // filter heap in shared memory
 constexpr uint32_t kMaxDim = 1024;
+constexpr int kNumWalkCounters = 11;  // see the counter enum in walk_scan.cu
 
 // Device-resident index. Point arrays are in Puck's "memory order": sorted by
 // (cell id, filter offset, input id), so every coarse cluster is one
@@ -32,6 +33,8 @@ struct DeviceIndex {
     float* fine = nullptr;        // [F][d]
     float* coarse_norms = nullptr;// [C]  0.5*|c|^2
     float* stationary = nullptr;  // [C][F] 0.5*|f|^2 + f.c ; sqrt(FLT_MAX) for empty cells
+    float* stat_sorted = nullptr; // [C][F] each coarse row of stationary, ascending
+    uint32_t* stat_fine = nullptr;// [C][F] fine id of each stat_sorted entry
     uint32_t* cell_start = nullptr; // [C*F + 1]
     float* min_dist_offset = nullptr; // [C]
     uint32_t* mem2local = nullptr;  // [n]
@@ -56,7 +59,7 @@ struct Scratch {
     float* hdist = nullptr;    // [B][T] filter heap values
     uint32_t* htag = nullptr;  // [B][T] filter heap memory ids
     uint32_t* hcnt = nullptr;  // [B]
-    unsigned long long* counters = nullptr; // [4] records scanned, cells scanned
+    unsigned long long* counters = nullptr; // [kNumWalkCounters] walk diagnostics
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;
 };

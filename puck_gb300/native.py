@@ -28,8 +28,11 @@ EXPORTED_SYMBOLS = (
     "pgpu_params_default", "pgpu_open", "pgpu_open_arrays", "pgpu_set_search_params",
     "pgpu_search_batch", "pgpu_search", "pgpu_search_batch_device", "pgpu_index_info_get",
     "pgpu_last_stats", "pgpu_close", "pgpu_nearest_center", "pgpu_last_error",
-    "pgpu_set_profiling", "pgpu_stage_times",
+    "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
 )
+WALK_COUNTERS = ("records", "cells", "fd_order_chunks", "enumerations", "fd_order_clusters",
+                 "heap_inserts", "cyc_replay", "cyc_total", "cyc_prologue", "cyc_candidates",
+                 "cyc_adc")
 STAGES = ("prep", "coarse_scores", "coarse_select", "fine_scores", "fine_order", "walk_scan",
           "rerank")
 
@@ -100,6 +103,7 @@ def load(build_if_missing=False):
     lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
     lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.pgpu_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), u32]
+    lib.pgpu_walk_counters.argtypes = [vp, ctypes.POINTER(u64), u32]
     lib.pgpu_last_error.restype = ctypes.c_char_p
     lib.pgpu_last_error.argtypes = []
     for name in EXPORTED_SYMBOLS:
@@ -217,6 +221,11 @@ class GpuIndex:
         arr = (ctypes.c_float * len(STAGES))()
         check(load().pgpu_stage_times(self._h, arr, len(STAGES)))
         return dict(zip(STAGES, list(arr)))
+
+    def walk_counters(self):
+        arr = (ctypes.c_uint64 * len(WALK_COUNTERS))()
+        check(load().pgpu_walk_counters(self._h, arr, len(WALK_COUNTERS)))
+        return dict(zip(WALK_COUNTERS, list(arr)))
 
     def last_stats(self):
         k, r, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
