@@ -32,6 +32,10 @@ extern "C" {
 
 /* Search modes. */
 #define PGPU_MODE_EXACT 0      /* reference-exact: the same cells, heap and ties as PuckIndex::search */
+#define PGPU_MODE_SCAN 1       /* every record of the probed coarse clusters is scanned (no pivot
+                                  pruning); the filter_topk smallest ADC distances, each bit-identical
+                                  to the reference's value for that record, go to the exact rerank.
+                                  filter_topk <= 1536. */
 
 /* Search parameters. Field names and meanings follow Puck's gflags
  * (puck/gflags/puck_gflags.cpp:68-78): search_coarse_count (default 200),

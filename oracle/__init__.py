@@ -85,6 +85,8 @@ def _load():
         lib.po_search_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Params), ctypes.c_uint32,
                                         ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.po_search_scan.argtypes = lib.po_search.argtypes
+        lib.po_search_scan_batch.argtypes = lib.po_search_batch.argtypes
         lib.po_nearest_center.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                           ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
                                           ctypes.c_void_p]
@@ -151,7 +153,7 @@ class OracleIndex:
         return _Params(search_coarse_count, filter_topk, topk_max, radius_rate)
 
     def search_one(self, q, topk, search_coarse_count, filter_topk, topk_max=None,
-                   radius_rate=1.0, trace=False):
+                   radius_rate=1.0, trace=False, scan=False):
         """Returns (rc, dist[topk], ids[topk], result_num, trace dict or None)."""
         lib = _load()
         P = min(search_coarse_count, self.C)
@@ -170,7 +172,8 @@ class OracleIndex:
             tr = _Trace(_ptr(arrs["coarse_tag"]), _ptr(arrs["coarse_dist"]),
                         _ptr(arrs["filter_tag"]), _ptr(arrs["filter_dist"]), 0, _ptr(arrs["lut"]),
                         0, 0, 0, 0)
-        rc = lib.po_search(self._h, ctypes.byref(p), q.ctypes.data, topk, dist.ctypes.data,
+        fn = lib.po_search_scan if scan else lib.po_search
+        rc = fn(self._h, ctypes.byref(p), q.ctypes.data, topk, dist.ctypes.data,
                            ids.ctypes.data, ctypes.byref(rn),
                            ctypes.byref(tr) if tr is not None else None)
         if trace:
@@ -182,7 +185,7 @@ class OracleIndex:
         return rc, dist, ids, rn.value, arrs
 
     def search_batch(self, q, topk, search_coarse_count, filter_topk, topk_max=None,
-                     radius_rate=1.0, nthreads=None):
+                     radius_rate=1.0, nthreads=None, scan=False):
         lib = _load()
         q = np.ascontiguousarray(q, np.float32)
         n = q.shape[0]
@@ -190,7 +193,8 @@ class OracleIndex:
         dist = np.zeros((n, topk), np.float32)
         ids = np.full((n, topk), 0xFFFFFFFF, np.uint32)
         status = np.zeros(n, np.int32)
-        lib.po_search_batch(self._h, ctypes.byref(p), n, q.ctypes.data, topk, dist.ctypes.data,
+        fn = lib.po_search_scan_batch if scan else lib.po_search_batch
+        fn(self._h, ctypes.byref(p), n, q.ctypes.data, topk, dist.ctypes.data,
                             ids.ctypes.data, status.ctypes.data, nthreads or os.cpu_count())
         return dist, ids, status
 

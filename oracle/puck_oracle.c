@@ -615,6 +615,116 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
     return 0;
 }
 
+/* ---------------------------------------------------------------- scan mode */
+/* Definition of the library's scan mode (test infrastructure): the reference's
+ * normalisation, coarse heap and LUT, then EVERY record of the probed coarse
+ * clusters gets the reference's per-point distance
+ *   t = (float)(2.0 * ((cd + stationary) + fd) + offset) + lookup_dist_table
+ * (puck_index.cpp:360-368, 539-540); the filter_topk smallest by (t, memory id),
+ * ascending, are reranked exactly as rank_topN_points does (puck_index.cpp:428-457). */
+typedef struct {
+    float t;
+    uint32_t mi;
+} po_cand;
+
+static int cmp_cand(const void* a, const void* b) {
+    const po_cand* x = (const po_cand*)a;
+    const po_cand* y = (const po_cand*)b;
+    if (x->t < y->t) return -1;
+    if (y->t < x->t) return 1;
+    return (x->mi > y->mi) - (x->mi < y->mi);
+}
+
+static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s,
+                           const float* query, uint32_t topk, float* dist, uint32_t* ids,
+                           uint32_t* result_num, po_trace* trace) {
+    const uint32_t d = ix->d, C = ix->C, F = ix->F, nsq = ix->nsq;
+    uint32_t P = p->search_coarse_count < C ? p->search_coarse_count : C;
+    const uint32_t T = p->filter_topk;
+    if (topk > p->topk || query == NULL || P == 0 || T == 0 || topk == 0) return -1;
+    memcpy(s->q, query, sizeof(float) * d);
+    if (ix->whether_norm) {
+        float norm = sqrtf(dotf(s->q, s->q, d));
+        if ((double)norm < 1e-6) return -2;
+        float alpha = (float)(1.0 / (double)norm);
+        for (uint32_t i = 0; i < d; ++i) s->q[i] = alpha * s->q[i];
+    }
+    const float* q = s->q;
+    po_heap ch;
+    heap_init(&ch, P, s->cd, s->ctag);
+    for (uint32_t c = 0; c < C; ++c) {
+        float ipc = dotf(ix->coarse + (uint64_t)c * d, q, d);
+        float cdv = ix->coarse_norms[c] - ipc;
+        if (cdv < ch.val[1]) heap_update(&ch, cdv, c);
+    }
+    heap_reorder(&ch);
+    for (uint32_t m = 0; m < nsq; ++m)
+        for (uint32_t j = 0; j < 256; ++j)
+            s->lut[m * 256 + j] = l2sqr_sse(q + (uint64_t)m * ix->lsq,
+                                            ix->codebook + ((uint64_t)m * 256 + j) * ix->lsq, ix->lsq);
+    for (uint32_t f = 0; f < F; ++f) s->fd[f] = -dotf(ix->fine + (uint64_t)f * d, q, d);
+    uint64_t total = 0;
+    for (uint32_t l = 0; l < P; ++l) {
+        const uint32_t c = s->ctag[l];
+        total += ix->cell_start[(uint64_t)c * F + F] - ix->cell_start[(uint64_t)c * F];
+    }
+    po_cand* cand = (po_cand*)malloc(sizeof(po_cand) * (total ? total : 1));
+    uint64_t nc = 0;
+    for (uint32_t l = 0; l < P; ++l) {
+        const uint32_t c = s->ctag[l];
+        const float cdl = s->cd[l];
+        for (uint32_t f = 0; f < F; ++f) {
+            const uint64_t cell = (uint64_t)c * F + f;
+            const float cell_dist = (cdl + ix->stationary[cell]) + s->fd[f];
+            for (uint32_t mi = ix->cell_start[cell]; mi < ix->cell_start[cell + 1]; ++mi) {
+                float t = (float)(2.0 * (double)cell_dist + (double)ix->offsets[mi]);
+                t = t + lookup_lut(ix->codes + (uint64_t)mi * nsq, s->lut, nsq);
+                cand[nc].t = t;
+                cand[nc].mi = mi;
+                ++nc;
+            }
+        }
+    }
+    qsort(cand, nc, sizeof(po_cand), cmp_cand);
+    const uint32_t cnt = nc < T ? (uint32_t)nc : T;
+    if (trace) {
+        if (trace->coarse_tag) memcpy(trace->coarse_tag, s->ctag, sizeof(uint32_t) * P);
+        if (trace->coarse_dist) memcpy(trace->coarse_dist, s->cd, sizeof(float) * P);
+        for (uint32_t i = 0; i < T; ++i) {
+            if (trace->filter_tag) trace->filter_tag[i] = i < cnt ? cand[i].mi : 0xFFFFFFFFu;
+            if (trace->filter_dist) trace->filter_dist[i] = i < cnt ? cand[i].t : 0.0f;
+        }
+        if (trace->lut) memcpy(trace->lut, s->lut, sizeof(float) * nsq * 256);
+        trace->filter_cnt = cnt;
+        trace->scanned_points = nc;
+    }
+    po_heap fin;
+    heap_init(&fin, topk, dist, ids);
+    for (uint32_t idx = 0; idx < cnt; ++idx) {
+        const float* x = ix->feat + (uint64_t)cand[idx].mi * d;
+        float t = 0.0f;
+        uint32_t m = 0;
+        for (; m + 16 <= d && t < fin.val[1]; m += 16) t = t + l2sqr16(x + m, q + m);
+        if (t < fin.val[1]) {
+            if (d - m > 0) t = t + l2sqr_ext(x + m, q + m, d - m);
+            heap_update(&fin, t, ix->mem2local[cand[idx].mi]);
+        }
+    }
+    heap_reorder(&fin);
+    *result_num = heap_count(&fin);
+    free(cand);
+    return 0;
+}
+
+int po_search_scan(const po_index* ix, const po_params* p, const float* q, uint32_t topk,
+                   float* dist, uint32_t* ids, uint32_t* result_num, po_trace* trace) {
+    po_scratch s;
+    scratch_alloc(&s, ix, p);
+    int rc = search_scan_one(ix, p, &s, q, topk, dist, ids, result_num, trace);
+    scratch_free(&s);
+    return rc;
+}
+
 int po_search(const po_index* ix, const po_params* p, const float* q, uint32_t topk, float* dist,
               uint32_t* ids, uint32_t* result_num, po_trace* trace) {
     po_scratch s;
@@ -632,6 +742,7 @@ typedef struct {
     float* dist;
     uint32_t* ids;
     int32_t* status;
+    int scan;
     atomic_uint_fast64_t next;
 } batch_job;
 
@@ -643,17 +754,23 @@ static void* batch_worker(void* arg) {
         uint64_t i = atomic_fetch_add(&job->next, 1);
         if (i >= job->n) break;
         uint32_t rn = 0;
-        int rc = search_one(job->ix, job->p, &s, job->q + i * job->ix->d, job->topk,
-                            job->dist + i * job->topk, job->ids + i * job->topk, &rn, NULL);
+        int rc = job->scan
+                     ? search_scan_one(job->ix, job->p, &s, job->q + i * job->ix->d, job->topk,
+                                       job->dist + i * job->topk, job->ids + i * job->topk, &rn,
+                                       NULL)
+                     : search_one(job->ix, job->p, &s, job->q + i * job->ix->d, job->topk,
+                                  job->dist + i * job->topk, job->ids + i * job->topk, &rn, NULL);
         if (job->status) job->status[i] = rc;
     }
     scratch_free(&s);
     return NULL;
 }
 
-int po_search_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
-                    uint32_t topk, float* dist, uint32_t* ids, int32_t* status, int nthreads) {
+static int batch_run(const po_index* ix, const po_params* p, uint32_t n, const float* q,
+                     uint32_t topk, float* dist, uint32_t* ids, int32_t* status, int nthreads,
+                     int scan) {
     batch_job job;
+    job.scan = scan;
     job.ix = ix;
     job.p = p;
     job.n = n;
@@ -669,6 +786,17 @@ int po_search_batch(const po_index* ix, const po_params* p, uint32_t n, const fl
     for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
     free(th);
     return 0;
+}
+
+int po_search_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
+                    uint32_t topk, float* dist, uint32_t* ids, int32_t* status, int nthreads) {
+    return batch_run(ix, p, n, q, topk, dist, ids, status, nthreads, 0);
+}
+
+int po_search_scan_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
+                         uint32_t topk, float* dist, uint32_t* ids, int32_t* status,
+                         int nthreads) {
+    return batch_run(ix, p, n, q, topk, dist, ids, status, nthreads, 1);
 }
 
 /* ------------------------------------------------------------------ assign */

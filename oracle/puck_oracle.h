@@ -62,6 +62,14 @@ int po_search(const po_index* ix, const po_params* p, const float* q, uint32_t t
 int po_search_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
                     uint32_t topk, float* dist, uint32_t* ids, int32_t* status, int nthreads);
 
+/* The library's scan mode: every record of the probed coarse clusters, exact
+ * top-filter_topk by (distance, memory id), exact rerank. */
+int po_search_scan(const po_index* ix, const po_params* p, const float* q, uint32_t topk,
+                   float* dist, uint32_t* ids, uint32_t* result_num, po_trace* trace);
+int po_search_scan_batch(const po_index* ix, const po_params* p, uint32_t n, const float* q,
+                         uint32_t topk, float* dist, uint32_t* ids, int32_t* status,
+                         int nthreads);
+
 /* k-means assignment step: nearest_center (kmeans.cpp:221-258). */
 void po_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* x,
                        uint64_t n, int32_t* assign, float* dis);

@@ -117,9 +117,14 @@ int check_config(const pgpu_index* h, const pgpu_params* p) {
     if (p->topk > pgpu::kMaxFilterTopk)
         return fail(PGPU_E_LIMIT, "topk above " + std::to_string(pgpu::kMaxFilterTopk));
     if (p->max_batch == 0) return fail(PGPU_E_INVALID, "max_batch must be positive");
-    if (p->mode != PGPU_MODE_EXACT) return fail(PGPU_E_INVALID, "unknown search mode");
+    if (p->mode != PGPU_MODE_EXACT && p->mode != PGPU_MODE_SCAN)
+        return fail(PGPU_E_INVALID, "unknown search mode");
+    if (p->mode == PGPU_MODE_SCAN && p->filter_topk > pgpu::scan_max_filter_topk())
+        return fail(PGPU_E_LIMIT, "filter_topk above " + std::to_string(pgpu::scan_max_filter_topk()) +
+                                      " in scan mode");
     if (h != nullptr) {
         if (pgpu::walk_smem_bytes(h->ix, p->filter_topk) > 220 * 1024 ||
+            pgpu::scan_smem_bytes(h->ix) > 220 * 1024 ||
             pgpu::rerank_smem_bytes(h->ix, p->filter_topk, p->topk) > 220 * 1024)
             return fail(PGPU_E_LIMIT, "filter_topk/topk/filter_nsq exceed the shared-memory budget");
     }
@@ -192,19 +197,28 @@ int run_pass(pgpu_index* h, uint32_t n, const float* d_q, uint32_t topk, float* 
                                           st)) != cudaSuccess)
         return cuda_fail(e, "fine scores");
     mark(4);
-    if ((e = pgpu::launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status,
-                                         st)) != cudaSuccess)
-        return cuda_fail(e, "fine order");
+    int launched = 6;
+    if (h->cfg.mode == PGPU_MODE_EXACT) {
+        if ((e = pgpu::launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status,
+                                             st)) != cudaSuccess)
+            return cuda_fail(e, "fine order");
+        launched = 7;
+    }
     mark(5);
-    if ((e = pgpu::launch_walk_scan(ix, h->cfg, n, s, st)) != cudaSuccess)
-        return cuda_fail(e, "walk_scan");
+    if (h->cfg.mode == PGPU_MODE_EXACT) {
+        if ((e = pgpu::launch_walk_scan(ix, h->cfg, n, s, st)) != cudaSuccess)
+            return cuda_fail(e, "walk_scan");
+    } else {
+        if ((e = pgpu::launch_scan_select(ix, n, s, st)) != cudaSuccess)
+            return cuda_fail(e, "scan_select");
+    }
     mark(6);
     if ((e = pgpu::launch_rerank(ix, h->cfg, n, topk, s, d_dist, d_ids, d_status, st)) !=
         cudaSuccess)
         return cuda_fail(e, "rerank");
     mark(7);
     if (prof) h->stage_pending = true;
-    h->kernels += 7;
+    h->kernels += launched;
     return PGPU_OK;
 }
 

@@ -273,6 +273,15 @@ int build_host_index(const pgpu_index_arrays& a, HostIndex* h, std::string* err)
                                  [off](uint32_t x, uint32_t y) { return off[x] < off[y]; });
         }
     });
+    h->rec_fine.assign(n, 0);
+    {
+        uint16_t* rf = h->rec_fine.data();
+        const uint32_t F = h->F;
+        parallel_for(cells, [&](uint64_t b, uint64_t e) {
+            for (uint64_t c = b; c < e; ++c)
+                for (uint32_t i = cs[c]; i < cs[c + 1]; ++i) rf[i] = (uint16_t)(c % F);
+        });
+    }
     h->code_stride = (h->nsq + 3) / 4 * 4;
     h->offsets_mem.assign(n, 0.0f);
     h->codes_mem.assign((uint64_t)n * h->code_stride, 0);
@@ -294,7 +303,7 @@ int build_host_index(const pgpu_index_arrays& a, HostIndex* h, std::string* err)
 
 void free_device_index(DeviceIndex* ix) {
     void* ptrs[] = {ix->coarse, ix->fine, ix->coarse_norms, ix->stationary, ix->stat_sorted,
-                    ix->stat_fine, ix->cell_start,
+                    ix->stat_fine, ix->rec_fine, ix->cell_start,
                     ix->min_dist_offset, ix->mem2local, ix->offsets, ix->codes, ix->feat,
                     ix->codebook};
     for (void* q : ptrs)

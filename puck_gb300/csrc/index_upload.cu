@@ -69,6 +69,7 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     PGPU_TRY(dev_copy(&ix->codebook, h.codebook.data(), h.codebook.size(), &bytes));
     PGPU_TRY(dev_copy(&ix->cell_start, h.cell_start.data(), h.cell_start.size(), &bytes));
     PGPU_TRY(dev_copy(&ix->mem2local, h.mem2local.data(), h.mem2local.size(), &bytes));
+    PGPU_TRY(dev_copy(&ix->rec_fine, h.rec_fine.data(), h.rec_fine.size(), &bytes));
     PGPU_TRY(dev_copy(&ix->offsets, h.offsets_mem.data(), h.offsets_mem.size(), &bytes));
     PGPU_TRY(dev_copy(&ix->codes, h.codes_mem.data(), h.codes_mem.size(), &bytes));
     PGPU_TRY(dev_alloc(&ix->coarse_norms, h.C, &bytes));

@@ -38,6 +38,7 @@ struct DeviceIndex {
     uint32_t* cell_start = nullptr; // [C*F + 1]
     float* min_dist_offset = nullptr; // [C]
     uint32_t* mem2local = nullptr;  // [n]
+    uint16_t* rec_fine = nullptr;   // [n] fine id of the cell each record belongs to
     float* offsets = nullptr;       // [n] filter offset per point
     uint8_t* codes = nullptr;       // [n][code_stride]
     float* feat = nullptr;          // [n][d] original vectors
@@ -96,6 +97,9 @@ cudaError_t launch_half_norms(const float* X, uint32_t rows, uint32_t d, float* 
 cudaError_t launch_cell_constants(float* stationary, const uint32_t* cell_start, float* mdo,
                                   uint32_t C, uint32_t F, float empty_value, cudaStream_t stream);
 size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T);
+size_t scan_smem_bytes(const DeviceIndex& ix);
+uint32_t scan_max_filter_topk();
+cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
 
 // Host-side loader (index_host.cpp).
@@ -104,6 +108,7 @@ struct HostIndex {
     int whether_norm = 0;
     std::vector<float> coarse, fine, codebook;
     std::vector<uint32_t> cell_start, mem2local;
+    std::vector<uint16_t> rec_fine;   // memory order
     std::vector<float> offsets_mem;   // memory order
     std::vector<uint8_t> codes_mem;   // memory order, code_stride bytes per row
     std::vector<float> feat_mem;      // memory order

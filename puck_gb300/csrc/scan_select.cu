@@ -1,0 +1,243 @@
+// k_scan_select: throughput-mode filter stage. For one query it streams every
+// filter record of its probed coarse clusters (each cluster is one contiguous
+// range in memory order) and keeps the filter_topk smallest ADC distances.
+//
+// Per record the distance is the reference's own expression for a scanned point
+// (puck/puck/puck_index.cpp:360-368 with cell_dist from :539-540):
+//     cell_dist = (coarse_term + stationary[c][f]) + fine_term[f]
+//     t         = (float)(2 * cell_dist + offset) + lookup_dist_table(codes)
+// so every t is bit-identical to the value PuckIndex::search would compute for
+// that point. Unlike the reference's pivot-pruned cell walk, no cell of a probed
+// cluster is skipped: the result is the exact top-filter_topk by (t, memory id)
+// over all records of the probed clusters, a superset search of the same cells.
+//
+// Selection: a candidate buffer in shared memory with a running threshold tau =
+// the (t, id) of the current filter_topk-th best; records with
+// (2*cell_dist + offset, id) >= tau are dropped before the table lookups (t can
+// only grow). When the buffer fills it is bitonic-sorted and cut back to
+// filter_topk entries. The output is sorted ascending by (t, id).
+#include "device_common.cuh"
+#include "pgpu_internal.h"
+
+namespace pgpu {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRecPerThread = 2;
+constexpr int kRound = kThreads * kRecPerThread;  // records per round
+constexpr uint32_t kCandCap = 2048;               // candidate buffer (power of two)
+
+struct ScanParams {
+    const float* q;
+    const float* qnorm;
+    const int32_t* status;
+    const float* cdist;
+    const uint32_t* ctag;
+    const float* fd_by_fine;  // [B][F]
+    float* hdist;
+    uint32_t* htag;
+    uint32_t* hcnt;
+    const float* stationary;  // [C][F]
+    const uint32_t* cell_start;
+    const uint16_t* rec_fine; // [n] fine id of each record
+    const float* offsets;
+    const uint8_t* codes;
+    const float* codebook;
+    unsigned long long* counters;
+    uint32_t d, C, F, nsq, lsq, code_stride, P, T;
+};
+
+__device__ __forceinline__ bool key_less(float a, uint32_t ia, float b, uint32_t ib) {
+    return a < b || (a == b && ia < ib);
+}
+
+// Sorts cv/ci[0..cap) ascending by (value, id); cap is a power of two.
+__device__ void bitonic_sort(float* cv, uint32_t* ci, uint32_t cap) {
+    for (uint32_t size = 2; size <= cap; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = threadIdx.x; t < cap / 2; t += kThreads) {
+                const uint32_t lo = 2 * t - (t & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const float a = cv[lo], b = cv[hi];
+                const uint32_t ia = ci[lo], ib = ci[hi];
+                const bool gt = key_less(b, ib, a, ia);
+                if (gt == asc) {
+                    cv[lo] = b;
+                    cv[hi] = a;
+                    ci[lo] = ib;
+                    ci[hi] = ia;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+struct ScanState {
+    float tau_v;
+    uint32_t tau_i;
+    uint32_t count;
+    uint32_t c;
+    float cdl;
+    uint32_t r0, r1;
+    unsigned long long evaluated, passed;
+};
+
+__global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ScanState st;
+    const uint32_t qi = blockIdx.x;
+    const int tid = threadIdx.x;
+    const uint32_t nsq = p.nsq, F = p.F, T = p.T;
+    float* lut = reinterpret_cast<float*>(smem);
+    float* fdk = lut + nsq * 256;          // [F]
+    float* srow = fdk + F;                 // [F] stationary row of the current cluster
+    float* cv = srow + F;                  // [kCandCap]
+    uint32_t* ci = reinterpret_cast<uint32_t*>(cv + kCandCap);
+    float* qv = reinterpret_cast<float*>(ci + kCandCap);  // [d]
+
+    if (p.status[qi] != 0) {
+        if (tid == 0) p.hcnt[qi] = 0;
+        return;
+    }
+    for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    for (uint32_t i = tid; i < F; i += kThreads) fdk[i] = p.fd_by_fine[(uint64_t)qi * F + i];
+    if (tid == 0) {
+        st.tau_v = __int_as_float(0x7f800000);
+        st.tau_i = 0xFFFFFFFFu;
+        st.count = 0;
+        st.evaluated = 0;
+        st.passed = 0;
+    }
+    __syncthreads();
+    for (uint32_t e = tid; e < nsq * 256; e += kThreads) {
+        const uint32_t m = e >> 8, j = e & 255;
+        lut[e] = l2sqr_sse(qv + m * p.lsq, p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
+    }
+    unsigned long long my_eval = 0, my_pass = 0;
+    for (uint32_t l = 0; l < p.P; ++l) {
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t c = p.ctag[(uint64_t)qi * p.P + l];
+            st.c = c;
+            st.cdl = p.cdist[(uint64_t)qi * p.P + l];
+            if (c < p.C) {
+                st.r0 = p.cell_start[(uint64_t)c * F];
+                st.r1 = p.cell_start[(uint64_t)c * F + F];
+            } else {
+                st.r0 = st.r1 = 0;  // never taken for finite queries
+            }
+        }
+        __syncthreads();
+        const uint32_t c = st.c, r0 = st.r0, r1 = st.r1;
+        const float cdl = st.cdl;
+        if (r0 >= r1) continue;
+        for (uint32_t i = tid; i < F; i += kThreads) srow[i] = p.stationary[(uint64_t)c * F + i];
+        __syncthreads();
+        for (uint32_t base = r0; base < r1; base += kRound) {
+            const float tv = st.tau_v;
+            const uint32_t ti = st.tau_i;
+#pragma unroll
+            for (int j = 0; j < kRecPerThread; ++j) {
+                const uint32_t mi = base + tid + j * kThreads;
+                if (mi >= r1) break;
+                const uint32_t f = p.rec_fine[mi];
+                const float cell_dist = __fadd_rn(__fadd_rn(cdl, srow[f]), fdk[f]);
+                const float t0 = adc_base(cell_dist, p.offsets[mi]);
+                ++my_eval;
+                if (!key_less(t0, mi, tv, ti)) continue;
+                const float t =
+                    __fadd_rn(t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
+                if (!key_less(t, mi, tv, ti)) continue;
+                ++my_pass;
+                const uint32_t slot = atomicAdd(&st.count, 1u);
+                cv[slot] = t;  // capacity is kept >= count + kRound by the compaction below
+                ci[slot] = mi;
+            }
+            __syncthreads();
+            if (st.count > kCandCap - kRound) {
+                // cut back to the T best; tau = the T-th (value, id)
+                for (uint32_t i = st.count + tid; i < kCandCap; i += kThreads) {
+                    cv[i] = __int_as_float(0x7f800000);
+                    ci[i] = 0xFFFFFFFFu;
+                }
+                __syncthreads();
+                bitonic_sort(cv, ci, kCandCap);
+                if (tid == 0) {
+                    st.count = T;
+                    st.tau_v = cv[T - 1];
+                    st.tau_i = ci[T - 1];
+                }
+                __syncthreads();
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t count = st.count;
+    for (uint32_t i = count + tid; i < kCandCap; i += kThreads) {
+        cv[i] = __int_as_float(0x7f800000);
+        ci[i] = 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    bitonic_sort(cv, ci, kCandCap);
+    const uint32_t out = count < T ? count : T;
+    for (uint32_t i = tid; i < T; i += kThreads) {
+        p.hdist[(uint64_t)qi * T + i] = i < out ? cv[i] : sentinel_f();
+        p.htag[(uint64_t)qi * T + i] = i < out ? ci[i] : kNoLabel;
+    }
+    if (tid == 0) p.hcnt[qi] = out;
+    if (p.counters) {
+        // records evaluated / passed the threshold (summed over the block)
+        atomicAdd(p.counters + 0, my_eval);
+        atomicAdd(p.counters + 2, my_pass);
+    }
+}
+
+}  // namespace
+
+size_t scan_smem_bytes(const DeviceIndex& ix) {
+    return sizeof(float) * ix.nsq * 256 + sizeof(float) * 2 * ix.F +
+           (sizeof(float) + sizeof(uint32_t)) * kCandCap + sizeof(float) * ix.d;
+}
+
+uint32_t scan_max_filter_topk() { return kCandCap - kRound; }
+
+cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s,
+                               cudaStream_t stream) {
+    ScanParams p;
+    p.q = s.q;
+    p.qnorm = s.qnorm;
+    p.status = s.status;
+    p.cdist = s.cdist;
+    p.ctag = s.ctag;
+    p.fd_by_fine = s.dots;
+    p.hdist = s.hdist;
+    p.htag = s.htag;
+    p.hcnt = s.hcnt;
+    p.stationary = ix.stationary;
+    p.cell_start = ix.cell_start;
+    p.rec_fine = ix.rec_fine;
+    p.offsets = ix.offsets;
+    p.codes = ix.codes;
+    p.codebook = ix.codebook;
+    p.counters = s.counters;
+    p.d = ix.d;
+    p.C = ix.C;
+    p.F = ix.F;
+    p.nsq = ix.nsq;
+    p.lsq = ix.lsq;
+    p.code_stride = ix.code_stride;
+    p.P = s.P;
+    p.T = s.T;
+    const size_t smem = scan_smem_bytes(ix);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_scan_select, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        attr_set = true;
+    }
+    k_scan_select<<<n, kThreads, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace pgpu

@@ -20,6 +20,7 @@ PGPU_E_CUDA = -5
 PGPU_E_NOMEM = -6
 PGPU_E_LIMIT = -7
 PGPU_MODE_EXACT = 0
+PGPU_MODE_SCAN = 1
 
 HEAP_SENTINEL = np.uint32(0x7F7F7F7F).view(np.float32)
 NO_LABEL = 0xFFFFFFFF

@@ -73,6 +73,22 @@ def test_golden_py_api_mirror(golden):
     py_puck_api.reset_gflags()
 
 
+def test_golden_scan_mode_matches_oracle(golden):
+    """Scan mode: every record of the probed clusters; bit-identical to the oracle's
+    restatement of the mode (same per-record distances as the reference)."""
+    name, z, index_dir = golden
+    P, T, k = [int(v) for v in z["params"]]
+    T = min(T, 1536)
+    ix = native.GpuIndex(index_dir, search_coarse_count=P, filter_topk=T, topk=k, max_batch=64,
+                         mode=native.PGPU_MODE_SCAN)
+    dist, ids, status = ix.search(z["queries"], k, return_status=True)
+    orc = oracle.OracleIndex(index_dir)
+    od, oi, ost = orc.search_batch(z["queries"], k, P, T, topk_max=k, scan=True)
+    assert (status == 0).all() and (ost == 0).all()
+    assert np.array_equal(_bits(dist), _bits(od)), name
+    assert np.array_equal(ids, oi), name
+
+
 def test_small_batches_and_chunking(golden):
     """max_batch smaller than n: several device passes give the same bits."""
     name, z, index_dir = golden
@@ -100,18 +116,21 @@ def _built_index(tmpdir, n, d, C, F, nsq, kind, seed, norm):
     return q
 
 
+@pytest.mark.parametrize("mode", [native.PGPU_MODE_EXACT, native.PGPU_MODE_SCAN])
 @pytest.mark.parametrize("n,d,C,F,nsq,kind,norm,P,T,k", [
     (60000, 64, 64, 64, 16, "int", False, 16, 200, 10),
     (80000, 96, 96, 80, 24, "unit", True, 24, 500, 100),
     (40000, 128, 50, 40, 32, "int", False, 50, 300, 20),
 ])
-def test_gpu_equals_oracle_builder_index(n, d, C, F, nsq, kind, norm, P, T, k):
+def test_gpu_equals_oracle_builder_index(n, d, C, F, nsq, kind, norm, P, T, k, mode):
     with tempfile.TemporaryDirectory() as tmp:
         q = _built_index(tmp, n, d, C, F, nsq, kind, 11, norm)
-        ix = native.GpuIndex(tmp, search_coarse_count=P, filter_topk=T, topk=k, max_batch=100)
+        ix = native.GpuIndex(tmp, search_coarse_count=P, filter_topk=T, topk=k, max_batch=100,
+                             mode=mode)
         dist, ids = ix.search(q, k)
         orc = oracle.OracleIndex(tmp)
-        od, oi, st = orc.search_batch(q, k, P, T, topk_max=k, nthreads=os.cpu_count())
+        od, oi, st = orc.search_batch(q, k, P, T, topk_max=k, nthreads=os.cpu_count(),
+                                      scan=(mode == native.PGPU_MODE_SCAN))
         assert (st == 0).all()
         assert np.array_equal(_bits(dist), _bits(od))
         assert np.array_equal(ids, oi)

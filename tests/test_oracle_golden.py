@@ -82,3 +82,26 @@ def test_nearest_cell_assign_is_exact_argmin():
     best = full.min(1)
     # the pruned walk must land on an exact minimiser (up to float rounding)
     assert np.all(full[np.arange(len(x)), cell] <= best + 1e-4)
+
+
+def test_scan_mode_distances_agree_with_walk(golden):
+    """Both modes compute a record's filter distance with the reference's formula:
+    every record in the walk's filter heap that the scan also keeps has the same
+    distance bits, and the scan keeps at least as good a filter_topk."""
+    name, z, index_dir = golden
+    P, T, k = [int(v) for v in z["params"]]
+    ix = oracle.OracleIndex(index_dir)
+    for i in range(0, z["queries"].shape[0], 4):
+        _, _, _, _, tw = ix.search_one(z["queries"][i], k, P, T, topk_max=k, trace=True)
+        _, _, _, _, ts = ix.search_one(z["queries"][i], k, P, T, topk_max=k, trace=True,
+                                       scan=True)
+        walk = dict(zip(tw["filter_tag"][:tw["filter_cnt"]].tolist(),
+                        _bits(tw["filter_dist"][:tw["filter_cnt"]]).tolist()))
+        scan = dict(zip(ts["filter_tag"][:ts["filter_cnt"]].tolist(),
+                        _bits(ts["filter_dist"][:ts["filter_cnt"]]).tolist()))
+        for tag in set(walk) & set(scan):
+            assert walk[tag] == scan[tag]
+        assert ts["filter_cnt"] >= tw["filter_cnt"]
+        ws = np.sort(tw["filter_dist"][:tw["filter_cnt"]])
+        ss = ts["filter_dist"][:ts["filter_cnt"]]
+        assert np.all(ss[:len(ws)] <= ws)
