@@ -39,11 +39,11 @@ METRIC = "QPS at recall@10=0.95, learned+BF16 vs plain GPU path, 1 GB300; p50/p9
 
 WORKLOADS = {
     "cosine_10m": dict(n=10_000_000, d=96, ncomp=4096, kind="unit", C=2000, F=2000, nsq=24,
-                       T=500, k=10, sweep=(50, 100, 200), scan_sweep=(4, 8, 16, 32),
+                       T=500, k=10, sweep=(50, 100, 200), scan_sweep=(1, 2, 3, 4, 8, 16),
                        nq=10000, norm=True, train_sample=500_000, iters=12, pq_sample=262_144),
     # reduced workload for quick checks only (never the reported line)
     "cosine_1m": dict(n=1_000_000, d=96, ncomp=4096, kind="unit", C=500, F=500, nsq=24,
-                      T=500, k=10, sweep=(25, 50, 100), scan_sweep=(4, 8, 16), nq=10000,
+                      T=500, k=10, sweep=(25, 50, 100), scan_sweep=(1, 2, 4, 8), nq=10000,
                       norm=True, train_sample=200_000, iters=10, pq_sample=131_072),
 }
 TARGET_RECALL = 0.95
