@@ -153,6 +153,22 @@ int pgpu_close(pgpu_index* index);
 int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* points,
                         uint64_t n, int32_t* assign, float* distance, void* stream);
 
+/* The k-means assignment step of pgpu_nearest_center, allocating no device
+ * memory. No counterpart in the reference: it exists for callers that must not
+ * allocate GPU memory (a process that hands out device memory from its own pool,
+ * or code that must not enter the CUDA allocator). pgpu_nearest_center allocates
+ * its norm scratch on every call; this variant keeps it in a fixed array inside
+ * the library instead (4.25 MiB held on each GPU that loads the library, until
+ * exit), so it takes at most 1048576 points and 65536 centroids per call
+ * (PGPU_E_LIMIT beyond). It runs on the calling thread's current device; its
+ * first call on a device looks up the array's device address and should come
+ * before any stream capture. All calls on a device share the array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller. Results
+ * are identical to pgpu_nearest_center's. */
+int pgpu_nearest_center_noalloc(uint32_t dim, const float* centroids, uint64_t k,
+                                const float* points, uint64_t n, int32_t* assign,
+                                float* distance, void* stream);
+
 const char* pgpu_last_error(void);
 
 #ifdef __cplusplus

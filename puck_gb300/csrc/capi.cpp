@@ -264,6 +264,10 @@ int open_common(const pgpu_index_arrays& a, const pgpu_params* params, pgpu_inde
 
 }  // namespace
 
+namespace pgpu {
+int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace pgpu
+
 extern "C" {
 
 void pgpu_params_default(pgpu_params* p) {

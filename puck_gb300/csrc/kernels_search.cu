@@ -542,4 +542,15 @@ cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, 
     return e;
 }
 
+cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint64_t k,
+                                          const float* x, uint64_t n, int32_t* assign, float* dis,
+                                          float* xnorm, float* cnorm, cudaStream_t stream) {
+    k_norms_full<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(x, n, dim, xnorm);
+    k_norms_full<<<(unsigned)((k + 255) / 256), 256, 0, stream>>>(cents, k, dim, cnorm);
+    k_nearest_center<<<(unsigned)((n + kTile - 1) / kTile), 256, 0, stream>>>(x, n, cents, k, dim,
+                                                                             xnorm, cnorm, assign,
+                                                                             dis);
+    return cudaGetLastError();
+}
+
 }  // namespace pgpu

@@ -86,6 +86,13 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
                           int32_t* out_status, cudaStream_t stream);
 cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, const float* x,
                                   uint64_t n, int32_t* assign, float* dis, cudaStream_t stream);
+// nearest_center with caller-provided scratch for the point and centroid norms
+// (xnorm: n floats, cnorm: k floats); launches the same kernels as launch_nearest_center.
+cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint64_t k,
+                                          const float* x, uint64_t n, int32_t* assign, float* dis,
+                                          float* xnorm, float* cnorm, cudaStream_t stream);
+// Records `msg` as the calling thread's last error (pgpu_last_error) and returns `code`.
+int set_last_error(int code, const std::string& msg);
 cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
                                   uint32_t K, float* out_val, uint32_t* out_idx,
                                   const int32_t* status, cudaStream_t stream);

@@ -30,7 +30,10 @@ EXPORTED_SYMBOLS = (
     "pgpu_search_batch", "pgpu_search", "pgpu_search_batch_device", "pgpu_index_info_get",
     "pgpu_last_stats", "pgpu_close", "pgpu_nearest_center", "pgpu_last_error",
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
+    "pgpu_nearest_center_noalloc",
 )
+NOALLOC_MAX_POINTS = 1 << 20
+NOALLOC_MAX_CENTROIDS = 1 << 16
 WALK_COUNTERS = ("records", "cells", "fd_order_chunks", "enumerations", "fd_order_clusters",
                  "heap_inserts", "cyc_replay", "cyc_total", "cyc_prologue", "cyc_candidates",
                  "cyc_adc")
@@ -102,6 +105,7 @@ def load(build_if_missing=False):
                                     ctypes.POINTER(u64)]
     lib.pgpu_close.argtypes = [vp]
     lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
+    lib.pgpu_nearest_center_noalloc.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
     lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.pgpu_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), u32]
     lib.pgpu_walk_counters.argtypes = [vp, ctypes.POINTER(u64), u32]
@@ -270,3 +274,15 @@ def nearest_center(centroids, points, assign, distance, stream=None):
         s = s.cuda_stream
     return check(load().pgpu_nearest_center(dim, _ptr(centroids), k, _ptr(points), n,
                                             _ptr(assign), _ptr(distance), s))
+
+
+def nearest_center_noalloc(centroids, points, assign, distance, stream=None):
+    """Same as nearest_center, without any device allocation inside the library
+    (at most NOALLOC_MAX_POINTS points and NOALLOC_MAX_CENTROIDS centroids)."""
+    k, dim = centroids.shape
+    n = points.shape[0]
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    return check(load().pgpu_nearest_center_noalloc(dim, _ptr(centroids), k, _ptr(points), n,
+                                                    _ptr(assign), _ptr(distance), s))
