@@ -212,104 +212,99 @@ __global__ void k_topsort(const float* __restrict__ vals, uint32_t L, uint32_t L
     }
 }
 
-// L2Sqr16Ext + L2SqrExt order of the AVX build
-// (puck/tinker/method/hnsw_distfunc_opt_impl_inline.h:41-122).
-__device__ __forceinline__ float l2_rerank(const float* __restrict__ x, const float* q, uint32_t d) {
-    float t = 0.0f;
-    uint32_t m = 0;
-    for (; m + 16 <= d; m += 16) {
-        float cs = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const float a = __fsub_rn(__ldg(x + m + i), q[m + i]);
-            const float b = __fsub_rn(__ldg(x + m + i + 8), q[m + i + 8]);
-            const float s = __fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b));
-            cs = (i == 0) ? s : __fadd_rn(cs, s);
-        }
-        t = __fadd_rn(t, cs);
-    }
-    if (m < d) {
-        const uint32_t qty = d - m;
-        float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f, l3 = 0.0f;
-        uint32_t i = 0;
-        for (; i + 4 <= qty; i += 4) {
-            const float a0 = __fsub_rn(__ldg(x + m + i), q[m + i]);
-            const float a1 = __fsub_rn(__ldg(x + m + i + 1), q[m + i + 1]);
-            const float a2 = __fsub_rn(__ldg(x + m + i + 2), q[m + i + 2]);
-            const float a3 = __fsub_rn(__ldg(x + m + i + 3), q[m + i + 3]);
-            l0 = __fadd_rn(l0, __fmul_rn(a0, a0));
-            l1 = __fadd_rn(l1, __fmul_rn(a1, a1));
-            l2 = __fadd_rn(l2, __fmul_rn(a2, a2));
-            l3 = __fadd_rn(l3, __fmul_rn(a3, a3));
-        }
-        float s = __fadd_rn(__fadd_rn(__fadd_rn(l0, l1), l2), l3);
-        for (; i < qty; ++i) {
-            const float a = __fsub_rn(__ldg(x + m + i), q[m + i]);
-            s = __fadd_rn(s, __fmul_rn(a, a));
-        }
-        t = __fadd_rn(t, s);
-    }
-    return t;
-}
-
-struct RerankParams {
-    const float* q;
-    const int32_t* status;
-    const float* hdist;
-    const uint32_t* htag;
-    const uint32_t* hcnt;
-    const float* feat;
-    const uint32_t* mem2local;
-    float* out_dist;
-    uint32_t* out_ids;
-    int32_t* out_status;
-    uint32_t d, T, topk;
-};
-
-constexpr int kRerankThreads = 128;
-
-// One block per query: exact distances of the filter survivors in the order the
-// reference walks them (heap layout when the filter heap is full, ascending
-// otherwise), then MaxHeap(topk) + reorder() on one thread.
-__global__ __launch_bounds__(kRerankThreads) void k_rerank(RerankParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    float* qv = reinterpret_cast<float*>(smem);
-    float* dist = qv + p.d;                         // [T]
-    float* hv = dist + p.T;                         // [topk + 1]
-    uint32_t* ht = reinterpret_cast<uint32_t*>(hv + p.topk + 1);
-    const uint32_t qi = blockIdx.x;
-    const uint32_t topk = p.topk;
-    float* od = p.out_dist + (uint64_t)qi * topk;
-    uint32_t* oi = p.out_ids + (uint64_t)qi * topk;
-    const int32_t stq = p.status[qi];
-    if (p.out_status && threadIdx.x == 0) p.out_status[qi] = stq;
-    if (stq != 0) {
-        for (uint32_t i = threadIdx.x; i < topk; i += kRerankThreads) {
-            od[i] = sentinel_f();
+// Top-K of a row for small K (K + 1 <= 32): K + 1 passes, each taking the smallest
+// (value, index) key above the previous one with a block-wide min. Same output
+// and tie rule as k_topsort: when no two of the K+1 smallest values are equal the
+// ascending order is what MaxHeap(K) + reorder() gives; otherwise thread 0
+// replays the heap exactly.
+constexpr int kSelThreads = 128;
+__global__ __launch_bounds__(kSelThreads) void k_topsel_small(
+    const float* __restrict__ vals, uint32_t L, uint32_t ld, uint32_t K, float* __restrict__ out_val,
+    uint32_t* __restrict__ out_idx, const int32_t* __restrict__ status) {
+    extern __shared__ float sval[];  // [L]
+    __shared__ float red_v[kSelThreads / 32];
+    __shared__ uint32_t red_i[kSelThreads / 32];
+    __shared__ float sel_v[33];
+    __shared__ uint32_t sel_i[33];
+    __shared__ float heap_v[33];
+    __shared__ uint32_t heap_t[33];
+    const uint32_t row = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float* ov = out_val + (uint64_t)row * K;
+    uint32_t* oi = out_idx + (uint64_t)row * K;
+    if (status != nullptr && status[row] != 0) {
+        for (uint32_t i = tid; i < K; i += kSelThreads) {
+            ov[i] = sentinel_f();
             oi[i] = kNoLabel;
         }
         return;
     }
-    const uint32_t cnt = p.hcnt[qi];
-    for (uint32_t i = threadIdx.x; i < p.d; i += kRerankThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    const float* v = vals + (uint64_t)row * ld;
+    for (uint32_t i = tid; i < L; i += kSelThreads) sval[i] = v[i];
     __syncthreads();
-    const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
-    for (uint32_t j = threadIdx.x; j < cnt; j += kRerankThreads)
-        dist[j] = l2_rerank(p.feat + (uint64_t)tags[j] * p.d, qv, p.d);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float* h1 = hv - 0;  // hv[0] unused, hv[1..topk]
-        for (uint32_t i = 1; i <= topk; ++i) h1[i] = sentinel_f();
-        uint32_t dpc = topk;
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const float v = dist[j];
-            if (v < h1[1]) heap_update(h1, ht, topk, dpc, v, p.mem2local[tags[j]]);
+    const uint32_t picks = K + 1 < L ? K + 1 : L;
+    float lv = __int_as_float(0xff800000);  // -inf
+    uint32_t li = 0;
+    bool first = true;
+    for (uint32_t r = 0; r < picks; ++r) {
+        float bv = __int_as_float(0x7f800000);
+        uint32_t bi = 0xFFFFFFFFu;
+        for (uint32_t i = tid; i < L; i += kSelThreads) {
+            const float x = sval[i];
+            const bool above = first || x > lv || (x == lv && i > li);
+            if (above && (x < bv || (x == bv && i < bi))) {
+                bv = x;
+                bi = i;
+            }
         }
-        heap_reorder(h1, ht, topk);
-        const uint32_t rn = topk - dpc;
-        for (uint32_t i = 0; i < topk; ++i) {
-            od[i] = h1[i + 1];
-            oi[i] = i < rn ? ht[i + 1] : kNoLabel;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov2 = __shfl_down_sync(0xffffffffu, bv, o);
+            const uint32_t oi2 = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ov2 < bv || (ov2 == bv && oi2 < bi)) {
+                bv = ov2;
+                bi = oi2;
+            }
+        }
+        if (lane == 0) {
+            red_v[warp] = bv;
+            red_i[warp] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            float fv = red_v[0];
+            uint32_t fi = red_i[0];
+            for (int w = 1; w < kSelThreads / 32; ++w)
+                if (red_v[w] < fv || (red_v[w] == fv && red_i[w] < fi)) {
+                    fv = red_v[w];
+                    fi = red_i[w];
+                }
+            sel_v[r] = fv;
+            sel_i[r] = fi;
+        }
+        __syncthreads();
+        lv = sel_v[r];
+        li = sel_i[r];
+        first = false;
+    }
+    bool tie = false;
+    for (uint32_t r = 0; r + 1 < picks; ++r) tie |= (sel_v[r] == sel_v[r + 1]);
+    if (!tie) {
+        for (uint32_t i = tid; i < K; i += kSelThreads) {
+            ov[i] = sel_v[i];
+            oi[i] = sel_i[i];
+        }
+        return;
+    }
+    if (tid == 0) {
+        // heap arrays are 1-based: slots 1..K of 33
+        for (uint32_t i = 1; i <= K; ++i) heap_v[i] = sentinel_f();
+        uint32_t dpc = K;
+        for (uint32_t i = 0; i < L; ++i) heap_update(heap_v, heap_t, K, dpc, sval[i], i);
+        heap_reorder(heap_v, heap_t, K);
+        for (uint32_t i = 0; i < K; ++i) {
+            ov[i] = heap_v[i + 1];
+            oi[i] = heap_t[i + 1];
         }
     }
 }
@@ -472,6 +467,17 @@ static uint32_t next_pow2(uint32_t v) {
 cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
                                   uint32_t K, float* out_val, uint32_t* out_idx,
                                   const int32_t* status, cudaStream_t stream) {
+    if (K < L && K + 1 <= 32) {
+        static bool sel_attr = false;
+        if (!sel_attr) {
+            cudaFuncSetAttribute(k_topsel_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 220 * 1024);
+            sel_attr = true;
+        }
+        k_topsel_small<<<nrows, kSelThreads, (size_t)L * sizeof(float), stream>>>(
+            vals, L, ld_vals, K, out_val, out_idx, status);
+        return cudaGetLastError();
+    }
     const uint32_t Lp = next_pow2(L < 2 ? 2 : L);
     const size_t smem = (size_t)Lp * 8;
     static bool attr_set = false;
@@ -486,38 +492,6 @@ cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L,
 cudaError_t launch_topsort(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
                            uint32_t K, float* out_val, uint32_t* out_idx, cudaStream_t stream) {
     return launch_topsort_status(vals, nrows, L, ld_vals, K, out_val, out_idx, nullptr, stream);
-}
-
-size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
-    return sizeof(float) * (ix.d + T) + (sizeof(float) + sizeof(uint32_t)) * (topk + 1);
-}
-
-cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
-                          uint32_t topk, const Scratch& s, float* out_dist, uint32_t* out_ids,
-                          int32_t* out_status, cudaStream_t stream) {
-    (void)cfg;
-    RerankParams p;
-    p.q = s.q;
-    p.status = s.status;
-    p.hdist = s.hdist;
-    p.htag = s.htag;
-    p.hcnt = s.hcnt;
-    p.feat = ix.feat;
-    p.mem2local = ix.mem2local;
-    p.out_dist = out_dist;
-    p.out_ids = out_ids;
-    p.out_status = out_status;
-    p.d = ix.d;
-    p.T = s.T;
-    p.topk = topk;
-    const size_t smem = rerank_smem_bytes(ix, s.T, topk);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr_set = true;
-    }
-    k_rerank<<<n, kRerankThreads, smem, stream>>>(p);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, const float* x,

@@ -1,0 +1,216 @@
+// k_rerank: rank_topN_points, Puck-Flat branch (puck/puck/puck_index.cpp:428-457):
+// the exact FP32 squared L2 of every filter survivor against its original vector,
+// then MaxHeap(topk) fed in the order the survivors are given, then reorder().
+//
+// One block per query. Each warp computes one candidate at a time with coalesced
+// row loads; the sum follows the AVX build of L2Sqr16Ext / L2SqrExt
+// (puck/tinker/method/hnsw_distfunc_opt_impl_inline.h:41-122): per 16-dim chunk,
+// lane i<8 holds d_i^2 + d_{i+8}^2, the 8 lanes are added left to right, chunks
+// are added to the running total in order; a tail under 16 dims uses 4 lane
+// accumulators, ((l0+l1)+l2)+l3, then a scalar loop. The early abandon of the
+// reference only ever rejects candidates the heap would reject, so full sums give
+// the same result.
+//
+// Selection: when no two of the topk+1 smallest distances are equal the heap's
+// output is just the ascending order, found by a bitonic sort of
+// (distance, position); otherwise thread 0 replays the heap exactly.
+#include "device_common.cuh"
+#include "pgpu_internal.h"
+
+namespace pgpu {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+struct RerankParams {
+    const float* q;
+    const int32_t* status;
+    const uint32_t* htag;
+    const uint32_t* hcnt;
+    const float* feat;
+    const uint32_t* mem2local;
+    float* out_dist;
+    uint32_t* out_ids;
+    int32_t* out_status;
+    uint32_t d, T, Tp, topk;
+};
+
+// Exact-order squared L2 of row x against q (shared memory), computed by one warp;
+// the value is returned on every lane.
+__device__ __forceinline__ float warp_l2_exact(const float* __restrict__ x, const float* q,
+                                               uint32_t d, int lane) {
+    const uint32_t d16 = d & ~15u;
+    float t = 0.0f;
+    for (uint32_t base = 0; base < d16; base += 32) {
+        const uint32_t e = base + lane;
+        float sq = 0.0f;
+        if (e < d16) {
+            const float a = __fsub_rn(__ldg(x + e), q[e]);
+            sq = __fmul_rn(a, a);
+        }
+        // lanes 0-7 (chunk at base) and 16-23 (chunk at base+16): d_i^2 + d_{i+8}^2
+        const float s = __fadd_rn(sq, __shfl_down_sync(0xffffffffu, sq, 8));
+        const int grp = lane & 16;
+        float acc = __shfl_sync(0xffffffffu, s, grp);
+#pragma unroll
+        for (int i = 1; i < 8; ++i) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, s, grp + i));
+        const float acc_b = __shfl_sync(0xffffffffu, acc, 16);
+        t = __fadd_rn(t, acc);                       // chunk at base (lane 0's acc)
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (base + 16 < d16) t = __fadd_rn(t, acc_b);  // chunk at base + 16
+    }
+    if (d16 < d) {  // L2SqrExt on the last d - d16 < 16 dims, serially
+        const uint32_t qty = d - d16;
+        float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f, l3 = 0.0f;
+        uint32_t i = 0;
+        for (; i + 4 <= qty; i += 4) {
+            const float a0 = __fsub_rn(__ldg(x + d16 + i), q[d16 + i]);
+            const float a1 = __fsub_rn(__ldg(x + d16 + i + 1), q[d16 + i + 1]);
+            const float a2 = __fsub_rn(__ldg(x + d16 + i + 2), q[d16 + i + 2]);
+            const float a3 = __fsub_rn(__ldg(x + d16 + i + 3), q[d16 + i + 3]);
+            l0 = __fadd_rn(l0, __fmul_rn(a0, a0));
+            l1 = __fadd_rn(l1, __fmul_rn(a1, a1));
+            l2 = __fadd_rn(l2, __fmul_rn(a2, a2));
+            l3 = __fadd_rn(l3, __fmul_rn(a3, a3));
+        }
+        float s = __fadd_rn(__fadd_rn(__fadd_rn(l0, l1), l2), l3);
+        for (; i < qty; ++i) {
+            const float a = __fsub_rn(__ldg(x + d16 + i), q[d16 + i]);
+            s = __fadd_rn(s, __fmul_rn(a, a));
+        }
+        t = __fadd_rn(t, s);
+    }
+    return t;
+}
+
+__global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* qv = reinterpret_cast<float*>(smem);
+    float* dist = qv + p.d;                                   // [T]
+    float* sv = dist + p.T;                                   // [Tp]
+    uint32_t* si = reinterpret_cast<uint32_t*>(sv + p.Tp);    // [Tp]
+    const uint32_t qi = blockIdx.x, topk = p.topk;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float* od = p.out_dist + (uint64_t)qi * topk;
+    uint32_t* oi = p.out_ids + (uint64_t)qi * topk;
+    const int32_t stq = p.status[qi];
+    if (p.out_status && tid == 0) p.out_status[qi] = stq;
+    if (stq != 0) {
+        for (uint32_t i = tid; i < topk; i += kThreads) {
+            od[i] = sentinel_f();
+            oi[i] = kNoLabel;
+        }
+        return;
+    }
+    const uint32_t cnt = p.hcnt[qi];
+    const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
+    for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    __syncthreads();
+    for (uint32_t j = warp; j < cnt; j += kWarps) {
+        const float v = warp_l2_exact(p.feat + (uint64_t)tags[j] * p.d, qv, p.d, lane);
+        if (lane == 0) dist[j] = v;
+    }
+    __syncthreads();
+    // (distance, position) pairs, ascending
+    for (uint32_t i = tid; i < p.Tp; i += kThreads) {
+        sv[i] = i < cnt ? dist[i] : __int_as_float(0x7f800000);
+        si[i] = i < cnt ? i : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= p.Tp; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = tid; t < p.Tp / 2; t += kThreads) {
+                const uint32_t lo = 2 * t - (t & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const float a = sv[lo], b = sv[hi];
+                const uint32_t ia = si[lo], ib = si[hi];
+                const bool gt = (a > b) || (a == b && ia > ib);
+                if (gt == asc) {
+                    sv[lo] = b;
+                    sv[hi] = a;
+                    si[lo] = ib;
+                    si[hi] = ia;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const uint32_t keep = cnt < topk ? cnt : topk;
+    // ties that the heap could resolve differently: among the topk+1 smallest, or
+    // anywhere among the results when there are no more candidates than topk
+    const uint32_t check = cnt <= topk ? (cnt > 0 ? cnt - 1 : 0) : topk;
+    int tie = 0;
+    for (uint32_t i = tid; i < check; i += kThreads)
+        if (sv[i] == sv[i + 1]) tie = 1;
+    tie = __syncthreads_or(tie);
+    if (!tie) {
+        for (uint32_t i = tid; i < topk; i += kThreads) {
+            od[i] = i < keep ? sv[i] : sentinel_f();
+            oi[i] = i < keep ? p.mem2local[tags[si[i]]] : kNoLabel;
+        }
+        return;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // exact MaxHeap(topk) replay in candidate order, then reorder()
+        float* hv = sv - 1;
+        uint32_t* ht = si - 1;
+        for (uint32_t i = 1; i <= topk; ++i) hv[i] = sentinel_f();
+        uint32_t dpc = topk;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const float v = dist[j];
+            if (v < hv[1]) heap_update(hv, ht, topk, dpc, v, p.mem2local[tags[j]]);
+        }
+        heap_reorder(hv, ht, topk);
+        const uint32_t rn = topk - dpc;
+        for (uint32_t i = 0; i < topk; ++i) {
+            od[i] = hv[i + 1];
+            oi[i] = i < rn ? ht[i + 1] : kNoLabel;
+        }
+    }
+}
+
+uint32_t pow2_at_least(uint32_t v) {
+    uint32_t p = 2;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
+    const uint32_t Tp = pow2_at_least(T > topk ? T : topk);
+    return sizeof(float) * (ix.d + T) + (sizeof(float) + sizeof(uint32_t)) * Tp;
+}
+
+cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
+                          uint32_t topk, const Scratch& s, float* out_dist, uint32_t* out_ids,
+                          int32_t* out_status, cudaStream_t stream) {
+    (void)cfg;
+    RerankParams p;
+    p.q = s.q;
+    p.status = s.status;
+    p.htag = s.htag;
+    p.hcnt = s.hcnt;
+    p.feat = ix.feat;
+    p.mem2local = ix.mem2local;
+    p.out_dist = out_dist;
+    p.out_ids = out_ids;
+    p.out_status = out_status;
+    p.d = ix.d;
+    p.T = s.T;
+    p.Tp = pow2_at_least(s.T > topk ? s.T : topk);
+    p.topk = topk;
+    const size_t smem = rerank_smem_bytes(ix, s.T, topk);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        attr_set = true;
+    }
+    k_rerank<<<n, kThreads, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace pgpu
