@@ -41,6 +41,10 @@ WORKLOADS = {
     "cosine_10m": dict(n=10_000_000, d=96, ncomp=4096, kind="unit", C=2000, F=2000, nsq=24,
                        T=500, k=10, sweep=(50, 100, 200), scan_sweep=(1, 2, 3, 4, 8, 16),
                        nq=10000, norm=True, train_sample=500_000, iters=12, pq_sample=262_144),
+    # profiling case for ncu: codes + offsets (150 MB) larger than L2, ~5 GB on the device
+    "cosine_5m": dict(n=5_000_000, d=96, ncomp=4096, kind="unit", C=1414, F=1414, nsq=24,
+                      T=500, k=10, sweep=(50,), scan_sweep=(4,), nq=10000, norm=True,
+                      train_sample=300_000, iters=10, pq_sample=131_072),
     # reduced workload for quick checks only (never the reported line)
     "cosine_1m": dict(n=1_000_000, d=96, ncomp=4096, kind="unit", C=500, F=500, nsq=24,
                       T=500, k=10, sweep=(25, 50, 100), scan_sweep=(1, 2, 4, 8), nq=10000,
