@@ -276,6 +276,7 @@ def run_gpu(args, w, rank, ws):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
+        torch.cuda.nvtx.range_push("timed")
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         start.record(stream)
@@ -285,6 +286,7 @@ def run_gpu(args, w, rank, ws):
             evs[i][1].record(stream)
         end.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     total_ms = start.elapsed_time(end)
     step_ms = np.array([a.elapsed_time(b) for a, b in evs])
     if ws > 1:

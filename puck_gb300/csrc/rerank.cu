@@ -36,52 +36,69 @@ struct RerankParams {
     uint32_t d, T, Tp, topk;
 };
 
-// Exact-order squared L2 of row x against q (shared memory), computed by one warp;
-// the value is returned on every lane.
-__device__ __forceinline__ float warp_l2_exact(const float* __restrict__ x, const float* q,
-                                               uint32_t d, int lane) {
+// Exact-order squared L2 of G rows against q (shared memory), computed by one
+// warp with the G rows' loads in flight together; results on every lane.
+template <int G>
+__device__ __forceinline__ void warp_l2_exact(const float* const* rows, const float* q, uint32_t d,
+                                              int lane, float* out) {
     const uint32_t d16 = d & ~15u;
-    float t = 0.0f;
+    float t[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) t[u] = 0.0f;
+    const int grp = lane & 16;
     for (uint32_t base = 0; base < d16; base += 32) {
         const uint32_t e = base + lane;
-        float sq = 0.0f;
-        if (e < d16) {
-            const float a = __fsub_rn(__ldg(x + e), q[e]);
-            sq = __fmul_rn(a, a);
-        }
-        // lanes 0-7 (chunk at base) and 16-23 (chunk at base+16): d_i^2 + d_{i+8}^2
-        const float s = __fadd_rn(sq, __shfl_down_sync(0xffffffffu, sq, 8));
-        const int grp = lane & 16;
-        float acc = __shfl_sync(0xffffffffu, s, grp);
+        float sq[G];
 #pragma unroll
-        for (int i = 1; i < 8; ++i) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, s, grp + i));
-        const float acc_b = __shfl_sync(0xffffffffu, acc, 16);
-        t = __fadd_rn(t, acc);                       // chunk at base (lane 0's acc)
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (base + 16 < d16) t = __fadd_rn(t, acc_b);  // chunk at base + 16
+        for (int u = 0; u < G; ++u) {
+            sq[u] = 0.0f;
+            if (e < d16) {
+                const float a = __fsub_rn(__ldg(rows[u] + e), q[e]);
+                sq[u] = __fmul_rn(a, a);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            // lanes 0-7 (chunk at base) and 16-23 (chunk at base+16): d_i^2 + d_{i+8}^2
+            const float s = __fadd_rn(sq[u], __shfl_down_sync(0xffffffffu, sq[u], 8));
+            float acc = __shfl_sync(0xffffffffu, s, grp);
+#pragma unroll
+            for (int i = 1; i < 8; ++i) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, s, grp + i));
+            const float acc_b = __shfl_sync(0xffffffffu, acc, 16);
+            float tu = __fadd_rn(t[u], acc);               // chunk at base (lane 0's acc)
+            tu = __shfl_sync(0xffffffffu, tu, 0);
+            if (base + 16 < d16) tu = __fadd_rn(tu, acc_b);  // chunk at base + 16
+            t[u] = tu;
+        }
     }
     if (d16 < d) {  // L2SqrExt on the last d - d16 < 16 dims, serially
         const uint32_t qty = d - d16;
-        float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f, l3 = 0.0f;
-        uint32_t i = 0;
-        for (; i + 4 <= qty; i += 4) {
-            const float a0 = __fsub_rn(__ldg(x + d16 + i), q[d16 + i]);
-            const float a1 = __fsub_rn(__ldg(x + d16 + i + 1), q[d16 + i + 1]);
-            const float a2 = __fsub_rn(__ldg(x + d16 + i + 2), q[d16 + i + 2]);
-            const float a3 = __fsub_rn(__ldg(x + d16 + i + 3), q[d16 + i + 3]);
-            l0 = __fadd_rn(l0, __fmul_rn(a0, a0));
-            l1 = __fadd_rn(l1, __fmul_rn(a1, a1));
-            l2 = __fadd_rn(l2, __fmul_rn(a2, a2));
-            l3 = __fadd_rn(l3, __fmul_rn(a3, a3));
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            const float* x = rows[u] + d16;
+            const float* qq = q + d16;
+            float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f, l3 = 0.0f;
+            uint32_t i = 0;
+            for (; i + 4 <= qty; i += 4) {
+                const float a0 = __fsub_rn(__ldg(x + i), qq[i]);
+                const float a1 = __fsub_rn(__ldg(x + i + 1), qq[i + 1]);
+                const float a2 = __fsub_rn(__ldg(x + i + 2), qq[i + 2]);
+                const float a3 = __fsub_rn(__ldg(x + i + 3), qq[i + 3]);
+                l0 = __fadd_rn(l0, __fmul_rn(a0, a0));
+                l1 = __fadd_rn(l1, __fmul_rn(a1, a1));
+                l2 = __fadd_rn(l2, __fmul_rn(a2, a2));
+                l3 = __fadd_rn(l3, __fmul_rn(a3, a3));
+            }
+            float sum = __fadd_rn(__fadd_rn(__fadd_rn(l0, l1), l2), l3);
+            for (; i < qty; ++i) {
+                const float a = __fsub_rn(__ldg(x + i), qq[i]);
+                sum = __fadd_rn(sum, __fmul_rn(a, a));
+            }
+            t[u] = __fadd_rn(t[u], sum);
         }
-        float s = __fadd_rn(__fadd_rn(__fadd_rn(l0, l1), l2), l3);
-        for (; i < qty; ++i) {
-            const float a = __fsub_rn(__ldg(x + d16 + i), q[d16 + i]);
-            s = __fadd_rn(s, __fmul_rn(a, a));
-        }
-        t = __fadd_rn(t, s);
     }
-    return t;
+#pragma unroll
+    for (int u = 0; u < G; ++u) out[u] = t[u];
 }
 
 __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
@@ -107,9 +124,22 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     __syncthreads();
-    for (uint32_t j = warp; j < cnt; j += kWarps) {
-        const float v = warp_l2_exact(p.feat + (uint64_t)tags[j] * p.d, qv, p.d, lane);
-        if (lane == 0) dist[j] = v;
+    // four rows per warp in flight: their tags are read up front so the row loads
+    // of the unrolled calls can overlap
+    for (uint32_t j0 = warp * 4; j0 < cnt; j0 += kWarps * 4) {
+        const float* rows[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t j = j0 + u;
+            rows[u] = p.feat + (uint64_t)tags[j < cnt ? j : j0] * p.d;
+        }
+        float v[4];
+        warp_l2_exact<4>(rows, qv, p.d, lane, v);
+        if (lane == 0) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j0 + u < cnt) dist[j0 + u] = v[u];
+        }
     }
     __syncthreads();
     // (distance, position) pairs, ascending

@@ -92,7 +92,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     const uint32_t nsq = p.nsq, F = p.F, T = p.T;
     float* lut = reinterpret_cast<float*>(smem);
     float* fdk = lut + nsq * 256;          // [F]
-    float* srow = fdk + F;                 // [F] stationary row of the current cluster
+    float* srow = fdk + F;                 // [F] 2 * cell_dist of the current cluster's cells
     float* cv = srow + F;                  // [kCandCap]
     uint32_t* ci = reinterpret_cast<uint32_t*>(cv + kCandCap);
     float* qv = reinterpret_cast<float*>(ci + kCandCap);  // [d]
@@ -133,7 +133,9 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         const uint32_t c = st.c, r0 = st.r0, r1 = st.r1;
         const float cdl = st.cdl;
         if (r0 >= r1) continue;
-        for (uint32_t i = tid; i < F; i += kThreads) srow[i] = p.stationary[(uint64_t)c * F + i];
+        // per fine id of this cluster: 2 * cell_dist, cell_dist = (cd + stationary) + fd
+        for (uint32_t i = tid; i < F; i += kThreads)
+            srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
         __syncthreads();
         for (uint32_t base = r0; base < r1; base += kRound) {
             const float tv = st.tau_v;
@@ -141,19 +143,33 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
 #pragma unroll
             for (int j = 0; j < kRecPerThread; ++j) {
                 const uint32_t mi = base + tid + j * kThreads;
-                if (mi >= r1) break;
-                const uint32_t f = p.rec_fine[mi];
-                const float cell_dist = __fadd_rn(__fadd_rn(cdl, srow[f]), fdk[f]);
-                const float t0 = adc_base(cell_dist, p.offsets[mi]);
-                ++my_eval;
-                if (!key_less(t0, mi, tv, ti)) continue;
-                const float t =
-                    __fadd_rn(t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
-                if (!key_less(t, mi, tv, ti)) continue;
-                ++my_pass;
-                const uint32_t slot = atomicAdd(&st.count, 1u);
-                cv[slot] = t;  // capacity is kept >= count + kRound by the compaction below
-                ci[slot] = mi;
+                bool keep = false;
+                float t = 0.0f;
+                if (mi < r1) {
+                    // (float)(2.0 * cell_dist + offset): one float add of the exact
+                    // 2 * cell_dist (see adc_base)
+                    const float t0 = __fadd_rn(srow[p.rec_fine[mi]], p.offsets[mi]);
+                    ++my_eval;
+                    if (key_less(t0, mi, tv, ti)) {
+                        t = __fadd_rn(t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
+                        keep = key_less(t, mi, tv, ti);
+                    }
+                }
+                // one shared atomic per warp for the kept records
+                const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+                if (ballot) {
+                    const int lane = tid & 31;
+                    uint32_t base_slot = 0;
+                    if (lane == __ffs(ballot) - 1) base_slot = atomicAdd(&st.count, (uint32_t)__popc(ballot));
+                    base_slot = __shfl_sync(0xffffffffu, base_slot, __ffs(ballot) - 1);
+                    if (keep) {
+                        // capacity is kept >= count + kRound by the compaction below
+                        const uint32_t slot = base_slot + __popc(ballot & ((1u << lane) - 1));
+                        cv[slot] = t;
+                        ci[slot] = mi;
+                        ++my_pass;
+                    }
+                }
             }
             __syncthreads();
             if (st.count > kCandCap - kRound) {
