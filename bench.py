@@ -400,7 +400,7 @@ def run_gpu(args, w, rank, ws):
             "stage_ms": {kk: round(v, 4) for kk, v in stage.items()},
             "walk_records_scanned": recs,
             "walk_cells_scanned": cells,
-            "walk_counters": walk_counters,
+            "filter_counters": walk_counters,
             "parallelism": f"replicas x{ws}",
         },
         "e2e": {"value": round(e2e_value, 1), "unit": "queries/s",

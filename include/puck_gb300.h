@@ -137,11 +137,14 @@ int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
 int pgpu_set_profiling(pgpu_index* index, int enable);
 int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
 
-/* Diagnostic counters of the cell walk for the last pgpu_search_batch call, summed
- * over queries: 0 filter records scanned, 1 cells scanned, 2 fine-order chunks,
- * 3 stationary-order enumerations, 4 coarse clusters walked in fine order, 5 heap
- * inserts, then thread-0 clock cycles: 6 replay, 7 whole walk, 8 prologue (LUT),
- * 9 candidate generation, 10 speculative ADC. Fills min(n, 11) values. */
+/* Diagnostic counters of the filter stage for the last pgpu_search_batch call,
+ * summed over queries. Exact mode: 0 filter records scanned, 1 cells scanned,
+ * 2 fine-order chunks, 3 stationary-order enumerations, 4 coarse clusters walked in
+ * fine order, 5 heap inserts, then thread-0 clock cycles: 6 replay, 7 whole walk,
+ * 8 prologue (LUT), 9 candidate generation, 10 speculative ADC. Scan mode:
+ * 0 records evaluated, 2 records kept, 3 buffer compactions, 5 most records of one
+ * query, then cycles: 6 prologue, 7 whole block, 8 record rounds, 9 compactions,
+ * 10 final sort. Fills min(n, 11) values. */
 int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
 
 int pgpu_close(pgpu_index* index);

@@ -74,6 +74,13 @@ __device__ void bitonic_sort(float* cv, uint32_t* ci, uint32_t cap) {
     }
 }
 
+// Diagnostic counters (pgpu_walk_counters slots, summed per launch): 0 records
+// evaluated, 2 records kept, 3 compactions, 5 max records of one query, and
+// thread-0 clock cycles: 6 prologue (LUT, fine terms), 7 whole block, 8 record
+// rounds, 9 compaction sorts, 10 final sort + output.
+enum { kScRecords = 0, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCycPrologue = 6,
+       kScCycTotal = 7, kScCycRounds = 8, kScCycCompact = 9, kScCycFinal = 10 };
+
 struct ScanState {
     float tau_v;
     uint32_t tau_i;
@@ -82,6 +89,7 @@ struct ScanState {
     float cdl;
     uint32_t r0, r1;
     unsigned long long evaluated, passed;
+    unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
 
 __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
@@ -101,6 +109,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         if (tid == 0) p.hcnt[qi] = 0;
         return;
     }
+    const long long t_start = clock64();
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     for (uint32_t i = tid; i < F; i += kThreads) fdk[i] = p.fd_by_fine[(uint64_t)qi * F + i];
     if (tid == 0) {
@@ -109,6 +118,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         st.count = 0;
         st.evaluated = 0;
         st.passed = 0;
+        st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
     }
     __syncthreads();
     for (uint32_t e = tid; e < nsq * 256; e += kThreads) {
@@ -116,6 +126,8 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         lut[e] = l2sqr_sse(qv + m * p.lsq, p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
     }
     unsigned long long my_eval = 0, my_pass = 0;
+    __syncthreads();
+    const long long t_pro = clock64();
     for (uint32_t l = 0; l < p.P; ++l) {
         __syncthreads();
         if (tid == 0) {
@@ -137,7 +149,9 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         for (uint32_t i = tid; i < F; i += kThreads)
             srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
         __syncthreads();
+        if (tid == 0) st.n_records += r1 - r0;
         for (uint32_t base = r0; base < r1; base += kRound) {
+            const long long t_round = clock64();
             const float tv = st.tau_v;
             const uint32_t ti = st.tau_i;
 #pragma unroll
@@ -172,6 +186,8 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
                 }
             }
             __syncthreads();
+            const long long t_round_end = clock64();
+            if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
             if (st.count > kCandCap - kRound) {
                 // cut back to the T best; tau = the T-th (value, id)
                 for (uint32_t i = st.count + tid; i < kCandCap; i += kThreads) {
@@ -184,12 +200,15 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
                     st.count = T;
                     st.tau_v = cv[T - 1];
                     st.tau_i = ci[T - 1];
+                    st.n_compact += 1;
+                    st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
                 }
                 __syncthreads();
             }
         }
     }
     __syncthreads();
+    const long long t_final = clock64();
     const uint32_t count = st.count;
     for (uint32_t i = count + tid; i < kCandCap; i += kThreads) {
         cv[i] = __int_as_float(0x7f800000);
@@ -204,9 +223,19 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     }
     if (tid == 0) p.hcnt[qi] = out;
     if (p.counters) {
-        // records evaluated / passed the threshold (summed over the block)
-        atomicAdd(p.counters + 0, my_eval);
-        atomicAdd(p.counters + 2, my_pass);
+        // records evaluated / kept (summed over the block's threads)
+        atomicAdd(p.counters + kScRecords, my_eval);
+        atomicAdd(p.counters + kScKept, my_pass);
+        if (tid == 0) {
+            const long long t_end = clock64();
+            atomicAdd(p.counters + kScCompactions, st.n_compact);
+            atomicMax(p.counters + kScMaxRecords, st.n_records);
+            atomicAdd(p.counters + kScCycPrologue, (unsigned long long)(t_pro - t_start));
+            atomicAdd(p.counters + kScCycTotal, (unsigned long long)(t_end - t_start));
+            atomicAdd(p.counters + kScCycRounds, st.cyc_rounds);
+            atomicAdd(p.counters + kScCycCompact, st.cyc_compact);
+            atomicAdd(p.counters + kScCycFinal, (unsigned long long)(t_end - t_final));
+        }
     }
 }
 
