@@ -11,11 +11,11 @@
 // cluster is skipped: the result is the exact top-filter_topk by (t, memory id)
 // over all records of the probed clusters, a superset search of the same cells.
 //
-// Selection: a candidate buffer in shared memory with a running threshold tau =
-// the (t, id) of the current filter_topk-th best; records with
-// (2*cell_dist + offset, id) >= tau are dropped before the table lookups (t can
-// only grow). When the buffer fills it is bitonic-sorted and cut back to
-// filter_topk entries. The output is sorted ascending by (t, id).
+// Selection: a buffer of (t, id) keys in shared memory with a running threshold
+// tau = the key of the current filter_topk-th best; records whose
+// (2*cell_dist + offset, id) key is not below tau are dropped before the table
+// lookups (t can only grow). When the buffer fills it is bitonic-sorted and cut
+// back to filter_topk keys. The output is sorted ascending by (t, id).
 #include "device_common.cuh"
 #include "pgpu_internal.h"
 
@@ -23,9 +23,9 @@ namespace pgpu {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRecPerThread = 2;
+constexpr int kRecPerThread = 4;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
-constexpr uint32_t kCandCap = 2048;               // candidate buffer (power of two)
+constexpr uint32_t kCandCap = 4096;               // candidate buffer (power of two)
 
 struct ScanParams {
     const float* q;
@@ -47,31 +47,45 @@ struct ScanParams {
     uint32_t d, C, F, nsq, lsq, code_stride, P, T;
 };
 
-__device__ __forceinline__ bool key_less(float a, uint32_t ia, float b, uint32_t ib) {
-    return a < b || (a == b && ia < ib);
+// (t, memory id) packed into one 64-bit key whose unsigned order is the
+// lexicographic order of (t as a float, id): -0 is folded onto +0 so that equal
+// floats compare equal, and the IEEE bit pattern is made monotone.
+__device__ __forceinline__ uint64_t pack_key(float t, uint32_t id) {
+    uint32_t b = __float_as_uint(t == 0.0f ? 0.0f : t);
+    b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    return ((uint64_t)b << 32) | id;
 }
 
-// Sorts cv/ci[0..cap) ascending by (value, id); cap is a power of two.
-__device__ void bitonic_sort(float* cv, uint32_t* ci, uint32_t cap) {
-    for (uint32_t size = 2; size <= cap; size <<= 1) {
+__device__ __forceinline__ float key_value(uint64_t k) {
+    uint32_t b = (uint32_t)(k >> 32);
+    b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
+    return __uint_as_float(b);
+}
+
+constexpr uint64_t kKeyMax = ~0ull;
+
+// Sorts keys[0..n) ascending; n is a power of two.
+__device__ void bitonic_sort_keys(uint64_t* keys, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
         for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            for (uint32_t t = threadIdx.x; t < cap / 2; t += kThreads) {
+            for (uint32_t t = threadIdx.x; t < n / 2; t += kThreads) {
                 const uint32_t lo = 2 * t - (t & (stride - 1));
                 const uint32_t hi = lo + stride;
-                const bool asc = (lo & size) == 0;
-                const float a = cv[lo], b = cv[hi];
-                const uint32_t ia = ci[lo], ib = ci[hi];
-                const bool gt = key_less(b, ib, a, ia);
-                if (gt == asc) {
-                    cv[lo] = b;
-                    cv[hi] = a;
-                    ci[lo] = ib;
-                    ci[hi] = ia;
+                const uint64_t a = keys[lo], b = keys[hi];
+                if ((a > b) == ((lo & size) == 0)) {
+                    keys[lo] = b;
+                    keys[hi] = a;
                 }
             }
             __syncthreads();
         }
     }
+}
+
+__device__ __forceinline__ uint32_t pow2_ceil(uint32_t v) {
+    uint32_t p = 2;
+    while (p < v) p <<= 1;
+    return p;
 }
 
 // Diagnostic counters (pgpu_walk_counters slots, summed per launch): 0 records
@@ -82,8 +96,7 @@ enum { kScRecords = 0, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCy
        kScCycTotal = 7, kScCycRounds = 8, kScCycCompact = 9, kScCycFinal = 10 };
 
 struct ScanState {
-    float tau_v;
-    uint32_t tau_i;
+    uint64_t tau;
     uint32_t count;
     uint32_t c;
     float cdl;
@@ -98,12 +111,11 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     const uint32_t qi = blockIdx.x;
     const int tid = threadIdx.x;
     const uint32_t nsq = p.nsq, F = p.F, T = p.T;
-    float* lut = reinterpret_cast<float*>(smem);
+    float* lut = reinterpret_cast<float*>(smem + sizeof(uint64_t) * kCandCap);
     float* fdk = lut + nsq * 256;          // [F]
     float* srow = fdk + F;                 // [F] 2 * cell_dist of the current cluster's cells
-    float* cv = srow + F;                  // [kCandCap]
-    uint32_t* ci = reinterpret_cast<uint32_t*>(cv + kCandCap);
-    float* qv = reinterpret_cast<float*>(ci + kCandCap);  // [d]
+    uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [kCandCap], first (8-byte aligned)
+    float* qv = srow + F;                  // [d]
 
     if (p.status[qi] != 0) {
         if (tid == 0) p.hcnt[qi] = 0;
@@ -113,8 +125,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     for (uint32_t i = tid; i < F; i += kThreads) fdk[i] = p.fd_by_fine[(uint64_t)qi * F + i];
     if (tid == 0) {
-        st.tau_v = __int_as_float(0x7f800000);
-        st.tau_i = 0xFFFFFFFFu;
+        st.tau = kKeyMax;
         st.count = 0;
         st.evaluated = 0;
         st.passed = 0;
@@ -152,21 +163,22 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         if (tid == 0) st.n_records += r1 - r0;
         for (uint32_t base = r0; base < r1; base += kRound) {
             const long long t_round = clock64();
-            const float tv = st.tau_v;
-            const uint32_t ti = st.tau_i;
+            const uint64_t tau = st.tau;
 #pragma unroll
             for (int j = 0; j < kRecPerThread; ++j) {
                 const uint32_t mi = base + tid + j * kThreads;
                 bool keep = false;
-                float t = 0.0f;
+                uint64_t key = 0;
                 if (mi < r1) {
                     // (float)(2.0 * cell_dist + offset): one float add of the exact
                     // 2 * cell_dist (see adc_base)
                     const float t0 = __fadd_rn(srow[p.rec_fine[mi]], p.offsets[mi]);
                     ++my_eval;
-                    if (key_less(t0, mi, tv, ti)) {
-                        t = __fadd_rn(t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
-                        keep = key_less(t, mi, tv, ti);
+                    if (pack_key(t0, mi) < tau) {  // t can only grow past t0
+                        const float t = __fadd_rn(
+                            t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
+                        key = pack_key(t, mi);
+                        keep = key < tau;
                     }
                 }
                 // one shared atomic per warp for the kept records
@@ -178,9 +190,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
                     base_slot = __shfl_sync(0xffffffffu, base_slot, __ffs(ballot) - 1);
                     if (keep) {
                         // capacity is kept >= count + kRound by the compaction below
-                        const uint32_t slot = base_slot + __popc(ballot & ((1u << lane) - 1));
-                        cv[slot] = t;
-                        ci[slot] = mi;
+                        keys[base_slot + __popc(ballot & ((1u << lane) - 1))] = key;
                         ++my_pass;
                     }
                 }
@@ -189,17 +199,14 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
             const long long t_round_end = clock64();
             if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
             if (st.count > kCandCap - kRound) {
-                // cut back to the T best; tau = the T-th (value, id)
-                for (uint32_t i = st.count + tid; i < kCandCap; i += kThreads) {
-                    cv[i] = __int_as_float(0x7f800000);
-                    ci[i] = 0xFFFFFFFFu;
-                }
+                // cut back to the T best; tau = the T-th key
+                const uint32_t cnt = st.count, n2 = pow2_ceil(cnt);
+                for (uint32_t i = cnt + tid; i < n2; i += kThreads) keys[i] = kKeyMax;
                 __syncthreads();
-                bitonic_sort(cv, ci, kCandCap);
+                bitonic_sort_keys(keys, n2);
                 if (tid == 0) {
                     st.count = T;
-                    st.tau_v = cv[T - 1];
-                    st.tau_i = ci[T - 1];
+                    st.tau = keys[T - 1];
                     st.n_compact += 1;
                     st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
                 }
@@ -209,17 +216,14 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     }
     __syncthreads();
     const long long t_final = clock64();
-    const uint32_t count = st.count;
-    for (uint32_t i = count + tid; i < kCandCap; i += kThreads) {
-        cv[i] = __int_as_float(0x7f800000);
-        ci[i] = 0xFFFFFFFFu;
-    }
+    const uint32_t count = st.count, n2 = pow2_ceil(count);
+    for (uint32_t i = count + tid; i < n2; i += kThreads) keys[i] = kKeyMax;
     __syncthreads();
-    bitonic_sort(cv, ci, kCandCap);
+    bitonic_sort_keys(keys, n2);
     const uint32_t out = count < T ? count : T;
     for (uint32_t i = tid; i < T; i += kThreads) {
-        p.hdist[(uint64_t)qi * T + i] = i < out ? cv[i] : sentinel_f();
-        p.htag[(uint64_t)qi * T + i] = i < out ? ci[i] : kNoLabel;
+        p.hdist[(uint64_t)qi * T + i] = i < out ? key_value(keys[i]) : sentinel_f();
+        p.htag[(uint64_t)qi * T + i] = i < out ? (uint32_t)keys[i] : kNoLabel;
     }
     if (tid == 0) p.hcnt[qi] = out;
     if (p.counters) {
@@ -242,8 +246,8 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
 }  // namespace
 
 size_t scan_smem_bytes(const DeviceIndex& ix) {
-    return sizeof(float) * ix.nsq * 256 + sizeof(float) * 2 * ix.F +
-           (sizeof(float) + sizeof(uint32_t)) * kCandCap + sizeof(float) * ix.d;
+    return sizeof(uint64_t) * kCandCap + sizeof(float) * ix.nsq * 256 + sizeof(float) * 2 * ix.F +
+           sizeof(float) * ix.d;
 }
 
 uint32_t scan_max_filter_topk() { return kCandCap - kRound; }
