@@ -136,6 +136,25 @@ __device__ __forceinline__ float lut_sum(const uint8_t* __restrict__ code, const
     return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
 }
 
+// lookup_dist_table over codes already in registers: NW 32-bit words holding the
+// record's nsq codes (4 per word, little-endian); same order as lut_sum.
+template <int NW>
+__device__ __forceinline__ float lut_sum_words(const uint32_t (&w)[NW], const float* lut,
+                                               uint32_t nsq) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+        const uint32_t m = 4u * i;
+        if (m >= nsq) break;
+        const uint32_t c = w[i];
+        a0 = __fadd_rn(a0, lut[(m + 0) * 256 + (c & 0xff)]);
+        if (m + 1 < nsq) a1 = __fadd_rn(a1, lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
+        if (m + 2 < nsq) a2 = __fadd_rn(a2, lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
+        if (m + 3 < nsq) a3 = __fadd_rn(a3, lut[(m + 3) * 256 + (c >> 24)]);
+    }
+    return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+}
+
 // First half of compute_quantized_distance's per-point value
 // (float)(2.0 * cell_dist + offset) (puck_index.cpp:360). The reference adds in
 // double and rounds to float; for float operands double rounding of a sum is

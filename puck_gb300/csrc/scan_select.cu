@@ -105,6 +105,8 @@ struct ScanState {
     unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
 
+// NW = code words per record (code_stride / 4).
+template <int NW>
 __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ScanState st;
@@ -164,6 +166,20 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         for (uint32_t base = r0; base < r1; base += kRound) {
             const long long t_round = clock64();
             const uint64_t tau = st.tau;
+            // all loads of the thread's records first, so their latencies overlap
+            uint32_t fine_id[kRecPerThread];
+            float off[kRecPerThread];
+            uint32_t words[kRecPerThread][NW];
+#pragma unroll
+            for (int j = 0; j < kRecPerThread; ++j) {
+                const uint32_t mi = base + tid + j * kThreads;
+                const uint32_t mr = mi < r1 ? mi : r0;
+                fine_id[j] = p.rec_fine[mr];
+                off[j] = p.offsets[mr];
+                const uint32_t* cw = reinterpret_cast<const uint32_t*>(p.codes + (uint64_t)mr * p.code_stride);
+#pragma unroll
+                for (int i = 0; i < NW; ++i) words[j][i] = __ldg(cw + i);
+            }
 #pragma unroll
             for (int j = 0; j < kRecPerThread; ++j) {
                 const uint32_t mi = base + tid + j * kThreads;
@@ -172,11 +188,10 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
                 if (mi < r1) {
                     // (float)(2.0 * cell_dist + offset): one float add of the exact
                     // 2 * cell_dist (see adc_base)
-                    const float t0 = __fadd_rn(srow[p.rec_fine[mi]], p.offsets[mi]);
+                    const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
                     ++my_eval;
                     if (pack_key(t0, mi) < tau) {  // t can only grow past t0
-                        const float t = __fadd_rn(
-                            t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, nsq));
+                        const float t = __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
                         key = pack_key(t, mi);
                         keep = key < tau;
                     }
@@ -280,12 +295,20 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s,
     p.P = s.P;
     p.T = s.T;
     const size_t smem = scan_smem_bytes(ix);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_scan_select, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr_set = true;
-    }
-    k_scan_select<<<n, kThreads, smem, stream>>>(p);
+    const uint32_t nw = ix.code_stride / 4;
+    auto launch = [&](auto kernel) {
+        static bool attr_set = false;  // one flag per instantiation
+        if (!attr_set) {
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+            attr_set = true;
+        }
+        kernel<<<n, kThreads, smem, stream>>>(p);
+    };
+    if (nw <= 2) launch(k_scan_select<2>);
+    else if (nw <= 4) launch(k_scan_select<4>);
+    else if (nw <= 6) launch(k_scan_select<6>);
+    else if (nw <= 8) launch(k_scan_select<8>);
+    else launch(k_scan_select<16>);
     return cudaGetLastError();
 }
 
