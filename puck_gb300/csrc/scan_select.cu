@@ -88,6 +88,95 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t v) {
     return p;
 }
 
+// The K-th smallest (1-based) of keys[0..count), all distinct: MSB-first radix
+// select with 8-bit digits. `hist` has 256 slots, `sel` 2. All threads call it.
+__device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint32_t K,
+                                     uint32_t* hist, uint64_t* sel) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint64_t prefix = 0, mask = 0;
+    uint32_t k = K;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int i = tid; i < 256; i += kThreads) hist[i] = 0;
+        __syncthreads();
+        for (uint32_t i0 = 0; i0 < count; i0 += kThreads) {
+            const uint32_t i = i0 + tid;
+            bool in = false;
+            uint32_t digit = 0;
+            if (i < count) {
+                const uint64_t key = keys[i];
+                in = (key & mask) == prefix;
+                digit = (uint32_t)(key >> shift) & 255u;
+            }
+            // one atomic per distinct digit in the warp
+            const unsigned active = __ballot_sync(0xffffffffu, in);
+            if (in) {
+                const unsigned same = __match_any_sync(active, digit);
+                if (lane == __ffs(same) - 1) atomicAdd(&hist[digit], (uint32_t)__popc(same));
+            }
+        }
+        __syncthreads();
+        if (tid < 32) {
+            // digit d with (count below d) < k <= (count up to d)
+            uint32_t c[8], run = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                c[j] = hist[tid * 8 + j];
+                run += c[j];
+            }
+            uint32_t incl = run;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            uint32_t below = incl - run;
+            if (below < k && k <= incl) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (below < k && k <= below + c[j]) {
+                        sel[0] = (uint64_t)(tid * 8 + j);
+                        sel[1] = k - below;
+                    }
+                    below += c[j];
+                }
+            }
+        }
+        __syncthreads();
+        prefix |= sel[0] << shift;
+        mask |= 255ull << shift;
+        k = (uint32_t)sel[1];
+        __syncthreads();
+    }
+    return prefix;
+}
+
+// Keeps the keys <= kth (exactly K of them, in arbitrary order) at the front;
+// returns nothing, every thread must call it. `cnt` is a shared counter.
+template <int PER>
+__device__ void block_compact_le(uint64_t* keys, uint32_t count, uint64_t kth, uint32_t* cnt) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint64_t mine[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const uint32_t i = tid + j * kThreads;
+        mine[j] = i < count ? keys[i] : ~0ull;
+    }
+    if (tid == 0) *cnt = 0;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const bool keep = mine[j] <= kth;
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        uint32_t base = 0;
+        if (b) {
+            if (lane == __ffs(b) - 1) base = atomicAdd(cnt, (uint32_t)__popc(b));
+            base = __shfl_sync(0xffffffffu, base, __ffs(b) - 1);
+        }
+        if (keep) keys[base + __popc(b & ((1u << lane) - 1))] = mine[j];
+    }
+    __syncthreads();
+}
+
 // Diagnostic counters (pgpu_walk_counters slots, summed per launch): 0 records
 // evaluated, 2 records kept, 3 compactions, 5 max records of one query, and
 // thread-0 clock cycles: 6 prologue (LUT, fine terms), 7 whole block, 8 record
@@ -97,6 +186,9 @@ enum { kScRecords = 0, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCy
 
 struct ScanState {
     uint64_t tau;
+    uint64_t sel[2];
+    uint32_t hist[256];
+    uint32_t ccount;
     uint32_t count;
     uint32_t c;
     float cdl;
@@ -214,14 +306,13 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
             const long long t_round_end = clock64();
             if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
             if (st.count > kCandCap - kRound) {
-                // cut back to the T best; tau = the T-th key
-                const uint32_t cnt = st.count, n2 = pow2_ceil(cnt);
-                for (uint32_t i = cnt + tid; i < n2; i += kThreads) keys[i] = kKeyMax;
-                __syncthreads();
-                bitonic_sort_keys(keys, n2);
+                // cut back to the T best (unordered); tau = the T-th key
+                const uint32_t cnt = st.count;
+                const uint64_t kth = block_select_kth(keys, cnt, T, st.hist, st.sel);
+                block_compact_le<kCandCap / kThreads>(keys, cnt, kth, &st.ccount);
                 if (tid == 0) {
                     st.count = T;
-                    st.tau = keys[T - 1];
+                    st.tau = kth;
                     st.n_compact += 1;
                     st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
                 }
@@ -231,7 +322,13 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     }
     __syncthreads();
     const long long t_final = clock64();
-    const uint32_t count = st.count, n2 = pow2_ceil(count);
+    uint32_t count = st.count;
+    if (count > T) {
+        const uint64_t kth = block_select_kth(keys, count, T, st.hist, st.sel);
+        block_compact_le<kCandCap / kThreads>(keys, count, kth, &st.ccount);
+        count = T;
+    }
+    const uint32_t n2 = pow2_ceil(count);
     for (uint32_t i = count + tid; i < n2; i += kThreads) keys[i] = kKeyMax;
     __syncthreads();
     bitonic_sort_keys(keys, n2);
