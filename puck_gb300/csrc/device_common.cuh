@@ -136,6 +136,38 @@ __device__ __forceinline__ float lut_sum(const uint8_t* __restrict__ code, const
     return __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
 }
 
+// get_dist_table (quantization.cpp:260-270) for one query into shared memory,
+// by all threads of the block (nthreads). lsq = 4 takes one 16-byte codebook load
+// per entry, four entries per thread in flight; other lsq use l2sqr_sse.
+__device__ __forceinline__ void build_lut(float* lut, const float* qv, const float* __restrict__ cb,
+                                          uint32_t nsq, uint32_t lsq, int nthreads) {
+    const uint32_t total = nsq * 256;
+    const int tid = threadIdx.x;
+    if (lsq == 4) {
+        const float4* cb4 = reinterpret_cast<const float4*>(cb);
+        for (uint32_t e0 = 4 * tid; e0 < total; e0 += 4 * nthreads) {
+            float4 y[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) y[u] = __ldg(cb4 + (e0 + u < total ? e0 + u : e0));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t e = e0 + u;
+                if (e >= total) break;
+                const float* x = qv + (e >> 8) * 4;
+                const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
+                const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
+                lut[e] = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                   __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
+            }
+        }
+    } else {
+        for (uint32_t e = tid; e < total; e += nthreads) {
+            const uint32_t m = e >> 8, j = e & 255;
+            lut[e] = l2sqr_sse(qv + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
+        }
+    }
+}
+
 // lookup_dist_table over codes already in registers: NW 32-bit words holding the
 // record's nsq codes (4 per word, little-endian); same order as lut_sum.
 template <int NW>

@@ -22,6 +22,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr int kRows = 8;  // candidate rows per warp in flight
 
 struct RerankParams {
     const float* q;
@@ -124,20 +125,19 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     __syncthreads();
-    // four rows per warp in flight: their tags are read up front so the row loads
-    // of the unrolled calls can overlap
-    for (uint32_t j0 = warp * 4; j0 < cnt; j0 += kWarps * 4) {
-        const float* rows[4];
+    // kRows rows per warp with their loads in flight together
+    for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
+        const float* rows[kRows];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kRows; ++u) {
             const uint32_t j = j0 + u;
             rows[u] = p.feat + (uint64_t)tags[j < cnt ? j : j0] * p.d;
         }
-        float v[4];
-        warp_l2_exact<4>(rows, qv, p.d, lane, v);
+        float v[kRows];
+        warp_l2_exact<kRows>(rows, qv, p.d, lane, v);
         if (lane == 0) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < kRows; ++u)
                 if (j0 + u < cnt) dist[j0 + u] = v[u];
         }
     }

@@ -226,10 +226,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
     }
     __syncthreads();
-    for (uint32_t e = tid; e < nsq * 256; e += kThreads) {
-        const uint32_t m = e >> 8, j = e & 255;
-        lut[e] = l2sqr_sse(qv + m * p.lsq, p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
-    }
+    build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
     unsigned long long my_eval = 0, my_pass = 0;
     __syncthreads();
     const long long t_pro = clock64();

@@ -223,10 +223,7 @@ __global__ __launch_bounds__(kThreads) void k_walk_scan(WalkParams p) {
     }
     __syncthreads();
     // get_dist_table (quantization.cpp:260-270)
-    for (uint32_t e = tid; e < nsq * 256; e += kThreads) {
-        const uint32_t m = e >> 8, j = e & 255;
-        lut[e] = l2sqr_sse(qv + m * p.lsq, p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
-    }
+    build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
     const float qn = p.qnorm[qi];
     if (tid == 0) {
         st.dpc = T;
