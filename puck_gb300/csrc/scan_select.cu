@@ -390,19 +390,19 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s,
     p.T = s.T;
     const size_t smem = scan_smem_bytes(ix);
     const uint32_t nw = ix.code_stride / 4;
-    auto launch = [&](auto kernel) {
-        static bool attr_set = false;  // one flag per instantiation
-        if (!attr_set) {
+    static bool attr_set[5] = {false, false, false, false, false};  // one per instantiation
+    auto launch = [&](void (*kernel)(ScanParams), int slot) {
+        if (!attr_set[slot]) {
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-            attr_set = true;
+            attr_set[slot] = true;
         }
         kernel<<<n, kThreads, smem, stream>>>(p);
     };
-    if (nw <= 2) launch(k_scan_select<2>);
-    else if (nw <= 4) launch(k_scan_select<4>);
-    else if (nw <= 6) launch(k_scan_select<6>);
-    else if (nw <= 8) launch(k_scan_select<8>);
-    else launch(k_scan_select<16>);
+    if (nw <= 2) launch(k_scan_select<2>, 0);
+    else if (nw <= 4) launch(k_scan_select<4>, 1);
+    else if (nw <= 6) launch(k_scan_select<6>, 2);
+    else if (nw <= 8) launch(k_scan_select<8>, 3);
+    else launch(k_scan_select<16>, 4);
     return cudaGetLastError();
 }
 
