@@ -329,14 +329,16 @@ def run_gpu(args, w, rank, ws):
     walk_ms = stage["walk_scan"]
     peak, peak_kind = measured_peaks()
     achieved = walk_bytes / (walk_ms / 1e3) / 1e9
+    # DRAM bytes per launch of the dominant kernel, from an ncu capture of the same
+    # workload and operating point (profiles/traffic.json), when one exists
     traffic = None
-    tf = os.path.join(REPO, "profiles", "walk_scan_traffic.json")
+    tf = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tf):
         with open(tf) as f:
-            tj = json.load(f)
-        if (tj.get("workload") == args.workload and tj.get("search_coarse_count") == op
-            and tj.get("mode") == best["mode"]):
-            traffic = tj.get("dram_bytes_per_launch")
+            for e in json.load(f).get("entries", []):
+                if (e.get("workload") == args.workload and e.get("search_coarse_count") == op
+                        and e.get("mode") == best["mode"]):
+                    traffic = e.get("dram_bytes_per_launch")
 
     # ---- e2e through the C ABI with pinned host buffers
     q_host = torch.empty((nq, w["d"]), dtype=torch.float32, pin_memory=True)
