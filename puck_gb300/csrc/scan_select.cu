@@ -25,7 +25,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRecPerThread = 4;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
-constexpr uint32_t kCandCap = 4096;               // candidate buffer (power of two)
+constexpr uint32_t kCandCap = 2048;               // candidate buffer (power of two)
 
 struct ScanParams {
     const float* q;
@@ -206,8 +206,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     const int tid = threadIdx.x;
     const uint32_t nsq = p.nsq, F = p.F, T = p.T;
     float* lut = reinterpret_cast<float*>(smem + sizeof(uint64_t) * kCandCap);
-    float* fdk = lut + nsq * 256;          // [F]
-    float* srow = fdk + F;                 // [F] 2 * cell_dist of the current cluster's cells
+    float* srow = lut + nsq * 256;         // [F] 2 * cell_dist of the current cluster's cells
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [kCandCap], first (8-byte aligned)
     float* qv = srow + F;                  // [d]
 
@@ -217,7 +216,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     }
     const long long t_start = clock64();
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
-    for (uint32_t i = tid; i < F; i += kThreads) fdk[i] = p.fd_by_fine[(uint64_t)qi * F + i];
+    const float* fdk = p.fd_by_fine + (uint64_t)qi * F;  // fine terms of this query
     if (tid == 0) {
         st.tau = kKeyMax;
         st.count = 0;
@@ -355,7 +354,7 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
 }  // namespace
 
 size_t scan_smem_bytes(const DeviceIndex& ix) {
-    return sizeof(uint64_t) * kCandCap + sizeof(float) * ix.nsq * 256 + sizeof(float) * 2 * ix.F +
+    return sizeof(uint64_t) * kCandCap + sizeof(float) * ix.nsq * 256 + sizeof(float) * ix.F +
            sizeof(float) * ix.d;
 }
 
