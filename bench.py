@@ -208,7 +208,77 @@ def cpu_port_baseline(arrays, queries_np, P, T, k, budget_s=20.0, max_q=4000):
                             f"{threads} threads, oracle C port of PuckIndex::search"), ids
 
 
-# ------------------------------------------------------------------ arms
+def run_serving(native, ix, q_np, loads_qps, seconds=2.0, max_batch=1024, seed=3):
+    """Serving form: Poisson request arrivals at several offered loads (queries/s),
+    request sizes uniform in 1..256, top-k uniform in {10, 100}; continuous batching
+    on CUDA graphs (pgpu_server). Latency is measured by the server from submit to
+    results delivered."""
+    import threading
+    rng = np.random.default_rng(seed)
+    srv = native.Server(ix, max_batch=max_batch, scratch_budget_bytes=2 << 30, max_slots=4)
+    nq = q_np.shape[0]
+
+    def one_rate(load, secs, record):
+        lam = load / 128.5  # mean request size of U{1..256}
+        n_req = max(1, int(lam * secs))
+        gaps = rng.exponential(1.0 / lam, n_req)
+        sizes = rng.integers(1, 257, n_req)
+        ks = rng.choice([10, 100], n_req)
+        starts = rng.integers(0, nq - 256, n_req)
+        tickets = []
+        done = []
+        lock = threading.Lock()
+        finished = threading.Event()
+
+        def waiter():
+            i = 0
+            while True:
+                with lock:
+                    if i >= len(tickets):
+                        if finished.is_set() and i >= n_req:
+                            return
+                        t = None
+                    else:
+                        t = tickets[i]
+                if t is None:
+                    time.sleep(0.0002)
+                    continue
+                _, _, _, us = srv.wait(t, timeout_ms=60000)
+                done.append(us)
+                i += 1
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        nxt = t0
+        for i in range(n_req):
+            nxt += gaps[i]
+            while time.perf_counter() < nxt:
+                pass
+            t = srv.submit(q_np[starts[i]:starts[i] + sizes[i]], int(ks[i]))
+            with lock:
+                tickets.append(t)
+        finished.set()
+        th.join()
+        wall = time.perf_counter() - t0
+        if not record:
+            return None
+        lat = np.array(done) / 1e3
+        return dict(offered_qps=round(load), achieved_qps=round(float(sizes.sum()) / wall, 1),
+                    requests=n_req, p50_ms=round(float(np.percentile(lat, 50)), 3),
+                    p99_ms=round(float(np.percentile(lat, 99)), 3))
+
+    one_rate(loads_qps[0], 0.5, False)  # warm-up: captures the slots' graphs
+    rates = [one_rate(load, seconds, True) for load in loads_qps]
+    st = srv.stats()
+    srv.close()
+    return dict(max_batch=max_batch, slots=st["slots"], graphs_captured=st["graphs_captured"],
+                mean_batch_queries=round(st["queries_done"] / max(1, st["batches"]), 1),
+                request_sizes="uniform 1..256", topk="uniform {10, 100}", arrivals="Poisson",
+                rates=rates)
+
+
+# ------------------------------------------------------------------ arms# ------------------------------------------------------------------ arms
 
 def run_gpu(args, w, rank, ws):
     import torch
@@ -356,6 +426,11 @@ def run_gpu(args, w, rank, ws):
     e2e_ids = i_host.numpy().view(np.uint32)
     assert np.array_equal(e2e_ids, i_dev.cpu().numpy().view(np.uint32)), "e2e != device results"
 
+    serving = None
+    if not args.no_serve:
+        serving = run_serving(native, ix, q_np, loads_qps=(250_000, 500_000, 1_000_000))
+        log(f"[bench] serving: {serving}")
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu_P = exact_best["search_coarse_count"] if exact_best else w["sweep"][0]
@@ -414,6 +489,7 @@ def run_gpu(args, w, rank, ws):
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(walk_bytes)},
         "gpu_launches": launches_per_step * args.steps,
+        "serving": serving,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
@@ -476,6 +552,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="cosine_10m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--reference-sample", type=int, default=500)
     ap.add_argument("--reference-coarse-count", type=int, default=0)
     args = ap.parse_args()

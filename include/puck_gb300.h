@@ -29,6 +29,7 @@ extern "C" {
 #define PGPU_E_CUDA (-5)        /* CUDA runtime error, or no usable GPU */
 #define PGPU_E_NOMEM (-6)       /* device allocation failed */
 #define PGPU_E_LIMIT (-7)       /* size beyond a documented limit of a kernel */
+#define PGPU_E_TIMEOUT (-8)     /* pgpu_server_wait: the request did not finish in time */
 
 /* Search modes. */
 #define PGPU_MODE_EXACT 0      /* reference-exact: the same cells, heap and ties as PuckIndex::search */
@@ -148,6 +149,51 @@ int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
 int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
 
 int pgpu_close(pgpu_index* index);
+
+/* ------------------------------------------------------------------ serving
+ * Continuous batching of search requests on one resident index. No counterpart in
+ * the reference, whose callers fan single searches out over threads
+ * (pyapi_wrapper/py_api_wrapper.cpp:110-170); here a scheduler thread fills device
+ * batches from all pending requests.
+ *
+ * The server owns S slots (S = min(max_slots, scratch_budget_bytes / slot size)),
+ * each with its own scratch, stream, pinned staging and one CUDA graph per
+ * (batch-size bucket, topk) holding the whole pass (query upload, the search
+ * kernels of the index's current mode, result download), captured on first use.
+ * A free slot takes requests from the head of the queue with the same topk, up to
+ * max_batch queries, padded to the next bucket (32, 64, ..., max_batch); slots run
+ * concurrently on separate streams. A request's results are bit-identical to
+ * pgpu_search_batch on the same queries. The index's search parameters must not
+ * change while a server is attached. Query, distance, labels and status buffers
+ * belong to the caller and must stay valid until pgpu_server_wait returns. */
+typedef struct pgpu_server pgpu_server;
+
+typedef struct {
+    uint32_t max_batch;            /* queries per device batch (and per request) */
+    uint64_t scratch_budget_bytes; /* device + pinned memory the slots may use */
+    uint32_t max_slots;
+} pgpu_server_params;
+
+typedef struct {
+    uint64_t requests_submitted, requests_done, queries_done;
+    uint64_t batches, graph_launches, graphs_captured, padded_queries;
+    double latency_us_sum; /* submit -> results delivered, summed over done requests */
+    uint32_t slots;
+    uint64_t slot_bytes;
+} pgpu_server_stats;
+
+/* max_batch 1024, scratch budget 1 GiB, 4 slots. */
+void pgpu_server_params_default(pgpu_server_params* params);
+int pgpu_server_create(pgpu_index* index, const pgpu_server_params* params, pgpu_server** out);
+/* Queues n (1..max_batch) host queries with their own topk; returns a ticket. */
+int pgpu_server_submit(pgpu_server* server, uint32_t n, const float* query, uint32_t topk,
+                       float* distance, uint32_t* labels, int32_t* status, uint64_t* ticket);
+/* Waits for a ticket (timeout_ms < 0: no limit); latency_us (optional) receives
+ * the time from submit to results delivered. A ticket can be waited for once. */
+int pgpu_server_wait(pgpu_server* server, uint64_t ticket, int32_t timeout_ms, double* latency_us);
+int pgpu_server_stats_get(pgpu_server* server, pgpu_server_stats* out);
+/* Finishes queued and running requests, then frees the server. */
+int pgpu_server_destroy(pgpu_server* server);
 
 /* k-means assignment step used by train (kmeans.cpp:221-258 nearest_center):
  * for each of n points (DEVICE pointer, [n][dim]) the id of the nearest of k

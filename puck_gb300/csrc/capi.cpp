@@ -46,14 +46,6 @@ int cuda_fail(cudaError_t e, const char* what) {
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-void free_scratch(pgpu::Scratch* s) {
-    void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
-                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
-    *s = pgpu::Scratch();
-}
-
 void free_staging(pgpu_index* h) {
     void* ptrs[] = {h->d_qin, h->d_dist, h->d_ids, h->d_status};
     for (void* p : ptrs)
@@ -74,35 +66,8 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
 }
 
 int alloc_scratch(pgpu_index* h) {
-    free_scratch(&h->s);
-    pgpu::Scratch& s = h->s;
-    const uint64_t B = h->max_batch;
-    const auto& ix = h->ix;
-    s.P = std::min(h->cfg.P, ix.C);
-    s.T = h->cfg.T;
-    uint64_t b = 0;
-    cudaError_t e;
-#define PGPU_ALLOC(ptr, cnt)                                   \
-    e = alloc(&(ptr), (cnt), &b);                              \
-    if (e != cudaSuccess) {                                    \
-        free_scratch(&s);                                      \
-        return cuda_fail(e, "scratch allocation");             \
-    }
-    PGPU_ALLOC(s.q, B * ix.d);
-    PGPU_ALLOC(s.qnorm, B);
-    PGPU_ALLOC(s.status, B);
-    PGPU_ALLOC(s.dots, B * std::max(ix.C, ix.F));
-    PGPU_ALLOC(s.cdist, B * s.P);
-    PGPU_ALLOC(s.ctag, B * s.P);
-    PGPU_ALLOC(s.fdist, B * ix.F);
-    PGPU_ALLOC(s.ftag, B * ix.F);
-    PGPU_ALLOC(s.hdist, B * s.T);
-    PGPU_ALLOC(s.htag, B * s.T);
-    PGPU_ALLOC(s.hcnt, B);
-    PGPU_ALLOC(s.counters, pgpu::kNumWalkCounters);
-#undef PGPU_ALLOC
-    s.cap = (uint32_t)B;
-    s.bytes = b;
+    std::string err;
+    if (int rc = pgpu::alloc_scratch(h->ix, h->cfg, h->max_batch, &h->s, &err)) return fail(rc, err);
     return PGPU_OK;
 }
 
@@ -171,52 +136,13 @@ void collect_stage_times(pgpu_index* h) {
 // One pass of <= max_batch queries, all buffers on the device.
 int run_pass(pgpu_index* h, uint32_t n, const float* d_q, uint32_t topk, float* d_dist,
              uint32_t* d_ids, int32_t* d_status, cudaStream_t st) {
-    auto& ix = h->ix;
-    auto& s = h->s;
-    cudaError_t e;
     const bool prof = h->profiling;
     if (prof) collect_stage_times(h);
-    auto mark = [&](int i) {
-        if (prof) cudaEventRecord(h->ev[i], st);
-    };
-    if ((e = cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * pgpu::kNumWalkCounters, st)) != cudaSuccess)
-        return cuda_fail(e, "memset");
-    mark(0);
-    if ((e = pgpu::launch_prep_queries(ix, d_q, n, s, st)) != cudaSuccess)
-        return cuda_fail(e, "prep_queries");
-    mark(1);
-    if ((e = pgpu::launch_centroid_scores(s.q, n, ix.coarse, ix.C, ix.d, ix.coarse_norms, false,
-                                          s.dots, ix.C, st)) != cudaSuccess)
-        return cuda_fail(e, "coarse scores");
-    mark(2);
-    if ((e = pgpu::launch_topsort_status(s.dots, n, ix.C, ix.C, s.P, s.cdist, s.ctag, s.status,
-                                         st)) != cudaSuccess)
-        return cuda_fail(e, "coarse select");
-    mark(3);
-    if ((e = pgpu::launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F,
-                                          st)) != cudaSuccess)
-        return cuda_fail(e, "fine scores");
-    mark(4);
-    int launched = 6;
-    if (h->cfg.mode == PGPU_MODE_EXACT) {
-        if ((e = pgpu::launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status,
-                                             st)) != cudaSuccess)
-            return cuda_fail(e, "fine order");
-        launched = 7;
-    }
-    mark(5);
-    if (h->cfg.mode == PGPU_MODE_EXACT) {
-        if ((e = pgpu::launch_walk_scan(ix, h->cfg, n, s, st)) != cudaSuccess)
-            return cuda_fail(e, "walk_scan");
-    } else {
-        if ((e = pgpu::launch_scan_select(ix, n, s, st)) != cudaSuccess)
-            return cuda_fail(e, "scan_select");
-    }
-    mark(6);
-    if ((e = pgpu::launch_rerank(ix, h->cfg, n, topk, s, d_dist, d_ids, d_status, st)) !=
-        cudaSuccess)
-        return cuda_fail(e, "rerank");
-    mark(7);
+    int launched = 0;
+    const char* what = "";
+    cudaError_t e = pgpu::run_pipeline(h->ix, h->cfg, h->s, n, d_q, topk, d_dist, d_ids, d_status,
+                                       st, prof ? h->ev : nullptr, &launched, &what);
+    if (e != cudaSuccess) return cuda_fail(e, what);
     if (prof) h->stage_pending = true;
     h->kernels += launched;
     return PGPU_OK;
@@ -266,6 +192,9 @@ int open_common(const pgpu_index_arrays& a, const pgpu_params* params, pgpu_inde
 
 namespace pgpu {
 int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+const DeviceIndex& index_device(const pgpu_index* h) { return h->ix; }
+const SearchConfig& index_config(const pgpu_index* h) { return h->cfg; }
+int index_device_ordinal(const pgpu_index* h) { return h->device; }
 }  // namespace pgpu
 
 extern "C" {
@@ -440,7 +369,7 @@ int pgpu_close(pgpu_index* h) {
         cudaStreamDestroy(h->stream);
     }
     free_staging(h);
-    free_scratch(&h->s);
+    pgpu::free_scratch(&h->s);
     pgpu::free_device_index(&h->ix);
     if (h->ev[0])
         for (auto& e : h->ev) cudaEventDestroy(e);

@@ -109,6 +109,19 @@ uint32_t scan_max_filter_topk();
 cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
 
+// Pass pipeline (pipeline.cpp).
+void free_scratch(Scratch* s);
+uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B);
+int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Scratch* s,
+                  std::string* err);
+// Enqueues one pass of n <= s.cap queries (all pointers on the device). `ev`, if not
+// null, holds PGPU_NUM_STAGES + 1 events recorded around the stages. On failure
+// *what names the step.
+cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch& s, uint32_t n,
+                         const float* d_q, uint32_t topk, float* d_dist, uint32_t* d_ids,
+                         int32_t* d_status, cudaStream_t st, cudaEvent_t* ev, int* launched,
+                         const char** what);
+
 // Host-side loader (index_host.cpp).
 struct HostIndex {
     uint32_t d = 0, n = 0, C = 0, F = 0, nsq = 0, lsq = 0;

@@ -1,0 +1,118 @@
+// One search pass on the device: query prep, coarse scores, coarse top-P, fine
+// terms (+ full fine order in exact mode), filter stage (exact walk or scan),
+// rerank. Shared by the synchronous entry points and the serving loop.
+#include <algorithm>
+#include <string>
+
+#include "pgpu_internal.h"
+
+namespace pgpu {
+namespace {
+template <class T>
+cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
+    const size_t sz = sizeof(T) * (count ? count : 1);
+    cudaError_t e = cudaMalloc((void**)p, sz);
+    if (e == cudaSuccess) *bytes += sz;
+    return e;
+}
+}  // namespace
+
+void free_scratch(Scratch* s) {
+    void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
+                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    *s = Scratch();
+}
+
+uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
+    const uint64_t P = std::min(cfg.P, ix.C), T = cfg.T;
+    const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
+    return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
+           fine_order + kNumWalkCounters * 8;
+}
+
+int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Scratch* out,
+                  std::string* err) {
+    free_scratch(out);
+    Scratch& s = *out;
+    s.P = std::min(cfg.P, ix.C);
+    s.T = cfg.T;
+    // the full fine order is only read by the exact walk
+    const uint64_t fine_rows = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F : 1;
+    uint64_t b = 0;
+    cudaError_t e = cudaSuccess;
+#define PGPU_ALLOC(ptr, cnt)                                                        \
+    if (e == cudaSuccess) e = alloc(&(ptr), (cnt), &b);
+    PGPU_ALLOC(s.q, (uint64_t)B * ix.d);
+    PGPU_ALLOC(s.qnorm, B);
+    PGPU_ALLOC(s.status, B);
+    PGPU_ALLOC(s.dots, (uint64_t)B * std::max(ix.C, ix.F));
+    PGPU_ALLOC(s.cdist, (uint64_t)B * s.P);
+    PGPU_ALLOC(s.ctag, (uint64_t)B * s.P);
+    PGPU_ALLOC(s.fdist, fine_rows);
+    PGPU_ALLOC(s.ftag, fine_rows);
+    PGPU_ALLOC(s.hdist, (uint64_t)B * s.T);
+    PGPU_ALLOC(s.htag, (uint64_t)B * s.T);
+    PGPU_ALLOC(s.hcnt, B);
+    PGPU_ALLOC(s.counters, kNumWalkCounters);
+#undef PGPU_ALLOC
+    if (e != cudaSuccess) {
+        free_scratch(&s);
+        *err = std::string("scratch allocation: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
+    }
+    s.cap = B;
+    s.bytes = b;
+    return PGPU_OK;
+}
+
+cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch& s, uint32_t n,
+                         const float* d_q, uint32_t topk, float* d_dist, uint32_t* d_ids,
+                         int32_t* d_status, cudaStream_t st, cudaEvent_t* ev, int* launched,
+                         const char** what) {
+    cudaError_t e;
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], st);
+    };
+#define PGPU_STEP(call, name)           \
+    if ((e = (call)) != cudaSuccess) {  \
+        *what = name;                   \
+        return e;                       \
+    }
+    PGPU_STEP(cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * kNumWalkCounters, st),
+              "memset");
+    mark(0);
+    PGPU_STEP(launch_prep_queries(ix, d_q, n, s, st), "prep_queries");
+    mark(1);
+    PGPU_STEP(launch_centroid_scores(s.q, n, ix.coarse, ix.C, ix.d, ix.coarse_norms, false, s.dots,
+                                     ix.C, st),
+              "coarse scores");
+    mark(2);
+    PGPU_STEP(launch_topsort_status(s.dots, n, ix.C, ix.C, s.P, s.cdist, s.ctag, s.status, st),
+              "coarse select");
+    mark(3);
+    PGPU_STEP(launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F, st),
+              "fine scores");
+    mark(4);
+    int k = 6;
+    if (cfg.mode == PGPU_MODE_EXACT) {
+        PGPU_STEP(launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status, st),
+                  "fine order");
+        k = 7;
+    }
+    mark(5);
+    if (cfg.mode == PGPU_MODE_EXACT) {
+        PGPU_STEP(launch_walk_scan(ix, cfg, n, s, st), "walk_scan");
+    } else {
+        PGPU_STEP(launch_scan_select(ix, n, s, st), "scan_select");
+    }
+    mark(6);
+    PGPU_STEP(launch_rerank(ix, cfg, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
+    mark(7);
+#undef PGPU_STEP
+    if (launched) *launched = k;
+    return cudaSuccess;
+}
+
+}  // namespace pgpu

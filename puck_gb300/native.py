@@ -19,6 +19,7 @@ PGPU_E_UNSUPPORTED = -4
 PGPU_E_CUDA = -5
 PGPU_E_NOMEM = -6
 PGPU_E_LIMIT = -7
+PGPU_E_TIMEOUT = -8
 PGPU_MODE_EXACT = 0
 PGPU_MODE_SCAN = 1
 
@@ -30,7 +31,8 @@ EXPORTED_SYMBOLS = (
     "pgpu_search_batch", "pgpu_search", "pgpu_search_batch_device", "pgpu_index_info_get",
     "pgpu_last_stats", "pgpu_close", "pgpu_nearest_center", "pgpu_last_error",
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
-    "pgpu_nearest_center_noalloc",
+    "pgpu_nearest_center_noalloc", "pgpu_server_params_default", "pgpu_server_create",
+    "pgpu_server_submit", "pgpu_server_wait", "pgpu_server_stats_get", "pgpu_server_destroy",
 )
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_CENTROIDS = 1 << 16
@@ -59,6 +61,19 @@ class IndexInfo(ctypes.Structure):
                 ("coarse_cluster_count", ctypes.c_uint32), ("fine_cluster_count", ctypes.c_uint32),
                 ("filter_nsq", ctypes.c_uint32), ("lsq", ctypes.c_uint32),
                 ("whether_norm", ctypes.c_int32), ("device_bytes", ctypes.c_uint64)]
+
+
+class ServerParams(ctypes.Structure):
+    _fields_ = [("max_batch", ctypes.c_uint32), ("scratch_budget_bytes", ctypes.c_uint64),
+                ("max_slots", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("requests_submitted", ctypes.c_uint64), ("requests_done", ctypes.c_uint64),
+                ("queries_done", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("graph_launches", ctypes.c_uint64), ("graphs_captured", ctypes.c_uint64),
+                ("padded_queries", ctypes.c_uint64), ("latency_us_sum", ctypes.c_double),
+                ("slots", ctypes.c_uint32), ("slot_bytes", ctypes.c_uint64)]
 
 
 class IndexArrays(ctypes.Structure):
@@ -109,6 +124,13 @@ def load(build_if_missing=False):
     lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.pgpu_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), u32]
     lib.pgpu_walk_counters.argtypes = [vp, ctypes.POINTER(u64), u32]
+    lib.pgpu_server_params_default.argtypes = [ctypes.POINTER(ServerParams)]
+    lib.pgpu_server_params_default.restype = None
+    lib.pgpu_server_create.argtypes = [vp, ctypes.POINTER(ServerParams), ctypes.POINTER(vp)]
+    lib.pgpu_server_submit.argtypes = [vp, u32, vp, u32, vp, vp, vp, ctypes.POINTER(u64)]
+    lib.pgpu_server_wait.argtypes = [vp, u64, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+    lib.pgpu_server_stats_get.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    lib.pgpu_server_destroy.argtypes = [vp]
     lib.pgpu_last_error.restype = ctypes.c_char_p
     lib.pgpu_last_error.argtypes = []
     for name in EXPORTED_SYMBOLS:
@@ -286,3 +308,57 @@ def nearest_center_noalloc(centroids, points, assign, distance, stream=None):
         s = s.cuda_stream
     return check(load().pgpu_nearest_center_noalloc(dim, _ptr(centroids), k, _ptr(points), n,
                                                     _ptr(assign), _ptr(distance), s))
+
+
+class Server:
+    """Continuous-batching server over a GpuIndex (pgpu_server_*).
+
+    submit() takes host numpy arrays that must stay alive until wait() returns;
+    the Server keeps references to them."""
+
+    def __init__(self, index, max_batch=1024, scratch_budget_bytes=1 << 30, max_slots=4):
+        lib = load()
+        p = ServerParams()
+        lib.pgpu_server_params_default(ctypes.byref(p))
+        p.max_batch, p.scratch_budget_bytes, p.max_slots = max_batch, scratch_budget_bytes, max_slots
+        self._h = ctypes.c_void_p()
+        check(lib.pgpu_server_create(index._h, ctypes.byref(p), ctypes.byref(self._h)))
+        self.index = index
+        self._live = {}
+
+    def submit(self, queries, topk):
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, self.index.d)
+        n = q.shape[0]
+        dist = np.empty((n, topk), np.float32)
+        ids = np.empty((n, topk), np.uint32)
+        status = np.empty(n, np.int32)
+        t = ctypes.c_uint64()
+        check(load().pgpu_server_submit(self._h, n, q.ctypes.data, topk, dist.ctypes.data,
+                                        ids.ctypes.data, status.ctypes.data, ctypes.byref(t)))
+        self._live[t.value] = (q, dist, ids, status)
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        """Returns (dist, ids, status, latency_us)."""
+        lat = ctypes.c_double()
+        rc = load().pgpu_server_wait(self._h, ticket, timeout_ms, ctypes.byref(lat))
+        q, dist, ids, status = self._live.pop(ticket) if rc == PGPU_OK else self._live[ticket]
+        check(rc)
+        return dist, ids, status, lat.value
+
+    def stats(self):
+        st = ServerStats()
+        check(load().pgpu_server_stats_get(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().pgpu_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
