@@ -36,7 +36,7 @@ extern "C" {
 #define PGPU_MODE_SCAN 1       /* every record of the probed coarse clusters is scanned (no pivot
                                   pruning); the filter_topk smallest ADC distances, each bit-identical
                                   to the reference's value for that record, go to the exact rerank.
-                                  filter_topk <= 1536. */
+                                  filter_topk <= 1024. */
 
 /* Search parameters. Field names and meanings follow Puck's gflags
  * (puck/gflags/puck_gflags.cpp:68-78): search_coarse_count (default 200),
@@ -145,7 +145,8 @@ int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
  * 8 prologue (LUT), 9 candidate generation, 10 speculative ADC. Scan mode:
  * 0 records evaluated, 2 records kept, 3 buffer compactions, 5 most records of one
  * query, then cycles: 6 prologue, 7 whole block, 8 record rounds, 9 compactions,
- * 10 final sort. Fills min(n, 11) values. */
+ * 10 final sort. Both modes: 11 queries whose coarse top-P was recomputed in full
+ * (exact ties at the cut of the tensor-core window). Fills min(n, 12) values. */
 int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
 
 int pgpu_close(pgpu_index* index);
@@ -198,7 +199,9 @@ int pgpu_server_destroy(pgpu_server* server);
 /* k-means assignment step used by train (kmeans.cpp:221-258 nearest_center):
  * for each of n points (DEVICE pointer, [n][dim]) the id of the nearest of k
  * centroids (DEVICE pointer, [k][dim]) and its distance
- * |x|^2 + |c|^2 - 2 x.c, first centroid wins ties. Enqueued on `stream`. */
+ * |x|^2 + |c|^2 - 2 x.c, first centroid wins ties. A BF16 tensor-core screen
+ * of every (point, centroid) pair bounds the window that is recomputed in the
+ * reference's FP32 order, so the result is the exact one. Enqueued on `stream`. */
 int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* points,
                         uint64_t n, int32_t* assign, float* distance, void* stream);
 
@@ -217,6 +220,26 @@ int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const 
 int pgpu_nearest_center_noalloc(uint32_t dim, const float* centroids, uint64_t k,
                                 const float* points, uint64_t n, int32_t* assign,
                                 float* distance, void* stream);
+
+/* BF16 tensor-core contraction (tcgen05.mma, FP32 accumulation in tensor memory)
+ * on DEVICE pointers of the calling thread's current device:
+ *   acc(i,j) = sum_{t<k} bf16(a[i*a_rs + t*a_ks]) * bf16(b[j*b_rs + t*b_ks]),
+ *   i < na, j < nb, and out[i*ld_out + j] = f(acc) with f by mode:
+ *   SCORE bias[j] - acc; NEG -acc; STORE alpha*acc + beta*out; BIAS acc + bias[j];
+ *   BIAS_GELU out2[i*ld_out + j] = acc + bias[j], out = GELU(out2) (erf form);
+ *   GELU_BWD acc * GELU'(aux[i*ld_aux + j]).
+ * The engine behind the coarse screen, nearest_center and the probe network;
+ * exported for tests and tools. Enqueued on `stream`; returns after it finished. */
+#define PGPU_CONTRACT_SCORE 0
+#define PGPU_CONTRACT_NEG 1
+#define PGPU_CONTRACT_STORE 2
+#define PGPU_CONTRACT_BIAS 3
+#define PGPU_CONTRACT_BIAS_GELU 4
+#define PGPU_CONTRACT_GELU_BWD 5
+int pgpu_contract_bf16(int32_t mode, uint32_t na, uint32_t nb, uint32_t k, const float* a,
+                       uint64_t a_rs, uint64_t a_ks, const float* b, uint64_t b_rs, uint64_t b_ks,
+                       const float* bias, const float* aux, uint64_t ld_aux, float* out,
+                       uint64_t ld_out, float* out2, float alpha, float beta, void* stream);
 
 const char* pgpu_last_error(void);
 

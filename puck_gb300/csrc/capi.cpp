@@ -409,9 +409,46 @@ int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const 
         distance == nullptr)
         return fail(PGPU_E_INVALID, "invalid argument");
     if (n == 0) return PGPU_OK;
-    cudaError_t e = pgpu::launch_nearest_center(dim, centroids, k, points, n, assign, distance,
-                                                (cudaStream_t)stream);
+    if (k > 0xFFFFFFFFull) return fail(PGPU_E_LIMIT, "more than 2^32-1 centroids");
+    cudaError_t e = pgpu::launch_nearest_center_tc(dim, centroids, k, points, n, assign, distance,
+                                                   (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "nearest_center");
+    return PGPU_OK;
+}
+
+int pgpu_contract_bf16(int32_t mode, uint32_t na, uint32_t nb, uint32_t k, const float* a,
+                       uint64_t a_rs, uint64_t a_ks, const float* b, uint64_t b_rs, uint64_t b_ks,
+                       const float* bias, const float* aux, uint64_t ld_aux, float* out,
+                       uint64_t ld_out, float* out2, float alpha, float beta, void* stream) {
+    if (mode < PGPU_CONTRACT_SCORE || mode > PGPU_CONTRACT_GELU_BWD || k == 0 || a == nullptr ||
+        b == nullptr || out == nullptr || ld_out < nb)
+        return fail(PGPU_E_INVALID, "invalid argument");
+    if ((na + 127u) / 128u > 65535u) return fail(PGPU_E_LIMIT, "na above 8388480");
+    cudaStream_t st = (cudaStream_t)stream;
+    int* err = nullptr;
+    cudaError_t e = cudaMallocAsync(&err, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "contract_bf16");
+    e = cudaMemsetAsync(err, 0, sizeof(int), st);
+    pgpu::TcOperand A{a, a_rs, a_ks, na};
+    pgpu::TcOperand B{b, b_rs, b_ks, nb};
+    pgpu::TcEpilogue ep{};
+    ep.mode = mode;
+    ep.out = out;
+    ep.ld = ld_out;
+    ep.bias = bias;
+    ep.aux = aux;
+    ep.ld_aux = ld_aux;
+    ep.out2 = out2;
+    ep.alpha = alpha;
+    ep.beta = beta;
+    if (e == cudaSuccess) e = pgpu::launch_tc_gemm(A, B, k, ep, err, st);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFreeAsync(err, st);
+    if (e == cudaErrorInvalidValue) return fail(PGPU_E_INVALID, "invalid contraction operands");
+    if (e != cudaSuccess) return cuda_fail(e, "contract_bf16");
+    if (flag) return fail(PGPU_E_TIMEOUT, "tensor-core wait expired");
     return PGPU_OK;
 }
 

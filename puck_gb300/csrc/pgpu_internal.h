@@ -19,7 +19,10 @@ constexpr uint32_t kMaxClusters = 8192;   // coarse or fine count: sorted in sha
 constexpr uint32_t kMaxFilterNsq = 64;    // LUT of nsq*256 floats in shared memory
 constexpr uint32_t kMaxFilterTopk = 4096; // filter heap in shared memory
 constexpr uint32_t kMaxDim = 1024;
-constexpr int kNumWalkCounters = 11;  // see the counter enum in walk_scan.cu
+constexpr int kNumWalkCounters = 12;  // see the counter enum in walk_scan.cu
+// Counter slot 11: queries whose coarse top-P fell back from the tensor-core
+// window to the full exact recompute (ties at the cut, or a wide window).
+constexpr int kCounterWindowFallbacks = 11;
 
 // Device-resident index. Point arrays are in Puck's "memory order": sorted by
 // (cell id, filter offset, input id), so every coarse cluster is one
@@ -32,6 +35,7 @@ struct DeviceIndex {
     float* coarse = nullptr;      // [C][d]
     float* fine = nullptr;        // [F][d]
     float* coarse_norms = nullptr;// [C]  0.5*|c|^2
+    float* coarse_abs = nullptr;  // [C]  |c| rounded up (error bound of the tensor-core screen)
     float* stationary = nullptr;  // [C][F] 0.5*|f|^2 + f.c ; sqrt(FLT_MAX) for empty cells
     float* stat_sorted = nullptr; // [C][F] each coarse row of stationary, ascending
     uint32_t* stat_fine = nullptr;// [C][F] fine id of each stat_sorted entry
@@ -61,6 +65,7 @@ struct Scratch {
     uint32_t* htag = nullptr;  // [B][T] filter heap memory ids
     uint32_t* hcnt = nullptr;  // [B]
     unsigned long long* counters = nullptr; // [kNumWalkCounters] walk diagnostics
+    int* tc_err = nullptr;     // set by a tensor-core contraction whose wait expired
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;
 };
@@ -108,6 +113,44 @@ size_t scan_smem_bytes(const DeviceIndex& ix);
 uint32_t scan_max_filter_topk();
 cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
+
+// BF16 tensor-core contraction (tc_gemm.cu): out = epilogue(sum_k A(i,k) B(j,k)).
+// A(i,k) = p[i*rs + k*ks] for i < rows; B likewise.
+struct TcOperand {
+    const float* p;
+    uint64_t rs, ks;
+    uint32_t rows;
+};
+enum TcEpi {
+    TC_EPI_SCORE = 0,     // bias[j] - acc
+    TC_EPI_NEG = 1,       // -acc
+    TC_EPI_STORE = 2,     // alpha*acc + beta*out
+    TC_EPI_BIAS = 3,      // acc + bias[j]
+    TC_EPI_BIAS_GELU = 4, // out2 = acc + bias[j]; out = GELU(out2)
+    TC_EPI_GELU_BWD = 5,  // acc * GELU'(aux[i][j])
+};
+struct TcEpilogue {
+    int mode;
+    float* out;
+    uint64_t ld;
+    const float* bias;
+    const float* aux;
+    uint64_t ld_aux;
+    float* out2;
+    float alpha, beta;
+};
+size_t tc_gemm_smem_bytes();
+cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
+                           const TcEpilogue& ep, int* err, cudaStream_t stream);
+// Exact selections over a tensor-core screen (tc_select.cu).
+size_t window_smem_bytes(uint32_t C, uint32_t d);
+cudaError_t launch_abs_from_half_norms(const float* half_norms, uint32_t n, float* out,
+                                       cudaStream_t stream);
+cudaError_t launch_coarse_tc(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
+cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
+                                 cudaStream_t stream);
+cudaError_t launch_nearest_center_tc(uint32_t dim, const float* cents, uint64_t k, const float* x,
+                                     uint64_t n, int32_t* assign, float* dis, cudaStream_t stream);
 
 // Pass pipeline (pipeline.cpp).
 void free_scratch(Scratch* s);

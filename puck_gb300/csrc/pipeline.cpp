@@ -19,7 +19,7 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
 
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
-                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters};
+                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *s = Scratch();
@@ -29,7 +29,7 @@ uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t 
     const uint64_t P = std::min(cfg.P, ix.C), T = cfg.T;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
-           fine_order + kNumWalkCounters * 8;
+           fine_order + kNumWalkCounters * 8 + 4;
 }
 
 int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Scratch* out,
@@ -56,6 +56,7 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     PGPU_ALLOC(s.htag, (uint64_t)B * s.T);
     PGPU_ALLOC(s.hcnt, B);
     PGPU_ALLOC(s.counters, kNumWalkCounters);
+    PGPU_ALLOC(s.tc_err, 1);
 #undef PGPU_ALLOC
     if (e != cudaSuccess) {
         free_scratch(&s);
@@ -82,15 +83,14 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     }
     PGPU_STEP(cudaMemsetAsync(s.counters, 0, sizeof(unsigned long long) * kNumWalkCounters, st),
               "memset");
+    PGPU_STEP(cudaMemsetAsync(s.tc_err, 0, sizeof(int), st), "memset");
     mark(0);
     PGPU_STEP(launch_prep_queries(ix, d_q, n, s, st), "prep_queries");
     mark(1);
-    PGPU_STEP(launch_centroid_scores(s.q, n, ix.coarse, ix.C, ix.d, ix.coarse_norms, false, s.dots,
-                                     ix.C, st),
-              "coarse scores");
+    // coarse: BF16 tensor-core screen, then the exact top-P from an FP32 window
+    PGPU_STEP(launch_coarse_tc(ix, n, s, st), "coarse scores");
     mark(2);
-    PGPU_STEP(launch_topsort_status(s.dots, n, ix.C, ix.C, s.P, s.cdist, s.ctag, s.status, st),
-              "coarse select");
+    PGPU_STEP(launch_coarse_window(ix, n, s, st), "coarse select");
     mark(3);
     PGPU_STEP(launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F, st),
               "fine scores");

@@ -1,0 +1,308 @@
+// BF16 tensor-core contraction on sm_103a (tcgen05 + TMEM).
+//
+//   acc[i][j] = sum_k bf16(A(i,k)) * bf16(B(j,k))          (FP32 accumulation)
+//
+// A(i,k) = A.p[i*A.rs + k*A.ks], B(j,k) likewise: FP32 operands in any 2-D
+// layout (row-major, or transposed for the weight gradients of the probe
+// network). They are rounded to BF16 while being staged into shared memory in
+// the canonical no-swizzle K-major layout of tcgen05: 8-row x 16-byte core
+// matrices, the 16 row groups of a 128-row tile 128 B apart (stride byte offset),
+// K groups of 8 elements 2 KiB apart (leading byte offset).
+//
+// One CTA (4 warps) owns one 128 x 128 output tile. K runs in chunks of 64 over
+// two shared-memory stages: all threads stage chunk c+1 while the tensor core
+// works on chunk c; thread 0 issues the tcgen05.mma (M=128, N=128, K=16) of a
+// chunk into a 128-column TMEM accumulator and commits them to that stage's
+// mbarrier, which frees the stage. Each warp then reads its 32 TMEM lanes (= 32
+// output rows) with tcgen05.ld and applies the epilogue. Every mbarrier wait is
+// bounded: on expiry the kernel sets *err = 1, waits (bounded) for the
+// last commit, skips the epilogue and releases its TMEM.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "pgpu_internal.h"
+
+namespace pgpu {
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTileM = 128, kTileN = 128, kChunkK = 64;
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kStageBytes = (kTileM + kTileN) * kChunkK * 2;  // 32 KiB
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading byte offset (between
+// core matrices along K), stride byte offset (between 8-row groups), the fixed
+// 0b001 at bits 46-48, base offset 0, no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t kInstrDesc = (1u << 4) | (1u << 7) | (1u << 10) | ((kTileN >> 3) << 17) |
+                                ((kTileM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.b32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Stages rows [row0, row0+128) x k [k0, k0 + 8*nkg) of an operand into `tile`.
+// Thread t owns row t of the tile and writes one 16-byte core-matrix row per K
+// group, so a quarter warp stores 128 contiguous bytes (no bank conflict).
+__device__ __forceinline__ void stage_operand(uint8_t* tile, const TcOperand& op, uint32_t row0,
+                                              uint32_t k0, uint32_t K, uint32_t nkg, bool vec) {
+    const uint32_t r = threadIdx.x;
+    const uint32_t row = row0 + r;
+    const bool in = row < op.rows;
+    const float* base = op.p + (uint64_t)row * op.rs;
+    uint8_t* dst = tile + (r >> 3) * 128u + (r & 7u) * 16u;
+    for (uint32_t kg = 0; kg < nkg; ++kg) {
+        const uint32_t k = k0 + kg * 8;
+        float x[8];
+        if (in && vec && k + 8 <= K) {
+            const float4 u = __ldg(reinterpret_cast<const float4*>(base + k));
+            const float4 v = __ldg(reinterpret_cast<const float4*>(base + k + 4));
+            x[0] = u.x; x[1] = u.y; x[2] = u.z; x[3] = u.w;
+            x[4] = v.x; x[5] = v.y; x[6] = v.z; x[7] = v.w;
+        } else {
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                x[t] = (in && k + t < K) ? __ldg(base + (uint64_t)(k + t) * op.ks) : 0.0f;
+        }
+        uint4 w;
+        w.x = bf16x2(x[0], x[1]);
+        w.y = bf16x2(x[2], x[3]);
+        w.z = bf16x2(x[4], x[5]);
+        w.w = bf16x2(x[6], x[7]);
+        *reinterpret_cast<uint4*>(dst + kg * (16u * 128u)) = w;
+    }
+}
+
+__device__ __forceinline__ float gelu_f(float x) {
+    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad_f(float x) {
+    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+    return cdf + x * pdf;
+}
+
+template <int EPI>
+__device__ __forceinline__ float epilogue(float acc, uint32_t i, uint32_t j, const TcEpilogue& ep) {
+    if (EPI == TC_EPI_SCORE) return __fsub_rn(ep.bias[j], acc);
+    if (EPI == TC_EPI_NEG) return -acc;
+    if (EPI == TC_EPI_STORE) {
+        float v = ep.alpha * acc;
+        if (ep.beta != 0.0f) v += ep.beta * ep.out[(uint64_t)i * ep.ld + j];
+        return v;
+    }
+    if (EPI == TC_EPI_BIAS) return acc + ep.bias[j];
+    if (EPI == TC_EPI_BIAS_GELU) {
+        const float pre = acc + ep.bias[j];
+        ep.out2[(uint64_t)i * ep.ld + j] = pre;
+        return gelu_f(pre);
+    }
+    // TC_EPI_GELU_BWD: upstream gradient times GELU'(pre-activation)
+    return acc * gelu_grad_f(ep.aux[(uint64_t)i * ep.ld_aux + j]);
+}
+
+template <int EPI>
+__global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B, uint32_t K,
+                                                         int a_vec, int b_vec, TcEpilogue ep,
+                                                         int* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int failed;
+    const uint32_t m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_base)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        failed = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[0])), "r"(1u));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[1])), "r"(1u));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+
+    const uint32_t nch = (K + kChunkK - 1) / kChunkK;
+    bool ok = true;
+    for (uint32_t c = 0; c < nch; ++c) {
+        const uint32_t b = c & 1u;
+        if (c >= 2 && !mbar_wait(smem_u32(&mbar[b]), ((c - 2) >> 1) & 1u)) ok = false;
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        const uint32_t k0 = c * kChunkK;
+        const uint32_t kc = min(kChunkK, K - k0);
+        const uint32_t nk16 = (kc + 15) / 16;
+        uint8_t* a_tile = smem + b * kStageBytes;
+        uint8_t* b_tile = a_tile + kTileM * kChunkK * 2;
+        stage_operand(a_tile, A, m0, k0, K, nk16 * 2, a_vec != 0);
+        stage_operand(b_tile, B, n0, k0, K, nk16 * 2, b_vec != 0);
+        // generic-proxy writes -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (tid == 0) {
+            const uint32_t lbo = 16u * 128u, sbo = 128u;
+            const uint32_t a_addr = smem_u32(a_tile), b_addr = smem_u32(b_tile);
+            for (uint32_t s = 0; s < nk16; ++s) {
+                const uint64_t ad = smem_desc(a_addr + s * 2u * lbo, lbo, sbo);
+                const uint64_t bd = smem_desc(b_addr + s * 2u * lbo, lbo, sbo);
+                const uint32_t accum = (c > 0 || s > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(kInstrDesc), "r"(accum)
+                    : "memory");
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&mbar[b]))
+                : "memory");
+        }
+    }
+    // The last commit covers every MMA issued before it.
+    if (nch > 0 && ok) {
+        const uint32_t L = nch - 1;
+        if (!mbar_wait(smem_u32(&mbar[L & 1u]), (L >> 1) & 1u)) ok = false;
+    }
+    if (!ok && lane == 0) {
+        atomicExch(&failed, 1);
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    __syncthreads();
+    if (!failed && nch > 0) {
+        const uint32_t row = m0 + warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        const bool vec_out = (EPI != TC_EPI_BIAS_GELU) && ((ep.ld & 3u) == 0) &&
+                             ((reinterpret_cast<uintptr_t>(ep.out) & 15u) == 0);
+#pragma unroll 1
+        for (uint32_t c = 0; c < kTileN / 16; ++c) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+                "%13,%14,%15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                  "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                  "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(lane_addr + c * 16));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row >= A.rows) continue;
+            const uint32_t col0 = n0 + c * 16;
+            float* orow = ep.out + (uint64_t)row * ep.ld;
+            if (vec_out && col0 + 16 <= B.rows) {
+#pragma unroll
+                for (int j = 0; j < 16; j += 4) {
+                    float4 v;
+                    v.x = epilogue<EPI>(__uint_as_float(r[j]), row, col0 + j, ep);
+                    v.y = epilogue<EPI>(__uint_as_float(r[j + 1]), row, col0 + j + 1, ep);
+                    v.z = epilogue<EPI>(__uint_as_float(r[j + 2]), row, col0 + j + 2, ep);
+                    v.w = epilogue<EPI>(__uint_as_float(r[j + 3]), row, col0 + j + 3, ep);
+                    *reinterpret_cast<float4*>(orow + col0 + j) = v;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const uint32_t col = col0 + j;
+                    if (col < B.rows) orow[col] = epilogue<EPI>(__uint_as_float(r[j]), row, col, ep);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
+    }
+}
+
+bool operand_vec(const TcOperand& op, uint32_t K) {
+    (void)K;
+    return op.ks == 1 && (op.rs & 3u) == 0 && (reinterpret_cast<uintptr_t>(op.p) & 15u) == 0;
+}
+
+}  // namespace
+
+// The two stages plus 32 KiB of slack: every descriptor-addressed byte stays
+// inside the CTA's allocation even for a misread of the leading/stride offsets.
+size_t tc_gemm_smem_bytes() { return 2 * (size_t)kStageBytes + 32768; }
+
+cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
+                           const TcEpilogue& ep, int* err, cudaStream_t stream) {
+    if (A.rows == 0 || B.rows == 0) return cudaSuccess;
+    if (K == 0 || A.p == nullptr || B.p == nullptr || ep.out == nullptr || err == nullptr)
+        return cudaErrorInvalidValue;
+    if ((ep.mode == TC_EPI_SCORE || ep.mode == TC_EPI_BIAS || ep.mode == TC_EPI_BIAS_GELU) &&
+        ep.bias == nullptr)
+        return cudaErrorInvalidValue;
+    if (ep.mode == TC_EPI_BIAS_GELU && ep.out2 == nullptr) return cudaErrorInvalidValue;
+    if (ep.mode == TC_EPI_GELU_BWD && ep.aux == nullptr) return cudaErrorInvalidValue;
+    const dim3 grid((B.rows + kTileN - 1) / kTileN, (A.rows + kTileM - 1) / kTileM);
+    if (grid.y > 65535) return cudaErrorInvalidValue;
+    const size_t smem = tc_gemm_smem_bytes();
+    const int av = operand_vec(A, K) ? 1 : 0, bv = operand_vec(B, K) ? 1 : 0;
+    static bool attr[6] = {false, false, false, false, false, false};
+#define PGPU_TC_CASE(M)                                                                      \
+    case M:                                                                                  \
+        if (!attr[M]) {                                                                      \
+            cudaFuncSetAttribute(k_tc_gemm<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 (int)smem);                                                 \
+            attr[M] = true;                                                                  \
+        }                                                                                    \
+        k_tc_gemm<M><<<grid, kTcThreads, smem, stream>>>(A, B, K, av, bv, ep, err);         \
+        break;
+    switch (ep.mode) {
+        PGPU_TC_CASE(TC_EPI_SCORE)
+        PGPU_TC_CASE(TC_EPI_NEG)
+        PGPU_TC_CASE(TC_EPI_STORE)
+        PGPU_TC_CASE(TC_EPI_BIAS)
+        PGPU_TC_CASE(TC_EPI_BIAS_GELU)
+        PGPU_TC_CASE(TC_EPI_GELU_BWD)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef PGPU_TC_CASE
+    return cudaGetLastError();
+}
+
+}  // namespace pgpu

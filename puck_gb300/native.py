@@ -33,12 +33,13 @@ EXPORTED_SYMBOLS = (
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
     "pgpu_nearest_center_noalloc", "pgpu_server_params_default", "pgpu_server_create",
     "pgpu_server_submit", "pgpu_server_wait", "pgpu_server_stats_get", "pgpu_server_destroy",
+    "pgpu_contract_bf16",
 )
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_CENTROIDS = 1 << 16
 WALK_COUNTERS = ("records", "cells", "fd_order_chunks", "enumerations", "fd_order_clusters",
                  "heap_inserts", "cyc_replay", "cyc_total", "cyc_prologue", "cyc_candidates",
-                 "cyc_adc")
+                 "cyc_adc", "coarse_window_fallbacks")
 STAGES = ("prep", "coarse_scores", "coarse_select", "fine_scores", "fine_order", "walk_scan",
           "rerank")
 
@@ -131,6 +132,9 @@ def load(build_if_missing=False):
     lib.pgpu_server_wait.argtypes = [vp, u64, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
     lib.pgpu_server_stats_get.argtypes = [vp, ctypes.POINTER(ServerStats)]
     lib.pgpu_server_destroy.argtypes = [vp]
+    f32 = ctypes.c_float
+    lib.pgpu_contract_bf16.argtypes = [ctypes.c_int32, u32, u32, u32, vp, u64, u64, vp, u64, u64,
+                                       vp, vp, u64, vp, u64, vp, f32, f32, vp]
     lib.pgpu_last_error.restype = ctypes.c_char_p
     lib.pgpu_last_error.argtypes = []
     for name in EXPORTED_SYMBOLS:
@@ -296,6 +300,29 @@ def nearest_center(centroids, points, assign, distance, stream=None):
         s = s.cuda_stream
     return check(load().pgpu_nearest_center(dim, _ptr(centroids), k, _ptr(points), n,
                                             _ptr(assign), _ptr(distance), s))
+
+
+CONTRACT_MODES = {"score": 0, "neg": 1, "store": 2, "bias": 3, "bias_gelu": 4, "gelu_bwd": 5}
+
+
+def contract_bf16(mode, a, b, out, bias=None, aux=None, out2=None, alpha=1.0, beta=0.0,
+                  stream=None):
+    """out = f(bf16(a) @ bf16(b).T) on the tensor cores (pgpu_contract_bf16).
+
+    a [na, k] and b [nb, k] are 2-D float32 CUDA tensors in any strides (a
+    transposed view is read in place); out is [na, >= nb] with unit column stride."""
+    na, k = a.shape
+    nb, kb = b.shape
+    assert k == kb and out.stride(1) == 1
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    ld_aux = aux.stride(0) if aux is not None else 0
+    return check(load().pgpu_contract_bf16(
+        CONTRACT_MODES[mode], na, nb, k, _ptr(a), a.stride(0), a.stride(1), _ptr(b),
+        b.stride(0), b.stride(1), _ptr(bias) if bias is not None else None,
+        _ptr(aux) if aux is not None else None, ld_aux, _ptr(out), out.stride(0),
+        _ptr(out2) if out2 is not None else None, alpha, beta, s))
 
 
 def nearest_center_noalloc(centroids, points, assign, distance, stream=None):

@@ -18,7 +18,7 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared_symbols():
     src = open(os.path.join(REPO, "include", "puck_gb300.h")).read()
-    return sorted(set(re.findall(r"\b(pgpu_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(pgpu_[a-z0-9_]+)\s*\(", src)))
 
 
 @pytest.fixture(scope="module")
