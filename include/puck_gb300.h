@@ -36,7 +36,22 @@ extern "C" {
 #define PGPU_MODE_SCAN 1       /* every record of the probed coarse clusters is scanned (no pivot
                                   pruning); the filter_topk smallest ADC distances, each bit-identical
                                   to the reference's value for that record, go to the exact rerank.
-                                  filter_topk <= 1024. */
+                                  filter_topk (+ filter_margin) <= 1024. */
+
+/* Arithmetic of the search (pgpu_params.precision).
+ * FP32: every distance in FP32 in the reference's operation order (the coarse
+ *       stage screens on the tensor cores and recomputes a provable window in
+ *       FP32, so results do not change).
+ * BF16: the precision form, scan mode only. Fine distances come from the BF16
+ *       tensor-core contraction (FP32 accumulation), the ADC scan reads an FP16
+ *       lookup table (accumulated in FP32) and keeps filter_topk + filter_margin
+ *       candidates; the rerank screens them on a BF16 copy of the vectors and
+ *       recomputes in FP32 every candidate within the screen's error bound of
+ *       the topk-th, so the returned distances are FP32 and the returned ids
+ *       are the FP32 rerank's over the same candidates. The BF16 copy (2 bytes
+ *       per dimension per point) is made on the first use. */
+#define PGPU_PRECISION_FP32 0
+#define PGPU_PRECISION_BF16 1
 
 /* Search parameters. Field names and meanings follow Puck's gflags
  * (puck/gflags/puck_gflags.cpp:68-78): search_coarse_count (default 200),
@@ -50,6 +65,8 @@ typedef struct {
     int32_t device;     /* CUDA device ordinal */
     uint32_t max_batch; /* queries per device pass; sizes the per-pass scratch */
     int32_t mode;       /* PGPU_MODE_* */
+    int32_t precision;  /* PGPU_PRECISION_* (default FP32) */
+    uint32_t filter_margin; /* BF16 only: extra filter candidates kept for the rerank */
 } pgpu_params;
 
 typedef struct pgpu_index pgpu_index;
@@ -81,7 +98,8 @@ typedef struct {
 } pgpu_index_arrays;
 
 /* Fills the reference's flag defaults (search_coarse_count 200, topk 100,
- * filter_topk 1100, radius_rate 1.0, device 0, max_batch 8192, exact mode). */
+ * filter_topk 1100, radius_rate 1.0, device 0, max_batch 8192, exact mode,
+ * FP32, filter_margin 0). */
 void pgpu_params_default(pgpu_params* params);
 
 /* Replaces Index::init() (puck/hierarchical_cluster/hierarchical_cluster_index.cpp:220-255,
@@ -148,6 +166,13 @@ int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
  * 10 final sort. Both modes: 11 queries whose coarse top-P was recomputed in full
  * (exact ties at the cut of the tensor-core window). Fills min(n, 12) values. */
 int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
+
+/* Diagnostic of the scan-mode filter stage: runs one pass of n <= max_batch HOST
+ * queries and returns, per query, the candidates handed to the rerank: labels
+ * (input-order ids) and filter distances, filter_topk (+ filter_margin in BF16)
+ * slots per query in ascending filter distance, and count[i] of them filled. */
+int pgpu_filter_candidates(pgpu_index* index, uint32_t n, const float* query, uint32_t* labels,
+                           float* distance, uint32_t* count);
 
 int pgpu_close(pgpu_index* index);
 

@@ -84,13 +84,21 @@ int check_config(const pgpu_index* h, const pgpu_params* p) {
     if (p->max_batch == 0) return fail(PGPU_E_INVALID, "max_batch must be positive");
     if (p->mode != PGPU_MODE_EXACT && p->mode != PGPU_MODE_SCAN)
         return fail(PGPU_E_INVALID, "unknown search mode");
-    if (p->mode == PGPU_MODE_SCAN && p->filter_topk > pgpu::scan_max_filter_topk())
-        return fail(PGPU_E_LIMIT, "filter_topk above " + std::to_string(pgpu::scan_max_filter_topk()) +
-                                      " in scan mode");
+    if (p->precision != PGPU_PRECISION_FP32 && p->precision != PGPU_PRECISION_BF16)
+        return fail(PGPU_E_INVALID, "unknown precision");
+    if (p->precision == PGPU_PRECISION_BF16 && p->mode != PGPU_MODE_SCAN)
+        return fail(PGPU_E_INVALID, "BF16 precision needs scan mode");
+    const uint64_t keep =
+        (uint64_t)p->filter_topk + (p->precision == PGPU_PRECISION_BF16 ? p->filter_margin : 0);
+    if (p->mode == PGPU_MODE_SCAN && keep > pgpu::scan_max_filter_topk())
+        return fail(PGPU_E_LIMIT, "filter_topk + filter_margin above " +
+                                      std::to_string(pgpu::scan_max_filter_topk()) + " in scan mode");
     if (h != nullptr) {
+        const bool bf16 = p->precision == PGPU_PRECISION_BF16;
         if (pgpu::walk_smem_bytes(h->ix, p->filter_topk) > 220 * 1024 ||
-            pgpu::scan_smem_bytes(h->ix) > 220 * 1024 ||
-            pgpu::rerank_smem_bytes(h->ix, p->filter_topk, p->topk) > 220 * 1024)
+            (bf16 ? pgpu::scan_smem_bytes_half(h->ix) : pgpu::scan_smem_bytes(h->ix)) > 220 * 1024 ||
+            (bf16 ? pgpu::rerank_screen_smem_bytes(h->ix, (uint32_t)keep, p->topk)
+                  : pgpu::rerank_smem_bytes(h->ix, (uint32_t)keep, p->topk)) > 220 * 1024)
             return fail(PGPU_E_LIMIT, "filter_topk/topk/filter_nsq exceed the shared-memory budget");
     }
     return PGPU_OK;
@@ -102,7 +110,16 @@ void apply_config(pgpu_index* h, const pgpu_params* p) {
     h->cfg.topk_max = p->topk;
     h->cfg.radius_rate = p->radius_rate;
     h->cfg.mode = p->mode;
+    h->cfg.precision = p->precision;
+    h->cfg.margin = p->filter_margin;
     h->max_batch = p->max_batch;
+}
+
+int ensure_precision_data(pgpu_index* h) {
+    if (h->cfg.precision != PGPU_PRECISION_BF16) return PGPU_OK;
+    std::string err;
+    if (int rc = pgpu::ensure_bf16_features(&h->ix, &err)) return fail(rc, err);
+    return PGPU_OK;
 }
 
 int ensure_staging(pgpu_index* h, uint32_t topk) {
@@ -173,6 +190,11 @@ int open_common(const pgpu_index_arrays& a, const pgpu_params* params, pgpu_inde
         return rc;
     }
     apply_config(h, &p);
+    if (int rc = ensure_precision_data(h)) {
+        pgpu::free_device_index(&h->ix);
+        delete h;
+        return rc;
+    }
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         pgpu::free_device_index(&h->ix);
         delete h;
@@ -207,6 +229,8 @@ void pgpu_params_default(pgpu_params* p) {
     p->device = 0;
     p->max_batch = 8192;
     p->mode = PGPU_MODE_EXACT;
+    p->precision = PGPU_PRECISION_FP32;
+    p->filter_margin = 0;
 }
 
 const char* pgpu_last_error(void) { return g_last_error.c_str(); }
@@ -238,6 +262,7 @@ int pgpu_set_search_params(pgpu_index* h, const pgpu_params* params) {
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
     apply_config(h, params);
+    if (int rc = ensure_precision_data(h)) return rc;
     free_staging(h);
     return alloc_scratch(h);
 }
@@ -413,6 +438,41 @@ int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const 
     cudaError_t e = pgpu::launch_nearest_center_tc(dim, centroids, k, points, n, assign, distance,
                                                    (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "nearest_center");
+    return PGPU_OK;
+}
+
+int pgpu_filter_candidates(pgpu_index* h, uint32_t n, const float* query, uint32_t* labels,
+                           float* distance, uint32_t* count) {
+    if (h == nullptr || query == nullptr || labels == nullptr || distance == nullptr ||
+        count == nullptr)
+        return fail(PGPU_E_INVALID, "null argument");
+    if (n == 0) return PGPU_OK;
+    std::lock_guard<std::mutex> g(h->mu);
+    if (n > h->max_batch) return fail(PGPU_E_LIMIT, "n above max_batch");
+    if (h->cfg.mode != PGPU_MODE_SCAN) return fail(PGPU_E_INVALID, "scan mode only");
+    cudaSetDevice(h->device);
+    const uint32_t topk = 1;
+    if (int rc = ensure_staging(h, topk)) return rc;
+    cudaStream_t st = h->stream;
+    const uint32_t keep = h->s.T;
+    cudaError_t e = cudaMemcpyAsync(h->d_qin, query, sizeof(float) * n * h->ix.d,
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "query upload");
+    if (int rc = run_pass(h, n, h->d_qin, topk, h->d_dist, h->d_ids, h->d_status, st)) return rc;
+    uint32_t* ids = nullptr;
+    e = cudaMallocAsync(&ids, sizeof(uint32_t) * (uint64_t)n * keep, st);
+    if (e == cudaSuccess) e = pgpu::launch_gather_u32(h->s.htag, (uint64_t)n * keep, h->ix.mem2local, ids, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(labels, ids, sizeof(uint32_t) * (uint64_t)n * keep,
+                            cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(distance, h->s.hdist, sizeof(float) * (uint64_t)n * keep,
+                            cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(count, h->s.hcnt, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st);
+    if (ids) cudaFreeAsync(ids, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "filter_candidates");
     return PGPU_OK;
 }
 

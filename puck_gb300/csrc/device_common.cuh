@@ -201,4 +201,84 @@ __device__ __forceinline__ float pivot_of(float top, float qn, double rr) {
     return __double2float_rn((double)__fsub_rn(top, qn) / rr / 2.0);
 }
 
+// ------------------------------------------------------- radix selection
+// Monotone 32-bit key of a float (total order of non-NaN values; -0 < +0).
+__device__ __forceinline__ uint32_t ordered_key(float v) {
+    const uint32_t b = __float_as_uint(v);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_to_float(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// K-th smallest (1-based) ordered key of vals[0..L) by a 4-pass 8-bit radix
+// select over NT threads; `hist` has 256 slots, `state` 2. Every thread returns it.
+template <int NT>
+__device__ uint32_t block_kth_key(const float* vals, uint32_t L, uint32_t K, uint32_t* hist,
+                                  uint32_t* state) {
+    uint32_t prefix = 0, mask = 0, kth = K;
+    const int tid = threadIdx.x;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int b = tid; b < 256; b += NT) hist[b] = 0;
+        __syncthreads();
+        for (uint32_t j = tid; j < L; j += NT) {
+            const uint32_t key = ordered_key(vals[j]);
+            if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (tid < 32) {
+            // lane l owns bins 8l .. 8l+7
+            uint32_t cnt[8], tot = 0;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                cnt[t] = hist[tid * 8 + t];
+                tot += cnt[t];
+            }
+            uint32_t incl = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (tid >= o) incl += u;
+            }
+            const uint32_t excl = incl - tot;
+            if (excl < kth && kth <= incl) {
+                uint32_t run = excl;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    if (run < kth && kth <= run + cnt[t]) {
+                        state[0] = prefix | ((uint32_t)(tid * 8 + t) << shift);
+                        state[1] = kth - run;
+                    }
+                    run += cnt[t];
+                }
+            }
+        }
+        __syncthreads();
+        prefix = state[0];
+        kth = state[1];
+        mask |= 255u << shift;
+        __syncthreads();
+    }
+    return prefix;
+}
+
+// Ascending bitonic sort of n (a power of two) 64-bit keys by NT threads.
+template <int NT>
+__device__ void bitonic_sort_u64(unsigned long long* keys, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = threadIdx.x; t < n / 2; t += NT) {
+                const uint32_t lo = 2 * t - (t & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const unsigned long long a = keys[lo], b = keys[hi];
+                if ((a > b) == ((lo & size) == 0)) {
+                    keys[lo] = b;
+                    keys[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 }  // namespace pgpu

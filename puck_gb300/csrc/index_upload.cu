@@ -3,6 +3,8 @@
 // constants of HierarchicalClusterIndex::read_coodbooks
 // (puck/hierarchical_cluster/hierarchical_cluster_index.cpp:278-320) and
 // PuckIndex::convert_local_to_memory_idx (puck/puck/puck_index.cpp:284-305).
+#include <cuda_bf16.h>
+
 #include <cfloat>
 #include <cmath>
 
@@ -20,6 +22,25 @@ __global__ void k_gather_rows(const float* __restrict__ src, const uint32_t* __r
     const float* s = src + (uint64_t)rows[w] * d;
     float* t = dst + w * d;
     for (uint32_t k = lane; k < d; k += 32) t[k] = s[k];
+}
+
+// BF16 copy of each row (round to nearest even) and |x| rounded up.
+__global__ void k_bf16_rows(const float* __restrict__ src, uint64_t n, uint32_t d,
+                            uint16_t* __restrict__ dst, float* __restrict__ absn) {
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const float* s = src + w * d;
+    uint16_t* t = dst + w * d;
+    float acc = 0.0f;
+    for (uint32_t k = lane; k < d; k += 32) {
+        const float x = s[k];
+        t[k] = __bfloat16_as_ushort(__float2bfloat16_rn(x));
+        acc += x * x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) absn[w] = sqrtf(acc) * (1.0f + 1e-5f) + 1e-30f;
 }
 
 template <class T>
@@ -54,6 +75,16 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     ix->lsq = h.lsq;
     ix->whether_norm = h.whether_norm;
     ix->code_stride = h.code_stride;
+    {
+        // largest codeword norm: bounds every lookup-table entry (precision form)
+        double mx = 0.0;
+        for (uint64_t e = 0; e + h.lsq <= h.codebook.size(); e += h.lsq) {
+            double s2 = 0.0;
+            for (uint32_t t = 0; t < h.lsq; ++t) s2 += (double)h.codebook[e + t] * h.codebook[e + t];
+            if (s2 > mx) mx = s2;
+        }
+        ix->codebook_max = (float)(std::sqrt(mx) * (1.0 + 1e-6));
+    }
     uint64_t bytes = 0;
     const uint64_t cells = (uint64_t)h.C * h.F;
     cudaError_t e = cudaSuccess;
@@ -110,6 +141,30 @@ fail:
     *err = std::string("CUDA error during index upload: ") + cudaGetErrorString(e);
     free_device_index(ix);
     return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
+}
+
+int ensure_bf16_features(DeviceIndex* ix, std::string* err) {
+    if (ix->feat_bf16 != nullptr) return PGPU_OK;
+    uint64_t bytes = 0;
+    cudaError_t e = dev_alloc(&ix->feat_bf16, (uint64_t)ix->n * ix->d, &bytes);
+    if (e == cudaSuccess) e = dev_alloc(&ix->feat_abs, ix->n, &bytes);
+    if (e == cudaSuccess && ix->n) {
+        const uint64_t threads = (uint64_t)ix->n * 32;
+        k_bf16_rows<<<(unsigned)((threads + 255) / 256), 256>>>(ix->feat, ix->n, ix->d,
+                                                                ix->feat_bf16, ix->feat_abs);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        if (ix->feat_bf16) cudaFree(ix->feat_bf16);
+        if (ix->feat_abs) cudaFree(ix->feat_abs);
+        ix->feat_bf16 = nullptr;
+        ix->feat_abs = nullptr;
+        *err = std::string("BF16 feature copy: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
+    }
+    ix->bytes += bytes;
+    return PGPU_OK;
 }
 
 }  // namespace pgpu

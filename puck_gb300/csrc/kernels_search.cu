@@ -405,6 +405,12 @@ __global__ __launch_bounds__(256) void k_nearest_center(const float* __restrict_
     }
 }
 
+__global__ void k_gather_u32(const uint32_t* __restrict__ idx, uint64_t n,
+                             const uint32_t* __restrict__ table, uint32_t* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = idx[i] == kNoLabel ? kNoLabel : table[idx[i]];
+}
+
 __global__ void k_norms_full(const float* __restrict__ X, uint64_t rows, uint32_t d,
                              float* __restrict__ out) {
     const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -524,6 +530,13 @@ cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint
     k_nearest_center<<<(unsigned)((n + kTile - 1) / kTile), 256, 0, stream>>>(x, n, cents, k, dim,
                                                                              xnorm, cnorm, assign,
                                                                              dis);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_u32(const uint32_t* idx, uint64_t n, const uint32_t* table,
+                              uint32_t* out, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    k_gather_u32<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(idx, n, table, out);
     return cudaGetLastError();
 }
 

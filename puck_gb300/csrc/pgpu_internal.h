@@ -46,6 +46,9 @@ struct DeviceIndex {
     float* offsets = nullptr;       // [n] filter offset per point
     uint8_t* codes = nullptr;       // [n][code_stride]
     float* feat = nullptr;          // [n][d] original vectors
+    uint16_t* feat_bf16 = nullptr;  // [n][d] BF16 copy (precision form; made on first use)
+    float* feat_abs = nullptr;      // [n] |x| rounded up (error bound of the BF16 screen)
+    float codebook_max = 0.0f;      // largest |codeword| (FP16 table scale bound)
     float* codebook = nullptr;      // [nsq][256][lsq]
     uint64_t bytes = 0;
 };
@@ -74,6 +77,10 @@ struct SearchConfig {
     uint32_t P = 200, T = 1100, topk_max = 100;
     double radius_rate = 1.0;
     int mode = PGPU_MODE_EXACT;
+    int precision = PGPU_PRECISION_FP32;
+    uint32_t margin = 0;  // BF16: extra filter candidates
+    // filter candidates kept per query
+    uint32_t filter_keep() const { return T + (precision == PGPU_PRECISION_BF16 ? margin : 0); }
 };
 
 // Kernel launchers (kernels_search.cu). All enqueue on `stream`.
@@ -96,6 +103,8 @@ cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, 
 cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint64_t k,
                                           const float* x, uint64_t n, int32_t* assign, float* dis,
                                           float* xnorm, float* cnorm, cudaStream_t stream);
+cudaError_t launch_gather_u32(const uint32_t* idx, uint64_t n, const uint32_t* table,
+                              uint32_t* out, cudaStream_t stream);
 // Records `msg` as the calling thread's last error (pgpu_last_error) and returns `code`.
 int set_last_error(int code, const std::string& msg);
 cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
@@ -111,7 +120,15 @@ cudaError_t launch_cell_constants(float* stationary, const uint32_t* cell_start,
 size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T);
 size_t scan_smem_bytes(const DeviceIndex& ix);
 uint32_t scan_max_filter_topk();
-cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
+cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                               cudaStream_t stream);
+size_t scan_smem_bytes_half(const DeviceIndex& ix);
+// BF16 copy of the vectors and their norms (precision form), synchronous.
+int ensure_bf16_features(DeviceIndex* ix, std::string* err);
+size_t rerank_screen_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
+cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t topk, const Scratch& s,
+                                 float* out_dist, uint32_t* out_ids, int32_t* out_status,
+                                 cudaStream_t stream);
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
 
 // BF16 tensor-core contraction (tc_gemm.cu): out = epilogue(sum_k A(i,k) B(j,k)).

@@ -26,7 +26,7 @@ void free_scratch(Scratch* s) {
 }
 
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
-    const uint64_t P = std::min(cfg.P, ix.C), T = cfg.T;
+    const uint64_t P = std::min(cfg.P, ix.C), T = cfg.filter_keep();
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
            fine_order + kNumWalkCounters * 8 + 4;
@@ -37,7 +37,7 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     free_scratch(out);
     Scratch& s = *out;
     s.P = std::min(cfg.P, ix.C);
-    s.T = cfg.T;
+    s.T = cfg.filter_keep();
     // the full fine order is only read by the exact walk
     const uint64_t fine_rows = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F : 1;
     uint64_t b = 0;
@@ -92,8 +92,21 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     mark(2);
     PGPU_STEP(launch_coarse_window(ix, n, s, st), "coarse select");
     mark(3);
-    PGPU_STEP(launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F, st),
-              "fine scores");
+    const bool bf16 = cfg.precision == PGPU_PRECISION_BF16;
+    if (bf16) {
+        // precision form: -q.f from the BF16 tensor-core contraction
+        TcOperand A{s.q, ix.d, 1, n};
+        TcOperand B{ix.fine, ix.d, 1, ix.F};
+        TcEpilogue ep{};
+        ep.mode = TC_EPI_NEG;
+        ep.out = s.dots;
+        ep.ld = ix.F;
+        PGPU_STEP(launch_tc_gemm(A, B, ix.d, ep, s.tc_err, st), "fine scores");
+    } else {
+        PGPU_STEP(launch_centroid_scores(s.q, n, ix.fine, ix.F, ix.d, nullptr, true, s.dots, ix.F,
+                                         st),
+                  "fine scores");
+    }
     mark(4);
     int k = 6;
     if (cfg.mode == PGPU_MODE_EXACT) {
@@ -105,10 +118,14 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     if (cfg.mode == PGPU_MODE_EXACT) {
         PGPU_STEP(launch_walk_scan(ix, cfg, n, s, st), "walk_scan");
     } else {
-        PGPU_STEP(launch_scan_select(ix, n, s, st), "scan_select");
+        PGPU_STEP(launch_scan_select(ix, n, s, bf16, st), "scan_select");
     }
     mark(6);
-    PGPU_STEP(launch_rerank(ix, cfg, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
+    if (bf16) {
+        PGPU_STEP(launch_rerank_screen(ix, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
+    } else {
+        PGPU_STEP(launch_rerank(ix, cfg, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
+    }
     mark(7);
 #undef PGPU_STEP
     if (launched) *launched = k;

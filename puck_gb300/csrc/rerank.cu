@@ -14,6 +14,16 @@
 // Selection: when no two of the topk+1 smallest distances are equal the heap's
 // output is just the ascending order, found by a bitonic sort of
 // (distance, position); otherwise thread 0 replays the heap exactly.
+//
+// k_rerank_screen (precision form): the same result from fewer bytes. Each
+// candidate is first measured on a BF16 copy of its vector; with |x~ - x| <=
+// 2^-8 |x| per row and both sums in FP32, |d~ - d| <= E (see screen_bound), so
+// every candidate whose exact distance can reach the topk-th lies in
+// W = { j : d~_j - E_j <= U }, U = the topk-th smallest d~_j + E_j. Only W is
+// recomputed with the exact FP32 order above, sorted and tie-checked like
+// k_rerank; a tie sends the block to the full exact heap replay.
+#include <cuda_bf16.h>
+
 #include "device_common.cuh"
 #include "pgpu_internal.h"
 
@@ -202,6 +212,180 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     }
 }
 
+// Bound on |d~ - d| for a row with |x| <= xabs and screened distance d~ (d dims).
+__device__ __forceinline__ float screen_bound(float dt, float xabs, uint32_t d) {
+    const float ta = sqrtf(fmaxf(dt, 0.0f)) * 1.0009765625f + 1e-20f;
+    const float dx = 0.00390625f * xabs * 1.0009765625f;
+    const float tb = ta + dx;
+    return dx * (2.0f * ta + dx) + (float)(3 * d + 8) * 1.1920928955078125e-07f * tb * tb + 1e-30f;
+}
+
+struct ScreenParams {
+    const float* q;
+    const int32_t* status;
+    const uint32_t* htag;
+    const uint32_t* hcnt;
+    const float* feat;
+    const uint16_t* feat_bf16;
+    const float* feat_abs;
+    const uint32_t* mem2local;
+    float* out_dist;
+    uint32_t* out_ids;
+    int32_t* out_status;
+    uint32_t d, T, Tp, topk;
+};
+
+__global__ __launch_bounds__(kThreads) void k_rerank_screen(ScreenParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);  // [Tp]
+    float* qv = reinterpret_cast<float*>(keys + p.Tp);                       // [d]
+    float* approx = qv + p.d;                                                // [T]
+    float* hi = approx + p.T;                                                // [T] d~ + E, then exact
+    float* bnd = hi + p.T;                                                   // [T]
+    float* hv = bnd + p.T;                                                   // [topk + 1]
+    uint32_t* ht = reinterpret_cast<uint32_t*>(hv + p.topk + 1);             // [topk + 1]
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t state[2];
+    __shared__ uint32_t wcount;
+    const uint32_t qi = blockIdx.x, topk = p.topk, d = p.d;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float* od = p.out_dist + (uint64_t)qi * topk;
+    uint32_t* oi = p.out_ids + (uint64_t)qi * topk;
+    const int32_t stq = p.status[qi];
+    if (p.out_status && tid == 0) p.out_status[qi] = stq;
+    if (stq != 0) {
+        for (uint32_t i = tid; i < topk; i += kThreads) {
+            od[i] = sentinel_f();
+            oi[i] = kNoLabel;
+        }
+        return;
+    }
+    const uint32_t cnt = p.hcnt[qi];
+    const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
+    for (uint32_t i = tid; i < d; i += kThreads) qv[i] = p.q[(uint64_t)qi * d + i];
+    if (tid == 0) wcount = 0;
+    __syncthreads();
+    bool full = cnt <= topk;
+    if (!full) {
+        // screen: kRows BF16 rows per warp in flight
+        for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
+            float acc[kRows];
+            const uint16_t* rows[kRows];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const uint32_t j = j0 + u;
+                rows[u] = p.feat_bf16 + (uint64_t)tags[j < cnt ? j : j0] * d;
+                acc[u] = 0.0f;
+            }
+            for (uint32_t k = lane; k < d; k += 32) {
+                const float qk = qv[k];
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const float x = __bfloat162float(__ushort_as_bfloat16(__ldg(rows[u] + k)));
+                    const float df = qk - x;
+                    acc[u] += df * df;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRows; ++u)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+            if (lane < kRows) {
+                float mine = acc[0];
+#pragma unroll
+                for (int u = 1; u < kRows; ++u)
+                    if (lane == u) mine = acc[u];
+                const uint32_t j = j0 + lane;
+                if (j < cnt) {
+                    const float e = screen_bound(mine, p.feat_abs[tags[j]], d);
+                    approx[j] = mine;
+                    bnd[j] = e;
+                    hi[j] = mine + e;
+                }
+            }
+        }
+        __syncthreads();
+        const float U = key_to_float(block_kth_key<kThreads>(hi, cnt, topk, hist, state));
+        for (uint32_t j = tid; j < cnt; j += kThreads)
+            if (approx[j] - bnd[j] <= U) keys[atomicAdd(&wcount, 1u)] = j;
+        __syncthreads();
+        const uint32_t m = wcount;
+        // exact FP32 distances of the window, in the reference's order
+        for (uint32_t i0 = warp * kRows; i0 < m; i0 += kWarps * kRows) {
+            const float* rows[kRows];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const uint32_t i = i0 + u;
+                rows[u] = p.feat + (uint64_t)tags[(uint32_t)keys[i < m ? i : i0]] * d;
+            }
+            float v[kRows];
+            warp_l2_exact<kRows>(rows, qv, d, lane, v);
+            __syncwarp();
+            if (lane == 0) {
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const uint32_t i = i0 + u;
+                    if (i < m) {
+                        const uint32_t j = (uint32_t)keys[i];
+                        keys[i] = ((unsigned long long)ordered_key(v[u]) << 32) | j;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        uint32_t mp = 2;
+        while (mp < m) mp <<= 1;
+        for (uint32_t i = m + tid; i < mp; i += kThreads) keys[i] = ~0ull;
+        __syncthreads();
+        bitonic_sort_u64<kThreads>(keys, mp);
+        const uint32_t check = m - 1 < topk ? m - 1 : topk;
+        int tie = 0;
+        for (uint32_t i = tid; i < check; i += kThreads)
+            if ((uint32_t)(keys[i] >> 32) == (uint32_t)(keys[i + 1] >> 32)) tie = 1;
+        tie = __syncthreads_or(tie);
+        if (!tie) {
+            for (uint32_t i = tid; i < topk; i += kThreads) {
+                od[i] = key_to_float((uint32_t)(keys[i] >> 32));
+                oi[i] = p.mem2local[tags[(uint32_t)keys[i]]];
+            }
+            return;
+        }
+        full = true;
+    }
+    // every candidate exactly, then MaxHeap(topk) in candidate order and reorder()
+    for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
+        const float* rows[kRows];
+#pragma unroll
+        for (int u = 0; u < kRows; ++u) {
+            const uint32_t j = j0 + u;
+            rows[u] = p.feat + (uint64_t)tags[j < cnt ? j : j0] * d;
+        }
+        float v[kRows];
+        warp_l2_exact<kRows>(rows, qv, d, lane, v);
+        if (lane == 0) {
+#pragma unroll
+            for (int u = 0; u < kRows; ++u)
+                if (j0 + u < cnt) hi[j0 + u] = v[u];
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float* h1 = hv;  // 1-based: slots 1..topk
+        for (uint32_t i = 1; i <= topk; ++i) h1[i] = sentinel_f();
+        uint32_t dpc = topk;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const float v = hi[j];
+            if (v < h1[1]) heap_update(h1, ht, topk, dpc, v, p.mem2local[tags[j]]);
+        }
+        heap_reorder(h1, ht, topk);
+        const uint32_t rn = topk - dpc;
+        for (uint32_t i = 0; i < topk; ++i) {
+            od[i] = h1[i + 1];
+            oi[i] = i < rn ? ht[i + 1] : kNoLabel;
+        }
+    }
+}
+
 uint32_t pow2_at_least(uint32_t v) {
     uint32_t p = 2;
     while (p < v) p <<= 1;
@@ -240,6 +424,43 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
         attr_set = true;
     }
     k_rerank<<<n, kThreads, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+size_t rerank_screen_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
+    const uint32_t Tp = pow2_at_least(T);
+    return sizeof(unsigned long long) * Tp + sizeof(float) * (ix.d + 3ull * T) +
+           (sizeof(float) + sizeof(uint32_t)) * (topk + 1ull);
+}
+
+cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t topk, const Scratch& s,
+                                 float* out_dist, uint32_t* out_ids, int32_t* out_status,
+                                 cudaStream_t stream) {
+    if (ix.feat_bf16 == nullptr || ix.feat_abs == nullptr) return cudaErrorInvalidValue;
+    ScreenParams p;
+    p.q = s.q;
+    p.status = s.status;
+    p.htag = s.htag;
+    p.hcnt = s.hcnt;
+    p.feat = ix.feat;
+    p.feat_bf16 = ix.feat_bf16;
+    p.feat_abs = ix.feat_abs;
+    p.mem2local = ix.mem2local;
+    p.out_dist = out_dist;
+    p.out_ids = out_ids;
+    p.out_status = out_status;
+    p.d = ix.d;
+    p.T = s.T;
+    p.Tp = pow2_at_least(s.T);
+    p.topk = topk;
+    const size_t smem = rerank_screen_smem_bytes(ix, s.T, topk);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_rerank_screen, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024);
+        attr_set = true;
+    }
+    k_rerank_screen<<<n, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 

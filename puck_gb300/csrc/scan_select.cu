@@ -16,6 +16,14 @@
 // (2*cell_dist + offset, id) key is not below tau are dropped before the table
 // lookups (t can only grow). When the buffer fills it is bitonic-sorted and cut
 // back to filter_topk keys. The output is sorted ascending by (t, id).
+//
+// Precision form (HALF): the table is stored in FP16, scaled per query by a
+// power of two 2^e chosen from the bound (|q| + max |codeword|)^2 >= every entry
+// so that all entries stay below 32768; lookups are accumulated in FP32 and the
+// sum is multiplied by 2^-e. Entries are non-negative, so t >= t0 still holds and
+// the threshold test before the lookups stays valid.
+#include <cuda_fp16.h>
+
 #include "device_common.cuh"
 #include "pgpu_internal.h"
 
@@ -45,7 +53,45 @@ struct ScanParams {
     const float* codebook;
     unsigned long long* counters;
     uint32_t d, C, F, nsq, lsq, code_stride, P, T;
+    float codebook_max;
 };
+
+// FP16 table of the precision form: entry * scale, rounded to nearest.
+__device__ __forceinline__ void build_lut_half(__half* lut, const float* qv,
+                                               const float* __restrict__ cb, uint32_t nsq,
+                                               uint32_t lsq, float scale) {
+    const uint32_t total = nsq * 256;
+    for (uint32_t e = threadIdx.x; e < total; e += kThreads) {
+        const uint32_t m = e >> 8, j = e & 255;
+        float v;
+        if (lsq == 4) {
+            const float4 y = __ldg(reinterpret_cast<const float4*>(cb) + e);
+            const float* x = qv + m * 4;
+            const float t0 = x[0] - y.x, t1 = x[1] - y.y, t2 = x[2] - y.z, t3 = x[3] - y.w;
+            v = (t0 * t0 + t1 * t1) + (t2 * t2 + t3 * t3);
+        } else {
+            v = l2sqr_sse(qv + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
+        }
+        lut[e] = __float2half_rn(v * scale);
+    }
+}
+
+template <int NW>
+__device__ __forceinline__ float lut_sum_words_half(const uint32_t (&w)[NW], const __half* lut,
+                                                    uint32_t nsq) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+        const uint32_t m = 4u * i;
+        if (m >= nsq) break;
+        const uint32_t c = w[i];
+        a0 += __half2float(lut[(m + 0) * 256 + (c & 0xff)]);
+        if (m + 1 < nsq) a1 += __half2float(lut[(m + 1) * 256 + ((c >> 8) & 0xff)]);
+        if (m + 2 < nsq) a2 += __half2float(lut[(m + 2) * 256 + ((c >> 16) & 0xff)]);
+        if (m + 3 < nsq) a3 += __half2float(lut[(m + 3) * 256 + (c >> 24)]);
+    }
+    return (a0 + a1) + (a2 + a3);
+}
 
 // (t, memory id) packed into one 64-bit key whose unsigned order is the
 // lexicographic order of (t as a float, id): -0 is folded onto +0 so that equal
@@ -197,8 +243,8 @@ struct ScanState {
     unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
 
-// NW = code words per record (code_stride / 4).
-template <int NW>
+// NW = code words per record (code_stride / 4); HALF = FP16 table.
+template <int NW, bool HALF>
 __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ScanState st;
@@ -206,7 +252,9 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
     const int tid = threadIdx.x;
     const uint32_t nsq = p.nsq, F = p.F, T = p.T;
     float* lut = reinterpret_cast<float*>(smem + sizeof(uint64_t) * kCandCap);
-    float* srow = lut + nsq * 256;         // [F] 2 * cell_dist of the current cluster's cells
+    __half* luth = reinterpret_cast<__half*>(lut);
+    float* srow = HALF ? reinterpret_cast<float*>(luth + nsq * 256)
+                       : lut + nsq * 256;  // [F] 2 * cell_dist of the current cluster's cells
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [kCandCap], first (8-byte aligned)
     float* qv = srow + F;                  // [d]
 
@@ -225,7 +273,17 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
     }
     __syncthreads();
-    build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
+    float inv_scale = 1.0f;
+    if (HALF) {
+        const float qa = sqrtf(p.qnorm[qi]) + p.codebook_max;
+        const float bound = qa * qa * 1.0001f + 1e-30f;
+        int e = (int)floorf(log2f(32768.0f / bound));
+        e = e < -60 ? -60 : (e > 60 ? 60 : e);
+        inv_scale = ldexpf(1.0f, -e);
+        build_lut_half(luth, qv, p.codebook, nsq, p.lsq, ldexpf(1.0f, e));
+    } else {
+        build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
+    }
     unsigned long long my_eval = 0, my_pass = 0;
     __syncthreads();
     const long long t_pro = clock64();
@@ -279,7 +337,9 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
                     const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
                     ++my_eval;
                     if (pack_key(t0, mi) < tau) {  // t can only grow past t0
-                        const float t = __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
+                        const float t =
+                            HALF ? t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale
+                                 : __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
                         key = pack_key(t, mi);
                         keep = key < tau;
                     }
@@ -358,9 +418,14 @@ size_t scan_smem_bytes(const DeviceIndex& ix) {
            sizeof(float) * ix.d;
 }
 
+size_t scan_smem_bytes_half(const DeviceIndex& ix) {
+    return sizeof(uint64_t) * kCandCap + sizeof(__half) * ix.nsq * 256 + sizeof(float) * ix.F +
+           sizeof(float) * ix.d;
+}
+
 uint32_t scan_max_filter_topk() { return kCandCap - kRound; }
 
-cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s,
+cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                cudaStream_t stream) {
     ScanParams p;
     p.q = s.q;
@@ -387,9 +452,10 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s,
     p.code_stride = ix.code_stride;
     p.P = s.P;
     p.T = s.T;
-    const size_t smem = scan_smem_bytes(ix);
+    p.codebook_max = ix.codebook_max;
+    const size_t smem = half_lut ? scan_smem_bytes_half(ix) : scan_smem_bytes(ix);
     const uint32_t nw = ix.code_stride / 4;
-    static bool attr_set[5] = {false, false, false, false, false};  // one per instantiation
+    static bool attr_set[10] = {};  // one per instantiation
     auto launch = [&](void (*kernel)(ScanParams), int slot) {
         if (!attr_set[slot]) {
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
@@ -397,11 +463,19 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s,
         }
         kernel<<<n, kThreads, smem, stream>>>(p);
     };
-    if (nw <= 2) launch(k_scan_select<2>, 0);
-    else if (nw <= 4) launch(k_scan_select<4>, 1);
-    else if (nw <= 6) launch(k_scan_select<6>, 2);
-    else if (nw <= 8) launch(k_scan_select<8>, 3);
-    else launch(k_scan_select<16>, 4);
+    if (half_lut) {
+        if (nw <= 2) launch(k_scan_select<2, true>, 5);
+        else if (nw <= 4) launch(k_scan_select<4, true>, 6);
+        else if (nw <= 6) launch(k_scan_select<6, true>, 7);
+        else if (nw <= 8) launch(k_scan_select<8, true>, 8);
+        else launch(k_scan_select<16, true>, 9);
+    } else {
+        if (nw <= 2) launch(k_scan_select<2, false>, 0);
+        else if (nw <= 4) launch(k_scan_select<4, false>, 1);
+        else if (nw <= 6) launch(k_scan_select<6, false>, 2);
+        else if (nw <= 8) launch(k_scan_select<8, false>, 3);
+        else launch(k_scan_select<16, false>, 4);
+    }
     return cudaGetLastError();
 }
 

@@ -263,9 +263,7 @@ bool operand_vec(const TcOperand& op, uint32_t K) {
 
 }  // namespace
 
-// The two stages plus 32 KiB of slack: every descriptor-addressed byte stays
-// inside the CTA's allocation even for a misread of the leading/stride offsets.
-size_t tc_gemm_smem_bytes() { return 2 * (size_t)kStageBytes + 32768; }
+size_t tc_gemm_smem_bytes() { return 2 * (size_t)kStageBytes; }
 
 cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
                            const TcEpilogue& ep, int* err, cudaStream_t stream) {

@@ -33,64 +33,6 @@ __device__ __forceinline__ float window_eps(uint32_t d) {
     return 0.0078125f + 3.0517578125e-05f + (float)(d + 8) * 4.76837158203125e-07f;
 }
 
-__device__ __forceinline__ uint32_t ordered_key(float v) {
-    const uint32_t b = __float_as_uint(v);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-__device__ __forceinline__ float key_to_float(uint32_t k) {
-    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
-}
-
-// K-th smallest (1-based) ordered key among vals[0..L) with a 4-pass 8-bit radix
-// select; every thread returns it.
-__device__ uint32_t block_kth_key(const float* vals, uint32_t L, uint32_t K, uint32_t* hist,
-                                  uint32_t* shared_state) {
-    uint32_t prefix = 0, mask = 0, kth = K;
-    const int tid = threadIdx.x;
-    for (int shift = 24; shift >= 0; shift -= 8) {
-        for (int b = tid; b < 256; b += kWinThreads) hist[b] = 0;
-        __syncthreads();
-        for (uint32_t j = tid; j < L; j += kWinThreads) {
-            const uint32_t key = ordered_key(vals[j]);
-            if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
-        }
-        __syncthreads();
-        if (tid < 32) {
-            // lane l owns bins 8l .. 8l+7
-            uint32_t cnt[8], tot = 0;
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                cnt[t] = hist[tid * 8 + t];
-                tot += cnt[t];
-            }
-            uint32_t incl = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-                if (tid >= o) incl += u;
-            }
-            const uint32_t excl = incl - tot;
-            if (excl < kth && kth <= incl) {
-                uint32_t run = excl;
-#pragma unroll
-                for (int t = 0; t < 8; ++t) {
-                    if (run < kth && kth <= run + cnt[t]) {
-                        shared_state[0] = prefix | ((uint32_t)(tid * 8 + t) << shift);
-                        shared_state[1] = kth - run;
-                    }
-                    run += cnt[t];
-                }
-            }
-        }
-        __syncthreads();
-        prefix = shared_state[0];
-        kth = shared_state[1];
-        mask |= 255u << shift;
-        __syncthreads();
-    }
-    return prefix;
-}
-
 // Exact top-P of bias_j - q.c_j per row (k_topsort's output and tie rule).
 __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     const float* __restrict__ approx, uint32_t ld, const float* __restrict__ Q, uint32_t d,
@@ -135,7 +77,7 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
             slo[j] = s - e;
         }
         __syncthreads();
-        const float U = key_to_float(block_kth_key(shi, C, P, hist, state));
+        const float U = key_to_float(block_kth_key<kWinThreads>(shi, C, P, hist, state));
         for (uint32_t j = tid; j < C; j += kWinThreads) {
             if (slo[j] <= U) {
                 const uint32_t pos = atomicAdd(&ncand, 1u);
@@ -160,21 +102,7 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
                 }
             }
             __syncthreads();
-            for (uint32_t size = 2; size <= mp; size <<= 1) {
-                for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-                    for (uint32_t t = tid; t < mp / 2; t += kWinThreads) {
-                        const uint32_t lo = 2 * t - (t & (stride - 1));
-                        const uint32_t hi = lo + stride;
-                        const bool asc = (lo & size) == 0;
-                        const unsigned long long x = ckey[lo], y = ckey[hi];
-                        if ((x > y) == asc) {
-                            ckey[lo] = y;
-                            ckey[hi] = x;
-                        }
-                    }
-                    __syncthreads();
-                }
-            }
+            bitonic_sort_u64<kWinThreads>(ckey, mp);
             int tie = 0;
             const uint32_t last = P < m ? P : m - 1;
             for (uint32_t i = tid; i < last; i += kWinThreads)
@@ -243,9 +171,9 @@ __global__ __launch_bounds__(256) void k_window_argmin(
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) U = fminf(U, __shfl_xor_sync(0xffffffffu, U, o));
     }
+    // the reference's scan: min starts at FLT_MAX, strict < in ascending id order
     float best = FLT_MAX;
-    uint32_t bidx = 0;
-    bool found = false;
+    uint32_t bidx = 0xFFFFFFFFu;
     for (uint32_t j = lane; j < K; j += 32) {
         if (screen) {
             const float s = a[j];
@@ -256,26 +184,22 @@ __global__ __launch_bounds__(256) void k_window_argmin(
         }
         const float cur =
             __fsub_rn(__fadd_rn(xn, cnorm[j]), 2.0f * dot_seq(x, cents + (uint64_t)j * d, d));
-        if (!found || cur < best) {  // j ascends within a lane
+        if (cur < best) {  // j ascends within a lane
             best = cur;
             bidx = j;
-            found = true;
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(0xffffffffu, best, o);
         const uint32_t oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-        const bool of = __shfl_xor_sync(0xffffffffu, found ? 1 : 0, o) != 0;
-        if (of && (!found || ov < best || (ov == best && oi < bidx))) {
+        if (ov < best || (ov == best && oi < bidx)) {
             best = ov;
             bidx = oi;
-            found = true;
         }
     }
     if (lane == 0) {
-        // The reference starts from min = FLT_MAX: no centroid below it -> id 0.
-        if (!found || !(best < FLT_MAX)) {
+        if (bidx == 0xFFFFFFFFu) {  // nothing below FLT_MAX: the reference keeps id 0
             best = FLT_MAX;
             bidx = 0;
         }

@@ -22,6 +22,8 @@ PGPU_E_LIMIT = -7
 PGPU_E_TIMEOUT = -8
 PGPU_MODE_EXACT = 0
 PGPU_MODE_SCAN = 1
+PGPU_PRECISION_FP32 = 0
+PGPU_PRECISION_BF16 = 1
 
 HEAP_SENTINEL = np.uint32(0x7F7F7F7F).view(np.float32)
 NO_LABEL = 0xFFFFFFFF
@@ -33,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
     "pgpu_nearest_center_noalloc", "pgpu_server_params_default", "pgpu_server_create",
     "pgpu_server_submit", "pgpu_server_wait", "pgpu_server_stats_get", "pgpu_server_destroy",
-    "pgpu_contract_bf16",
+    "pgpu_contract_bf16", "pgpu_filter_candidates",
 )
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_CENTROIDS = 1 << 16
@@ -54,7 +56,8 @@ class Params(ctypes.Structure):
     _fields_ = [("search_coarse_count", ctypes.c_uint32), ("topk", ctypes.c_uint32),
                 ("filter_topk", ctypes.c_uint32), ("radius_rate", ctypes.c_double),
                 ("device", ctypes.c_int32), ("max_batch", ctypes.c_uint32),
-                ("mode", ctypes.c_int32)]
+                ("mode", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("filter_margin", ctypes.c_uint32)]
 
 
 class IndexInfo(ctypes.Structure):
@@ -133,6 +136,7 @@ def load(build_if_missing=False):
     lib.pgpu_server_stats_get.argtypes = [vp, ctypes.POINTER(ServerStats)]
     lib.pgpu_server_destroy.argtypes = [vp]
     f32 = ctypes.c_float
+    lib.pgpu_filter_candidates.argtypes = [vp, u32, vp, vp, vp, vp]
     lib.pgpu_contract_bf16.argtypes = [ctypes.c_int32, u32, u32, u32, vp, u64, u64, vp, u64, u64,
                                        vp, vp, u64, vp, u64, vp, f32, f32, vp]
     lib.pgpu_last_error.restype = ctypes.c_char_p
@@ -257,6 +261,20 @@ class GpuIndex:
         arr = (ctypes.c_uint64 * len(WALK_COUNTERS))()
         check(load().pgpu_walk_counters(self._h, arr, len(WALK_COUNTERS)))
         return dict(zip(WALK_COUNTERS, list(arr)))
+
+    def filter_candidates(self, queries):
+        """Scan-mode filter candidates of one pass: (labels [n, keep], filter
+        distances [n, keep], counts [n]), keep = filter_topk (+ filter_margin in BF16)."""
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, self.d)
+        n = q.shape[0]
+        p = self.params
+        keep = p.filter_topk + (p.filter_margin if p.precision == PGPU_PRECISION_BF16 else 0)
+        labels = np.empty((n, keep), np.uint32)
+        dist = np.empty((n, keep), np.float32)
+        cnt = np.empty(n, np.uint32)
+        check(load().pgpu_filter_candidates(self._h, n, q.ctypes.data, labels.ctypes.data,
+                                            dist.ctypes.data, cnt.ctypes.data))
+        return labels, dist, cnt
 
     def last_stats(self):
         k, r, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()

@@ -43,6 +43,7 @@ def test_params_default_matches_reference_flags(lib):
     assert p.filter_topk == 1100
     assert p.radius_rate == 1.0
     assert p.mode == native.PGPU_MODE_EXACT
+    assert p.precision == native.PGPU_PRECISION_FP32 and p.filter_margin == 0
 
 
 def test_null_arguments_rejected(lib):
@@ -61,6 +62,14 @@ def test_bad_search_params_rejected_before_device(lib, tmp_path):
     p = native.default_params(filter_topk=50, topk=100)
     assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_INVALID
     p = native.default_params(filter_topk=100000)
+    assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_LIMIT
+    # the precision form runs in scan mode only, within the scan's candidate buffer
+    p = native.default_params(precision=native.PGPU_PRECISION_BF16)
+    assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_INVALID
+    p = native.default_params(precision=7, mode=native.PGPU_MODE_SCAN, filter_topk=500)
+    assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_INVALID
+    p = native.default_params(precision=native.PGPU_PRECISION_BF16, mode=native.PGPU_MODE_SCAN,
+                              filter_topk=900, filter_margin=200)
     assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_LIMIT
 
 
