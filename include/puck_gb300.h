@@ -170,7 +170,8 @@ int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
 /* Diagnostic of the scan-mode filter stage: runs one pass of n <= max_batch HOST
  * queries and returns, per query, the candidates handed to the rerank: labels
  * (input-order ids) and filter distances, filter_topk (+ filter_margin in BF16)
- * slots per query in ascending filter distance, and count[i] of them filled. */
+ * slots per query (the set of the smallest filter distances, unordered), and
+ * count[i] of them filled. */
 int pgpu_filter_candidates(pgpu_index* index, uint32_t n, const float* query, uint32_t* labels,
                            float* distance, uint32_t* count);
 

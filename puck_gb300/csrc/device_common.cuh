@@ -281,4 +281,49 @@ __device__ void bitonic_sort_u64(unsigned long long* keys, uint32_t n) {
     }
 }
 
+// (t, memory id) of a filter candidate as one 64-bit key whose unsigned order is
+// the lexicographic order of (t as a float, id); -0 is folded onto +0 so that
+// equal floats compare equal.
+__device__ __forceinline__ uint64_t filter_key(float t, uint32_t id) {
+    uint32_t b = __float_as_uint(t == 0.0f ? 0.0f : t);
+    b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    return ((uint64_t)b << 32) | id;
+}
+
+// Ascending bitonic sort of n (a power of two) keys with companion values.
+template <int NT>
+__device__ void bitonic_sort_pairs(unsigned long long* keys, uint32_t* vals, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = threadIdx.x; t < n / 2; t += NT) {
+                const uint32_t lo = 2 * t - (t & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const unsigned long long a = keys[lo], b = keys[hi];
+                if ((a > b) == ((lo & size) == 0)) {
+                    keys[lo] = b;
+                    keys[hi] = a;
+                    const uint32_t va = vals[lo];
+                    vals[lo] = vals[hi];
+                    vals[hi] = va;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Positions 0..cnt of scan-mode candidates in the filter's (t, memory id) order
+// (the order in which the reference's heap would have been fed); n2 >= cnt is a
+// power of two. All NT threads call it.
+template <int NT>
+__device__ void order_by_filter_key(const float* t, const uint32_t* mem_id, uint32_t cnt,
+                                    uint32_t n2, unsigned long long* keys, uint32_t* pos) {
+    for (uint32_t i = threadIdx.x; i < n2; i += NT) {
+        keys[i] = i < cnt ? filter_key(t[i], mem_id[i]) : ~0ull;
+        pos[i] = i;
+    }
+    __syncthreads();
+    bitonic_sort_pairs<NT>(keys, pos, n2);
+}
+
 }  // namespace pgpu

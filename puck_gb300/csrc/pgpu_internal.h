@@ -68,7 +68,8 @@ struct Scratch {
     uint32_t* htag = nullptr;  // [B][T] filter heap memory ids
     uint32_t* hcnt = nullptr;  // [B]
     unsigned long long* counters = nullptr; // [kNumWalkCounters] walk diagnostics
-    int* tc_err = nullptr;     // set by a tensor-core contraction whose wait expired
+    int* tc_err = nullptr;     // set by a tensor-core contraction or table copy whose wait expired
+    unsigned char* luts = nullptr; // scan mode: [B][nsq*256] lookup tables (FP32, or FP16)
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;
 };

@@ -19,7 +19,7 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
 
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
-                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err};
+                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err, s->luts};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *s = Scratch();
@@ -28,8 +28,9 @@ void free_scratch(Scratch* s) {
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
     const uint64_t P = std::min(cfg.P, ix.C), T = cfg.filter_keep();
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
+    const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * ix.nsq * 256 * 4 : 0;
     return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
-           fine_order + kNumWalkCounters * 8 + 4;
+           fine_order + tables + kNumWalkCounters * 8 + 4;
 }
 
 int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Scratch* out,
@@ -57,6 +58,7 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     PGPU_ALLOC(s.hcnt, B);
     PGPU_ALLOC(s.counters, kNumWalkCounters);
     PGPU_ALLOC(s.tc_err, 1);
+    if (cfg.mode == PGPU_MODE_SCAN) PGPU_ALLOC(s.luts, (uint64_t)B * ix.nsq * 256 * 4);
 #undef PGPU_ALLOC
     if (e != cudaSuccess) {
         free_scratch(&s);

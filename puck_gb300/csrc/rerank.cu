@@ -37,6 +37,8 @@ constexpr int kRows = 8;  // candidate rows per warp in flight
 struct RerankParams {
     const float* q;
     const int32_t* status;
+    const float* hdist;
+    int sort_ties;  // scan mode: replay ties in the filter's (t, memory id) order
     const uint32_t* htag;
     const uint32_t* hcnt;
     const float* feat;
@@ -114,10 +116,12 @@ __device__ __forceinline__ void warp_l2_exact(const float* const* rows, const fl
 
 __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    float* qv = reinterpret_cast<float*>(smem);
+    unsigned long long* okey = reinterpret_cast<unsigned long long*>(smem);  // [Tp]
+    float* qv = reinterpret_cast<float*>(okey + p.Tp);
     float* dist = qv + p.d;                                   // [T]
     float* sv = dist + p.T;                                   // [Tp]
     uint32_t* si = reinterpret_cast<uint32_t*>(sv + p.Tp);    // [Tp]
+    uint32_t* opos = si + p.Tp;                               // [Tp]
     const uint32_t qi = blockIdx.x, topk = p.topk;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float* od = p.out_dist + (uint64_t)qi * topk;
@@ -193,13 +197,16 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
         return;
     }
     __syncthreads();
+    if (p.sort_ties)
+        order_by_filter_key<kThreads>(p.hdist + (uint64_t)qi * p.T, tags, cnt, p.Tp, okey, opos);
     if (tid == 0) {
         // exact MaxHeap(topk) replay in candidate order, then reorder()
         float* hv = sv - 1;
         uint32_t* ht = si - 1;
         for (uint32_t i = 1; i <= topk; ++i) hv[i] = sentinel_f();
         uint32_t dpc = topk;
-        for (uint32_t j = 0; j < cnt; ++j) {
+        for (uint32_t r = 0; r < cnt; ++r) {
+            const uint32_t j = p.sort_ties ? opos[r] : r;
             const float v = dist[j];
             if (v < hv[1]) heap_update(hv, ht, topk, dpc, v, p.mem2local[tags[j]]);
         }
@@ -223,6 +230,7 @@ __device__ __forceinline__ float screen_bound(float dt, float xabs, uint32_t d) 
 struct ScreenParams {
     const float* q;
     const int32_t* status;
+    const float* hdist;
     const uint32_t* htag;
     const uint32_t* hcnt;
     const float* feat;
@@ -244,6 +252,7 @@ __global__ __launch_bounds__(kThreads) void k_rerank_screen(ScreenParams p) {
     float* bnd = hi + p.T;                                                   // [T]
     float* hv = bnd + p.T;                                                   // [topk + 1]
     uint32_t* ht = reinterpret_cast<uint32_t*>(hv + p.topk + 1);             // [topk + 1]
+    uint32_t* opos = ht + p.topk + 1;                                        // [Tp]
     __shared__ uint32_t hist[256];
     __shared__ uint32_t state[2];
     __shared__ uint32_t wcount;
@@ -369,11 +378,14 @@ __global__ __launch_bounds__(kThreads) void k_rerank_screen(ScreenParams p) {
         }
     }
     __syncthreads();
+    // the heap is fed in the filter's (t, memory id) order
+    order_by_filter_key<kThreads>(p.hdist + (uint64_t)qi * p.T, tags, cnt, p.Tp, keys, opos);
     if (tid == 0) {
         float* h1 = hv;  // 1-based: slots 1..topk
         for (uint32_t i = 1; i <= topk; ++i) h1[i] = sentinel_f();
         uint32_t dpc = topk;
-        for (uint32_t j = 0; j < cnt; ++j) {
+        for (uint32_t r = 0; r < cnt; ++r) {
+            const uint32_t j = opos[r];
             const float v = hi[j];
             if (v < h1[1]) heap_update(h1, ht, topk, dpc, v, p.mem2local[tags[j]]);
         }
@@ -396,16 +408,17 @@ uint32_t pow2_at_least(uint32_t v) {
 
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
     const uint32_t Tp = pow2_at_least(T > topk ? T : topk);
-    return sizeof(float) * (ix.d + T) + (sizeof(float) + sizeof(uint32_t)) * Tp;
+    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp;
 }
 
 cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
                           uint32_t topk, const Scratch& s, float* out_dist, uint32_t* out_ids,
                           int32_t* out_status, cudaStream_t stream) {
-    (void)cfg;
     RerankParams p;
     p.q = s.q;
     p.status = s.status;
+    p.hdist = s.hdist;
+    p.sort_ties = cfg.mode == PGPU_MODE_SCAN ? 1 : 0;
     p.htag = s.htag;
     p.hcnt = s.hcnt;
     p.feat = ix.feat;
@@ -430,7 +443,7 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
 size_t rerank_screen_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
     const uint32_t Tp = pow2_at_least(T);
     return sizeof(unsigned long long) * Tp + sizeof(float) * (ix.d + 3ull * T) +
-           (sizeof(float) + sizeof(uint32_t)) * (topk + 1ull);
+           (sizeof(float) + sizeof(uint32_t)) * (topk + 1ull) + sizeof(uint32_t) * Tp;
 }
 
 cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t topk, const Scratch& s,
@@ -440,6 +453,7 @@ cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t top
     ScreenParams p;
     p.q = s.q;
     p.status = s.status;
+    p.hdist = s.hdist;
     p.htag = s.htag;
     p.hcnt = s.hcnt;
     p.feat = ix.feat;

@@ -15,7 +15,8 @@
 // tau = the key of the current filter_topk-th best; records whose
 // (2*cell_dist + offset, id) key is not below tau are dropped before the table
 // lookups (t can only grow). When the buffer fills it is bitonic-sorted and cut
-// back to filter_topk keys. The output is sorted ascending by (t, id).
+// back to filter_topk keys. The output is the set of the filter_topk smallest
+// (t, id) keys, unordered.
 //
 // Precision form (HALF): the table is stored in FP16, scaled per query by a
 // power of two 2^e chosen from the bound (|q| + max |codeword|)^2 >= every entry
@@ -52,27 +53,39 @@ struct ScanParams {
     const uint8_t* codes;
     const float* codebook;
     unsigned long long* counters;
-    uint32_t d, C, F, nsq, lsq, code_stride, P, T;
+    const unsigned char* luts;  // [B][lut_bytes] tables from k_build_luts
+    int* err;                   // set when the table copy did not arrive in time
+    uint32_t d, C, F, nsq, lsq, code_stride, P, T, lut_bytes;
     float codebook_max;
 };
 
-// FP16 table of the precision form: entry * scale, rounded to nearest.
-__device__ __forceinline__ void build_lut_half(__half* lut, const float* qv,
-                                               const float* __restrict__ cb, uint32_t nsq,
-                                               uint32_t lsq, float scale) {
-    const uint32_t total = nsq * 256;
-    for (uint32_t e = threadIdx.x; e < total; e += kThreads) {
-        const uint32_t m = e >> 8, j = e & 255;
-        float v;
-        if (lsq == 4) {
-            const float4 y = __ldg(reinterpret_cast<const float4*>(cb) + e);
-            const float* x = qv + m * 4;
-            const float t0 = x[0] - y.x, t1 = x[1] - y.y, t2 = x[2] - y.z, t3 = x[3] - y.w;
-            v = (t0 * t0 + t1 * t1) + (t2 * t2 + t3 * t3);
-        } else {
-            v = l2sqr_sse(qv + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
-        }
-        lut[e] = __float2half_rn(v * scale);
+// Power-of-two scale of the FP16 table: 2^e with every entry * 2^e < 32768, from
+// the bound (|q| + max |codeword|)^2 on |q_m - c|^2.
+__device__ __forceinline__ int half_lut_exponent(float qnorm, float codebook_max) {
+    const float qa = sqrtf(qnorm) + codebook_max;
+    const float bound = qa * qa * 1.0001f + 1e-30f;
+    int e = (int)floorf(log2f(32768.0f / bound));
+    return e < -60 ? -60 : (e > 60 ? 60 : e);
+}
+
+// get_dist_table (quantization.cpp:260-270) for a batch: block (query, subspace),
+// thread j = codeword j; the reference's lane order via l2sqr_sse.
+template <bool HALF>
+__global__ __launch_bounds__(256) void k_build_luts(const float* __restrict__ q,
+                                                    const float* __restrict__ qnorm,
+                                                    const int32_t* __restrict__ status,
+                                                    const float* __restrict__ cb, uint32_t d,
+                                                    uint32_t nsq, uint32_t lsq, float codebook_max,
+                                                    unsigned char* __restrict__ luts) {
+    const uint32_t qi = blockIdx.x, m = blockIdx.y, j = threadIdx.x;
+    if (status[qi] != 0) return;
+    const float v = l2sqr_sse(q + (uint64_t)qi * d + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
+    const uint64_t e = (uint64_t)qi * nsq * 256 + m * 256 + j;
+    if (HALF) {
+        const float scale = ldexpf(1.0f, half_lut_exponent(qnorm[qi], codebook_max));
+        reinterpret_cast<__half*>(luts)[e] = __float2half_rn(v * scale);
+    } else {
+        reinterpret_cast<float*>(luts)[e] = v;
     }
 }
 
@@ -93,15 +106,6 @@ __device__ __forceinline__ float lut_sum_words_half(const uint32_t (&w)[NW], con
     return (a0 + a1) + (a2 + a3);
 }
 
-// (t, memory id) packed into one 64-bit key whose unsigned order is the
-// lexicographic order of (t as a float, id): -0 is folded onto +0 so that equal
-// floats compare equal, and the IEEE bit pattern is made monotone.
-__device__ __forceinline__ uint64_t pack_key(float t, uint32_t id) {
-    uint32_t b = __float_as_uint(t == 0.0f ? 0.0f : t);
-    b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-    return ((uint64_t)b << 32) | id;
-}
-
 __device__ __forceinline__ float key_value(uint64_t k) {
     uint32_t b = (uint32_t)(k >> 32);
     b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
@@ -110,32 +114,10 @@ __device__ __forceinline__ float key_value(uint64_t k) {
 
 constexpr uint64_t kKeyMax = ~0ull;
 
-// Sorts keys[0..n) ascending; n is a power of two.
-__device__ void bitonic_sort_keys(uint64_t* keys, uint32_t n) {
-    for (uint32_t size = 2; size <= n; size <<= 1) {
-        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            for (uint32_t t = threadIdx.x; t < n / 2; t += kThreads) {
-                const uint32_t lo = 2 * t - (t & (stride - 1));
-                const uint32_t hi = lo + stride;
-                const uint64_t a = keys[lo], b = keys[hi];
-                if ((a > b) == ((lo & size) == 0)) {
-                    keys[lo] = b;
-                    keys[hi] = a;
-                }
-            }
-            __syncthreads();
-        }
-    }
-}
-
-__device__ __forceinline__ uint32_t pow2_ceil(uint32_t v) {
-    uint32_t p = 2;
-    while (p < v) p <<= 1;
-    return p;
-}
-
 // The K-th smallest (1-based) of keys[0..count), all distinct: MSB-first radix
-// select with 8-bit digits. `hist` has 256 slots, `sel` 2. All threads call it.
+// select with 8-bit digits, stopping as soon as the chosen digit's bucket holds
+// one key (usually after the 2nd or 3rd digit of the float). `hist` has 256
+// slots, `sel` 4. All threads call it.
 __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint32_t K,
                                      uint32_t* hist, uint64_t* sel) {
     const int tid = threadIdx.x, lane = tid & 31;
@@ -182,6 +164,7 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
                     if (below < k && k <= below + c[j]) {
                         sel[0] = (uint64_t)(tid * 8 + j);
                         sel[1] = k - below;
+                        sel[2] = c[j];
                     }
                     below += c[j];
                 }
@@ -191,7 +174,17 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
         prefix |= sel[0] << shift;
         mask |= 255ull << shift;
         k = (uint32_t)sel[1];
+        const bool unique = sel[2] == 1;
         __syncthreads();
+        if (unique && shift > 0) {
+            // the one key under this prefix is the K-th
+            for (uint32_t i = tid; i < count; i += kThreads)
+                if ((keys[i] & mask) == prefix) sel[3] = keys[i];
+            __syncthreads();
+            const uint64_t r = sel[3];
+            __syncthreads();
+            return r;
+        }
     }
     return prefix;
 }
@@ -232,7 +225,8 @@ enum { kScRecords = 0, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCy
 
 struct ScanState {
     uint64_t tau;
-    uint64_t sel[2];
+    uint64_t sel[4];
+    uint64_t lut_bar;
     uint32_t hist[256];
     uint32_t ccount;
     uint32_t count;
@@ -263,6 +257,21 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         return;
     }
     const long long t_start = clock64();
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&st.lut_bar);
+    if (tid == 0) {
+        // the query's table: one bulk async copy global -> shared (TMA), completion
+        // counted in bytes on an mbarrier
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1u));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                     "r"(p.lut_bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+            "[%3];" ::"r"((uint32_t)__cvta_generic_to_shared(lut)),
+            "l"(p.luts + (uint64_t)qi * p.lut_bytes), "r"(p.lut_bytes), "r"(bar)
+            : "memory");
+    }
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     const float* fdk = p.fd_by_fine + (uint64_t)qi * F;  // fine terms of this query
     if (tid == 0) {
@@ -273,16 +282,32 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
     }
     __syncthreads();
-    float inv_scale = 1.0f;
-    if (HALF) {
-        const float qa = sqrtf(p.qnorm[qi]) + p.codebook_max;
-        const float bound = qa * qa * 1.0001f + 1e-30f;
-        int e = (int)floorf(log2f(32768.0f / bound));
-        e = e < -60 ? -60 : (e > 60 ? 60 : e);
-        inv_scale = ldexpf(1.0f, -e);
-        build_lut_half(luth, qv, p.codebook, nsq, p.lsq, ldexpf(1.0f, e));
-    } else {
-        build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
+    const float inv_scale = HALF ? ldexpf(1.0f, -half_lut_exponent(p.qnorm[qi], p.codebook_max)) : 1.0f;
+    {
+        // bounded wait for the table (phase 0)
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < (1u << 22) && !done; ++it) {
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                "selp.b32 %0, 1, 0, p;\n}"
+                : "=r"(done)
+                : "r"(bar), "r"(0u)
+                : "memory");
+        }
+        if (!__syncthreads_and(done != 0)) {
+            // the copy did not land: flag it and build the same table here
+            if (tid == 0) atomicExch(p.err, 2);
+            if (HALF) {
+                const float scale = 1.0f / inv_scale;
+                for (uint32_t e = tid; e < nsq * 256; e += kThreads)
+                    luth[e] = __float2half_rn(
+                        l2sqr_sse(qv + (e >> 8) * p.lsq, p.codebook + (uint64_t)e * p.lsq, p.lsq) *
+                        scale);
+            } else {
+                build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
+            }
+            __syncthreads();
+        }
     }
     unsigned long long my_eval = 0, my_pass = 0;
     __syncthreads();
@@ -336,11 +361,11 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
                     // 2 * cell_dist (see adc_base)
                     const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
                     ++my_eval;
-                    if (pack_key(t0, mi) < tau) {  // t can only grow past t0
+                    if (filter_key(t0, mi) < tau) {  // t can only grow past t0
                         const float t =
                             HALF ? t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale
                                  : __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
-                        key = pack_key(t, mi);
+                        key = filter_key(t, mi);
                         keep = key < tau;
                     }
                 }
@@ -384,10 +409,8 @@ __global__ __launch_bounds__(kThreads) void k_scan_select(ScanParams p) {
         block_compact_le<kCandCap / kThreads>(keys, count, kth, &st.ccount);
         count = T;
     }
-    const uint32_t n2 = pow2_ceil(count);
-    for (uint32_t i = count + tid; i < n2; i += kThreads) keys[i] = kKeyMax;
-    __syncthreads();
-    bitonic_sort_keys(keys, n2);
+    // the T survivors leave unordered: only the rerank's tie path needs their
+    // (t, id) order, and it sorts them itself
     const uint32_t out = count < T ? count : T;
     for (uint32_t i = tid; i < T; i += kThreads) {
         p.hdist[(uint64_t)qi * T + i] = i < out ? key_value(keys[i]) : sentinel_f();
@@ -453,6 +476,21 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.P = s.P;
     p.T = s.T;
     p.codebook_max = ix.codebook_max;
+    p.luts = reinterpret_cast<const unsigned char*>(s.luts);
+    p.err = s.tc_err;
+    p.lut_bytes = ix.nsq * 256 * (half_lut ? 2 : 4);
+    if (s.luts == nullptr) return cudaErrorInvalidValue;
+    {
+        const dim3 g(n, ix.nsq);
+        if (half_lut)
+            k_build_luts<true><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, ix.d,
+                                                      ix.nsq, ix.lsq, ix.codebook_max, s.luts);
+        else
+            k_build_luts<false><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, ix.d,
+                                                       ix.nsq, ix.lsq, ix.codebook_max, s.luts);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     const size_t smem = half_lut ? scan_smem_bytes_half(ix) : scan_smem_bytes(ix);
     const uint32_t nw = ix.code_stride / 4;
     static bool attr_set[10] = {};  // one per instantiation
