@@ -164,7 +164,9 @@ int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
  * 0 records evaluated, 2 records kept, 3 buffer compactions, 5 most records of one
  * query, then cycles: 6 prologue, 7 whole block, 8 record rounds, 9 compactions,
  * 10 final sort. Both modes: 11 queries whose coarse top-P was recomputed in full
- * (exact ties at the cut of the tensor-core window). Fills min(n, 12) values. */
+ * (exact ties at the cut of the tensor-core window); with a learned probe, 12
+ * queries that kept the fixed count and 13 clusters the probe chose for the
+ * others. Fills min(n, 14) values. */
 int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
 
 /* Diagnostic of the scan-mode filter stage: runs one pass of n <= max_batch HOST
@@ -266,6 +268,51 @@ int pgpu_contract_bf16(int32_t mode, uint32_t na, uint32_t nb, uint32_t k, const
                        uint64_t a_rs, uint64_t a_ks, const float* b, uint64_t b_rs, uint64_t b_ks,
                        const float* bias, const float* aux, uint64_t ld_aux, float* out,
                        uint64_t ld_out, float* out2, float alpha, float beta, void* stream);
+
+/* ------------------------------------------------------------ learned probe
+ * A small MLP (query -> coarse-cluster scores, GELU, 2 hidden layers) trained and
+ * evaluated on the GPU with the BF16 tensor-core contraction (FP32 accumulation,
+ * FP32 master weights, Adam). No counterpart in the reference: it replaces the
+ * fixed search_coarse_count by a per-query count in scan mode.
+ * Parameter layout (pgpu_probe_get/set_params, pgpu_probe_gradients):
+ *   W1 [hidden][dim], b1 [hidden], W2 [hidden][hidden], b2 [hidden],
+ *   W3 [clusters][hidden], b3 [clusters]. */
+typedef struct pgpu_probe pgpu_probe;
+int pgpu_probe_create(uint32_t dim, uint32_t hidden, uint32_t clusters, uint64_t seed,
+                      int32_t device, pgpu_probe** out);
+int pgpu_probe_destroy(pgpu_probe* probe);
+int pgpu_probe_info(const pgpu_probe* probe, uint32_t* dim, uint32_t* hidden, uint32_t* clusters,
+                    uint64_t* params);
+/* One Adam step on a batch. queries [n][dim] (normalised as the index normalises
+ * them) and labels [n][L] (coarse cluster ids of each query's nearest points,
+ * 0xFFFFFFFF = none; the target is their distribution) are DEVICE pointers whose
+ * contents are complete when the call is made. loss (optional, host) receives
+ * the batch's mean softmax cross-entropy before the step. */
+int pgpu_probe_train_step(pgpu_probe* probe, const float* queries, const uint32_t* labels,
+                          uint32_t n, uint32_t L, float lr, float* loss);
+/* Loss and gradients of a batch without an update; grads is a HOST buffer of
+ * the parameter count, in the parameter layout. */
+int pgpu_probe_gradients(pgpu_probe* probe, const float* queries, const uint32_t* labels,
+                         uint32_t n, uint32_t L, float* loss, float* grads);
+/* Scores [n][clusters] (DEVICE) of n DEVICE queries. */
+int pgpu_probe_forward(pgpu_probe* probe, const float* queries, uint32_t n, float* scores);
+int pgpu_probe_get_params(const pgpu_probe* probe, float* params, uint64_t count);
+int pgpu_probe_set_params(pgpu_probe* probe, const float* params, uint64_t count);
+/* Attaches a probe to a scan-mode index (NULL detaches; the probe must outlive
+ * the attachment). Per query the clusters are taken in descending predicted
+ * probability until their mass reaches `mass` (at most max_probe <= 64
+ * clusters); a query whose max_probe best clusters stay below `mass` keeps the
+ * fixed search_coarse_count selection. Walk counters 12 and 13 report the
+ * fallbacks and the clusters the probe chose. */
+int pgpu_set_probe(pgpu_index* index, pgpu_probe* probe, float mass, uint32_t max_probe);
+
+/* Brute-force k nearest neighbours (k <= 64) by squared L2 of nq DEVICE queries
+ * over n DEVICE base vectors: a BF16 tensor-core screen of every pair keeps 64
+ * candidates per query, which are rescored in FP32; labels and distances
+ * ([nq][k], DEVICE) ascend. The labels of the learned probe's training set.
+ * Enqueued on `stream`; returns after it finished. */
+int pgpu_knn(const float* base, uint64_t n, uint32_t dim, const float* queries, uint32_t nq,
+             uint32_t k, uint32_t* labels, float* distance, void* stream);
 
 const char* pgpu_last_error(void);
 

@@ -93,6 +93,8 @@ int check_config(const pgpu_index* h, const pgpu_params* p) {
     if (p->mode == PGPU_MODE_SCAN && keep > pgpu::scan_max_filter_topk())
         return fail(PGPU_E_LIMIT, "filter_topk + filter_margin above " +
                                       std::to_string(pgpu::scan_max_filter_topk()) + " in scan mode");
+    if (h != nullptr && h->cfg.probe != nullptr && p->mode != PGPU_MODE_SCAN)
+        return fail(PGPU_E_INVALID, "a learned probe is attached: scan mode only");
     if (h != nullptr) {
         const bool bf16 = p->precision == PGPU_PRECISION_BF16;
         if (pgpu::walk_smem_bytes(h->ix, p->filter_topk) > 220 * 1024 ||
@@ -473,6 +475,51 @@ int pgpu_filter_candidates(pgpu_index* h, uint32_t n, const float* query, uint32
     if (ids) cudaFreeAsync(ids, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "filter_candidates");
+    return PGPU_OK;
+}
+
+int pgpu_set_probe(pgpu_index* h, pgpu_probe* probe, float mass, uint32_t max_probe) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    std::lock_guard<std::mutex> g(h->mu);
+    if (probe != nullptr) {
+        const pgpu::ProbeNet* net = pgpu::probe_net(probe);
+        if (h->cfg.mode != PGPU_MODE_SCAN) return fail(PGPU_E_INVALID, "the learned probe needs scan mode");
+        if (pgpu::probe_device(probe) != h->device)
+            return fail(PGPU_E_INVALID, "probe and index are on different devices");
+        if (net->d != h->ix.d || net->C != h->ix.C)
+            return fail(PGPU_E_INVALID, "probe dimension or cluster count does not match the index");
+        if (!(mass > 0.0f && mass <= 1.0f)) return fail(PGPU_E_INVALID, "mass must be in (0, 1]");
+        if (max_probe == 0 || max_probe > 64 || max_probe > h->ix.C)
+            return fail(PGPU_E_INVALID, "max_probe must be in [1, min(64, coarse_cluster_count)]");
+    }
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    h->cfg.probe = probe ? pgpu::probe_net(probe) : nullptr;
+    h->cfg.probe_mass = mass;
+    h->cfg.probe_max = probe ? max_probe : 0;
+    free_staging(h);
+    return alloc_scratch(h);
+}
+
+int pgpu_knn(const float* base, uint64_t n, uint32_t dim, const float* queries, uint32_t nq,
+             uint32_t k, uint32_t* labels, float* distance, void* stream) {
+    if (base == nullptr || queries == nullptr || labels == nullptr || distance == nullptr ||
+        dim == 0 || k == 0)
+        return fail(PGPU_E_INVALID, "invalid argument");
+    if (k > 64) return fail(PGPU_E_LIMIT, "k above 64");
+    if (n > 0xFFFFFFFFull) return fail(PGPU_E_LIMIT, "more than 2^32-1 base points");
+    if (n == 0 || nq == 0) return PGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int* err = nullptr;
+    cudaError_t e = cudaMallocAsync(&err, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = pgpu::launch_knn(base, n, dim, queries, nq, k, labels, distance, err, st);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (err) cudaFreeAsync(err, st);
+    if (e != cudaSuccess) return cuda_fail(e, "knn");
+    if (flag) return fail(PGPU_E_TIMEOUT, "tensor-core wait expired");
     return PGPU_OK;
 }
 

@@ -19,10 +19,36 @@ constexpr uint32_t kMaxClusters = 8192;   // coarse or fine count: sorted in sha
 constexpr uint32_t kMaxFilterNsq = 64;    // LUT of nsq*256 floats in shared memory
 constexpr uint32_t kMaxFilterTopk = 4096; // filter heap in shared memory
 constexpr uint32_t kMaxDim = 1024;
-constexpr int kNumWalkCounters = 12;  // see the counter enum in walk_scan.cu
+constexpr int kNumWalkCounters = 14;  // see the counter enum in walk_scan.cu
 // Counter slot 11: queries whose coarse top-P fell back from the tensor-core
 // window to the full exact recompute (ties at the cut, or a wide window).
 constexpr int kCounterWindowFallbacks = 11;
+// Slots 12, 13: queries that kept the fixed-count selection because the probe was
+// not confident, and clusters chosen by the probe for the others.
+constexpr int kCounterProbeFallbacks = 12;
+constexpr int kCounterProbeClusters = 13;
+
+// Probe network parameters: views into one contiguous FP32 block laid out
+// W1 [h][d], b1 [h], W2 [h][h], b2 [h], W3 [C][h], b3 [C].
+struct ProbeNet {
+    uint32_t d = 0, h = 0, C = 0;
+    float *W1 = nullptr, *b1 = nullptr, *W2 = nullptr, *b2 = nullptr, *W3 = nullptr, *b3 = nullptr;
+    uint64_t param_count() const;
+    void bind(float* base) {
+        W1 = base;
+        b1 = W1 + (uint64_t)h * d;
+        W2 = b1 + h;
+        b2 = W2 + (uint64_t)h * h;
+        W3 = b2 + h;
+        b3 = W3 + (uint64_t)C * h;
+    }
+};
+// Activations and gradients of one training batch (rows <= cap).
+struct ProbeWork {
+    uint32_t cap = 0;
+    float *H1 = nullptr, *Z1 = nullptr, *H2 = nullptr, *Z2 = nullptr, *Z = nullptr, *dZ = nullptr,
+          *dH2 = nullptr, *dH1 = nullptr;
+};
 
 // Device-resident index. Point arrays are in Puck's "memory order": sorted by
 // (cell id, filter offset, input id), so every coarse cluster is one
@@ -70,6 +96,9 @@ struct Scratch {
     unsigned long long* counters = nullptr; // [kNumWalkCounters] walk diagnostics
     int* tc_err = nullptr;     // set by a tensor-core contraction or table copy whose wait expired
     unsigned char* luts = nullptr; // scan mode: [B][nsq*256] lookup tables (FP32, or FP16)
+    float* ph1 = nullptr;      // probe hidden activations [B][h] (with a probe attached)
+    float* ph2 = nullptr;
+    uint32_t Pfix = 0;         // fixed coarse count (<= P when a probe widens the slots)
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;
 };
@@ -80,6 +109,15 @@ struct SearchConfig {
     int mode = PGPU_MODE_EXACT;
     int precision = PGPU_PRECISION_FP32;
     uint32_t margin = 0;  // BF16: extra filter candidates
+    const ProbeNet* probe = nullptr;  // learned probe (scan mode), not owned
+    float probe_mass = 0.9f;
+    uint32_t probe_max = 0;
+    // coarse slots per query: the fixed count, or the probe's cap when larger
+    uint32_t coarse_slots(uint32_t C) const {
+        uint32_t p = P < C ? P : C;
+        if (probe && probe_max > p) p = probe_max;
+        return p;
+    }
     // filter candidates kept per query
     uint32_t filter_keep() const { return T + (precision == PGPU_PRECISION_BF16 ? margin : 0); }
 };
@@ -169,6 +207,25 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
                                  cudaStream_t stream);
 cudaError_t launch_nearest_center_tc(uint32_t dim, const float* cents, uint64_t k, const float* x,
                                      uint64_t n, int32_t* assign, float* dis, cudaStream_t stream);
+
+// Learned probe (probe.cu).
+cudaError_t probe_forward(const ProbeNet& net, const float* X, uint32_t n, float* H1, float* Z1,
+                          float* H2, float* Z2, float* Z, int* err, cudaStream_t st);
+cudaError_t probe_backward(const ProbeNet& net, const float* X, uint32_t n,
+                           const uint32_t* labels, uint32_t L, ProbeWork& w, ProbeNet& grad,
+                           float* loss_sum, int* err, cudaStream_t st);
+cudaError_t probe_init(ProbeNet& net, uint64_t seed, cudaStream_t st);
+cudaError_t probe_adam(ProbeNet& net, const ProbeNet& grad, ProbeNet& m, ProbeNet& v, float lr,
+                       uint64_t step, cudaStream_t st);
+cudaError_t launch_probe_select(const ProbeNet& net, const DeviceIndex& ix, uint32_t n,
+                                const float* Z, float mass, uint32_t max_probe, Scratch& s,
+                                cudaStream_t st);
+
+// Brute-force kNN on the tensor-core screen with FP32 rescoring (knn.cu); k <= 64.
+cudaError_t launch_knn(const float* base, uint64_t n, uint32_t d, const float* Q, uint32_t nq,
+                       uint32_t k, uint32_t* ids, float* dist, int* err, cudaStream_t st);
+const ProbeNet* probe_net(const pgpu_probe* p);
+int probe_device(const pgpu_probe* p);
 
 // Pass pipeline (pipeline.cpp).
 void free_scratch(Scratch* s);

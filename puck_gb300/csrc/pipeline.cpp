@@ -19,25 +19,28 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
 
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
-                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err, s->luts};
+                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err, s->luts,
+                    s->ph1, s->ph2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *s = Scratch();
 }
 
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
-    const uint64_t P = std::min(cfg.P, ix.C), T = cfg.filter_keep();
+    const uint64_t P = cfg.coarse_slots(ix.C), T = cfg.filter_keep();
+    const uint64_t probe = cfg.probe ? (uint64_t)B * cfg.probe->h * 8 : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * ix.nsq * 256 * 4 : 0;
     return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
-           fine_order + tables + kNumWalkCounters * 8 + 4;
+           fine_order + tables + probe + kNumWalkCounters * 8 + 4;
 }
 
 int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Scratch* out,
                   std::string* err) {
     free_scratch(out);
     Scratch& s = *out;
-    s.P = std::min(cfg.P, ix.C);
+    s.P = cfg.coarse_slots(ix.C);
+    s.Pfix = std::min(cfg.P, ix.C);
     s.T = cfg.filter_keep();
     // the full fine order is only read by the exact walk
     const uint64_t fine_rows = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F : 1;
@@ -59,6 +62,10 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     PGPU_ALLOC(s.counters, kNumWalkCounters);
     PGPU_ALLOC(s.tc_err, 1);
     if (cfg.mode == PGPU_MODE_SCAN) PGPU_ALLOC(s.luts, (uint64_t)B * ix.nsq * 256 * 4);
+    if (cfg.probe) {
+        PGPU_ALLOC(s.ph1, (uint64_t)B * cfg.probe->h);
+        PGPU_ALLOC(s.ph2, (uint64_t)B * cfg.probe->h);
+    }
 #undef PGPU_ALLOC
     if (e != cudaSuccess) {
         free_scratch(&s);
@@ -93,6 +100,18 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     PGPU_STEP(launch_coarse_tc(ix, n, s, st), "coarse scores");
     mark(2);
     PGPU_STEP(launch_coarse_window(ix, n, s, st), "coarse select");
+    int probe_kernels = 0;
+    if (cfg.probe) {
+        // learned probe: scores of the coarse clusters (into the score buffer),
+        // then the adaptive choice that replaces the fixed count where confident
+        PGPU_STEP(probe_forward(*cfg.probe, s.q, n, s.ph1, nullptr, s.ph2, nullptr, s.dots,
+                                s.tc_err, st),
+                  "probe forward");
+        PGPU_STEP(launch_probe_select(*cfg.probe, ix, n, s.dots, cfg.probe_mass, cfg.probe_max, s,
+                                      st),
+                  "probe select");
+        probe_kernels = 4;
+    }
     mark(3);
     const bool bf16 = cfg.precision == PGPU_PRECISION_BF16;
     if (bf16) {
@@ -130,7 +149,7 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     }
     mark(7);
 #undef PGPU_STEP
-    if (launched) *launched = k;
+    if (launched) *launched = k + probe_kernels + (cfg.mode == PGPU_MODE_SCAN ? 1 : 0);
     return cudaSuccess;
 }
 

@@ -121,7 +121,7 @@ __device__ __forceinline__ float epilogue(float acc, uint32_t i, uint32_t j, con
     if (EPI == TC_EPI_BIAS) return acc + ep.bias[j];
     if (EPI == TC_EPI_BIAS_GELU) {
         const float pre = acc + ep.bias[j];
-        ep.out2[(uint64_t)i * ep.ld + j] = pre;
+        if (ep.out2) ep.out2[(uint64_t)i * ep.ld + j] = pre;
         return gelu_f(pre);
     }
     // TC_EPI_GELU_BWD: upstream gradient times GELU'(pre-activation)
@@ -273,7 +273,6 @@ cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
     if ((ep.mode == TC_EPI_SCORE || ep.mode == TC_EPI_BIAS || ep.mode == TC_EPI_BIAS_GELU) &&
         ep.bias == nullptr)
         return cudaErrorInvalidValue;
-    if (ep.mode == TC_EPI_BIAS_GELU && ep.out2 == nullptr) return cudaErrorInvalidValue;
     if (ep.mode == TC_EPI_GELU_BWD && ep.aux == nullptr) return cudaErrorInvalidValue;
     const dim3 grid((B.rows + kTileN - 1) / kTileN, (A.rows + kTileM - 1) / kTileM);
     if (grid.y > 65535) return cudaErrorInvalidValue;

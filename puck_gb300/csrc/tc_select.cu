@@ -38,7 +38,8 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     const float* __restrict__ approx, uint32_t ld, const float* __restrict__ Q, uint32_t d,
     const float* __restrict__ qnorm, const float* __restrict__ cents,
     const float* __restrict__ bias, const float* __restrict__ cabs, uint32_t C, uint32_t P,
-    float* __restrict__ out_val, uint32_t* __restrict__ out_idx, const int32_t* __restrict__ status,
+    uint32_t ld_out, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
+    const int32_t* __restrict__ status,
     const int* __restrict__ tc_err, unsigned long long* __restrict__ fallbacks) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* shi = reinterpret_cast<float*>(smem);                 // [C]   s^ + E, later exact s
@@ -52,8 +53,13 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     __shared__ uint32_t ncand;
     const uint32_t row = blockIdx.x;
     const int tid = threadIdx.x;
-    float* ov = out_val + (uint64_t)row * P;
-    uint32_t* oi = out_idx + (uint64_t)row * P;
+    float* ov = out_val + (uint64_t)row * ld_out;
+    uint32_t* oi = out_idx + (uint64_t)row * ld_out;
+    // slots past P (a probe's wider cap): unused
+    for (uint32_t i = P + tid; i < ld_out; i += kWinThreads) {
+        ov[i] = sentinel_f();
+        oi[i] = kNoLabel;
+    }
     if (status != nullptr && status[row] != 0) {
         for (uint32_t i = tid; i < P; i += kWinThreads) {
             ov[i] = sentinel_f();
@@ -256,8 +262,8 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
         attr = true;
     }
     k_window_topk<<<n, kWinThreads, smem, stream>>>(s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse,
-                                                    ix.coarse_norms, ix.coarse_abs, ix.C, s.P,
-                                                    s.cdist, s.ctag, s.status, s.tc_err,
+                                                    ix.coarse_norms, ix.coarse_abs, ix.C, s.Pfix,
+                                                    s.P, s.cdist, s.ctag, s.status, s.tc_err,
                                                     s.counters + kCounterWindowFallbacks);
     return cudaGetLastError();
 }

@@ -35,13 +35,15 @@ EXPORTED_SYMBOLS = (
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
     "pgpu_nearest_center_noalloc", "pgpu_server_params_default", "pgpu_server_create",
     "pgpu_server_submit", "pgpu_server_wait", "pgpu_server_stats_get", "pgpu_server_destroy",
-    "pgpu_contract_bf16", "pgpu_filter_candidates",
+    "pgpu_contract_bf16", "pgpu_filter_candidates", "pgpu_probe_create", "pgpu_probe_destroy",
+    "pgpu_probe_info", "pgpu_probe_train_step", "pgpu_probe_gradients", "pgpu_probe_forward",
+    "pgpu_probe_get_params", "pgpu_probe_set_params", "pgpu_set_probe", "pgpu_knn",
 )
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_CENTROIDS = 1 << 16
 WALK_COUNTERS = ("records", "cells", "fd_order_chunks", "enumerations", "fd_order_clusters",
                  "heap_inserts", "cyc_replay", "cyc_total", "cyc_prologue", "cyc_candidates",
-                 "cyc_adc", "coarse_window_fallbacks")
+                 "cyc_adc", "coarse_window_fallbacks", "probe_fallbacks", "probe_clusters")
 STAGES = ("prep", "coarse_scores", "coarse_select", "fine_scores", "fine_order", "walk_scan",
           "rerank")
 
@@ -137,6 +139,17 @@ def load(build_if_missing=False):
     lib.pgpu_server_destroy.argtypes = [vp]
     f32 = ctypes.c_float
     lib.pgpu_filter_candidates.argtypes = [vp, u32, vp, vp, vp, vp]
+    lib.pgpu_probe_create.argtypes = [u32, u32, u32, u64, ctypes.c_int32, ctypes.POINTER(vp)]
+    lib.pgpu_probe_destroy.argtypes = [vp]
+    lib.pgpu_probe_info.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                    ctypes.POINTER(u32), ctypes.POINTER(u64)]
+    lib.pgpu_probe_train_step.argtypes = [vp, vp, vp, u32, u32, f32, ctypes.POINTER(f32)]
+    lib.pgpu_probe_gradients.argtypes = [vp, vp, vp, u32, u32, ctypes.POINTER(f32), vp]
+    lib.pgpu_probe_forward.argtypes = [vp, vp, u32, vp]
+    lib.pgpu_probe_get_params.argtypes = [vp, vp, u64]
+    lib.pgpu_probe_set_params.argtypes = [vp, vp, u64]
+    lib.pgpu_set_probe.argtypes = [vp, vp, f32, u32]
+    lib.pgpu_knn.argtypes = [vp, u64, u32, vp, u32, u32, vp, vp, vp]
     lib.pgpu_contract_bf16.argtypes = [ctypes.c_int32, u32, u32, u32, vp, u64, u64, vp, u64, u64,
                                        vp, vp, u64, vp, u64, vp, f32, f32, vp]
     lib.pgpu_last_error.restype = ctypes.c_char_p
@@ -196,6 +209,12 @@ class GpuIndex:
         check(lib.pgpu_index_info_get(self._h, ctypes.byref(info)))
         self.info = info
         self.d = info.feature_dim
+
+    def set_probe(self, probe, mass=0.9, max_probe=8):
+        """Attach a learned Probe (None detaches); scan mode only."""
+        check(load().pgpu_set_probe(self._h, probe._h if probe is not None else None, mass,
+                                    max_probe))
+        self._probe = probe
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -353,6 +372,80 @@ def nearest_center_noalloc(centroids, points, assign, distance, stream=None):
         s = s.cuda_stream
     return check(load().pgpu_nearest_center_noalloc(dim, _ptr(centroids), k, _ptr(points), n,
                                                     _ptr(assign), _ptr(distance), s))
+
+
+def knn(base, queries, k, labels, distance, stream=None):
+    """Brute-force top-k (squared L2) on device tensors (pgpu_knn)."""
+    n, d = base.shape
+    nq = queries.shape[0]
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    return check(load().pgpu_knn(_ptr(base), n, d, _ptr(queries), nq, k, _ptr(labels),
+                                 _ptr(distance), s))
+
+
+class Probe:
+    """Learned probe network (pgpu_probe_*): queries -> coarse-cluster scores."""
+
+    def __init__(self, dim, hidden, clusters, seed=0, device=0):
+        lib = load()
+        self._h = ctypes.c_void_p()
+        check(lib.pgpu_probe_create(dim, hidden, clusters, seed, device, ctypes.byref(self._h)))
+        self.dim, self.hidden, self.clusters = dim, hidden, clusters
+        pc = ctypes.c_uint64()
+        check(lib.pgpu_probe_info(self._h, None, None, None, ctypes.byref(pc)))
+        self.param_count = pc.value
+
+    def train_step(self, queries, labels, lr):
+        """queries [n, dim] float32 and labels [n, L] int32/uint32 CUDA tensors."""
+        loss = ctypes.c_float()
+        n, L = labels.shape
+        check(load().pgpu_probe_train_step(self._h, _ptr(queries), _ptr(labels), n, L, lr,
+                                           ctypes.byref(loss)))
+        return loss.value
+
+    def gradients(self, queries, labels):
+        n, L = labels.shape
+        g = np.empty(self.param_count, np.float32)
+        loss = ctypes.c_float()
+        check(load().pgpu_probe_gradients(self._h, _ptr(queries), _ptr(labels), n, L,
+                                          ctypes.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+    def forward(self, queries, scores):
+        check(load().pgpu_probe_forward(self._h, _ptr(queries), queries.shape[0], _ptr(scores)))
+
+    def get_params(self):
+        p = np.empty(self.param_count, np.float32)
+        check(load().pgpu_probe_get_params(self._h, p.ctypes.data, self.param_count))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(load().pgpu_probe_set_params(self._h, p.ctypes.data, self.param_count))
+
+    def split(self, flat):
+        """Views W1, b1, W2, b2, W3, b3 of a flat parameter (or gradient) vector."""
+        d, h, C = self.dim, self.hidden, self.clusters
+        sizes = [(h, d), (h,), (h, h), (h,), (C, h), (C,)]
+        out, o = [], 0
+        for sh in sizes:
+            m = int(np.prod(sh))
+            out.append(flat[o:o + m].reshape(sh))
+            o += m
+        return out
+
+    def close(self):
+        if self._h:
+            load().pgpu_probe_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:
