@@ -40,15 +40,20 @@ METRIC = "QPS at recall@10=0.95, learned+BF16 vs plain GPU path, 1 GB300; p50/p9
 WORKLOADS = {
     "cosine_10m": dict(n=10_000_000, d=96, ncomp=4096, kind="unit", C=2000, F=2000, nsq=24,
                        T=500, k=10, sweep=(50, 100, 200), scan_sweep=(1, 2, 3, 4, 8, 16),
-                       nq=10000, norm=True, train_sample=500_000, iters=12, pq_sample=262_144),
+                       nq=10000, norm=True, train_sample=500_000, iters=12, pq_sample=262_144,
+                       probe_train=200_000, probe_mass=(0.5, 0.8, 0.9, 0.95, 0.99), probe_max=8,
+                       probe_fallback=4),
     # profiling case for ncu: codes + offsets (150 MB) larger than L2, ~5 GB on the device
     "cosine_5m": dict(n=5_000_000, d=96, ncomp=4096, kind="unit", C=1414, F=1414, nsq=24,
                       T=500, k=10, sweep=(50,), scan_sweep=(4,), nq=10000, norm=True,
-                      train_sample=300_000, iters=10, pq_sample=131_072),
+                      train_sample=300_000, iters=10, pq_sample=131_072,
+                      probe_train=100_000, probe_mass=(0.9,), probe_max=8, probe_fallback=4),
     # reduced workload for quick checks only (never the reported line)
     "cosine_1m": dict(n=1_000_000, d=96, ncomp=4096, kind="unit", C=500, F=500, nsq=24,
                       T=500, k=10, sweep=(25, 50, 100), scan_sweep=(1, 2, 4, 8), nq=10000,
-                      norm=True, train_sample=200_000, iters=10, pq_sample=131_072),
+                      norm=True, train_sample=200_000, iters=10, pq_sample=131_072,
+                      probe_train=100_000, probe_mass=(0.5, 0.9, 0.99), probe_max=8,
+                      probe_fallback=4),
 }
 TARGET_RECALL = 0.95
 
@@ -290,7 +295,25 @@ def run_gpu(args, w, rank, ws):
     nq, k = w["nq"], w["k"]
     qnorm = queries / queries.norm(dim=1, keepdim=True)
     gt_ids, gt_dist = brute_force_gt(base, qnorm, k)
-    del base
+    # ---- learned probe: fresh training queries of the same mixture, labelled with the
+    # coarse clusters of their brute-force top-10, trained on the GPU
+    from puck_gb300 import builder, probe as probe_mod
+    t0 = time.time()
+    qtr = builder.gmm(w["probe_train"], w["d"], w["ncomp"], w["kind"], seed=0, row_seed=3,
+                      device=dev)
+    qtr = qtr / qtr.norm(dim=1, keepdim=True)
+    cell = torch.from_numpy(arrays["cell_assign"].astype(np.int64)).to(dev)
+    ltr, _, _ = probe_mod.knn_cluster_labels(base, qtr, cell, w["F"])
+    torch.cuda.synchronize()
+    label_s = time.time() - t0
+    t0 = time.time()
+    probe, probe_losses = probe_mod.train_probe(qtr, ltr, w["C"], hidden=512, epochs=3,
+                                                batch=4096, lr=2e-3, seed=0, log=log)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    log(f"[bench] probe: {w['probe_train']} training queries labelled in {label_s:.1f}s, "
+        f"trained in {train_s:.1f}s, loss {probe_losses[0]:.3f} -> {probe_losses[-1]:.3f}")
+    del qtr, ltr, cell, base
     torch.cuda.empty_cache()
     t0 = time.time()
     ix = native.GpuIndex(arrays=arrays, search_coarse_count=w["sweep"][0], filter_topk=w["T"],
@@ -308,19 +331,26 @@ def run_gpu(args, w, rank, ws):
 
     sweep = []
     bf16_margin = max(1, w["T"] // 10)
-    # (form, mode, P): the plain FP32 path in both modes, and the precision form
+    fallback_P = w["probe_fallback"]
+    # (form, mode, P or probe mass): the plain FP32 path in both modes, the precision
+    # form, and the learned probe on top of the precision form
     configs = [("plain", native.PGPU_MODE_EXACT, P) for P in w["sweep"]] + \
               [("plain", native.PGPU_MODE_SCAN, P) for P in w["scan_sweep"]] + \
-              [("bf16", native.PGPU_MODE_SCAN, P) for P in w["scan_sweep"]]
+              [("bf16", native.PGPU_MODE_SCAN, P) for P in w["scan_sweep"]] + \
+              [("learned+bf16", native.PGPU_MODE_SCAN, m) for m in w["probe_mass"]]
     mode_name = {native.PGPU_MODE_EXACT: "exact", native.PGPU_MODE_SCAN: "scan"}
 
-    def set_form(form, mode, P):
-        prec = native.PGPU_PRECISION_BF16 if form == "bf16" else native.PGPU_PRECISION_FP32
+    def set_form(form, mode, x):
+        ix.set_probe(None)
+        prec = native.PGPU_PRECISION_FP32 if form == "plain" else native.PGPU_PRECISION_BF16
+        P = fallback_P if form == "learned+bf16" else x
         ix.set_search_params(search_coarse_count=P, mode=mode, precision=prec,
-                             filter_margin=bf16_margin if form == "bf16" else 0)
+                             filter_margin=0 if form == "plain" else bf16_margin)
+        if form == "learned+bf16":
+            ix.set_probe(probe, mass=x, max_probe=w["probe_max"])
 
-    for form, mode, P in configs:
-        set_form(form, mode, P)
+    for form, mode, x in configs:
+        set_form(form, mode, x)
         step()
         torch.cuda.synchronize()
         ids = i_dev.cpu().numpy().view(np.uint32)
@@ -332,10 +362,20 @@ def run_gpu(args, w, rank, ws):
         ev1.record(stream)
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1) / 3
-        sweep.append(dict(form=form, mode=mode_name[mode], search_coarse_count=P,
-                          recall_at_10=round(rec, 5), qps=round(nq / (ms / 1e3), 1),
-                          ms=round(ms, 3)))
-        log(f"[bench] {form} {mode_name[mode]} P={P}: recall@10={rec:.4f} "
+        entry = dict(form=form, mode=mode_name[mode], recall_at_10=round(rec, 5),
+                     qps=round(nq / (ms / 1e3), 1), ms=round(ms, 3))
+        if form == "learned+bf16":
+            ix.search(queries.cpu().numpy(), k)  # host path: per-call probe counters
+            wc = ix.walk_counters()
+            entry.update(probe_mass=x, search_coarse_count=fallback_P,
+                         probe_max=w["probe_max"],
+                         mean_clusters=round((wc["probe_clusters"] +
+                                              fallback_P * wc["probe_fallbacks"]) / nq, 3),
+                         fallback_queries=int(wc["probe_fallbacks"]))
+        else:
+            entry.update(search_coarse_count=x)
+        sweep.append(entry)
+        log(f"[bench] {form} {mode_name[mode]} {x}: recall@10={rec:.4f} "
             f"{nq / (ms / 1e3):.0f} QPS")
 
     def best_of(form):
@@ -346,14 +386,15 @@ def run_gpu(args, w, rank, ws):
         return max(cand, key=lambda c: c["recall_at_10"]), False
 
     plain_best, plain_reached = best_of("plain")
-    best, reached = best_of("bf16")
+    bf16_best, _ = best_of("bf16")
+    best, reached = best_of("learned+bf16")
     exact_ok = [c for c in sweep if c["form"] == "plain" and c["mode"] == "exact"
                 and c["recall_at_10"] >= TARGET_RECALL]
     exact_best = max(exact_ok, key=lambda c: c["qps"]) if exact_ok else None
 
     def timed(entry):
         mode = native.PGPU_MODE_EXACT if entry["mode"] == "exact" else native.PGPU_MODE_SCAN
-        set_form(entry["form"], mode, entry["search_coarse_count"])
+        set_form(entry["form"], mode, entry.get("probe_mass", entry["search_coarse_count"]))
         for _ in range(args.warmup):
             step()
         torch.cuda.synchronize()
@@ -391,7 +432,9 @@ def run_gpu(args, w, rank, ws):
     op_mode = native.PGPU_MODE_EXACT if best["mode"] == "exact" else native.PGPU_MODE_SCAN
     op = best["search_coarse_count"]
     op_recall = best["recall_at_10"]
-    launches_per_step = 7 if op_mode == native.PGPU_MODE_EXACT else 6
+    step()
+    torch.cuda.synchronize()
+    launches_per_step = int(ix.last_stats()["kernels"])
 
     # ---- per-stage device time (CUDA events inside the library, same stream)
     ix.set_profiling(True)
@@ -455,8 +498,16 @@ def run_gpu(args, w, rank, ws):
 
     serving = None
     if not args.no_serve:
-        serving = run_serving(native, ix, q_np, loads_qps=(250_000, 500_000, 1_000_000))
-        log(f"[bench] serving: {serving}")
+        serving = {}
+        for name, entry in (("plain", plain_best), (best["form"], best)):
+            set_form(entry["form"],
+                     native.PGPU_MODE_EXACT if entry["mode"] == "exact" else native.PGPU_MODE_SCAN,
+                     entry.get("probe_mass", entry["search_coarse_count"]))
+            serving[name] = dict(run_serving(native, ix, q_np,
+                                             loads_qps=(250_000, 500_000, 1_000_000)),
+                                 recall_at_10=entry["recall_at_10"])
+            log(f"[bench] serving {name}: {serving[name]}")
+        set_form(best["form"], op_mode, best.get("probe_mass", op))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -480,13 +531,15 @@ def run_gpu(args, w, rank, ws):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "bf16" if best["form"] == "bf16" else "fp32",
+        "dtype": "fp32" if best["form"] == "plain" else "bf16",
         "data": "synthetic (seeded Gaussian mixture, built on the GPU in Puck's index format)",
         "config": {
             "workload": f"{args.workload}: {w['n']} x d{w['d']} L2-normalised GMM "
                         f"({w['ncomp']} comps), {nq} queries, coarse={w['C']} fine={w['F']}, "
                         f"filter PQ {w['nsq']}x256, filter_topk={w['T']}, top-{k}",
-            "path": ("precision form: BF16 tensor-core fine terms, FP16 ADC table, "
+            "path": ("learned probe (adaptive clusters, confidence fallback) on the "
+                     "precision form" if best["form"] == "learned+bf16" else
+                     "precision form: BF16 tensor-core fine terms, FP16 ADC table, "
                      f"filter margin {bf16_margin}, BF16 rerank screen + FP32 window"
                      if best["form"] == "bf16" else
                      "plain GPU path, exact mode (reference-identical results)"
@@ -495,6 +548,13 @@ def run_gpu(args, w, rank, ws):
                      "reference per-record distances, exact rerank)"),
             "form": best["form"],
             "mode": best["mode"],
+            "bf16_best": bf16_best,
+            "probe": dict(hidden=512, layers="d->512->512->C, GELU", train_queries=w["probe_train"],
+                          labels="coarse clusters of each query's brute-force top-10",
+                          label_seconds=round(label_s, 1), train_seconds=round(train_s, 1),
+                          epochs=3, loss_first_epoch=round(probe_losses[0], 4),
+                          loss_last_epoch=round(probe_losses[-1], 4),
+                          fallback_search_coarse_count=fallback_P, max_probe=w["probe_max"]),
             "plain": dict(plain_best, timed_qps=round(plain_value, 1),
                           ms_per_step=round(plain_ms / args.steps, 4),
                           p50_ms=round(float(np.percentile(plain_steps, 50)), 4),

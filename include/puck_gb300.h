@@ -150,7 +150,7 @@ int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
 /* Per-stage device timing (CUDA events recorded on the launching stream around
  * each kernel). With profiling enabled, pgpu_stage_times returns, for the last
  * search call, the milliseconds spent in each stage, summed over its passes:
- * 0 query prep, 1 coarse scores, 2 coarse select, 3 fine scores, 4 fine order,
+ * 0 query prep, 1 coarse scores, 2 coarse select (+ the learned probe), 3 fine scores, 4 fine order,
  * 5 cell walk + ADC scan, 6 rerank. It waits for the call's work to finish. */
 #define PGPU_NUM_STAGES 7
 int pgpu_set_profiling(pgpu_index* index, int enable);

@@ -314,6 +314,7 @@ int pgpu_search_batch(pgpu_index* h, uint32_t n, const float* query, uint32_t to
     for (float& v : h->stage_ms) v = 0.0f;
     h->records = 0;
     h->cells = 0;
+    for (uint64_t& c : h->walk_counters) c = 0;
     cudaError_t e;
     for (uint32_t off = 0; off < n; off += h->max_batch) {
         const uint32_t m = std::min(h->max_batch, n - off);
