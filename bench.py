@@ -42,18 +42,18 @@ WORKLOADS = {
                        T=500, k=10, sweep=(50, 100, 200), scan_sweep=(1, 2, 3, 4, 8, 16),
                        nq=10000, norm=True, train_sample=500_000, iters=12, pq_sample=262_144,
                        probe_train=200_000, probe_mass=(0.5, 0.8, 0.9, 0.95, 0.99), probe_max=8,
-                       probe_fallback=4),
+                       probe_fallback=4, probe_epochs=8),
     # profiling case for ncu: codes + offsets (150 MB) larger than L2, ~5 GB on the device
     "cosine_5m": dict(n=5_000_000, d=96, ncomp=4096, kind="unit", C=1414, F=1414, nsq=24,
                       T=500, k=10, sweep=(50,), scan_sweep=(4,), nq=10000, norm=True,
                       train_sample=300_000, iters=10, pq_sample=131_072,
-                      probe_train=100_000, probe_mass=(0.9,), probe_max=8, probe_fallback=4),
+                      probe_train=100_000, probe_mass=(0.9,), probe_max=8, probe_fallback=4, probe_epochs=8),
     # reduced workload for quick checks only (never the reported line)
     "cosine_1m": dict(n=1_000_000, d=96, ncomp=4096, kind="unit", C=500, F=500, nsq=24,
                       T=500, k=10, sweep=(25, 50, 100), scan_sweep=(1, 2, 4, 8), nq=10000,
                       norm=True, train_sample=200_000, iters=10, pq_sample=131_072,
                       probe_train=100_000, probe_mass=(0.5, 0.9, 0.99), probe_max=8,
-                      probe_fallback=4),
+                      probe_fallback=4, probe_epochs=8),
 }
 TARGET_RECALL = 0.95
 
@@ -307,8 +307,9 @@ def run_gpu(args, w, rank, ws):
     torch.cuda.synchronize()
     label_s = time.time() - t0
     t0 = time.time()
-    probe, probe_losses = probe_mod.train_probe(qtr, ltr, w["C"], hidden=512, epochs=3,
-                                                batch=4096, lr=2e-3, seed=0, log=log)
+    probe, probe_losses = probe_mod.train_probe(qtr, ltr, w["C"], hidden=512,
+                                                epochs=w["probe_epochs"], batch=2048, lr=2e-3,
+                                                seed=0, log=log)
     torch.cuda.synchronize()
     train_s = time.time() - t0
     log(f"[bench] probe: {w['probe_train']} training queries labelled in {label_s:.1f}s, "
@@ -552,7 +553,7 @@ def run_gpu(args, w, rank, ws):
             "probe": dict(hidden=512, layers="d->512->512->C, GELU", train_queries=w["probe_train"],
                           labels="coarse clusters of each query's brute-force top-10",
                           label_seconds=round(label_s, 1), train_seconds=round(train_s, 1),
-                          epochs=3, loss_first_epoch=round(probe_losses[0], 4),
+                          epochs=w["probe_epochs"], batch=2048, loss_first_epoch=round(probe_losses[0], 4),
                           loss_last_epoch=round(probe_losses[-1], 4),
                           fallback_search_coarse_count=fallback_P, max_probe=w["probe_max"]),
             "plain": dict(plain_best, timed_qps=round(plain_value, 1),

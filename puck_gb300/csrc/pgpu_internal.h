@@ -33,6 +33,8 @@ constexpr int kCounterProbeClusters = 13;
 struct ProbeNet {
     uint32_t d = 0, h = 0, C = 0;
     float *W1 = nullptr, *b1 = nullptr, *W2 = nullptr, *b2 = nullptr, *W3 = nullptr, *b3 = nullptr;
+    // BF16 copies of the weight matrices for inference (refreshed after every update)
+    uint16_t *W1b = nullptr, *W2b = nullptr, *W3b = nullptr;
     uint64_t param_count() const;
     void bind(float* base) {
         W1 = base;
@@ -96,8 +98,8 @@ struct Scratch {
     unsigned long long* counters = nullptr; // [kNumWalkCounters] walk diagnostics
     int* tc_err = nullptr;     // set by a tensor-core contraction or table copy whose wait expired
     unsigned char* luts = nullptr; // scan mode: [B][nsq*256] lookup tables (FP32, or FP16)
-    float* ph1 = nullptr;      // probe hidden activations [B][h] (with a probe attached)
-    float* ph2 = nullptr;
+    uint16_t* ph1 = nullptr;   // probe hidden activations [B][h], BF16 (with a probe attached)
+    uint16_t* ph2 = nullptr;
     uint32_t Pfix = 0;         // fixed coarse count (<= P when a probe widens the slots)
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;
@@ -176,6 +178,7 @@ struct TcOperand {
     const float* p;
     uint64_t rs, ks;
     uint32_t rows;
+    const uint16_t* pb = nullptr;  // BF16 operand instead of p (same strides, in elements)
 };
 enum TcEpi {
     TC_EPI_SCORE = 0,     // bias[j] - acc
@@ -187,7 +190,8 @@ enum TcEpi {
 };
 struct TcEpilogue {
     int mode;
-    float* out;
+    float* out;             // FP32 output, or
+    uint16_t* out_bf16;     // BF16 output (when set, out is not written)
     uint64_t ld;
     const float* bias;
     const float* aux;
@@ -215,6 +219,11 @@ cudaError_t probe_backward(const ProbeNet& net, const float* X, uint32_t n,
                            const uint32_t* labels, uint32_t L, ProbeWork& w, ProbeNet& grad,
                            float* loss_sum, int* err, cudaStream_t st);
 cudaError_t probe_init(ProbeNet& net, uint64_t seed, cudaStream_t st);
+// Refreshes the BF16 weight copies from the FP32 weights.
+cudaError_t probe_sync_bf16(const ProbeNet& net, cudaStream_t st);
+// Inference: scores Z [n][C] (FP32) with BF16 hidden activations H1b, H2b [n][h].
+cudaError_t probe_infer(const ProbeNet& net, const float* X, uint32_t n, uint16_t* H1b,
+                        uint16_t* H2b, float* Z, int* err, cudaStream_t st);
 cudaError_t probe_adam(ProbeNet& net, const ProbeNet& grad, ProbeNet& m, ProbeNet& v, float lr,
                        uint64_t step, cudaStream_t st);
 cudaError_t launch_probe_select(const ProbeNet& net, const DeviceIndex& ix, uint32_t n,

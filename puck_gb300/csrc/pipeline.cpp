@@ -28,7 +28,7 @@ void free_scratch(Scratch* s) {
 
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
     const uint64_t P = cfg.coarse_slots(ix.C), T = cfg.filter_keep();
-    const uint64_t probe = cfg.probe ? (uint64_t)B * cfg.probe->h * 8 : 0;
+    const uint64_t probe = cfg.probe ? (uint64_t)B * cfg.probe->h * 4 : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * ix.nsq * 256 * 4 : 0;
     return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
@@ -104,8 +104,7 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     if (cfg.probe) {
         // learned probe: scores of the coarse clusters (into the score buffer),
         // then the adaptive choice that replaces the fixed count where confident
-        PGPU_STEP(probe_forward(*cfg.probe, s.q, n, s.ph1, nullptr, s.ph2, nullptr, s.dots,
-                                s.tc_err, st),
+        PGPU_STEP(probe_infer(*cfg.probe, s.q, n, s.ph1, s.ph2, s.dots, s.tc_err, st),
                   "probe forward");
         PGPU_STEP(launch_probe_select(*cfg.probe, ix, n, s.dots, cfg.probe_mass, cfg.probe_max, s,
                                       st),

@@ -17,6 +17,8 @@
 // search_coarse_count); when max_probe clusters do not reach it, the query keeps
 // the plain fixed-count coarse selection (confidence fallback). The coarse
 // distance of a chosen cluster is the reference's exact FP32 value.
+#include <cuda_bf16.h>
+
 #include <cfloat>
 #include <cstdint>
 
@@ -109,6 +111,11 @@ __global__ void k_colsum(const float* __restrict__ G, uint32_t rows, uint32_t co
     float s = 0.0f;
     for (uint32_t i = 0; i < rows; ++i) s += G[(uint64_t)i * cols + j];
     out[j] = s;
+}
+
+__global__ void k_to_bf16(const float* __restrict__ x, uint64_t n, uint16_t* __restrict__ y) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = __bfloat16_as_ushort(__float2bfloat16_rn(x[i]));
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
@@ -275,6 +282,46 @@ cudaError_t probe_forward(const ProbeNet& net, const float* X, uint32_t n, float
     e3.bias = net.b3;
     return launch_tc_gemm(TcOperand{H2, net.h, 1, n}, TcOperand{net.W3, net.h, 1, net.C}, net.h, e3,
                           err, st);
+}
+
+cudaError_t probe_sync_bf16(const ProbeNet& net, cudaStream_t st) {
+    const struct {
+        const float* w;
+        uint16_t* b;
+        uint64_t n;
+    } mats[] = {{net.W1, net.W1b, (uint64_t)net.h * net.d},
+                {net.W2, net.W2b, (uint64_t)net.h * net.h},
+                {net.W3, net.W3b, (uint64_t)net.C * net.h}};
+    for (const auto& m : mats)
+        k_to_bf16<<<(unsigned)((m.n + 255) / 256), 256, 0, st>>>(m.w, m.n, m.b);
+    return cudaGetLastError();
+}
+
+cudaError_t probe_infer(const ProbeNet& net, const float* X, uint32_t n, uint16_t* H1b,
+                        uint16_t* H2b, float* Z, int* err, cudaStream_t st) {
+    TcEpilogue e1{};
+    e1.mode = TC_EPI_BIAS_GELU;
+    e1.out_bf16 = H1b;
+    e1.ld = net.h;
+    e1.bias = net.b1;
+    TcOperand w1{nullptr, net.d, 1, net.h, net.W1b};
+    cudaError_t e = launch_tc_gemm(TcOperand{X, net.d, 1, n}, w1, net.d, e1, err, st);
+    if (e != cudaSuccess) return e;
+    TcEpilogue e2{};
+    e2.mode = TC_EPI_BIAS_GELU;
+    e2.out_bf16 = H2b;
+    e2.ld = net.h;
+    e2.bias = net.b2;
+    e = launch_tc_gemm(TcOperand{nullptr, net.h, 1, n, H1b},
+                       TcOperand{nullptr, net.h, 1, net.h, net.W2b}, net.h, e2, err, st);
+    if (e != cudaSuccess) return e;
+    TcEpilogue e3{};
+    e3.mode = TC_EPI_BIAS;
+    e3.out = Z;
+    e3.ld = net.C;
+    e3.bias = net.b3;
+    return launch_tc_gemm(TcOperand{nullptr, net.h, 1, n, H2b},
+                          TcOperand{nullptr, net.h, 1, net.C, net.W3b}, net.h, e3, err, st);
 }
 
 cudaError_t probe_backward(const ProbeNet& net, const float* X, uint32_t n,

@@ -11,6 +11,7 @@ struct pgpu_probe {
     int device = 0;
     pgpu::ProbeNet net, grad, m, v;
     float* block = nullptr;  // 4 parameter-sized blocks: weights, gradients, Adam m, Adam v
+    uint16_t* bf16 = nullptr;  // BF16 copies of W1, W2, W3
     pgpu::ProbeWork work;
     float* loss = nullptr;   // device scalar
     int* err = nullptr;      // device flag of the tensor-core waits
@@ -107,6 +108,8 @@ int pgpu_probe_create(uint32_t dim, uint32_t hidden, uint32_t clusters, uint64_t
     }
     const uint64_t np = p->net.param_count();
     cudaError_t e = cudaMalloc((void**)&p->block, sizeof(float) * np * 4);
+    const uint64_t nw = (uint64_t)hidden * dim + (uint64_t)hidden * hidden + (uint64_t)clusters * hidden;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&p->bf16, sizeof(uint16_t) * nw);
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->loss, sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->err, sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
@@ -115,13 +118,18 @@ int pgpu_probe_create(uint32_t dim, uint32_t hidden, uint32_t clusters, uint64_t
         p->grad.bind(p->block + np);
         p->m.bind(p->block + 2 * np);
         p->v.bind(p->block + 3 * np);
+        p->net.W1b = p->bf16;
+        p->net.W2b = p->net.W1b + (uint64_t)hidden * dim;
+        p->net.W3b = p->net.W2b + (uint64_t)hidden * hidden;
         e = cudaMemsetAsync(p->block + np, 0, sizeof(float) * np * 3, p->stream);
     }
     if (e == cudaSuccess) e = pgpu::probe_init(p->net, seed, p->stream);
+    if (e == cudaSuccess) e = pgpu::probe_sync_bf16(p->net, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) {
         int rc = cuda_fail(e, "probe create");
         if (p->block) cudaFree(p->block);
+        if (p->bf16) cudaFree(p->bf16);
         if (p->loss) cudaFree(p->loss);
         if (p->err) cudaFree(p->err);
         if (p->stream) cudaStreamDestroy(p->stream);
@@ -138,6 +146,7 @@ int pgpu_probe_destroy(pgpu_probe* p) {
     cudaStreamSynchronize(p->stream);
     free_work(&p->work);
     cudaFree(p->block);
+    cudaFree(p->bf16);
     cudaFree(p->loss);
     cudaFree(p->err);
     cudaStreamDestroy(p->stream);
@@ -164,6 +173,7 @@ int pgpu_probe_train_step(pgpu_probe* p, const float* queries, const uint32_t* l
     if (int rc = run_backward(p, queries, labels, n, L)) return rc;
     p->step += 1;
     cudaError_t e = pgpu::probe_adam(p->net, p->grad, p->m, p->v, lr, p->step, p->stream);
+    if (e == cudaSuccess) e = pgpu::probe_sync_bf16(p->net, p->stream);
     if (e != cudaSuccess) return cuda_fail(e, "probe update");
     return finish(p, loss);
 }
@@ -191,8 +201,9 @@ int pgpu_probe_forward(pgpu_probe* p, const float* queries, uint32_t n, float* s
     cudaError_t e = ensure_work(p, n);
     if (e != cudaSuccess) return cuda_fail(e, "probe work buffers");
     cudaMemsetAsync(p->err, 0, sizeof(int), p->stream);
-    e = pgpu::probe_forward(p->net, queries, n, p->work.H1, nullptr, p->work.H2, nullptr, scores,
-                            p->err, p->stream);
+    // the search's own inference path: BF16 weights and activations
+    e = pgpu::probe_infer(p->net, queries, n, reinterpret_cast<uint16_t*>(p->work.H1),
+                          reinterpret_cast<uint16_t*>(p->work.H2), scores, p->err, p->stream);
     if (e != cudaSuccess) return cuda_fail(e, "probe forward");
     return finish(p, nullptr);
 }
@@ -213,6 +224,8 @@ int pgpu_probe_set_params(pgpu_probe* p, const float* params, uint64_t count) {
     cudaSetDevice(p->device);
     cudaStreamSynchronize(p->stream);
     cudaError_t e = cudaMemcpy(p->net.W1, params, sizeof(float) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = pgpu::probe_sync_bf16(p->net, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) return cuda_fail(e, "probe params");
     return PGPU_OK;
 }

@@ -70,33 +70,71 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 // Stages rows [row0, row0+128) x k [k0, k0 + 8*nkg) of an operand into `tile`.
 // Thread t owns row t of the tile and writes one 16-byte core-matrix row per K
-// group, so a quarter warp stores 128 contiguous bytes (no bank conflict).
+// group, so a quarter warp stores 128 contiguous bytes (no bank conflict). All of
+// a thread's global loads for a group of K groups are issued before any store.
 __device__ __forceinline__ void stage_operand(uint8_t* tile, const TcOperand& op, uint32_t row0,
                                               uint32_t k0, uint32_t K, uint32_t nkg, bool vec) {
     const uint32_t r = threadIdx.x;
     const uint32_t row = row0 + r;
     const bool in = row < op.rows;
-    const float* base = op.p + (uint64_t)row * op.rs;
     uint8_t* dst = tile + (r >> 3) * 128u + (r & 7u) * 16u;
-    for (uint32_t kg = 0; kg < nkg; ++kg) {
-        const uint32_t k = k0 + kg * 8;
-        float x[8];
-        if (in && vec && k + 8 <= K) {
-            const float4 u = __ldg(reinterpret_cast<const float4*>(base + k));
-            const float4 v = __ldg(reinterpret_cast<const float4*>(base + k + 4));
-            x[0] = u.x; x[1] = u.y; x[2] = u.z; x[3] = u.w;
-            x[4] = v.x; x[5] = v.y; x[6] = v.z; x[7] = v.w;
-        } else {
+    if (op.pb != nullptr) {
+        const uint16_t* base = op.pb + (uint64_t)row * op.rs;
+        uint4 w[8];
 #pragma unroll
-            for (int t = 0; t < 8; ++t)
-                x[t] = (in && k + t < K) ? __ldg(base + (uint64_t)(k + t) * op.ks) : 0.0f;
+        for (int kg = 0; kg < 8; ++kg) {
+            if ((uint32_t)kg >= nkg) break;
+            const uint32_t k = k0 + kg * 8;
+            if (in && vec && k + 8 <= K) {
+                w[kg] = __ldg(reinterpret_cast<const uint4*>(base + k));
+            } else {
+                uint32_t h[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    h[t] = (in && k + t < K) ? (uint32_t)__ldg(base + (uint64_t)(k + t) * op.ks) : 0u;
+                w[kg] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16),
+                                   h[6] | (h[7] << 16));
+            }
         }
-        uint4 w;
-        w.x = bf16x2(x[0], x[1]);
-        w.y = bf16x2(x[2], x[3]);
-        w.z = bf16x2(x[4], x[5]);
-        w.w = bf16x2(x[6], x[7]);
-        *reinterpret_cast<uint4*>(dst + kg * (16u * 128u)) = w;
+#pragma unroll
+        for (int kg = 0; kg < 8; ++kg) {
+            if ((uint32_t)kg >= nkg) break;
+            *reinterpret_cast<uint4*>(dst + kg * (16u * 128u)) = w[kg];
+        }
+        return;
+    }
+    const float* base = op.p + (uint64_t)row * op.rs;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        float4 x[4][2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t kg = half * 4 + u;
+            if (kg >= nkg) break;
+            const uint32_t k = k0 + kg * 8;
+            if (in && vec && k + 8 <= K) {
+                x[u][0] = __ldg(reinterpret_cast<const float4*>(base + k));
+                x[u][1] = __ldg(reinterpret_cast<const float4*>(base + k + 4));
+            } else {
+                float e[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    e[t] = (in && k + t < K) ? __ldg(base + (uint64_t)(k + t) * op.ks) : 0.0f;
+                x[u][0] = make_float4(e[0], e[1], e[2], e[3]);
+                x[u][1] = make_float4(e[4], e[5], e[6], e[7]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t kg = half * 4 + u;
+            if (kg >= nkg) break;
+            uint4 w;
+            w.x = bf16x2(x[u][0].x, x[u][0].y);
+            w.y = bf16x2(x[u][0].z, x[u][0].w);
+            w.z = bf16x2(x[u][1].x, x[u][1].y);
+            w.w = bf16x2(x[u][1].z, x[u][1].w);
+            *reinterpret_cast<uint4*>(dst + kg * (16u * 128u)) = w;
+        }
     }
 }
 
@@ -211,8 +249,10 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
     if (!failed && nch > 0) {
         const uint32_t row = m0 + warp * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-        const bool vec_out = (EPI != TC_EPI_BIAS_GELU) && ((ep.ld & 3u) == 0) &&
+        const bool vec_out = ((ep.ld & 3u) == 0) &&
                              ((reinterpret_cast<uintptr_t>(ep.out) & 15u) == 0);
+        const bool vec_out_b = ((ep.ld & 7u) == 0) &&
+                               ((reinterpret_cast<uintptr_t>(ep.out_bf16) & 15u) == 0);
 #pragma unroll 1
         for (uint32_t c = 0; c < kTileN / 16; ++c) {
             uint32_t r[16];
@@ -226,23 +266,43 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (row >= A.rows) continue;
             const uint32_t col0 = n0 + c * 16;
+            float v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                v[j] = (col0 + j < B.rows) ? epilogue<EPI>(__uint_as_float(r[j]), row, col0 + j, ep)
+                                           : 0.0f;
+            if (ep.out_bf16 != nullptr) {
+                uint16_t* orow = ep.out_bf16 + (uint64_t)row * ep.ld;
+                if (vec_out_b && col0 + 16 <= B.rows) {
+                    uint4 lo, hi;
+                    lo.x = bf16x2(v[0], v[1]);
+                    lo.y = bf16x2(v[2], v[3]);
+                    lo.z = bf16x2(v[4], v[5]);
+                    lo.w = bf16x2(v[6], v[7]);
+                    hi.x = bf16x2(v[8], v[9]);
+                    hi.y = bf16x2(v[10], v[11]);
+                    hi.z = bf16x2(v[12], v[13]);
+                    hi.w = bf16x2(v[14], v[15]);
+                    *reinterpret_cast<uint4*>(orow + col0) = lo;
+                    *reinterpret_cast<uint4*>(orow + col0 + 8) = hi;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (col0 + j < B.rows)
+                            orow[col0 + j] = __bfloat16_as_ushort(__float2bfloat16_rn(v[j]));
+                }
+                continue;
+            }
             float* orow = ep.out + (uint64_t)row * ep.ld;
             if (vec_out && col0 + 16 <= B.rows) {
 #pragma unroll
-                for (int j = 0; j < 16; j += 4) {
-                    float4 v;
-                    v.x = epilogue<EPI>(__uint_as_float(r[j]), row, col0 + j, ep);
-                    v.y = epilogue<EPI>(__uint_as_float(r[j + 1]), row, col0 + j + 1, ep);
-                    v.z = epilogue<EPI>(__uint_as_float(r[j + 2]), row, col0 + j + 2, ep);
-                    v.w = epilogue<EPI>(__uint_as_float(r[j + 3]), row, col0 + j + 3, ep);
-                    *reinterpret_cast<float4*>(orow + col0 + j) = v;
-                }
+                for (int j = 0; j < 16; j += 4)
+                    *reinterpret_cast<float4*>(orow + col0 + j) =
+                        make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
             } else {
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const uint32_t col = col0 + j;
-                    if (col < B.rows) orow[col] = epilogue<EPI>(__uint_as_float(r[j]), row, col, ep);
-                }
+                for (int j = 0; j < 16; ++j)
+                    if (col0 + j < B.rows) orow[col0 + j] = v[j];
             }
         }
     }
@@ -256,8 +316,9 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
     }
 }
 
-bool operand_vec(const TcOperand& op, uint32_t K) {
-    (void)K;
+bool operand_vec(const TcOperand& op) {
+    if (op.pb != nullptr)
+        return op.ks == 1 && (op.rs & 7u) == 0 && (reinterpret_cast<uintptr_t>(op.pb) & 15u) == 0;
     return op.ks == 1 && (op.rs & 3u) == 0 && (reinterpret_cast<uintptr_t>(op.p) & 15u) == 0;
 }
 
@@ -268,8 +329,10 @@ size_t tc_gemm_smem_bytes() { return 2 * (size_t)kStageBytes; }
 cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
                            const TcEpilogue& ep, int* err, cudaStream_t stream) {
     if (A.rows == 0 || B.rows == 0) return cudaSuccess;
-    if (K == 0 || A.p == nullptr || B.p == nullptr || ep.out == nullptr || err == nullptr)
+    if (K == 0 || (A.p == nullptr && A.pb == nullptr) || (B.p == nullptr && B.pb == nullptr) ||
+        (ep.out == nullptr && ep.out_bf16 == nullptr) || err == nullptr)
         return cudaErrorInvalidValue;
+    if (ep.out == nullptr && ep.mode == TC_EPI_STORE && ep.beta != 0.0f) return cudaErrorInvalidValue;
     if ((ep.mode == TC_EPI_SCORE || ep.mode == TC_EPI_BIAS || ep.mode == TC_EPI_BIAS_GELU) &&
         ep.bias == nullptr)
         return cudaErrorInvalidValue;
@@ -277,7 +340,7 @@ cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
     const dim3 grid((B.rows + kTileN - 1) / kTileN, (A.rows + kTileM - 1) / kTileM);
     if (grid.y > 65535) return cudaErrorInvalidValue;
     const size_t smem = tc_gemm_smem_bytes();
-    const int av = operand_vec(A, K) ? 1 : 0, bv = operand_vec(B, K) ? 1 : 0;
+    const int av = operand_vec(A) ? 1 : 0, bv = operand_vec(B) ? 1 : 0;
     static bool attr[6] = {false, false, false, false, false, false};
 #define PGPU_TC_CASE(M)                                                                      \
     case M:                                                                                  \
