@@ -54,6 +54,7 @@ struct ScanParams {
     const float* codebook;
     unsigned long long* counters;
     const unsigned char* luts;  // [B][lut_bytes] tables from k_build_luts
+    int* err;                   // set when the table copy did not arrive in time
     uint32_t d, C, F, nsq, lsq, code_stride, P, T, lut_bytes;
     float codebook_max;
 };
@@ -225,6 +226,7 @@ enum { kScRecords = 0, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCy
 struct ScanState {
     uint64_t tau;
     uint64_t sel[4];
+    uint64_t lut_bar;
     uint32_t hist[256];
     uint32_t ccount;
     uint32_t count;
@@ -237,7 +239,7 @@ struct ScanState {
 
 // NW = code words per record (code_stride / 4); HALF = FP16 table.
 template <int NW, bool HALF>
-__global__ __launch_bounds__(kThreads, 4) void k_scan_select(ScanParams p) {
+__global__ __launch_bounds__(kThreads, 3) void k_scan_select(ScanParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ScanState st;
     const uint32_t qi = blockIdx.x;
@@ -255,26 +257,51 @@ __global__ __launch_bounds__(kThreads, 4) void k_scan_select(ScanParams p) {
         return;
     }
     const long long t_start = clock64();
-    {
-        // the query's table from k_build_luts: every thread's 16-byte pieces in flight at once
-        const uint4* src = reinterpret_cast<const uint4*>(p.luts + (uint64_t)qi * p.lut_bytes);
-        uint4* dst = reinterpret_cast<uint4*>(lut);
-        const uint32_t n16 = p.lut_bytes / 16;
-        constexpr int kPer = 8;
-        uint4 v[kPer];
-        for (uint32_t i0 = 0; i0 < n16; i0 += kPer * kThreads) {
-#pragma unroll
-            for (int u = 0; u < kPer; ++u) {
-                const uint32_t i = i0 + u * kThreads + tid;
-                if (i < n16) v[u] = __ldcs(src + i);
-            }
-#pragma unroll
-            for (int u = 0; u < kPer; ++u) {
-                const uint32_t i = i0 + u * kThreads + tid;
-                if (i < n16) dst[i] = v[u];
-            }
-        }
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&st.lut_bar);
+    if (tid == 0) {
+        // the query's table (from k_build_luts): one bulk async copy global -> shared
+        // (TMA), counted in bytes on an mbarrier; it lands while the block sets up
+        // its first cluster
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1u));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                     "r"(p.lut_bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+            "[%3];" ::"r"((uint32_t)__cvta_generic_to_shared(lut)),
+            "l"(p.luts + (uint64_t)qi * p.lut_bytes), "r"(p.lut_bytes), "r"(bar)
+            : "memory");
     }
+    bool lut_ready = false;
+    // Waits (bounded) for the table; on expiry flags the pass and builds the same
+    // table here. Every thread calls it.
+    auto wait_lut = [&]() {
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < (1u << 22) && !done; ++it) {
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                "selp.b32 %0, 1, 0, p;\n}"
+                : "=r"(done)
+                : "r"(bar), "r"(0u)
+                : "memory");
+        }
+        if (!__syncthreads_and(done != 0)) {
+            if (tid == 0) atomicExch(p.err, 2);
+            if (HALF) {
+                const float scale =
+                    ldexpf(1.0f, half_lut_exponent(p.qnorm[qi], p.codebook_max));
+                for (uint32_t e = tid; e < nsq * 256; e += kThreads)
+                    luth[e] = __float2half_rn(
+                        l2sqr_sse(qv + (e >> 8) * p.lsq, p.codebook + (uint64_t)e * p.lsq, p.lsq) *
+                        scale);
+            } else {
+                build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
+            }
+            __syncthreads();
+        }
+        lut_ready = true;
+    };
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     const float* fdk = p.fd_by_fine + (uint64_t)qi * F;  // fine terms of this query
     if (tid == 0) {
@@ -309,6 +336,7 @@ __global__ __launch_bounds__(kThreads, 4) void k_scan_select(ScanParams p) {
         // per fine id of this cluster: 2 * cell_dist, cell_dist = (cd + stationary) + fd
         for (uint32_t i = tid; i < F; i += kThreads)
             srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
+        if (!lut_ready) wait_lut();
         __syncthreads();
         if (tid == 0) st.n_records += r1 - r0;
         for (uint32_t base = r0; base < r1; base += kRound) {
@@ -378,6 +406,7 @@ __global__ __launch_bounds__(kThreads, 4) void k_scan_select(ScanParams p) {
             }
         }
     }
+    if (!lut_ready) wait_lut();  // no copy may be in flight when the block exits
     __syncthreads();
     const long long t_final = clock64();
     uint32_t count = st.count;
@@ -455,6 +484,7 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.codebook_max = ix.codebook_max;
     p.luts = reinterpret_cast<const unsigned char*>(s.luts);
     p.lut_bytes = ix.nsq * 256 * (half_lut ? 2 : 4);
+    p.err = s.tc_err;
     if (s.luts == nullptr) return cudaErrorInvalidValue;
     {
         const dim3 g(n, ix.nsq);
