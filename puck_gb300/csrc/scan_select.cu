@@ -31,8 +31,8 @@
 namespace pgpu {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kRecPerThread = 4;
+constexpr int kThreads = 128;
+constexpr int kRecPerThread = 8;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
 constexpr uint32_t kCandCap = 2048;               // candidate buffer (power of two)
 
@@ -239,7 +239,7 @@ struct ScanState {
 
 // NW = code words per record (code_stride / 4); HALF = FP16 table.
 template <int NW, bool HALF>
-__global__ __launch_bounds__(kThreads, 3) void k_scan_select(ScanParams p) {
+__global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ScanState st;
     const uint32_t qi = blockIdx.x;
