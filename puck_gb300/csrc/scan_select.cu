@@ -68,8 +68,9 @@ __device__ __forceinline__ int half_lut_exponent(float qnorm, float codebook_max
     return e < -60 ? -60 : (e > 60 ? 60 : e);
 }
 
-// get_dist_table (quantization.cpp:260-270) for a batch: block (query, subspace),
-// thread j = codeword j; the reference's lane order via l2sqr_sse.
+// get_dist_table (quantization.cpp:260-270) for a batch: one block per query,
+// thread j computes codeword j of every subspace (coalesced 16-byte codebook
+// loads, 8 subspaces in flight), in the reference's lane order (l2sqr_sse).
 template <bool HALF>
 __global__ __launch_bounds__(256) void k_build_luts(const float* __restrict__ q,
                                                     const float* __restrict__ qnorm,
@@ -77,15 +78,40 @@ __global__ __launch_bounds__(256) void k_build_luts(const float* __restrict__ q,
                                                     const float* __restrict__ cb, uint32_t d,
                                                     uint32_t nsq, uint32_t lsq, float codebook_max,
                                                     unsigned char* __restrict__ luts) {
-    const uint32_t qi = blockIdx.x, m = blockIdx.y, j = threadIdx.x;
+    __shared__ float qs[kMaxDim];
+    const uint32_t qi = blockIdx.x, j = threadIdx.x;
     if (status[qi] != 0) return;
-    const float v = l2sqr_sse(q + (uint64_t)qi * d + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
-    const uint64_t e = (uint64_t)qi * nsq * 256 + m * 256 + j;
-    if (HALF) {
-        const float scale = ldexpf(1.0f, half_lut_exponent(qnorm[qi], codebook_max));
-        reinterpret_cast<__half*>(luts)[e] = __float2half_rn(v * scale);
+    for (uint32_t k = j; k < d; k += 256) qs[k] = q[(uint64_t)qi * d + k];
+    __syncthreads();
+    const float scale = HALF ? ldexpf(1.0f, half_lut_exponent(qnorm[qi], codebook_max)) : 1.0f;
+    float* out32 = reinterpret_cast<float*>(luts) + (uint64_t)qi * nsq * 256;
+    __half* out16 = reinterpret_cast<__half*>(luts) + (uint64_t)qi * nsq * 256;
+    if (lsq == 4) {
+        const float4* cb4 = reinterpret_cast<const float4*>(cb);
+        for (uint32_t m0 = 0; m0 < nsq; m0 += 8) {
+            float4 y[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (m0 + u < nsq) y[u] = __ldg(cb4 + (uint64_t)(m0 + u) * 256 + j);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t m = m0 + u;
+                if (m >= nsq) break;
+                const float* x = qs + m * 4;
+                const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
+                const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
+                const float v = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                          __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
+                if (HALF) out16[m * 256 + j] = __float2half_rn(v * scale);
+                else out32[m * 256 + j] = v;
+            }
+        }
     } else {
-        reinterpret_cast<float*>(luts)[e] = v;
+        for (uint32_t m = 0; m < nsq; ++m) {
+            const float v = l2sqr_sse(qs + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
+            if (HALF) out16[m * 256 + j] = __float2half_rn(v * scale);
+            else out32[m * 256 + j] = v;
+        }
     }
 }
 
@@ -487,7 +513,7 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.err = s.tc_err;
     if (s.luts == nullptr) return cudaErrorInvalidValue;
     {
-        const dim3 g(n, ix.nsq);
+        const dim3 g(n);
         if (half_lut)
             k_build_luts<true><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, ix.d,
                                                       ix.nsq, ix.lsq, ix.codebook_max, s.luts);

@@ -143,6 +143,162 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     }
 }
 
+// The same selection for small P (P <= kSmallP), one warp per query row: the P-th
+// smallest s^ + E by P rounds of warp minima over (value, id), the window's exact
+// values recomputed one per lane, a warp bitonic sort of at most 64 candidates,
+// and the tie check. With a tie or a wider window the warp feeds every exact
+// value, 32 at a time in index order, to lane 0's MaxHeap(P).
+constexpr uint32_t kSmallP = 16;
+constexpr uint32_t kSmallCap = 64;
+__global__ __launch_bounds__(256) void k_window_small(
+    const float* __restrict__ approx, uint32_t ld, const float* __restrict__ Q, uint32_t d,
+    const float* __restrict__ qnorm, const float* __restrict__ cents,
+    const float* __restrict__ bias, const float* __restrict__ cabs, uint32_t C, uint32_t P,
+    uint32_t ld_out, uint32_t nrows, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
+    const int32_t* __restrict__ status, const int* __restrict__ tc_err,
+    unsigned long long* __restrict__ fallbacks) {
+    __shared__ unsigned long long wkey[8][kSmallCap];
+    __shared__ float hv_s[8][kSmallP + 1];
+    __shared__ uint32_t ht_s[8][kSmallP + 1];
+    __shared__ float chunk[8][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t row = blockIdx.x * 8 + warp;
+    if (row >= nrows) return;
+    float* ov = out_val + (uint64_t)row * ld_out;
+    uint32_t* oi = out_idx + (uint64_t)row * ld_out;
+    for (uint32_t i = P + lane; i < ld_out; i += 32) {
+        ov[i] = sentinel_f();
+        oi[i] = kNoLabel;
+    }
+    if (status != nullptr && status[row] != 0) {
+        for (uint32_t i = lane; i < P; i += 32) {
+            ov[i] = sentinel_f();
+            oi[i] = kNoLabel;
+        }
+        return;
+    }
+    const float* q = Q + (uint64_t)row * d;
+    const float* a = approx + (uint64_t)row * ld;
+    unsigned long long* keys = wkey[warp];
+    bool exact_all = (*tc_err != 0);
+    if (!exact_all) {
+        const float eps = window_eps(d);
+        const float qa = sqrtf(qnorm[row]);
+        // P-th smallest (hi, id)
+        float lv = -FLT_MAX;
+        uint32_t li = 0;
+        bool first = true;
+        for (uint32_t r = 0; r < P; ++r) {
+            float bv = FLT_MAX;
+            uint32_t bi = 0xFFFFFFFFu;
+            for (uint32_t j = lane; j < C; j += 32) {
+                const float sv = a[j];
+                const float hi = sv + (eps * qa * cabs[j] +
+                                       9.5367431640625e-07f * (fabsf(bias[j]) + fabsf(sv)) + 1e-30f);
+                const bool above = first || hi > lv || (hi == lv && j > li);
+                if (above && (hi < bv || (hi == bv && j < bi))) {
+                    bv = hi;
+                    bi = j;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ov2 = __shfl_xor_sync(0xffffffffu, bv, o);
+                const uint32_t oi2 = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov2 < bv || (ov2 == bv && oi2 < bi)) {
+                    bv = ov2;
+                    bi = oi2;
+                }
+            }
+            lv = bv;
+            li = bi;
+            first = false;
+        }
+        const float U = lv;
+        // window: lo <= U, exact value per candidate
+        uint32_t m = 0;
+        for (uint32_t j0 = 0; j0 < C; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            bool in = false;
+            if (j < C) {
+                const float sv = a[j];
+                const float e = eps * qa * cabs[j] + 9.5367431640625e-07f * (fabsf(bias[j]) + fabsf(sv)) +
+                                1e-30f;
+                in = (sv - e) <= U;
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, in);
+            if (m + __popc(b) > kSmallCap) {
+                m = kSmallCap + 1;
+                break;
+            }
+            if (in) {
+                const float v = __fsub_rn(bias[j], dot_seq(q, cents + (uint64_t)j * d, d));
+                keys[m + __popc(b & ((1u << lane) - 1))] =
+                    ((unsigned long long)ordered_key(v) << 32) | j;
+            }
+            m += __popc(b);
+        }
+        __syncwarp();
+        if (m > kSmallCap) {
+            exact_all = true;
+        } else {
+            for (uint32_t i = m + lane; i < kSmallCap; i += 32) keys[i] = ~0ull;
+            __syncwarp();
+            // bitonic sort of 64 keys, two compare-exchanges per lane and step
+            for (uint32_t size = 2; size <= kSmallCap; size <<= 1) {
+                for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                    const uint32_t t = lane;
+                    const uint32_t lo = 2 * t - (t & (stride - 1));
+                    const uint32_t hi = lo + stride;
+                    const unsigned long long x = keys[lo], y = keys[hi];
+                    if ((x > y) == ((lo & size) == 0)) {
+                        keys[lo] = y;
+                        keys[hi] = x;
+                    }
+                    __syncwarp();
+                }
+            }
+            bool tie = false;
+            const uint32_t last = P < m ? P : m - 1;
+            for (uint32_t i = lane; i < last; i += 32)
+                tie |= (uint32_t)(keys[i] >> 32) == (uint32_t)(keys[i + 1] >> 32);
+            if (!__any_sync(0xffffffffu, tie)) {
+                for (uint32_t i = lane; i < P; i += 32) {
+                    ov[i] = key_to_float((uint32_t)(keys[i] >> 32));
+                    oi[i] = (uint32_t)keys[i];
+                }
+                return;
+            }
+            exact_all = true;
+        }
+    }
+    // Reference path: every exact value, in index order, into MaxHeap(P).
+    float* hv = hv_s[warp];
+    uint32_t* ht = ht_s[warp];
+    uint32_t dpc = P;
+    if (lane == 0) {
+        atomicAdd(fallbacks, 1ull);
+        for (uint32_t i = 1; i <= P; ++i) hv[i] = sentinel_f();
+    }
+    for (uint32_t j0 = 0; j0 < C; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        if (j < C) chunk[warp][lane] = __fsub_rn(bias[j], dot_seq(q, cents + (uint64_t)j * d, d));
+        __syncwarp();
+        if (lane == 0) {
+            const uint32_t cnt = C - j0 < 32 ? C - j0 : 32;
+            for (uint32_t t = 0; t < cnt; ++t) heap_update(hv, ht, P, dpc, chunk[warp][t], j0 + t);
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        heap_reorder(hv, ht, P);
+        for (uint32_t i = 0; i < P; ++i) {
+            ov[i] = hv[i + 1];
+            oi[i] = ht[i + 1];
+        }
+    }
+}
+
 // nearest_center (kmeans.cpp:221-258) from a tensor-core screen: one warp per
 // point. s^_j ~ 0.5|c_j|^2 - x.c_j orders the centroids like the reference's
 // cur_j = (|x|^2 + |c_j|^2) - 2 x.c_j; the window around the screened minimum
@@ -255,6 +411,12 @@ cudaError_t launch_coarse_tc(const DeviceIndex& ix, uint32_t n, Scratch& s, cuda
 
 cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
                                  cudaStream_t stream) {
+    if (s.Pfix <= kSmallP) {
+        k_window_small<<<(n + 7) / 8, 256, 0, stream>>>(
+            s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse, ix.coarse_norms, ix.coarse_abs, ix.C,
+            s.Pfix, s.P, n, s.cdist, s.ctag, s.status, s.tc_err, s.counters + kCounterWindowFallbacks);
+        return cudaGetLastError();
+    }
     const size_t smem = window_smem_bytes(ix.C, ix.d);
     static bool attr = false;
     if (!attr) {
