@@ -302,7 +302,8 @@ int build_host_index(const pgpu_index_arrays& a, HostIndex* h, std::string* err)
 }
 
 void free_device_index(DeviceIndex* ix) {
-    void* ptrs[] = {ix->coarse, ix->fine, ix->coarse_norms, ix->coarse_abs, ix->feat_bf16,
+    void* ptrs[] = {ix->coarse, ix->fine, ix->coarse_norms, ix->coarse_abs, ix->coarse_bf16,
+                    ix->fine_bf16, ix->feat_bf16,
                     ix->feat_abs, ix->stationary, ix->stat_sorted, ix->stat_fine, ix->rec_fine,
                     ix->cell_start,
                     ix->min_dist_offset, ix->mem2local, ix->offsets, ix->codes, ix->feat,

@@ -105,6 +105,8 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     PGPU_TRY(dev_copy(&ix->codes, h.codes_mem.data(), h.codes_mem.size(), &bytes));
     PGPU_TRY(dev_alloc(&ix->coarse_norms, h.C, &bytes));
     PGPU_TRY(dev_alloc(&ix->coarse_abs, h.C, &bytes));
+    PGPU_TRY(dev_alloc(&ix->coarse_bf16, (uint64_t)h.C * h.d, &bytes));
+    PGPU_TRY(dev_alloc(&ix->fine_bf16, (uint64_t)h.F * h.d, &bytes));
     PGPU_TRY(dev_alloc(&ix->stationary, cells, &bytes));
     PGPU_TRY(dev_alloc(&ix->stat_sorted, cells, &bytes));
     PGPU_TRY(dev_alloc(&ix->stat_fine, cells, &bytes));
@@ -122,6 +124,8 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     }
     PGPU_TRY(launch_half_norms(ix->coarse, h.C, h.d, ix->coarse_norms, 0));
     PGPU_TRY(launch_abs_from_half_norms(ix->coarse_norms, h.C, ix->coarse_abs, 0));
+    PGPU_TRY(launch_to_bf16(ix->coarse, (uint64_t)h.C * h.d, ix->coarse_bf16, 0));
+    PGPU_TRY(launch_to_bf16(ix->fine, (uint64_t)h.F * h.d, ix->fine_bf16, 0));
     PGPU_TRY(launch_half_norms(ix->fine, h.F, h.d, fine_half, 0));
     PGPU_TRY(launch_stationary(ix->coarse, h.C, ix->fine, h.F, h.d, fine_half, ix->stationary, 0));
     PGPU_TRY(launch_cell_constants(ix->stationary, ix->cell_start, ix->min_dist_offset, h.C, h.F,

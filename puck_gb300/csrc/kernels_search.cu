@@ -13,6 +13,8 @@
 //   k_topsort          top-P coarse / full fine order max_heap.cpp (exact heap on ties)
 //   k_walk_scan        cell walk + filter-PQ ADC      puck_index.cpp:346-390, 485-557
 //   k_rerank           exact L2 of the survivors      puck_index.cpp:392-457
+#include <cuda_bf16.h>
+
 #include <cfloat>
 #include <cstdint>
 
@@ -25,8 +27,9 @@ namespace {
 // ---------------------------------------------------------------- kernels
 
 __global__ void k_prep_queries(const float* __restrict__ q_in, float* __restrict__ q_out,
-                               float* __restrict__ qnorm, int32_t* __restrict__ status,
-                               uint32_t n, uint32_t d, int whether_norm) {
+                               uint16_t* __restrict__ q_bf16, float* __restrict__ qnorm,
+                               int32_t* __restrict__ status, uint32_t n, uint32_t d,
+                               int whether_norm) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* x = q_in + (uint64_t)i * d;
@@ -53,6 +56,8 @@ __global__ void k_prep_queries(const float* __restrict__ q_in, float* __restrict
     }
     qnorm[i] = dot_seq(y, y, d);
     if (st == 0 && !isfinite(qnorm[i])) st = PGPU_E_INVALID;
+    uint16_t* yb = q_bf16 + (uint64_t)i * d;
+    for (uint32_t k = 0; k < d; ++k) yb[k] = __bfloat16_as_ushort(__float2bfloat16_rn(y[k]));
     status[i] = st;
 }
 
@@ -405,6 +410,11 @@ __global__ __launch_bounds__(256) void k_nearest_center(const float* __restrict_
     }
 }
 
+__global__ void k_to_bf16_rows(const float* __restrict__ x, uint64_t n, uint16_t* __restrict__ y) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = __bfloat16_as_ushort(__float2bfloat16_rn(x[i]));
+}
+
 __global__ void k_gather_u32(const uint32_t* __restrict__ idx, uint64_t n,
                              const uint32_t* __restrict__ table, uint32_t* __restrict__ out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -424,8 +434,8 @@ __global__ void k_norms_full(const float* __restrict__ X, uint64_t rows, uint32_
 
 cudaError_t launch_prep_queries(const DeviceIndex& ix, const float* q_in, uint32_t n, Scratch& s,
                                 cudaStream_t stream) {
-    k_prep_queries<<<(n + 127) / 128, 128, 0, stream>>>(q_in, s.q, s.qnorm, s.status, n, ix.d,
-                                                       ix.whether_norm);
+    k_prep_queries<<<(n + 127) / 128, 128, 0, stream>>>(q_in, s.q, s.qb, s.qnorm, s.status, n,
+                                                       ix.d, ix.whether_norm);
     return cudaGetLastError();
 }
 
@@ -537,6 +547,12 @@ cudaError_t launch_gather_u32(const uint32_t* idx, uint64_t n, const uint32_t* t
                               uint32_t* out, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
     k_gather_u32<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(idx, n, table, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float* x, uint64_t n, uint16_t* y, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    k_to_bf16_rows<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(x, n, y);
     return cudaGetLastError();
 }
 

@@ -64,6 +64,8 @@ struct DeviceIndex {
     float* fine = nullptr;        // [F][d]
     float* coarse_norms = nullptr;// [C]  0.5*|c|^2
     float* coarse_abs = nullptr;  // [C]  |c| rounded up (error bound of the tensor-core screen)
+    uint16_t* coarse_bf16 = nullptr;  // [C][d] BF16 copy: operand of the tensor-core screen
+    uint16_t* fine_bf16 = nullptr;    // [F][d]
     float* stationary = nullptr;  // [C][F] 0.5*|f|^2 + f.c ; sqrt(FLT_MAX) for empty cells
     float* stat_sorted = nullptr; // [C][F] each coarse row of stationary, ascending
     uint32_t* stat_fine = nullptr;// [C][F] fine id of each stat_sorted entry
@@ -85,6 +87,7 @@ struct DeviceIndex {
 struct Scratch {
     uint32_t cap = 0;
     float* q = nullptr;        // [B][d] normalised queries
+    uint16_t* qb = nullptr;    // [B][d] the same, BF16 (tensor-core operand)
     float* qnorm = nullptr;    // [B]
     int32_t* status = nullptr; // [B]
     float* dots = nullptr;     // [B][max(C,F)]
@@ -156,6 +159,7 @@ cudaError_t launch_stationary(const float* coarse, uint32_t C, const float* fine
                               cudaStream_t stream);
 cudaError_t launch_half_norms(const float* X, uint32_t rows, uint32_t d, float* out,
                               cudaStream_t stream);
+cudaError_t launch_to_bf16(const float* x, uint64_t n, uint16_t* y, cudaStream_t stream);
 cudaError_t launch_cell_constants(float* stationary, const uint32_t* cell_start, float* mdo,
                                   uint32_t C, uint32_t F, float empty_value, cudaStream_t stream);
 size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T);
@@ -222,8 +226,9 @@ cudaError_t probe_init(ProbeNet& net, uint64_t seed, cudaStream_t st);
 // Refreshes the BF16 weight copies from the FP32 weights.
 cudaError_t probe_sync_bf16(const ProbeNet& net, cudaStream_t st);
 // Inference: scores Z [n][C] (FP32) with BF16 hidden activations H1b, H2b [n][h].
-cudaError_t probe_infer(const ProbeNet& net, const float* X, uint32_t n, uint16_t* H1b,
-                        uint16_t* H2b, float* Z, int* err, cudaStream_t st);
+// X: FP32 queries, or their BF16 copy Xb when not null.
+cudaError_t probe_infer(const ProbeNet& net, const float* X, const uint16_t* Xb, uint32_t n,
+                        uint16_t* H1b, uint16_t* H2b, float* Z, int* err, cudaStream_t st);
 cudaError_t probe_adam(ProbeNet& net, const ProbeNet& grad, ProbeNet& m, ProbeNet& v, float lr,
                        uint64_t step, cudaStream_t st);
 cudaError_t launch_probe_select(const ProbeNet& net, const DeviceIndex& ix, uint32_t n,

@@ -18,7 +18,7 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
 }  // namespace
 
 void free_scratch(Scratch* s) {
-    void* ptrs[] = {s->q, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
+    void* ptrs[] = {s->q, s->qb, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
                     s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err, s->luts,
                     s->ph1, s->ph2};
     for (void* p : ptrs)
@@ -31,7 +31,7 @@ uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t 
     const uint64_t probe = cfg.probe ? (uint64_t)B * cfg.probe->h * 4 : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * ix.nsq * 256 * 4 : 0;
-    return (uint64_t)B * (ix.d * 4 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
+    return (uint64_t)B * (ix.d * 6 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
            fine_order + tables + probe + kNumWalkCounters * 8 + 4;
 }
 
@@ -49,6 +49,7 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
 #define PGPU_ALLOC(ptr, cnt)                                                        \
     if (e == cudaSuccess) e = alloc(&(ptr), (cnt), &b);
     PGPU_ALLOC(s.q, (uint64_t)B * ix.d);
+    PGPU_ALLOC(s.qb, (uint64_t)B * ix.d);
     PGPU_ALLOC(s.qnorm, B);
     PGPU_ALLOC(s.status, B);
     PGPU_ALLOC(s.dots, (uint64_t)B * std::max(ix.C, ix.F));
@@ -104,7 +105,7 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     if (cfg.probe) {
         // learned probe: scores of the coarse clusters (into the score buffer),
         // then the adaptive choice that replaces the fixed count where confident
-        PGPU_STEP(probe_infer(*cfg.probe, s.q, n, s.ph1, s.ph2, s.dots, s.tc_err, st),
+        PGPU_STEP(probe_infer(*cfg.probe, s.q, s.qb, n, s.ph1, s.ph2, s.dots, s.tc_err, st),
                   "probe forward");
         PGPU_STEP(launch_probe_select(*cfg.probe, ix, n, s.dots, cfg.probe_mass, cfg.probe_max, s,
                                       st),
@@ -115,8 +116,8 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     const bool bf16 = cfg.precision == PGPU_PRECISION_BF16;
     if (bf16) {
         // precision form: -q.f from the BF16 tensor-core contraction
-        TcOperand A{s.q, ix.d, 1, n};
-        TcOperand B{ix.fine, ix.d, 1, ix.F};
+        TcOperand A{nullptr, ix.d, 1, n, s.qb};
+        TcOperand B{nullptr, ix.d, 1, ix.F, ix.fine_bf16};
         TcEpilogue ep{};
         ep.mode = TC_EPI_NEG;
         ep.out = s.dots;

@@ -297,15 +297,15 @@ cudaError_t probe_sync_bf16(const ProbeNet& net, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t probe_infer(const ProbeNet& net, const float* X, uint32_t n, uint16_t* H1b,
-                        uint16_t* H2b, float* Z, int* err, cudaStream_t st) {
+cudaError_t probe_infer(const ProbeNet& net, const float* X, const uint16_t* Xb, uint32_t n,
+                        uint16_t* H1b, uint16_t* H2b, float* Z, int* err, cudaStream_t st) {
     TcEpilogue e1{};
     e1.mode = TC_EPI_BIAS_GELU;
     e1.out_bf16 = H1b;
     e1.ld = net.h;
     e1.bias = net.b1;
     TcOperand w1{nullptr, net.d, 1, net.h, net.W1b};
-    cudaError_t e = launch_tc_gemm(TcOperand{X, net.d, 1, n}, w1, net.d, e1, err, st);
+    cudaError_t e = launch_tc_gemm(TcOperand{X, net.d, 1, n, Xb}, w1, net.d, e1, err, st);
     if (e != cudaSuccess) return e;
     TcEpilogue e2{};
     e2.mode = TC_EPI_BIAS_GELU;

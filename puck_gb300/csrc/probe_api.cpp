@@ -202,7 +202,7 @@ int pgpu_probe_forward(pgpu_probe* p, const float* queries, uint32_t n, float* s
     if (e != cudaSuccess) return cuda_fail(e, "probe work buffers");
     cudaMemsetAsync(p->err, 0, sizeof(int), p->stream);
     // the search's own inference path: BF16 weights and activations
-    e = pgpu::probe_infer(p->net, queries, n, reinterpret_cast<uint16_t*>(p->work.H1),
+    e = pgpu::probe_infer(p->net, queries, nullptr, n, reinterpret_cast<uint16_t*>(p->work.H1),
                           reinterpret_cast<uint16_t*>(p->work.H2), scores, p->err, p->stream);
     if (e != cudaSuccess) return cuda_fail(e, "probe forward");
     return finish(p, nullptr);

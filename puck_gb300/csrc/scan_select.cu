@@ -417,7 +417,9 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
             __syncthreads();
             const long long t_round_end = clock64();
             if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
-            if (st.count > kCandCap - kRound) {
+            // cut back when the buffer could not take another round, and once as soon
+            // as it holds more than T keys, so that the threshold prunes early
+            if (st.count > kCandCap - kRound || (st.tau == kKeyMax && st.count > T)) {
                 // cut back to the T best (unordered); tau = the T-th key
                 const uint32_t cnt = st.count;
                 const uint64_t kth = block_select_kth(keys, cnt, T, st.hist, st.sel);

@@ -138,6 +138,27 @@ __device__ __forceinline__ void stage_operand(uint8_t* tile, const TcOperand& op
     }
 }
 
+// Stages rows [row0, row0+128) x k [k0, k0 + 8*nkg) of a BF16 operand whose rows
+// are 16-byte aligned with cp.async (global -> shared, no registers), zero-filling
+// rows past op.rows and elements past K. Same layout as stage_operand.
+__device__ __forceinline__ void stage_operand_async(uint8_t* tile, const TcOperand& op,
+                                                    uint32_t row0, uint32_t k0, uint32_t K,
+                                                    uint32_t nkg) {
+    const uint32_t r = threadIdx.x;
+    const uint32_t row = row0 + r;
+    const bool in = row < op.rows;
+    const uint16_t* base = op.pb + (uint64_t)(in ? row : 0) * op.rs;
+    const uint32_t dst = smem_u32(tile) + (r >> 3) * 128u + (r & 7u) * 16u;
+    for (uint32_t kg = 0; kg < nkg; ++kg) {
+        const uint32_t k = k0 + kg * 8;
+        const uint32_t bytes = (in && k < K) ? (K - k >= 8 ? 16u : 2u * (K - k)) : 0u;
+        const uint16_t* src = base + (k < K ? k : 0);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst + kg * (16u * 128u)),
+                     "l"(src), "r"(bytes)
+                     : "memory");
+    }
+}
+
 __device__ __forceinline__ float gelu_f(float x) {
     return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
 }
@@ -166,12 +187,16 @@ __device__ __forceinline__ float epilogue(float acc, uint32_t i, uint32_t j, con
     return acc * gelu_grad_f(ep.aux[(uint64_t)i * ep.ld_aux + j]);
 }
 
-template <int EPI>
+// ASYNC: both operands BF16 with 16-byte aligned rows, staged by cp.async through
+// kAsyncStages buffers so that the loads of the next chunks overlap the MMAs.
+constexpr uint32_t kAsyncStages = 3;
+
+template <int EPI, bool ASYNC>
 __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B, uint32_t K,
                                                          int a_vec, int b_vec, TcEpilogue ep,
                                                          int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar[kAsyncStages];
     __shared__ uint32_t tmem_base;
     __shared__ int failed;
     const uint32_t m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
@@ -186,8 +211,8 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
     }
     if (tid == 0) {
         failed = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[0])), "r"(1u));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[1])), "r"(1u));
+        for (uint32_t i = 0; i < kAsyncStages; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[i])), "r"(1u));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -197,7 +222,68 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
 
     const uint32_t nch = (K + kChunkK - 1) / kChunkK;
     bool ok = true;
-    for (uint32_t c = 0; c < nch; ++c) {
+    auto issue_mma = [&](uint32_t c, uint8_t* a_tile, uint8_t* b_tile, uint32_t bar) {
+        const uint32_t kc = min(kChunkK, K - c * kChunkK);
+        const uint32_t nk16 = (kc + 15) / 16;
+        const uint32_t lbo = 16u * 128u, sbo = 128u;
+        const uint32_t a_addr = smem_u32(a_tile), b_addr = smem_u32(b_tile);
+        for (uint32_t s = 0; s < nk16; ++s) {
+            const uint64_t ad = smem_desc(a_addr + s * 2u * lbo, lbo, sbo);
+            const uint64_t bd = smem_desc(b_addr + s * 2u * lbo, lbo, sbo);
+            const uint32_t accum = (c > 0 || s > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(kInstrDesc), "r"(accum)
+                : "memory");
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+            : "memory");
+    };
+    if (ASYNC) {
+        constexpr uint32_t S = kAsyncStages;
+        auto stage = [&](uint32_t c) {
+            uint8_t* a_tile = smem + (c % S) * kStageBytes;
+            uint8_t* b_tile = a_tile + kTileM * kChunkK * 2;
+            const uint32_t k0 = c * kChunkK;
+            const uint32_t nkg = ((min(kChunkK, K - k0) + 15) / 16) * 2;
+            stage_operand_async(a_tile, A, m0, k0, K, nkg);
+            stage_operand_async(b_tile, B, n0, k0, K, nkg);
+        };
+        for (uint32_t c = 0; c + 1 < S; ++c) {
+            if (c < nch) stage(c);
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        }
+        for (uint32_t c = 0; c < nch; ++c) {
+            const uint32_t nc = c + S - 1;
+            // the buffer of chunk nc held chunk c-1: its MMAs must be done
+            if (nc < nch && c >= 1 &&
+                !mbar_wait(smem_u32(&mbar[(c - 1) % S]), ((c - 1) / S) & 1u))
+                ok = false;
+            if (!__syncthreads_and(ok)) {
+                ok = false;
+                break;
+            }
+            if (nc < nch) stage(nc);
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            asm volatile("cp.async.wait_group %0;" ::"n"(S - 1) : "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            if (tid == 0) {
+                uint8_t* a_tile = smem + (c % S) * kStageBytes;
+                issue_mma(c, a_tile, a_tile + kTileM * kChunkK * 2, smem_u32(&mbar[c % S]));
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (nch > 0 && ok) {
+            const uint32_t L = nch - 1;
+            if (!mbar_wait(smem_u32(&mbar[L % S]), (L / S) & 1u)) ok = false;
+        }
+    }
+    for (uint32_t c = 0; !ASYNC && c < nch; ++c) {
         const uint32_t b = c & 1u;
         if (c >= 2 && !mbar_wait(smem_u32(&mbar[b]), ((c - 2) >> 1) & 1u)) ok = false;
         if (!__syncthreads_and(ok)) {
@@ -216,27 +302,10 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
-        if (tid == 0) {
-            const uint32_t lbo = 16u * 128u, sbo = 128u;
-            const uint32_t a_addr = smem_u32(a_tile), b_addr = smem_u32(b_tile);
-            for (uint32_t s = 0; s < nk16; ++s) {
-                const uint64_t ad = smem_desc(a_addr + s * 2u * lbo, lbo, sbo);
-                const uint64_t bd = smem_desc(b_addr + s * 2u * lbo, lbo, sbo);
-                const uint32_t accum = (c > 0 || s > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(kInstrDesc), "r"(accum)
-                    : "memory");
-            }
-            asm volatile(
-                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                    smem_u32(&mbar[b]))
-                : "memory");
-        }
+        if (tid == 0) issue_mma(c, a_tile, b_tile, smem_u32(&mbar[b]));
     }
     // The last commit covers every MMA issued before it.
-    if (nch > 0 && ok) {
+    if (!ASYNC && nch > 0 && ok) {
         const uint32_t L = nch - 1;
         if (!mbar_wait(smem_u32(&mbar[L & 1u]), (L >> 1) & 1u)) ok = false;
     }
@@ -325,6 +394,7 @@ bool operand_vec(const TcOperand& op) {
 }  // namespace
 
 size_t tc_gemm_smem_bytes() { return 2 * (size_t)kStageBytes; }
+size_t tc_gemm_async_smem_bytes() { return kAsyncStages * (size_t)kStageBytes; }
 
 cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
                            const TcEpilogue& ep, int* err, cudaStream_t stream) {
@@ -339,17 +409,27 @@ cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
     if (ep.mode == TC_EPI_GELU_BWD && ep.aux == nullptr) return cudaErrorInvalidValue;
     const dim3 grid((B.rows + kTileN - 1) / kTileN, (A.rows + kTileM - 1) / kTileM);
     if (grid.y > 65535) return cudaErrorInvalidValue;
-    const size_t smem = tc_gemm_smem_bytes();
     const int av = operand_vec(A) ? 1 : 0, bv = operand_vec(B) ? 1 : 0;
-    static bool attr[6] = {false, false, false, false, false, false};
-#define PGPU_TC_CASE(M)                                                                      \
-    case M:                                                                                  \
-        if (!attr[M]) {                                                                      \
-            cudaFuncSetAttribute(k_tc_gemm<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                 (int)smem);                                                 \
-            attr[M] = true;                                                                  \
-        }                                                                                    \
-        k_tc_gemm<M><<<grid, kTcThreads, smem, stream>>>(A, B, K, av, bv, ep, err);         \
+    const bool async = A.pb != nullptr && B.pb != nullptr && av && bv;
+    const size_t smem = async ? tc_gemm_async_smem_bytes() : tc_gemm_smem_bytes();
+    static bool attr[12] = {};
+#define PGPU_TC_CASE(M)                                                                        \
+    case M:                                                                                    \
+        if (async) {                                                                           \
+            if (!attr[M + 6]) {                                                                \
+                cudaFuncSetAttribute(k_tc_gemm<M, true>,                                       \
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
+                attr[M + 6] = true;                                                            \
+            }                                                                                  \
+            k_tc_gemm<M, true><<<grid, kTcThreads, smem, stream>>>(A, B, K, av, bv, ep, err); \
+        } else {                                                                               \
+            if (!attr[M]) {                                                                    \
+                cudaFuncSetAttribute(k_tc_gemm<M, false>,                                      \
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
+                attr[M] = true;                                                                \
+            }                                                                                  \
+            k_tc_gemm<M, false><<<grid, kTcThreads, smem, stream>>>(A, B, K, av, bv, ep, err);\
+        }                                                                                      \
         break;
     switch (ep.mode) {
         PGPU_TC_CASE(TC_EPI_SCORE)

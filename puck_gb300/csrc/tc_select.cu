@@ -399,8 +399,8 @@ cudaError_t launch_abs_from_half_norms(const float* half_norms, uint32_t n, floa
 }
 
 cudaError_t launch_coarse_tc(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream) {
-    TcOperand A{s.q, ix.d, 1, n};
-    TcOperand B{ix.coarse, ix.d, 1, ix.C};
+    TcOperand A{nullptr, ix.d, 1, n, s.qb};
+    TcOperand B{nullptr, ix.d, 1, ix.C, ix.coarse_bf16};
     TcEpilogue ep{};
     ep.mode = TC_EPI_SCORE;
     ep.out = s.dots;
