@@ -103,6 +103,8 @@ struct Scratch {
     unsigned char* luts = nullptr; // scan mode: [B][nsq*256] lookup tables (FP32, or FP16)
     uint16_t* ph1 = nullptr;   // probe hidden activations [B][h], BF16 (with a probe attached)
     uint16_t* ph2 = nullptr;
+    int32_t* pconf = nullptr;  // [B] 1 where the probe chose the clusters (null: no probe)
+    float* pz = nullptr;       // [B][C] probe scores
     uint32_t Pfix = 0;         // fixed coarse count (<= P when a probe widens the slots)
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;

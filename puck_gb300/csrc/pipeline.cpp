@@ -20,7 +20,7 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qb, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
                     s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err, s->luts,
-                    s->ph1, s->ph2};
+                    s->ph1, s->ph2, s->pconf, s->pz};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *s = Scratch();
@@ -28,7 +28,7 @@ void free_scratch(Scratch* s) {
 
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
     const uint64_t P = cfg.coarse_slots(ix.C), T = cfg.filter_keep();
-    const uint64_t probe = cfg.probe ? (uint64_t)B * cfg.probe->h * 4 : 0;
+    const uint64_t probe = cfg.probe ? (uint64_t)B * (cfg.probe->h * 4 + 4 + ix.C * 4ull) : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * ix.nsq * 256 * 4 : 0;
     return (uint64_t)B * (ix.d * 6 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
@@ -66,6 +66,8 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     if (cfg.probe) {
         PGPU_ALLOC(s.ph1, (uint64_t)B * cfg.probe->h);
         PGPU_ALLOC(s.ph2, (uint64_t)B * cfg.probe->h);
+        PGPU_ALLOC(s.pconf, B);
+        PGPU_ALLOC(s.pz, (uint64_t)B * ix.C);
     }
 #undef PGPU_ALLOC
     if (e != cudaSuccess) {
@@ -100,18 +102,18 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     // coarse: BF16 tensor-core screen, then the exact top-P from an FP32 window
     PGPU_STEP(launch_coarse_tc(ix, n, s, st), "coarse scores");
     mark(2);
-    PGPU_STEP(launch_coarse_window(ix, n, s, st), "coarse select");
     int probe_kernels = 0;
     if (cfg.probe) {
-        // learned probe: scores of the coarse clusters (into the score buffer),
-        // then the adaptive choice that replaces the fixed count where confident
-        PGPU_STEP(probe_infer(*cfg.probe, s.q, s.qb, n, s.ph1, s.ph2, s.dots, s.tc_err, st),
+        // learned probe: scores of the coarse clusters, then the adaptive choice; the
+        // fixed-count window below only runs for the queries the probe leaves to it
+        float* pz = s.pz;
+        PGPU_STEP(probe_infer(*cfg.probe, s.q, s.qb, n, s.ph1, s.ph2, pz, s.tc_err, st),
                   "probe forward");
-        PGPU_STEP(launch_probe_select(*cfg.probe, ix, n, s.dots, cfg.probe_mass, cfg.probe_max, s,
-                                      st),
+        PGPU_STEP(launch_probe_select(*cfg.probe, ix, n, pz, cfg.probe_mass, cfg.probe_max, s, st),
                   "probe select");
         probe_kernels = 4;
     }
+    PGPU_STEP(launch_coarse_window(ix, n, s, st), "coarse select");
     mark(3);
     const bool bf16 = cfg.precision == PGPU_PRECISION_BF16;
     if (bf16) {

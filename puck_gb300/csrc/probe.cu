@@ -131,14 +131,16 @@ __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float
     w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// Adaptive cluster choice from the probe's scores (see the file comment).
-// ctag/cdist [n][Pcap] hold the plain coarse top-P on entry (P <= Pcap); rows
-// that the probe answers are overwritten, unused slots get kNoLabel.
+// Adaptive cluster choice from the probe's scores (see the file comment). Rows
+// that the probe answers get their clusters in ctag/cdist [n][Pcap] (unused slots
+// kNoLabel) and pconf = 1; the others get pconf = 0 and are left to the
+// fixed-count selection.
 __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     const float* __restrict__ Z, uint32_t C, const float* __restrict__ Q, uint32_t d,
     const float* __restrict__ cents, const float* __restrict__ bias, const int32_t* __restrict__ status,
     float mass, uint32_t max_probe, uint32_t Pcap, float* __restrict__ cdist,
-    uint32_t* __restrict__ ctag, unsigned long long* __restrict__ counters) {
+    uint32_t* __restrict__ ctag, int32_t* __restrict__ pconf,
+    unsigned long long* __restrict__ counters) {
     extern __shared__ float sp[];  // [C] probabilities
     __shared__ float red_v[kProbeThreads / 32];
     __shared__ uint32_t red_i[kProbeThreads / 32];
@@ -148,6 +150,7 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     __shared__ int confident;
     const uint32_t row = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) pconf[row] = 0;
     if (status[row] != 0) return;
     const float* z = Z + (uint64_t)row * C;
     float m = -FLT_MAX;
@@ -232,8 +235,9 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     __syncthreads();
     if (!confident) {
         if (tid == 0) atomicAdd(counters + kCounterProbeFallbacks, 1ull);
-        return;  // keep the plain fixed-count selection
+        return;  // the fixed-count selection fills this row
     }
+    if (tid == 0) pconf[row] = 1;
     const uint32_t np = npick;
     const float* q = Q + (uint64_t)row * d;
     for (uint32_t i = tid; i < Pcap; i += kProbeThreads) {
@@ -414,7 +418,7 @@ cudaError_t launch_probe_select(const ProbeNet& net, const DeviceIndex& ix, uint
     }
     k_probe_select<<<n, kProbeThreads, sizeof(float) * net.C, st>>>(
         Z, net.C, s.q, ix.d, ix.coarse, ix.coarse_norms, s.status, mass, max_probe, s.P, s.cdist,
-        s.ctag, s.counters);
+        s.ctag, s.pconf, s.counters);
     return cudaGetLastError();
 }
 

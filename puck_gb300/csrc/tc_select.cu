@@ -40,7 +40,8 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     const float* __restrict__ bias, const float* __restrict__ cabs, uint32_t C, uint32_t P,
     uint32_t ld_out, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
     const int32_t* __restrict__ status,
-    const int* __restrict__ tc_err, unsigned long long* __restrict__ fallbacks) {
+    const int* __restrict__ tc_err, unsigned long long* __restrict__ fallbacks,
+    const int32_t* __restrict__ skip) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* shi = reinterpret_cast<float*>(smem);                 // [C]   s^ + E, later exact s
     float* slo = shi + C;                                        // [C+1] s^ - E, later heap values
@@ -53,6 +54,7 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     __shared__ uint32_t ncand;
     const uint32_t row = blockIdx.x;
     const int tid = threadIdx.x;
+    if (skip != nullptr && skip[row]) return;  // the learned probe answered this query
     float* ov = out_val + (uint64_t)row * ld_out;
     uint32_t* oi = out_idx + (uint64_t)row * ld_out;
     // slots past P (a probe's wider cap): unused
@@ -156,7 +158,7 @@ __global__ __launch_bounds__(256) void k_window_small(
     const float* __restrict__ bias, const float* __restrict__ cabs, uint32_t C, uint32_t P,
     uint32_t ld_out, uint32_t nrows, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
     const int32_t* __restrict__ status, const int* __restrict__ tc_err,
-    unsigned long long* __restrict__ fallbacks) {
+    unsigned long long* __restrict__ fallbacks, const int32_t* __restrict__ skip) {
     __shared__ unsigned long long wkey[8][kSmallCap];
     __shared__ float hv_s[8][kSmallP + 1];
     __shared__ uint32_t ht_s[8][kSmallP + 1];
@@ -164,6 +166,7 @@ __global__ __launch_bounds__(256) void k_window_small(
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t row = blockIdx.x * 8 + warp;
     if (row >= nrows) return;
+    if (skip != nullptr && skip[row]) return;  // the learned probe answered this query
     float* ov = out_val + (uint64_t)row * ld_out;
     uint32_t* oi = out_idx + (uint64_t)row * ld_out;
     for (uint32_t i = P + lane; i < ld_out; i += 32) {
@@ -184,23 +187,50 @@ __global__ __launch_bounds__(256) void k_window_small(
     if (!exact_all) {
         const float eps = window_eps(d);
         const float qa = sqrtf(qnorm[row]);
-        // P-th smallest (hi, id)
-        float lv = -FLT_MAX;
-        uint32_t li = 0;
-        bool first = true;
-        for (uint32_t r = 0; r < P; ++r) {
-            float bv = FLT_MAX;
-            uint32_t bi = 0xFFFFFFFFu;
-            for (uint32_t j = lane; j < C; j += 32) {
-                const float sv = a[j];
-                const float hi = sv + (eps * qa * cabs[j] +
-                                       9.5367431640625e-07f * (fabsf(bias[j]) + fabsf(sv)) + 1e-30f);
-                const bool above = first || hi > lv || (hi == lv && j > li);
-                if (above && (hi < bv || (hi == bv && j < bi))) {
-                    bv = hi;
-                    bi = j;
+        // P-th smallest (hi, id): each lane keeps its P smallest in ascending order
+        // (one pass), then P rounds of warp minima over the lanes' heads
+        float tv[kSmallP];
+        uint32_t ti[kSmallP];
+#pragma unroll
+        for (uint32_t r = 0; r < kSmallP; ++r) {
+            tv[r] = FLT_MAX;
+            ti[r] = 0xFFFFFFFFu;
+        }
+        float worst = FLT_MAX;  // tv[P - 1]
+        for (uint32_t j = lane; j < C; j += 32) {
+            const float sv = a[j];
+            const float hi = sv + (eps * qa * cabs[j] +
+                                   9.5367431640625e-07f * (fabsf(bias[j]) + fabsf(sv)) + 1e-30f);
+            if (hi < worst) {  // ids ascend within a lane: equal values keep the earlier
+                float v = hi;
+                uint32_t id = j;
+#pragma unroll
+                for (uint32_t r = 0; r < kSmallP; ++r) {
+                    if (r < P && v < tv[r]) {
+                        const float t1 = tv[r];
+                        const uint32_t t2 = ti[r];
+                        tv[r] = v;
+                        ti[r] = id;
+                        v = t1;
+                        id = t2;
+                    }
+                    if (r + 1 == P) worst = tv[r];
                 }
             }
+        }
+        uint32_t head = 0;
+        float lv = FLT_MAX;
+        for (uint32_t r = 0; r < P; ++r) {
+            float hv = FLT_MAX;
+            uint32_t hid = 0xFFFFFFFFu;
+#pragma unroll
+            for (uint32_t t = 0; t < kSmallP; ++t)
+                if (t == head) {
+                    hv = tv[t];
+                    hid = ti[t];
+                }
+            float bv = hv;
+            uint32_t bi = hid;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const float ov2 = __shfl_xor_sync(0xffffffffu, bv, o);
@@ -210,9 +240,8 @@ __global__ __launch_bounds__(256) void k_window_small(
                     bi = oi2;
                 }
             }
+            if (hid == bi && hv == bv && bi != 0xFFFFFFFFu) ++head;
             lv = bv;
-            li = bi;
-            first = false;
         }
         const float U = lv;
         // window: lo <= U, exact value per candidate
@@ -414,7 +443,8 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
     if (s.Pfix <= kSmallP) {
         k_window_small<<<(n + 7) / 8, 256, 0, stream>>>(
             s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse, ix.coarse_norms, ix.coarse_abs, ix.C,
-            s.Pfix, s.P, n, s.cdist, s.ctag, s.status, s.tc_err, s.counters + kCounterWindowFallbacks);
+            s.Pfix, s.P, n, s.cdist, s.ctag, s.status, s.tc_err, s.counters + kCounterWindowFallbacks,
+            s.pconf);
         return cudaGetLastError();
     }
     const size_t smem = window_smem_bytes(ix.C, ix.d);
@@ -426,7 +456,7 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
     k_window_topk<<<n, kWinThreads, smem, stream>>>(s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse,
                                                     ix.coarse_norms, ix.coarse_abs, ix.C, s.Pfix,
                                                     s.P, s.cdist, s.ctag, s.status, s.tc_err,
-                                                    s.counters + kCounterWindowFallbacks);
+                                                    s.counters + kCounterWindowFallbacks, s.pconf);
     return cudaGetLastError();
 }
 
