@@ -243,7 +243,7 @@ struct ScreenParams {
     uint32_t d, T, Tp, topk;
 };
 
-__global__ __launch_bounds__(kThreads) void k_rerank_screen(ScreenParams p) {
+__global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);  // [Tp]
     float* qv = reinterpret_cast<float*>(keys + p.Tp);                       // [d]
@@ -276,6 +276,56 @@ __global__ __launch_bounds__(kThreads) void k_rerank_screen(ScreenParams p) {
     __syncthreads();
     bool full = cnt <= topk;
     if (!full) {
+        if ((d & 7u) == 0 && d <= 128) {
+            // screen, vector form: a half warp per row, 8 dimensions (one 16-byte
+            // load) per lane, kRows rows per half warp in flight
+            const int half = lane >> 4, hl = lane & 15;
+            const bool active = (uint32_t)hl * 8 < d;
+            float qr[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) qr[t] = active ? qv[hl * 8 + t] : 0.0f;
+            for (uint32_t j0 = (warp * 2 + half) * kRows; j0 < cnt; j0 += kWarps * 2 * kRows) {
+                uint4 x[kRows];
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const uint32_t j = j0 + u < cnt ? j0 + u : j0;
+                    x[u] = active ? __ldg(reinterpret_cast<const uint4*>(
+                                        p.feat_bf16 + (uint64_t)tags[j] * d) + hl)
+                                  : make_uint4(0, 0, 0, 0);
+                }
+                float acc[kRows];
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const uint32_t w[4] = {x[u].x, x[u].y, x[u].z, x[u].w};
+                    float a = 0.0f;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const float lo = __uint_as_float(w[t] << 16);
+                        const float hi2 = __uint_as_float(w[t] & 0xFFFF0000u);
+                        const float d0 = qr[2 * t] - lo, d1 = qr[2 * t + 1] - hi2;
+                        a += d0 * d0 + d1 * d1;
+                    }
+                    acc[u] = active ? a : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < kRows; ++u)
+#pragma unroll
+                    for (int o = 8; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+                if (hl < kRows) {
+                    float mine = acc[0];
+#pragma unroll
+                    for (int u = 1; u < kRows; ++u)
+                        if (hl == u) mine = acc[u];
+                    const uint32_t j = j0 + hl;
+                    if (j < cnt) {
+                        const float e = screen_bound(mine, p.feat_abs[tags[j]], d);
+                        approx[j] = mine;
+                        bnd[j] = e;
+                        hi[j] = mine + e;
+                    }
+                }
+            }
+        } else {
         // screen: kRows BF16 rows per warp in flight
         for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
             float acc[kRows];
@@ -312,6 +362,7 @@ __global__ __launch_bounds__(kThreads) void k_rerank_screen(ScreenParams p) {
                     hi[j] = mine + e;
                 }
             }
+        }
         }
         __syncthreads();
         const float U = key_to_float(block_kth_key<kThreads>(hi, cnt, topk, hist, state));

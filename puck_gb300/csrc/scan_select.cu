@@ -146,10 +146,46 @@ constexpr uint64_t kKeyMax = ~0ull;
 // slots, `sel` 4. All threads call it.
 __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint32_t K,
                                      uint32_t* hist, uint64_t* sel) {
-    const int tid = threadIdx.x, lane = tid & 31;
-    uint64_t prefix = 0, mask = 0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // the leading bits every key shares need no pass: start at the digit where the
+    // smallest and the largest key first differ
+    uint64_t lo = ~0ull, hi = 0;
+    for (uint32_t i = tid; i < count; i += kThreads) {
+        const uint64_t x = keys[i];
+        lo = x < lo ? x : lo;
+        hi = x > hi ? x : hi;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t a = __shfl_xor_sync(0xffffffffu, lo, o);
+        const uint64_t b = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    __shared__ uint64_t red_lo[kThreads / 32], red_hi[kThreads / 32];
+    if (lane == 0) {
+        red_lo[warp] = lo;
+        red_hi[warp] = hi;
+    }
+    __syncthreads();
+    lo = red_lo[0];
+    hi = red_hi[0];
+    for (int w = 1; w < kThreads / 32; ++w) {
+        lo = red_lo[w] < lo ? red_lo[w] : lo;
+        hi = red_hi[w] > hi ? red_hi[w] : hi;
+    }
+    __syncthreads();
+    int top = 56;
+    if (lo != hi) {
+        const int msb = 63 - __clzll((long long)(lo ^ hi));
+        top = (msb / 8) * 8;
+    } else {
+        top = 0;
+    }
+    uint64_t mask = top >= 56 ? 0ull : ~((1ull << (top + 8)) - 1);
+    uint64_t prefix = lo & mask;
     uint32_t k = K;
-    for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int shift = top; shift >= 0; shift -= 8) {
         for (int i = tid; i < 256; i += kThreads) hist[i] = 0;
         __syncthreads();
         for (uint32_t i0 = 0; i0 < count; i0 += kThreads) {
