@@ -284,11 +284,14 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
             float qr[8];
 #pragma unroll
             for (int t = 0; t < 8; ++t) qr[t] = active ? qv[hl * 8 + t] : 0.0f;
-            for (uint32_t j0 = (warp * 2 + half) * kRows; j0 < cnt; j0 += kWarps * 2 * kRows) {
+            // the loop runs the same iterations on both half warps (the shuffles below
+            // take the full mask): a warp owns 2 * kRows rows per iteration
+            for (uint32_t jw = warp * 2 * kRows; jw < cnt; jw += kWarps * 2 * kRows) {
+                const uint32_t j0 = jw + half * kRows;
                 uint4 x[kRows];
 #pragma unroll
                 for (int u = 0; u < kRows; ++u) {
-                    const uint32_t j = j0 + u < cnt ? j0 + u : j0;
+                    const uint32_t j = j0 + u < cnt ? j0 + u : jw;
                     x[u] = active ? __ldg(reinterpret_cast<const uint4*>(
                                         p.feat_bf16 + (uint64_t)tags[j] * d) + hl)
                                   : make_uint4(0, 0, 0, 0);
