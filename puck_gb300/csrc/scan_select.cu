@@ -34,7 +34,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kRecPerThread = 8;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
-constexpr uint32_t kCandCap = 2048;               // candidate buffer (power of two)
+constexpr uint32_t kCandCap = 1792;               // candidate buffer (keys)
 
 struct ScanParams {
     const float* q;
