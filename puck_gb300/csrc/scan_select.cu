@@ -34,7 +34,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kRecPerThread = 8;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
-constexpr uint32_t kCandCap = 1792;               // candidate buffer (keys)
+constexpr uint32_t kCandCap = 2048;               // candidate buffer (keys)
 
 struct ScanParams {
     const float* q;
@@ -453,9 +453,8 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
             __syncthreads();
             const long long t_round_end = clock64();
             if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
-            // cut back when the buffer could not take another round, and once as soon
-            // as it holds more than T keys, so that the threshold prunes early
-            if (st.count > kCandCap - kRound || (st.tau == kKeyMax && st.count > T)) {
+            // cut back when the buffer could not take another round
+            if (st.count > kCandCap - kRound) {
                 // cut back to the T best (unordered); tau = the T-th key
                 const uint32_t cnt = st.count;
                 const uint64_t kth = block_select_kth(keys, cnt, T, st.hist, st.sel);
