@@ -48,6 +48,13 @@ WORKLOADS = {
                       T=500, k=10, sweep=(50,), scan_sweep=(4,), nq=10000, norm=True,
                       train_sample=300_000, iters=10, pq_sample=131_072,
                       probe_train=100_000, probe_mass=(0.9,), probe_max=8, probe_fallback=4, probe_epochs=8),
+    # the learned-probe configuration: 100M x 96 normalised, 16384 components, C = F = 4000
+    # (run on request: building the index takes minutes)
+    "learned_100m": dict(n=100_000_000, d=96, ncomp=16384, kind="unit", C=4000, F=4000, nsq=24,
+                         T=500, k=10, sweep=(50,), scan_sweep=(1, 2, 4, 8), nq=10000, norm=True,
+                         train_sample=1_000_000, iters=10, pq_sample=262_144,
+                         probe_train=200_000, probe_mass=(0.5, 0.8, 0.9, 0.95), probe_max=8,
+                         probe_fallback=4, probe_epochs=8),
     # reduced workload for quick checks only (never the reported line)
     "cosine_1m": dict(n=1_000_000, d=96, ncomp=4096, kind="unit", C=500, F=500, nsq=24,
                       T=500, k=10, sweep=(25, 50, 100), scan_sweep=(1, 2, 4, 8), nq=10000,
