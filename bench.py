@@ -78,6 +78,22 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(value, ws, device=None):
+    """The largest of one float over all ranks (the slowest rank's time); ws == 1: itself."""
+    if ws <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_qps(total_ms, ws, nq, steps):
+    """Whole-job queries/s: every rank searched nq queries per step (weak scaling),
+    over the slowest rank's time."""
+    return ws * nq * steps / (total_ms / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
 
@@ -425,18 +441,16 @@ def run_gpu(args, w, rank, ws):
             torch.cuda.nvtx.range_pop()
         total = start.elapsed_time(end)
         per_step = np.array([a.elapsed_time(b) for a, b in evs])
+        total = max_over_ranks(total, ws, dev)
         if ws > 1:
-            t = torch.tensor([total], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total = float(t.item())
             torch.distributed.barrier()
         return total, per_step, clk.summary()
 
     # ---- timed regions (device-resident inputs): the plain path, then the headline form
     plain_ms, plain_steps, _ = timed(plain_best)
-    plain_value = ws * nq * args.steps / (plain_ms / 1e3)
+    plain_value = job_qps(plain_ms, ws, nq, args.steps)
     total_ms, step_ms, clocks = timed(best)
-    value = ws * nq * args.steps / (total_ms / 1e3)
+    value = job_qps(total_ms, ws, nq, args.steps)
     op_mode = native.PGPU_MODE_EXACT if best["mode"] == "exact" else native.PGPU_MODE_SCAN
     op = best["search_coarse_count"]
     op_recall = best["recall_at_10"]
