@@ -6,10 +6,11 @@
  * the last failure on the calling thread is available from pgpu_last_error().
  *
  * The index is the reference's on-disk Puck index (index.dat, coarse.dat,
- * fine.dat, cell_assign.dat, filter_codebook.dat, filter_data.dat,
- * all_data.feat.bin) with whether_pq = false ("Puck-Flat"): filter-PQ ADC scan
- * followed by an exact FP32 rerank against the original vectors. The search
- * runs on one GPU; there is no CPU fallback.
+ * fine.dat, cell_assign.dat, filter_codebook.dat, filter_data.dat, and
+ * all_data.feat.bin or, with whether_pq = 1, learn_codebooks.dat + pq_data.dat):
+ * filter-PQ ADC scan followed by an exact FP32 rerank against the original
+ * vectors ("Puck-Flat") or by the second-level PQ rerank. The search runs on one
+ * GPU; there is no CPU fallback.
  */
 #ifndef PUCK_GB300_H
 #define PUCK_GB300_H
@@ -25,7 +26,7 @@ extern "C" {
 #define PGPU_E_INVALID (-1)     /* bad argument: topk > configured topk, null feature, ... */
 #define PGPU_E_ZERO_NORM (-2)   /* whether_norm index and a query with norm < 1e-6 */
 #define PGPU_E_IO (-3)          /* index file missing, short or inconsistent */
-#define PGPU_E_UNSUPPORTED (-4) /* index feature outside Puck-Flat (whether_pq, ip2cos, ks != 256) */
+#define PGPU_E_UNSUPPORTED (-4) /* index feature outside the supported set (ip2cos, ks != 256) */
 #define PGPU_E_CUDA (-5)        /* CUDA runtime error, or no usable GPU */
 #define PGPU_E_NOMEM (-6)       /* device allocation failed */
 #define PGPU_E_LIMIT (-7)       /* size beyond a documented limit of a kernel */
@@ -95,6 +96,13 @@ typedef struct {
     const float* filter_codebook; /* [filter_nsq][256][feature_dim / filter_nsq] */
     const float* filter_offsets;  /* [total_point_count] */
     const uint8_t* filter_codes;  /* [total_point_count][filter_nsq] */
+    /* second-level PQ (whether_pq = 1, the reference's default): the rerank uses it
+     * instead of the original vectors, and base may be NULL */
+    int32_t whether_pq;
+    uint32_t pq_nsq;              /* PQ subspaces (feature_dim by default, lsq = 1) */
+    const float* pq_codebook;     /* [pq_nsq][256][feature_dim / pq_nsq] */
+    const float* pq_offsets;      /* [total_point_count] */
+    const uint8_t* pq_codes;      /* [total_point_count][pq_nsq] */
 } pgpu_index_arrays;
 
 /* Fills the reference's flag defaults (search_coarse_count 200, topk 100,

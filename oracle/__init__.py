@@ -68,6 +68,9 @@ def _load():
         lib.po_load.restype = ctypes.c_void_p
         lib.po_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         lib.po_free.argtypes = [ctypes.c_void_p]
+        lib.po_load_arrays_pq.restype = ctypes.c_void_p
+        lib.po_load_arrays_pq.argtypes = [ctypes.c_uint32] * 5 + [ctypes.c_int] + [ctypes.c_void_p] * 7 + [
+            ctypes.c_uint32] + [ctypes.c_void_p] * 3 + [ctypes.POINTER(ctypes.c_int)]
         lib.po_load_arrays.restype = ctypes.c_void_p
         lib.po_load_arrays.argtypes = [ctypes.c_uint32] * 5 + [ctypes.c_int] + [ctypes.c_void_p] * 7 + [
             ctypes.POINTER(ctypes.c_int)]
@@ -102,7 +105,8 @@ def _ptr(a):
 
 
 class OracleIndex:
-    """The C restatement loaded on one Puck-Flat index directory."""
+    """The C restatement loaded on one Puck index directory (Puck-Flat, or with the
+    second-level PQ)."""
 
     def __init__(self, index_dir=None, arrays=None):
         lib = _load()
@@ -110,17 +114,25 @@ class OracleIndex:
         if index_dir is not None:
             self._h = lib.po_load(index_dir.encode(), ctypes.byref(err))
         else:
-            a = {k: np.ascontiguousarray(arrays[k], t) for k, t in (
-                ("coarse", np.float32), ("fine", np.float32), ("base", np.float32),
-                ("cell_assign", np.uint32), ("filter_codebook", np.float32),
-                ("filter_offsets", np.float32), ("filter_codes", np.uint8))}
-            n, d = a["base"].shape
-            self._h = lib.po_load_arrays(
+            keys = [("coarse", np.float32), ("fine", np.float32), ("cell_assign", np.uint32),
+                    ("filter_codebook", np.float32), ("filter_offsets", np.float32),
+                    ("filter_codes", np.uint8)]
+            pq = arrays.get("pq_codes") is not None
+            keys += [("pq_codebook", np.float32), ("pq_offsets", np.float32),
+                     ("pq_codes", np.uint8)] if pq else [("base", np.float32)]
+            a = {k: np.ascontiguousarray(arrays[k], t) for k, t in keys}
+            n = a["cell_assign"].shape[0]
+            d = a["coarse"].shape[1]
+            self._h = lib.po_load_arrays_pq(
                 d, n, a["coarse"].shape[0], a["fine"].shape[0], a["filter_codes"].shape[1],
                 int(bool(arrays.get("whether_norm", False))), a["coarse"].ctypes.data,
-                a["fine"].ctypes.data, a["base"].ctypes.data, a["cell_assign"].ctypes.data,
-                a["filter_codebook"].ctypes.data, a["filter_offsets"].ctypes.data,
-                a["filter_codes"].ctypes.data, ctypes.byref(err))
+                a["fine"].ctypes.data, a["base"].ctypes.data if not pq else None,
+                a["cell_assign"].ctypes.data, a["filter_codebook"].ctypes.data,
+                a["filter_offsets"].ctypes.data, a["filter_codes"].ctypes.data,
+                a["pq_codes"].shape[1] if pq else 0,
+                a["pq_codebook"].ctypes.data if pq else None,
+                a["pq_offsets"].ctypes.data if pq else None,
+                a["pq_codes"].ctypes.data if pq else None, ctypes.byref(err))
         if not self._h:
             raise RuntimeError(f"oracle could not load the index (error {err.value})")
         vals = [ctypes.c_uint32() for _ in range(6)]

@@ -33,8 +33,13 @@ struct po_index {
     uint32_t* mem2local;    /* n */
     float* offsets;         /* n, memory order */
     uint8_t* codes;         /* n*nsq, memory order */
-    float* feat;            /* n*d, memory order */
+    float* feat;            /* n*d, memory order (NULL with the second-level PQ) */
     float* codebook;        /* nsq*256*lsq */
+    /* second-level PQ (whether_pq, puck_index.cpp:402-427) */
+    uint32_t pq_nsq, pq_lsq;
+    float* pq_offsets;      /* n, memory order */
+    uint8_t* pq_codes;      /* n*pq_nsq, memory order */
+    float* pq_codebook;     /* pq_nsq*256*pq_lsq */
 };
 
 /* ---------------------------------------------------------------- BLAS order */
@@ -191,13 +196,19 @@ void po_free(po_index* ix) {
     free(ix->codes);
     free(ix->feat);
     free(ix->codebook);
+    free(ix->pq_offsets);
+    free(ix->pq_codes);
+    free(ix->pq_codebook);
     free(ix);
 }
 
-po_index* po_load_arrays(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_t nsq,
-                         int whether_norm, const float* coarse, const float* fine,
-                         const float* base, const uint32_t* cell_assign, const float* codebook,
-                         const float* offsets_local, const uint8_t* codes_local, int* err) {
+po_index* po_load_arrays_pq(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_t nsq,
+                            int whether_norm, const float* coarse, const float* fine,
+                            const float* base, const uint32_t* cell_assign, const float* codebook,
+                            const float* offsets_local, const uint8_t* codes_local,
+                            uint32_t pq_nsq, const float* pq_codebook,
+                            const float* pq_offsets_local, const uint8_t* pq_codes_local,
+                            int* err) {
     int e = 0;
     mem_order* order = NULL;
     po_index* ix = (po_index*)calloc(1, sizeof(po_index));
@@ -264,15 +275,39 @@ po_index* po_load_arrays(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_
         if (st < ix->min_dist_offset[c]) ix->min_dist_offset[c] = st;
     }
 
-    /* read_feature_index: filter records and original vectors in memory order. */
+    /* read_feature_index: filter records and the original vectors (or, with the
+     * second-level PQ, its records) in memory order. */
+    if (pq_nsq) {
+        if (pq_nsq > d || d % pq_nsq != 0 || !pq_codebook || !pq_offsets_local || !pq_codes_local) {
+            e = -13;
+            goto fail;
+        }
+        ix->pq_nsq = pq_nsq;
+        ix->pq_lsq = d / pq_nsq;
+    } else if (!base) {
+        e = -14;
+        goto fail;
+    }
     ix->offsets = (float*)malloc(sizeof(float) * (n ? n : 1));
     ix->codes = (uint8_t*)malloc((uint64_t)nsq * (n ? n : 1));
-    ix->feat = (float*)malloc(sizeof(float) * (uint64_t)d * (n ? n : 1));
+    if (pq_nsq) {
+        ix->pq_offsets = (float*)malloc(sizeof(float) * (n ? n : 1));
+        ix->pq_codes = (uint8_t*)malloc((uint64_t)pq_nsq * (n ? n : 1));
+        ix->pq_codebook = (float*)malloc(sizeof(float) * (uint64_t)pq_nsq * 256 * ix->pq_lsq);
+        memcpy(ix->pq_codebook, pq_codebook, sizeof(float) * (uint64_t)pq_nsq * 256 * ix->pq_lsq);
+    } else {
+        ix->feat = (float*)malloc(sizeof(float) * (uint64_t)d * (n ? n : 1));
+    }
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t l = ix->mem2local[i];
         ix->offsets[i] = offsets_local[l];
         memcpy(ix->codes + (uint64_t)i * nsq, codes_local + (uint64_t)l * nsq, nsq);
-        memcpy(ix->feat + (uint64_t)i * d, base + (uint64_t)l * d, 4ull * d);
+        if (pq_nsq) {
+            ix->pq_offsets[i] = pq_offsets_local[l];
+            memcpy(ix->pq_codes + (uint64_t)i * pq_nsq, pq_codes_local + (uint64_t)l * pq_nsq, pq_nsq);
+        } else {
+            memcpy(ix->feat + (uint64_t)i * d, base + (uint64_t)l * d, 4ull * d);
+        }
     }
     ix->codebook = (float*)malloc(sizeof(float) * (uint64_t)nsq * 256 * ix->lsq);
     memcpy(ix->codebook, codebook, sizeof(float) * (uint64_t)nsq * 256 * ix->lsq);
@@ -286,6 +321,14 @@ fail:
     return NULL;
 }
 
+po_index* po_load_arrays(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_t nsq,
+                         int whether_norm, const float* coarse, const float* fine,
+                         const float* base, const uint32_t* cell_assign, const float* codebook,
+                         const float* offsets_local, const uint8_t* codes_local, int* err) {
+    return po_load_arrays_pq(d, n, C, F, nsq, whether_norm, coarse, fine, base, cell_assign,
+                             codebook, offsets_local, codes_local, 0, NULL, NULL, NULL, err);
+}
+
 po_index* po_load(const char* dir, int* err) {
     int e = 0;
     void* raw = NULL;
@@ -293,9 +336,10 @@ po_index* po_load(const char* dir, int* err) {
     uint32_t* cell_assign = NULL;
     uint8_t* rec = NULL;
     float *coarse = NULL, *fine = NULL, *feat = NULL, *codebook = NULL, *offsets = NULL;
-    uint8_t* codes = NULL;
+    float *pq_cb = NULL, *pq_off = NULL;
+    uint8_t *codes = NULL, *pq_rec = NULL, *pq_codes = NULL;
     po_index* ix = NULL;
-    uint32_t d, n, C, F, nsq;
+    uint32_t d, n, C, F, nsq, pq_nsq = 0;
     int whether_norm;
 
     /* index.dat: size_t length + packed config (hierarchical_cluster_index.cpp:551-567) */
@@ -314,9 +358,10 @@ po_index* po_load(const char* dir, int* err) {
         memcpy(&u, p, 4); p += 4; /* ks */
         if (u != 256 || !whether_filter) { e = -3; goto done; }
         uint8_t whether_pq = *p; p += 1;
-        if (whether_pq) { e = -4; goto done; } /* Puck-Flat only */
-        p += 4; /* nsq */
-        p += 4; /* ks */
+        memcpy(&u, p, 4); p += 4; /* nsq of the second-level PQ */
+        if (whether_pq) pq_nsq = u;
+        memcpy(&u, p, 4); p += 4; /* its ks */
+        if (whether_pq && u != 256) { e = -4; goto done; }
         memcpy(&u, p, 4); p += 4;
         if (u != 0) { e = -5; goto done; } /* ip2cos */
         memcpy(&C, p, 4); p += 4;
@@ -329,9 +374,27 @@ po_index* po_load(const char* dir, int* err) {
         const uint32_t lsq = d / nsq;
         coarse = read_fvecs(dir, "coarse.dat", d, C);
         fine = read_fvecs(dir, "fine.dat", d, F);
-        feat = read_fvecs(dir, "all_data.feat.bin", d, n);
+        if (!pq_nsq) feat = read_fvecs(dir, "all_data.feat.bin", d, n);
         codebook = read_fvecs(dir, "filter_codebook.dat", lsq, (uint64_t)nsq * 256);
-        if (!coarse || !fine || !feat || !codebook) { e = -8; goto done; }
+        if (!coarse || !fine || (!feat && !pq_nsq) || !codebook) { e = -8; goto done; }
+        if (pq_nsq) {
+            if (pq_nsq > d || d % pq_nsq != 0) { e = -7; goto done; }
+            /* learn_codebooks.dat / pq_data.dat (puck/gflags/puck_gflags.cpp defaults) */
+            pq_cb = read_fvecs(dir, "learn_codebooks.dat", d / pq_nsq, (uint64_t)pq_nsq * 256);
+            const uint32_t prb = 4 + pq_nsq;
+            if (!pq_cb || read_file(dir, "pq_data.dat", &raw, &len) != 0 || len != (uint64_t)prb * n) {
+                e = -15;
+                goto done;
+            }
+            pq_rec = (uint8_t*)raw;
+            raw = NULL;
+            pq_off = (float*)malloc(sizeof(float) * (n ? n : 1));
+            pq_codes = (uint8_t*)malloc((uint64_t)pq_nsq * (n ? n : 1));
+            for (uint32_t i = 0; i < n; ++i) {
+                memcpy(&pq_off[i], pq_rec + (uint64_t)i * prb, 4);
+                memcpy(pq_codes + (uint64_t)i * pq_nsq, pq_rec + (uint64_t)i * prb + 4, pq_nsq);
+            }
+        }
         if (read_file(dir, "cell_assign.dat", &raw, &len) != 0 || len != 4ull * n) { e = -9; goto done; }
         cell_assign = (uint32_t*)raw;
         raw = NULL;
@@ -345,8 +408,8 @@ po_index* po_load(const char* dir, int* err) {
             memcpy(&offsets[i], rec + (uint64_t)i * rb, 4);
             memcpy(codes + (uint64_t)i * nsq, rec + (uint64_t)i * rb + 4, nsq);
         }
-        ix = po_load_arrays(d, n, C, F, nsq, whether_norm, coarse, fine, feat, cell_assign, codebook,
-                            offsets, codes, &e);
+        ix = po_load_arrays_pq(d, n, C, F, nsq, whether_norm, coarse, fine, feat, cell_assign,
+                               codebook, offsets, codes, pq_nsq, pq_cb, pq_off, pq_codes, &e);
     }
 done:
     free(raw);
@@ -358,6 +421,10 @@ done:
     free(codebook);
     free(offsets);
     free(codes);
+    free(pq_cb);
+    free(pq_off);
+    free(pq_rec);
+    free(pq_codes);
     if (err) *err = e;
     return ix;
 }
@@ -449,6 +516,28 @@ static float l2sqr_ext(const float* x, const float* q, uint32_t qty) {
         s = s + sq;
     }
     return s;
+}
+
+/* rank_topN_points, second-level PQ branch (puck_index.cpp:402-427): candidates in
+ * the given order, temp = (filter distance - |q|^2) + pq offset, then
+ * += lookup_dist_table over the PQ table, into MaxHeap(topk). */
+static void rerank_pq(const po_index* ix, const float* q, const uint32_t* tags, const float* fdist,
+                      uint32_t stride, uint32_t cnt, po_heap* fin) {
+    const uint32_t pq_nsq = ix->pq_nsq, lsq = ix->pq_lsq;
+    float* lut = (float*)malloc(sizeof(float) * (uint64_t)pq_nsq * 256);
+    for (uint32_t m = 0; m < pq_nsq; ++m)
+        for (uint32_t j = 0; j < 256; ++j)
+            lut[m * 256 + j] = l2sqr_sse(q + (uint64_t)m * lsq,
+                                         ix->pq_codebook + ((uint64_t)m * 256 + j) * lsq, lsq);
+    const float qn = dotf(q, q, ix->d);
+    for (uint32_t idx = 0; idx < cnt; ++idx) {
+        const uint32_t mi = tags[(uint64_t)idx * stride];
+        float t = fdist[(uint64_t)idx * stride] - qn;
+        t = t + ix->pq_offsets[mi];
+        t = t + lookup_lut(ix->pq_codes + (uint64_t)mi * pq_nsq, lut, pq_nsq);
+        if (t < fin->val[1]) heap_update(fin, t, ix->mem2local[mi]);
+    }
+    free(lut);
 }
 
 /* -------------------------------------------------------------------- search */
@@ -600,6 +689,12 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
     /* rank_topN_points, Puck-Flat branch (puck_index.cpp:428-457) */
     po_heap fin;
     heap_init(&fin, topk, dist, ids);
+    if (ix->pq_nsq) {
+        rerank_pq(ix, q, s->rtag, s->rdist, 1, cnt, &fin);
+        heap_reorder(&fin);
+        *result_num = heap_count(&fin);
+        return 0;
+    }
     for (uint32_t idx = 0; idx < cnt; ++idx) {
         const float* x = ix->feat + (uint64_t)s->rtag[idx] * d;
         float t = 0.0f;
@@ -700,6 +795,13 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
     }
     po_heap fin;
     heap_init(&fin, topk, dist, ids);
+    if (ix->pq_nsq) {
+        rerank_pq(ix, q, &cand[0].mi, &cand[0].t, sizeof(po_cand) / sizeof(float), cnt, &fin);
+        heap_reorder(&fin);
+        *result_num = heap_count(&fin);
+        free(cand);
+        return 0;
+    }
     for (uint32_t idx = 0; idx < cnt; ++idx) {
         const float* x = ix->feat + (uint64_t)cand[idx].mi * d;
         float t = 0.0f;

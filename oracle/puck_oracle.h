@@ -1,8 +1,9 @@
 /*
  * ORACLE — test infrastructure, not the product.
  *
- * A plain-C restatement of Puck's Puck-Flat batched search path (index load,
- * normalisation, coarse/fine stage, filter-PQ ADC walk, exact rerank) and of
+ * A plain-C restatement of Puck's batched search path (index load,
+ * normalisation, coarse/fine stage, filter-PQ ADC walk, exact rerank or the
+ * second-level PQ rerank of whether_pq indexes) and of
  * the k-means assignment step, following the reference's float operation order
  * exactly (every product and sum rounded separately, BLAS dot products summed
  * sequentially). Only tests/, __graft_entry__.smoke() and bench.py's CPU
@@ -46,6 +47,16 @@ po_index* po_load_arrays(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_
                          int whether_norm, const float* coarse, const float* fine,
                          const float* base, const uint32_t* cell_assign, const float* codebook,
                          const float* offsets_local, const uint8_t* codes_local, int* err);
+/* The same with the second-level PQ (whether_pq): pq_nsq subspaces, its codebook
+ * [pq_nsq][256][d/pq_nsq] and per-point offsets and codes in input order; base may
+ * then be NULL. pq_nsq = 0 is po_load_arrays. */
+po_index* po_load_arrays_pq(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint32_t nsq,
+                            int whether_norm, const float* coarse, const float* fine,
+                            const float* base, const uint32_t* cell_assign, const float* codebook,
+                            const float* offsets_local, const uint8_t* codes_local,
+                            uint32_t pq_nsq, const float* pq_codebook,
+                            const float* pq_offsets_local, const uint8_t* pq_codes_local,
+                            int* err);
 void po_free(po_index* ix);
 int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,
             uint32_t* filter_nsq, uint32_t* lsq, int* whether_norm);

@@ -96,11 +96,15 @@ def assign_cells(x, coarse, fine, probe=8, chunk=32768):
 
 
 def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters=12,
-                pq_sample=131072, probe=8, seed=0):
-    """Trains and builds a Puck-Flat index from a device tensor `base` [n, d].
+                pq_sample=131072, probe=8, seed=0, whether_pq=False, pq_nsq=None):
+    """Trains and builds a Puck index from a device tensor `base` [n, d].
 
     Returns host numpy arrays in input order (the contents of the index files):
-    coarse, fine, base, cell_assign, filter_codebook, filter_offsets, filter_codes.
+    coarse, fine, base, cell_assign, filter_codebook, filter_offsets, filter_codes,
+    and with whether_pq the second-level PQ (pq_nsq subspaces, d by default):
+    pq_codebook, pq_offsets, pq_codes. As in puck_assign (puck_index.cpp:602-709)
+    the PQ encodes the residual left by the filter quantization, and each
+    quantization's offset is 2 * decoded . (coarse + fine + the earlier decodings).
     """
     dev = base.device
     n, d = base.shape
@@ -118,6 +122,14 @@ def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters
     pcell = cell[pq_idx]
     res = base[pq_idx] - coarse[pcell // F] - fine[pcell % F]
     books = _pq_train(res.contiguous(), filter_nsq, iters=10, seed=seed + 3)
+    pn = (d if pq_nsq is None else pq_nsq) if whether_pq else 0
+    if whether_pq:
+        assert d % pn == 0, "feature_dim must be a multiple of pq_nsq"
+        sc = _pq_encode(res.contiguous(), books)
+        sdec = books[torch.arange(filter_nsq, device=dev)[None, :], sc.long()].reshape(-1, d)
+        pq_books = _pq_train((res - sdec).contiguous(), pn, iters=10, seed=seed + 4)
+        pq_codes = torch.empty(n, pn, dtype=torch.uint8, device=dev)
+        pq_offsets = torch.empty(n, dtype=torch.float32, device=dev)
 
     codes = torch.empty(n, filter_nsq, dtype=torch.uint8, device=dev)
     offsets = torch.empty(n, dtype=torch.float32, device=dev)
@@ -132,11 +144,20 @@ def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters
         codes[s:s + chunk] = cd
         dec = books[torch.arange(filter_nsq, device=dev)[None, :], cd.long()].reshape(-1, d)
         offsets[s:s + chunk] = 2 * (dec * vocab).sum(1)
-    return dict(coarse=coarse.cpu().numpy(), fine=fine.cpu().numpy(),
-                base=base.cpu().numpy(), cell_assign=cell.to(torch.int64).cpu().numpy().astype(np.uint32),
-                filter_codebook=books.reshape(filter_nsq, 256, lsq).cpu().numpy(),
-                filter_offsets=offsets.cpu().numpy(), filter_codes=codes.cpu().numpy(),
-                whether_norm=bool(whether_norm))
+        if whether_pq:
+            cp = _pq_encode((r - dec).contiguous(), pq_books)
+            pq_codes[s:s + chunk] = cp
+            dec2 = pq_books[torch.arange(pn, device=dev)[None, :], cp.long()].reshape(-1, d)
+            pq_offsets[s:s + chunk] = 2 * (dec2 * (vocab + dec)).sum(1)
+    out = dict(coarse=coarse.cpu().numpy(), fine=fine.cpu().numpy(),
+               base=base.cpu().numpy(), cell_assign=cell.to(torch.int64).cpu().numpy().astype(np.uint32),
+               filter_codebook=books.reshape(filter_nsq, 256, lsq).cpu().numpy(),
+               filter_offsets=offsets.cpu().numpy(), filter_codes=codes.cpu().numpy(),
+               whether_norm=bool(whether_norm))
+    if whether_pq:
+        out.update(pq_codebook=pq_books.reshape(pn, 256, d // pn).cpu().numpy(),
+                   pq_offsets=pq_offsets.cpu().numpy(), pq_codes=pq_codes.cpu().numpy())
+    return out
 
 
 def gmm(n, d, ncomp, kind, seed, row_seed=None, device="cuda", chunk=1 << 21):

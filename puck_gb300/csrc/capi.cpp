@@ -99,7 +99,8 @@ int check_config(const pgpu_index* h, const pgpu_params* p) {
         const bool bf16 = p->precision == PGPU_PRECISION_BF16;
         if (pgpu::walk_smem_bytes(h->ix, p->filter_topk) > 220 * 1024 ||
             (bf16 ? pgpu::scan_smem_bytes_half(h->ix) : pgpu::scan_smem_bytes(h->ix)) > 220 * 1024 ||
-            (bf16 ? pgpu::rerank_screen_smem_bytes(h->ix, (uint32_t)keep, p->topk)
+            (bf16 && h->ix.pq_nsq == 0
+                 ? pgpu::rerank_screen_smem_bytes(h->ix, (uint32_t)keep, p->topk)
                   : pgpu::rerank_smem_bytes(h->ix, (uint32_t)keep, p->topk)) > 220 * 1024)
             return fail(PGPU_E_LIMIT, "filter_topk/topk/filter_nsq exceed the shared-memory budget");
     }
@@ -118,7 +119,8 @@ void apply_config(pgpu_index* h, const pgpu_params* p) {
 }
 
 int ensure_precision_data(pgpu_index* h) {
-    if (h->cfg.precision != PGPU_PRECISION_BF16) return PGPU_OK;
+    // the BF16 screen reranks original vectors; a PQ index reranks by its PQ
+    if (h->cfg.precision != PGPU_PRECISION_BF16 || h->ix.pq_nsq != 0) return PGPU_OK;
     std::string err;
     if (int rc = pgpu::ensure_bf16_features(&h->ix, &err)) return fail(rc, err);
     return PGPU_OK;

@@ -131,14 +131,17 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
     std::memcpy(&ip2cos, p, 4); p += 4;
     std::memcpy(&C, p, 4); p += 4;
     std::memcpy(&F, p, 4); p += 4;
-    (void)nsq;
     (void)ks2;
     if (index_type != 1) {
         *err = "index_type is not PUCK";
         return PGPU_E_UNSUPPORTED;
     }
-    if (whether_pq || !whether_filter || ks != 256 || ip2cos != 0) {
-        *err = "only Puck-Flat indexes (whether_pq=false, whether_filter, ks=256, ip2cos=0)";
+    if (!whether_filter || ks != 256 || ip2cos != 0 || (whether_pq && ks2 != 256)) {
+        *err = "unsupported index (needs whether_filter, ks=256, ip2cos=0)";
+        return PGPU_E_UNSUPPORTED;
+    }
+    if (whether_pq && (nsq == 0 || nsq > d || d % nsq != 0)) {
+        *err = "inconsistent PQ config (feature_dim must be a multiple of nsq)";
         return PGPU_E_UNSUPPORTED;
     }
     if (d == 0 || filter_nsq == 0 || filter_nsq > d || d % filter_nsq != 0 || C == 0 || F == 0) {
@@ -147,9 +150,13 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
     }
     const uint32_t lsq = d / filter_nsq;
     const uint64_t fl_coarse = (uint64_t)C * d, fl_fine = (uint64_t)F * d;
-    const uint64_t fl_base = (uint64_t)n * d, fl_cb = (uint64_t)filter_nsq * 256 * lsq;
-    const uint64_t floats = fl_coarse + fl_fine + fl_base + fl_cb + (uint64_t)n;
-    const uint64_t bytes = floats * 4 + (uint64_t)n * 4 + (uint64_t)n * filter_nsq + 64;
+    const uint64_t fl_base = whether_pq ? 0 : (uint64_t)n * d;
+    const uint64_t fl_cb = (uint64_t)filter_nsq * 256 * lsq;
+    const uint32_t pq_nsq = whether_pq ? nsq : 0;
+    const uint64_t fl_pq = whether_pq ? (uint64_t)pq_nsq * 256 * (d / pq_nsq) + n : 0;
+    const uint64_t floats = fl_coarse + fl_fine + fl_base + fl_cb + (uint64_t)n + fl_pq;
+    const uint64_t bytes = floats * 4 + (uint64_t)n * 4 + (uint64_t)n * filter_nsq +
+                           (uint64_t)n * pq_nsq + 64;
     try {
         storage.assign((size_t)bytes, 0);
     } catch (...) {
@@ -161,13 +168,19 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
     float* basev = fine + fl_fine;
     float* cb = basev + fl_base;
     float* offsets = cb + fl_cb;
-    uint32_t* cell_assign = reinterpret_cast<uint32_t*>(offsets + n);
+    float* pq_cb = offsets + n;                     // [pq_nsq][256][lsq_pq]
+    float* pq_off = pq_cb + (whether_pq ? (uint64_t)pq_nsq * 256 * (d / pq_nsq) : 0);
+    uint32_t* cell_assign = reinterpret_cast<uint32_t*>(pq_off + (whether_pq ? n : 0));
     uint8_t* codes = reinterpret_cast<uint8_t*>(cell_assign + n);
+    uint8_t* pq_codes = codes + (uint64_t)n * filter_nsq;
     if (!read_fvecs(base + "/coarse.dat", d, C, coarse, err)) return PGPU_E_IO;
     if (!read_fvecs(base + "/fine.dat", d, F, fine, err)) return PGPU_E_IO;
     if (!read_fvecs(base + "/filter_codebook.dat", lsq, (uint64_t)filter_nsq * 256, cb, err))
         return PGPU_E_IO;
-    if (!read_fvecs(base + "/all_data.feat.bin", d, n, basev, err)) return PGPU_E_IO;
+    if (!whether_pq && !read_fvecs(base + "/all_data.feat.bin", d, n, basev, err)) return PGPU_E_IO;
+    if (whether_pq &&
+        !read_fvecs(base + "/learn_codebooks.dat", d / pq_nsq, (uint64_t)pq_nsq * 256, pq_cb, err))
+        return PGPU_E_IO;
     // cell_assign.dat: n uint32
     const std::string ca = base + "/cell_assign.dat";
     if (!file_size(ca, &sz) || sz != 4ull * n || !read_all(ca, (char*)cell_assign, sz)) {
@@ -203,6 +216,40 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
         }
         std::fclose(f);
     }
+    if (whether_pq) {
+        // pq_data.dat: n records of [f32 offset][pq_nsq u8]
+        const std::string pd = base + "/pq_data.dat";
+        const uint64_t prb = 4ull + pq_nsq;
+        if (!file_size(pd, &sz) || sz != prb * n) {
+            *err = "file length check failed: " + pd;
+            return PGPU_E_IO;
+        }
+        std::vector<char> rec((size_t)std::min<uint64_t>(sz, 1ull << 26) + 1);
+        FILE* f = std::fopen(pd.c_str(), "rb");
+        if (!f) {
+            *err = "cannot open " + pd;
+            return PGPU_E_IO;
+        }
+        const uint64_t block = std::max<uint64_t>(1, (1ull << 26) / prb);
+        for (uint64_t r0 = 0; r0 < n; r0 += block) {
+            const uint64_t nr = std::min<uint64_t>(block, n - r0);
+            if (std::fread(rec.data(), 1, (size_t)(nr * prb), f) != nr * prb) {
+                std::fclose(f);
+                *err = "short read: " + pd;
+                return PGPU_E_IO;
+            }
+            for (uint64_t i = 0; i < nr; ++i) {
+                std::memcpy(pq_off + r0 + i, rec.data() + i * prb, 4);
+                std::memcpy(pq_codes + (r0 + i) * pq_nsq, rec.data() + i * prb + 4, pq_nsq);
+            }
+        }
+        std::fclose(f);
+    }
+    a->whether_pq = whether_pq ? 1 : 0;
+    a->pq_nsq = pq_nsq;
+    a->pq_codebook = whether_pq ? pq_cb : nullptr;
+    a->pq_offsets = whether_pq ? pq_off : nullptr;
+    a->pq_codes = whether_pq ? pq_codes : nullptr;
     a->feature_dim = d;
     a->total_point_count = n;
     a->coarse_cluster_count = C;
@@ -211,7 +258,7 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
     a->whether_norm = whether_norm ? 1 : 0;
     a->coarse = coarse;
     a->fine = fine;
-    a->base = basev;
+    a->base = whether_pq ? nullptr : basev;
     a->cell_assign = cell_assign;
     a->filter_codebook = cb;
     a->filter_offsets = offsets;
@@ -298,6 +345,33 @@ int build_host_index(const pgpu_index_arrays& a, HostIndex* h, std::string* err)
     h->coarse.assign(a.coarse, a.coarse + (uint64_t)h->C * h->d);
     h->fine.assign(a.fine, a.fine + (uint64_t)h->F * h->d);
     h->codebook.assign(a.filter_codebook, a.filter_codebook + (uint64_t)nsq * 256 * h->lsq);
+    if (a.whether_pq) {
+        const uint32_t pn = a.pq_nsq;
+        if (pn == 0 || pn > h->d || h->d % pn != 0 || pn > kMaxPqNsq || !a.pq_codebook ||
+            !a.pq_offsets || !a.pq_codes) {
+            *err = "inconsistent second-level PQ arrays";
+            return PGPU_E_INVALID;
+        }
+        h->pq_nsq = pn;
+        h->pq_lsq = h->d / pn;
+        h->pq_code_stride = (pn + 3) / 4 * 4;
+        h->pq_codebook.assign(a.pq_codebook, a.pq_codebook + (uint64_t)pn * 256 * h->pq_lsq);
+        h->pq_offsets_mem.assign(n, 0.0f);
+        h->pq_codes_mem.assign((uint64_t)n * h->pq_code_stride, 0);
+        float* po = h->pq_offsets_mem.data();
+        uint8_t* pc = h->pq_codes_mem.data();
+        const uint32_t ps = h->pq_code_stride;
+        parallel_for(n, [&](uint64_t b, uint64_t e) {
+            for (uint64_t i = b; i < e; ++i) {
+                const uint32_t l = m2l[i];
+                po[i] = a.pq_offsets[l];
+                std::memcpy(pc + i * ps, a.pq_codes + (uint64_t)l * pn, pn);
+            }
+        });
+    } else if (a.base == nullptr) {
+        *err = "base vectors are required without the second-level PQ";
+        return PGPU_E_INVALID;
+    }
     return PGPU_OK;
 }
 
@@ -307,7 +381,7 @@ void free_device_index(DeviceIndex* ix) {
                     ix->feat_abs, ix->stationary, ix->stat_sorted, ix->stat_fine, ix->rec_fine,
                     ix->cell_start,
                     ix->min_dist_offset, ix->mem2local, ix->offsets, ix->codes, ix->feat,
-                    ix->codebook};
+                    ix->codebook, ix->pq_codebook, ix->pq_offsets, ix->pq_codes};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     *ix = DeviceIndex();

@@ -111,12 +111,23 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     PGPU_TRY(dev_alloc(&ix->stat_sorted, cells, &bytes));
     PGPU_TRY(dev_alloc(&ix->stat_fine, cells, &bytes));
     PGPU_TRY(dev_alloc(&ix->min_dist_offset, h.C, &bytes));
-    PGPU_TRY(dev_alloc(&ix->feat, (uint64_t)h.n * h.d, &bytes));
+    if (base != nullptr) PGPU_TRY(dev_alloc(&ix->feat, (uint64_t)h.n * h.d, &bytes));
+    if (h.pq_nsq) {
+        ix->pq_nsq = h.pq_nsq;
+        ix->pq_lsq = h.pq_lsq;
+        ix->pq_code_stride = h.pq_code_stride;
+        PGPU_TRY(dev_copy(&ix->pq_codebook, h.pq_codebook.data(), h.pq_codebook.size(), &bytes));
+        PGPU_TRY(dev_copy(&ix->pq_offsets, h.pq_offsets_mem.data(), h.pq_offsets_mem.size(), &bytes));
+        PGPU_TRY(dev_copy(&ix->pq_codes, h.pq_codes_mem.data(), h.pq_codes_mem.size(), &bytes));
+    }
     PGPU_TRY(cudaMalloc(&fine_half, sizeof(float) * h.F));
-    PGPU_TRY(cudaMalloc(&base_dev, sizeof(float) * ((uint64_t)h.n * h.d + 1)));
-    if (h.n) PGPU_TRY(cudaMemcpy(base_dev, base, sizeof(float) * (uint64_t)h.n * h.d,
-                                 cudaMemcpyHostToDevice));
-    if (h.n) {
+    if (base != nullptr) {
+        PGPU_TRY(cudaMalloc(&base_dev, sizeof(float) * ((uint64_t)h.n * h.d + 1)));
+        if (h.n)
+            PGPU_TRY(cudaMemcpy(base_dev, base, sizeof(float) * (uint64_t)h.n * h.d,
+                                cudaMemcpyHostToDevice));
+    }
+    if (h.n && base != nullptr) {
         const uint64_t threads = (uint64_t)h.n * 32;
         k_gather_rows<<<(unsigned)((threads + 255) / 256), 256>>>(base_dev, ix->mem2local, h.n, h.d,
                                                                   ix->feat);

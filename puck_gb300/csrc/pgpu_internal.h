@@ -19,6 +19,7 @@ constexpr uint32_t kMaxClusters = 8192;   // coarse or fine count: sorted in sha
 constexpr uint32_t kMaxFilterNsq = 64;    // LUT of nsq*256 floats in shared memory
 constexpr uint32_t kMaxFilterTopk = 4096; // filter heap in shared memory
 constexpr uint32_t kMaxDim = 1024;
+constexpr uint32_t kMaxPqNsq = 192;       // PQ table of pq_nsq*256 floats in shared memory
 constexpr int kNumWalkCounters = 14;  // see the counter enum in walk_scan.cu
 // Counter slot 11: queries whose coarse top-P fell back from the tensor-core
 // window to the full exact recompute (ties at the cut, or a wide window).
@@ -79,6 +80,11 @@ struct DeviceIndex {
     uint16_t* feat_bf16 = nullptr;  // [n][d] BF16 copy (precision form; made on first use)
     float* feat_abs = nullptr;      // [n] |x| rounded up (error bound of the BF16 screen)
     float codebook_max = 0.0f;      // largest |codeword| (FP16 table scale bound)
+    // second-level PQ (whether_pq): the rerank's table and records; feat is null
+    uint32_t pq_nsq = 0, pq_lsq = 0, pq_code_stride = 0;
+    float* pq_codebook = nullptr;   // [pq_nsq][256][pq_lsq]
+    float* pq_offsets = nullptr;    // [n] memory order
+    uint8_t* pq_codes = nullptr;    // [n][pq_code_stride] memory order
     float* codebook = nullptr;      // [nsq][256][lsq]
     uint64_t bytes = 0;
 };
@@ -267,6 +273,10 @@ struct HostIndex {
     std::vector<uint8_t> codes_mem;   // memory order, code_stride bytes per row
     std::vector<float> feat_mem;      // memory order
     uint32_t code_stride = 0;
+    // second-level PQ, memory order (empty without it)
+    uint32_t pq_nsq = 0, pq_lsq = 0, pq_code_stride = 0;
+    std::vector<float> pq_codebook, pq_offsets_mem;
+    std::vector<uint8_t> pq_codes_mem;
 };
 int read_index_files(const char* dir, pgpu_index_arrays* arrays, std::vector<char>& storage,
                      std::string* err);

@@ -144,9 +144,9 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
         PGPU_STEP(launch_scan_select(ix, n, s, bf16, st), "scan_select");
     }
     mark(6);
-    if (bf16) {
+    if (bf16 && ix.pq_nsq == 0) {
         PGPU_STEP(launch_rerank_screen(ix, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
-    } else {
+    } else {  // the original vectors, or the second-level PQ
         PGPU_STEP(launch_rerank(ix, cfg, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
     }
     mark(7);

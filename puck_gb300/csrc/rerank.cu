@@ -36,6 +36,7 @@ constexpr int kRows = 8;  // candidate rows per warp in flight
 
 struct RerankParams {
     const float* q;
+    const float* qnorm;
     const int32_t* status;
     const float* hdist;
     int sort_ties;  // scan mode: replay ties in the filter's (t, memory id) order
@@ -47,6 +48,11 @@ struct RerankParams {
     uint32_t* out_ids;
     int32_t* out_status;
     uint32_t d, T, Tp, topk;
+    // second-level PQ (whether_pq)
+    const float* pq_codebook;
+    const float* pq_offsets;
+    const uint8_t* pq_codes;
+    uint32_t pq_nsq, pq_lsq, pq_code_stride;
 };
 
 // Exact-order squared L2 of G rows against q (shared memory), computed by one
@@ -114,6 +120,11 @@ __device__ __forceinline__ void warp_l2_exact(const float* const* rows, const fl
     for (int u = 0; u < G; ++u) out[u] = t[u];
 }
 
+// PQ: the second-level PQ branch of rank_topN_points (puck_index.cpp:402-427): per
+// candidate (filter distance - |q|^2) + pq offset, then + lookup_dist_table over
+// the PQ table (get_dist_table, quantization.cpp:260-270), in the reference's
+// float order; the same heap semantics as the Puck-Flat branch.
+template <bool PQ>
 __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* okey = reinterpret_cast<unsigned long long*>(smem);  // [Tp]
@@ -122,6 +133,7 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     float* sv = dist + p.T;                                   // [Tp]
     uint32_t* si = reinterpret_cast<uint32_t*>(sv + p.Tp);    // [Tp]
     uint32_t* opos = si + p.Tp;                               // [Tp]
+    float* pq_lut = reinterpret_cast<float*>(opos + p.Tp);    // [pq_nsq * 256] (PQ)
     const uint32_t qi = blockIdx.x, topk = p.topk;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float* od = p.out_dist + (uint64_t)qi * topk;
@@ -139,8 +151,23 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     __syncthreads();
+    if (PQ) {
+        for (uint32_t e = tid; e < p.pq_nsq * 256; e += kThreads)
+            pq_lut[e] = l2sqr_sse(qv + (e >> 8) * p.pq_lsq, p.pq_codebook + (uint64_t)e * p.pq_lsq,
+                                  p.pq_lsq);
+        __syncthreads();
+        const float qn = p.qnorm[qi];
+        const float* hd = p.hdist + (uint64_t)qi * p.T;
+        for (uint32_t j = tid; j < cnt; j += kThreads) {
+            const uint32_t mi = tags[j];
+            float t = __fsub_rn(hd[j], qn);
+            t = __fadd_rn(t, p.pq_offsets[mi]);
+            t = __fadd_rn(t, lut_sum(p.pq_codes + (uint64_t)mi * p.pq_code_stride, pq_lut, p.pq_nsq));
+            dist[j] = t;
+        }
+    }
     // kRows rows per warp with their loads in flight together
-    for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
+    for (uint32_t j0 = warp * kRows; !PQ && j0 < cnt; j0 += kWarps * kRows) {
         const float* rows[kRows];
 #pragma unroll
         for (int u = 0; u < kRows; ++u) {
@@ -462,7 +489,8 @@ uint32_t pow2_at_least(uint32_t v) {
 
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
     const uint32_t Tp = pow2_at_least(T > topk ? T : topk);
-    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp;
+    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp +
+           sizeof(float) * ix.pq_nsq * 256;
 }
 
 cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
@@ -470,9 +498,16 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
                           int32_t* out_status, cudaStream_t stream) {
     RerankParams p;
     p.q = s.q;
+    p.qnorm = s.qnorm;
     p.status = s.status;
     p.hdist = s.hdist;
     p.sort_ties = cfg.mode == PGPU_MODE_SCAN ? 1 : 0;
+    p.pq_codebook = ix.pq_codebook;
+    p.pq_offsets = ix.pq_offsets;
+    p.pq_codes = ix.pq_codes;
+    p.pq_nsq = ix.pq_nsq;
+    p.pq_lsq = ix.pq_lsq;
+    p.pq_code_stride = ix.pq_code_stride;
     p.htag = s.htag;
     p.hcnt = s.hcnt;
     p.feat = ix.feat;
@@ -485,12 +520,22 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
     p.Tp = pow2_at_least(s.T > topk ? s.T : topk);
     p.topk = topk;
     const size_t smem = rerank_smem_bytes(ix, s.T, topk);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr_set = true;
+    static bool attr_set[2] = {false, false};
+    if (ix.pq_nsq) {
+        if (!attr_set[1]) {
+            cudaFuncSetAttribute(k_rerank<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 220 * 1024);
+            attr_set[1] = true;
+        }
+        k_rerank<true><<<n, kThreads, smem, stream>>>(p);
+    } else {
+        if (!attr_set[0]) {
+            cudaFuncSetAttribute(k_rerank<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 220 * 1024);
+            attr_set[0] = true;
+        }
+        k_rerank<false><<<n, kThreads, smem, stream>>>(p);
     }
-    k_rerank<<<n, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 

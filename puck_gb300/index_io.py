@@ -30,6 +30,9 @@ FEATURE_FILE = "all_data.feat.bin"
 CELL_ASSIGN_FILE = "cell_assign.dat"
 FILTER_CODEBOOK_FILE = "filter_codebook.dat"
 FILTER_DATA_FILE = "filter_data.dat"
+# second-level PQ (puck/gflags/puck_gflags.cpp defaults of pq_codebook_file_name, pq_data_file_name)
+PQ_CODEBOOK_FILE = "learn_codebooks.dat"
+PQ_DATA_FILE = "pq_data.dat"
 
 _CONF_FMT = "<iI?I?II?IIIII"
 _CONF_FIELDS = ("index_type", "feature_dim", "whether_norm", "total_point_count",
@@ -109,17 +112,27 @@ def read_filter_data(path, n, filter_nsq):
 
 
 def write_index(dirpath, *, base, coarse, fine, cell_assign, filter_codebook, filter_offsets,
-                filter_codes, whether_norm):
-    """Write a complete Puck-Flat index directory in the reference's formats."""
+                filter_codes, whether_norm, pq_codebook=None, pq_offsets=None, pq_codes=None):
+    """Write a complete Puck index directory in the reference's formats: Puck-Flat,
+    or with the second-level PQ when pq_codebook/pq_offsets/pq_codes are given
+    (base, the build's input vectors, is then optional)."""
     os.makedirs(dirpath, exist_ok=True)
-    n, d = base.shape
+    d = np.asarray(coarse).shape[1]
+    n = np.asarray(cell_assign).shape[0]
     nsq = filter_codes.shape[1]
+    pq = pq_codes is not None
     write_index_conf(os.path.join(dirpath, INDEX_FILE), feature_dim=d, total_point_count=n,
                      coarse_cluster_count=coarse.shape[0], fine_cluster_count=fine.shape[0],
-                     filter_nsq=nsq, whether_norm=whether_norm)
+                     filter_nsq=nsq, whether_norm=whether_norm, whether_pq=pq,
+                     nsq=pq_codes.shape[1] if pq else None)
     write_fvecs(os.path.join(dirpath, COARSE_FILE), coarse)
     write_fvecs(os.path.join(dirpath, FINE_FILE), fine)
-    write_fvecs(os.path.join(dirpath, FEATURE_FILE), base)
+    if base is not None:
+        write_fvecs(os.path.join(dirpath, FEATURE_FILE), base)
+    if pq:
+        plsq = pq_codebook.shape[-1]
+        write_fvecs(os.path.join(dirpath, PQ_CODEBOOK_FILE), pq_codebook.reshape(-1, plsq))
+        write_filter_data(os.path.join(dirpath, PQ_DATA_FILE), pq_offsets, pq_codes)
     np.ascontiguousarray(cell_assign, np.uint32).tofile(os.path.join(dirpath, CELL_ASSIGN_FILE))
     lsq = filter_codebook.shape[-1]
     write_fvecs(os.path.join(dirpath, FILTER_CODEBOOK_FILE), filter_codebook.reshape(-1, lsq))
@@ -127,7 +140,8 @@ def write_index(dirpath, *, base, coarse, fine, cell_assign, filter_codebook, fi
 
 
 def read_index(dirpath):
-    """Read every Puck-Flat index file into numpy arrays (input/local order)."""
+    """Read every index file into numpy arrays (input/local order); with the
+    second-level PQ also pq_codebook [pq_nsq, 256, lsq], pq_offsets, pq_codes."""
     conf = read_index_conf(os.path.join(dirpath, INDEX_FILE))
     d, n = conf["feature_dim"], conf["total_point_count"]
     nsq = conf["filter_nsq"]
@@ -135,12 +149,20 @@ def read_index(dirpath):
     out = dict(conf=conf)
     out["coarse"] = read_fvecs(os.path.join(dirpath, COARSE_FILE), d)
     out["fine"] = read_fvecs(os.path.join(dirpath, FINE_FILE), d)
-    out["base"] = read_fvecs(os.path.join(dirpath, FEATURE_FILE), d)
+    fp = os.path.join(dirpath, FEATURE_FILE)
+    out["base"] = read_fvecs(fp, d) if os.path.exists(fp) or not conf["whether_pq"] else None
     out["cell_assign"] = np.fromfile(os.path.join(dirpath, CELL_ASSIGN_FILE), np.uint32)
     out["filter_codebook"] = read_fvecs(os.path.join(dirpath, FILTER_CODEBOOK_FILE),
                                         lsq).reshape(nsq, 256, lsq)
     out["filter_offsets"], out["filter_codes"] = read_filter_data(
         os.path.join(dirpath, FILTER_DATA_FILE), n, nsq)
+    if conf["whether_pq"]:
+        pn = conf["nsq"]
+        plsq = d // pn
+        out["pq_codebook"] = read_fvecs(os.path.join(dirpath, PQ_CODEBOOK_FILE),
+                                        plsq).reshape(pn, 256, plsq)
+        out["pq_offsets"], out["pq_codes"] = read_filter_data(
+            os.path.join(dirpath, PQ_DATA_FILE), n, pn)
     return out
 
 

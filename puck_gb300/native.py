@@ -88,7 +88,10 @@ class IndexArrays(ctypes.Structure):
                 ("filter_nsq", ctypes.c_uint32), ("whether_norm", ctypes.c_int32),
                 ("coarse", ctypes.c_void_p), ("fine", ctypes.c_void_p), ("base", ctypes.c_void_p),
                 ("cell_assign", ctypes.c_void_p), ("filter_codebook", ctypes.c_void_p),
-                ("filter_offsets", ctypes.c_void_p), ("filter_codes", ctypes.c_void_p)]
+                ("filter_offsets", ctypes.c_void_p), ("filter_codes", ctypes.c_void_p),
+                ("whether_pq", ctypes.c_int32), ("pq_nsq", ctypes.c_uint32),
+                ("pq_codebook", ctypes.c_void_p), ("pq_offsets", ctypes.c_void_p),
+                ("pq_codes", ctypes.c_void_p)]
 
 
 _lib = None
@@ -313,18 +316,25 @@ def _arrays_struct(arr):
     codes = np.asarray(arr["filter_codes"])
     s = IndexArrays()
     s.feature_dim = coarse.shape[1]
-    s.total_point_count = np.asarray(arr["base"]).shape[0]
+    s.total_point_count = np.asarray(arr["cell_assign"]).shape[0]
     s.coarse_cluster_count = coarse.shape[0]
     s.fine_cluster_count = np.asarray(arr["fine"]).shape[0]
     s.filter_nsq = codes.shape[1]
     s.whether_norm = int(bool(arr.get("whether_norm", False)))
     s.coarse = c("coarse", np.float32)
     s.fine = c("fine", np.float32)
-    s.base = c("base", np.float32)
+    pq = arr.get("pq_codes") is not None
+    s.base = c("base", np.float32) if not pq else None
     s.cell_assign = c("cell_assign", np.uint32)
     s.filter_codebook = c("filter_codebook", np.float32)
     s.filter_offsets = c("filter_offsets", np.float32)
     s.filter_codes = c("filter_codes", np.uint8)
+    if pq:
+        s.whether_pq = 1
+        s.pq_nsq = np.asarray(arr["pq_codes"]).shape[1]
+        s.pq_codebook = c("pq_codebook", np.float32)
+        s.pq_offsets = c("pq_offsets", np.float32)
+        s.pq_codes = c("pq_codes", np.uint8)
     return s, keep
 
 

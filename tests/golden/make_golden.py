@@ -5,8 +5,8 @@ For each small case below this script
      the benchmark workloads, at test sizes),
   2. runs the reference's own ``PuckIndex::train()`` and ``build()``
      (puck/puck/puck_index.cpp:764-874, hierarchical_cluster_index.cpp:987-1017)
-     to produce a Puck-Flat index (whether_pq=false) in the reference's file
-     formats,
+     to produce a Puck index in the reference's file formats: Puck-Flat
+     (whether_pq=false) or, for the pq_* cases, with the second-level PQ,
   3. runs the reference's batch entry point ``PySearcher::search``
      (pyapi_wrapper/py_api_wrapper.cpp:154-170) over the queries, and probes
      the per-query intermediates with the reference's own stage functions
@@ -53,6 +53,13 @@ CASES = {
     # and topk > candidates for some queries.
     "l2_small_heap": dict(n=1500, d=16, C=8, F=8, norm=False, mix="int", P=2, T=400, topk=100,
                           nq=32, dup=50),
+    # whether_pq=true (the reference's default): the rerank ranks the filter survivors
+    # by the second-level PQ (nsq = feature_dim, lsq = 1) instead of the original
+    # vectors (puck_index.cpp:402-427).
+    "pq_l2_int_d32": dict(n=6000, d=32, C=16, F=16, norm=False, mix="int", P=8, T=64, topk=10,
+                          nq=64, dup=200, pq=True),
+    "pq_cos_d24": dict(n=8000, d=24, C=24, F=24, norm=True, mix="gauss", P=12, T=100, topk=20,
+                       nq=64, dup=0, pq=True),
 }
 
 
@@ -106,7 +113,7 @@ def run_case(name):
         flag("coarse_cluster_count", case["C"])
         flag("fine_cluster_count", case["F"])
         flag("whether_norm", "true" if case["norm"] else "false")
-        flag("whether_pq", "false")
+        flag("whether_pq", "true" if case.get("pq") else "false")
         flag("kmeans_iterations_count", 2)
         flag("train_points_count", case["n"])
         flag("pq_train_points_count", case["n"])

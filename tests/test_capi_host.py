@@ -89,7 +89,9 @@ def test_index_io_roundtrip(tmp_path, golden):
     index_io.write_index(out, base=ix["base"], coarse=ix["coarse"], fine=ix["fine"],
                          cell_assign=ix["cell_assign"], filter_codebook=ix["filter_codebook"],
                          filter_offsets=ix["filter_offsets"], filter_codes=ix["filter_codes"],
-                         whether_norm=ix["conf"]["whether_norm"])
+                         whether_norm=ix["conf"]["whether_norm"],
+                         pq_codebook=ix.get("pq_codebook"), pq_offsets=ix.get("pq_offsets"),
+                         pq_codes=ix.get("pq_codes"))
     for fn in os.listdir(index_dir):
         assert open(os.path.join(index_dir, fn), "rb").read() == \
             open(os.path.join(out, fn), "rb").read(), fn

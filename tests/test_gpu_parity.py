@@ -99,17 +99,19 @@ def test_small_batches_and_chunking(golden):
     assert np.array_equal(ids, z["labels"])
 
 
-def _built_index(tmpdir, n, d, C, F, nsq, kind, seed, norm):
+def _built_index(tmpdir, n, d, C, F, nsq, kind, seed, norm, pq=False):
     import torch
     from puck_gb300 import builder
     base = builder.gmm(n, d, 256, kind, seed)
     arrays = builder.build_index(base, C, F, nsq, norm, train_sample=min(n, 65536), iters=6,
-                                 pq_sample=min(n, 32768), seed=seed)
+                                 pq_sample=min(n, 32768), seed=seed, whether_pq=pq)
     index_io.write_index(tmpdir, base=arrays["base"], coarse=arrays["coarse"],
                          fine=arrays["fine"], cell_assign=arrays["cell_assign"],
                          filter_codebook=arrays["filter_codebook"],
                          filter_offsets=arrays["filter_offsets"],
-                         filter_codes=arrays["filter_codes"], whether_norm=norm)
+                         filter_codes=arrays["filter_codes"], whether_norm=norm,
+                         pq_codebook=arrays.get("pq_codebook"),
+                         pq_offsets=arrays.get("pq_offsets"), pq_codes=arrays.get("pq_codes"))
     q = builder.gmm(256, d, 256, kind, seed, row_seed=seed + 77).cpu().numpy()
     del base
     torch.cuda.empty_cache()
@@ -117,14 +119,15 @@ def _built_index(tmpdir, n, d, C, F, nsq, kind, seed, norm):
 
 
 @pytest.mark.parametrize("mode", [native.PGPU_MODE_EXACT, native.PGPU_MODE_SCAN])
-@pytest.mark.parametrize("n,d,C,F,nsq,kind,norm,P,T,k", [
-    (60000, 64, 64, 64, 16, "int", False, 16, 200, 10),
-    (80000, 96, 96, 80, 24, "unit", True, 24, 500, 100),
-    (40000, 128, 50, 40, 32, "int", False, 50, 300, 20),
+@pytest.mark.parametrize("n,d,C,F,nsq,kind,norm,P,T,k,pq", [
+    (60000, 64, 64, 64, 16, "int", False, 16, 200, 10, False),
+    (80000, 96, 96, 80, 24, "unit", True, 24, 500, 100, False),
+    (40000, 128, 50, 40, 32, "int", False, 50, 300, 20, False),
+    (50000, 96, 64, 64, 24, "unit", True, 8, 300, 10, True),   # second-level PQ rerank
 ])
-def test_gpu_equals_oracle_builder_index(n, d, C, F, nsq, kind, norm, P, T, k, mode):
+def test_gpu_equals_oracle_builder_index(n, d, C, F, nsq, kind, norm, P, T, k, pq, mode):
     with tempfile.TemporaryDirectory() as tmp:
-        q = _built_index(tmp, n, d, C, F, nsq, kind, 11, norm)
+        q = _built_index(tmp, n, d, C, F, nsq, kind, 11, norm, pq=pq)
         ix = native.GpuIndex(tmp, search_coarse_count=P, filter_topk=T, topk=k, max_batch=100,
                              mode=mode)
         dist, ids = ix.search(q, k)
