@@ -207,7 +207,8 @@ def make_workload(w, device):
     t0 = time.time()
     arrays = builder.build_index(base, w["C"], w["F"], w["nsq"], w["norm"],
                                  train_sample=w["train_sample"], iters=w["iters"],
-                                 pq_sample=w["pq_sample"], seed=0)
+                                 pq_sample=w["pq_sample"], seed=0,
+                                 whether_pq=bool(w.get("whether_pq", False)))
     torch.cuda.synchronize()
     log(f"[bench] index built in {time.time() - t0:.1f}s")
     return base, queries, arrays
@@ -556,7 +557,8 @@ def run_gpu(args, w, rank, ws):
         "dtype": "fp32" if best["form"] == "plain" else "bf16",
         "data": "synthetic (seeded Gaussian mixture, built on the GPU in Puck's index format)",
         "config": {
-            "workload": f"{args.workload}: {w['n']} x d{w['d']} L2-normalised GMM "
+            "workload": f"{args.workload}{' + second-level PQ (whether_pq)' if w.get('whether_pq') else ''}: "
+                        f"{w['n']} x d{w['d']} L2-normalised GMM "
                         f"({w['ncomp']} comps), {nq} queries, coarse={w['C']} fine={w['F']}, "
                         f"filter PQ {w['nsq']}x256, filter_topk={w['T']}, top-{k}",
             "path": ("learned probe (adaptive clusters, confidence fallback) on the "
@@ -669,6 +671,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="cosine_10m", choices=sorted(WORKLOADS))
+    ap.add_argument("--pq", action="store_true",
+                    help="build the index with the second-level PQ (whether_pq, the "
+                         "reference's default): the rerank ranks by PQ, not the vectors")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--reference-sample", type=int, default=500)
@@ -680,7 +685,9 @@ def main():
         import torch
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.pq:
+        w["whether_pq"] = True
     try:
         if args.impl == "reference":
             run_reference(args, w, rank, ws)
