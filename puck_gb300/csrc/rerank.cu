@@ -152,18 +152,47 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     __syncthreads();
     if (PQ) {
-        for (uint32_t e = tid; e < p.pq_nsq * 256; e += kThreads)
-            pq_lut[e] = l2sqr_sse(qv + (e >> 8) * p.pq_lsq, p.pq_codebook + (uint64_t)e * p.pq_lsq,
-                                  p.pq_lsq);
-        __syncthreads();
         const float qn = p.qnorm[qi];
         const float* hd = p.hdist + (uint64_t)qi * p.T;
-        for (uint32_t j = tid; j < cnt; j += kThreads) {
-            const uint32_t mi = tags[j];
-            float t = __fsub_rn(hd[j], qn);
-            t = __fadd_rn(t, p.pq_offsets[mi]);
-            t = __fadd_rn(t, lut_sum(p.pq_codes + (uint64_t)mi * p.pq_code_stride, pq_lut, p.pq_nsq));
-            dist[j] = t;
+        if (p.pq_lsq == 1) {
+            // one-dimensional subspaces: each table entry (q_m - c)^2 is formed when
+            // it is looked up (one subtraction, one product: the same bits as the
+            // table), summed in lookup_dist_table's lane order
+            for (uint32_t j = tid; j < cnt; j += kThreads) {
+                const uint32_t mi = tags[j];
+                const uint32_t* w = reinterpret_cast<const uint32_t*>(
+                    p.pq_codes + (uint64_t)mi * p.pq_code_stride);
+                float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                for (uint32_t m0 = 0; m0 < p.pq_nsq; m0 += 4) {
+                    const uint32_t c4 = __ldg(w + (m0 >> 2));
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t m = m0 + k;
+                        if (m < p.pq_nsq) {
+                            const float y = __ldg(p.pq_codebook + (uint64_t)m * 256 + ((c4 >> (8 * k)) & 255u));
+                            const float df = __fsub_rn(qv[m], y);
+                            a[k] = __fadd_rn(a[k], __fmul_rn(df, df));
+                        }
+                    }
+                }
+                float t = __fsub_rn(hd[j], qn);
+                t = __fadd_rn(t, p.pq_offsets[mi]);
+                t = __fadd_rn(t, __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3])));
+                dist[j] = t;
+            }
+        } else {
+            for (uint32_t e = tid; e < p.pq_nsq * 256; e += kThreads)
+                pq_lut[e] = l2sqr_sse(qv + (e >> 8) * p.pq_lsq,
+                                      p.pq_codebook + (uint64_t)e * p.pq_lsq, p.pq_lsq);
+            __syncthreads();
+            for (uint32_t j = tid; j < cnt; j += kThreads) {
+                const uint32_t mi = tags[j];
+                float t = __fsub_rn(hd[j], qn);
+                t = __fadd_rn(t, p.pq_offsets[mi]);
+                t = __fadd_rn(t,
+                              lut_sum(p.pq_codes + (uint64_t)mi * p.pq_code_stride, pq_lut, p.pq_nsq));
+                dist[j] = t;
+            }
         }
     }
     // kRows rows per warp with their loads in flight together
@@ -489,8 +518,9 @@ uint32_t pow2_at_least(uint32_t v) {
 
 size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
     const uint32_t Tp = pow2_at_least(T > topk ? T : topk);
-    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp +
-           sizeof(float) * ix.pq_nsq * 256;
+    // the PQ table is only held for subspaces of more than one dimension
+    const size_t pq_table = ix.pq_lsq > 1 ? sizeof(float) * ix.pq_nsq * 256 : 0;
+    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp + pq_table;
 }
 
 cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
