@@ -134,6 +134,9 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     uint32_t* si = reinterpret_cast<uint32_t*>(sv + p.Tp);    // [Tp]
     uint32_t* opos = si + p.Tp;                               // [Tp]
     float* pq_lut = reinterpret_cast<float*>(opos + p.Tp);    // [pq_nsq * 256] (PQ)
+    __shared__ uint32_t sel_hist[256];
+    __shared__ uint32_t sel_state[2];
+    __shared__ uint32_t sel_count;
     const uint32_t qi = blockIdx.x, topk = p.topk;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float* od = p.out_dist + (uint64_t)qi * topk;
@@ -212,15 +215,38 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
         }
     }
     __syncthreads();
-    // (distance, position) pairs, ascending
-    for (uint32_t i = tid; i < p.Tp; i += kThreads) {
-        sv[i] = i < cnt ? dist[i] : __int_as_float(0x7f800000);
-        si[i] = i < cnt ? i : 0xFFFFFFFFu;
+    // (distance, position) pairs, ascending. Only the topk+1 smallest matter (result
+    // and tie check): with more candidates, keep every one at or below the
+    // (topk+1)-th smallest distance (ties included) and sort just those.
+    uint32_t m2 = p.Tp;
+    if (cnt > topk + 1) {
+        const float U = key_to_float(block_kth_key<kThreads>(dist, cnt, topk + 1, sel_hist, sel_state));
+        if (tid == 0) sel_count = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < cnt; i += kThreads)
+            if (dist[i] <= U) {
+                const uint32_t pos = atomicAdd(&sel_count, 1u);
+                sv[pos] = dist[i];
+                si[pos] = i;
+            }
+        __syncthreads();
+        const uint32_t m = sel_count;
+        m2 = 2;
+        while (m2 < m) m2 <<= 1;
+        for (uint32_t i = m + tid; i < m2; i += kThreads) {
+            sv[i] = __int_as_float(0x7f800000);
+            si[i] = 0xFFFFFFFFu;
+        }
+    } else {
+        for (uint32_t i = tid; i < p.Tp; i += kThreads) {
+            sv[i] = i < cnt ? dist[i] : __int_as_float(0x7f800000);
+            si[i] = i < cnt ? i : 0xFFFFFFFFu;
+        }
     }
     __syncthreads();
-    for (uint32_t size = 2; size <= p.Tp; size <<= 1) {
+    for (uint32_t size = 2; size <= m2; size <<= 1) {
         for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            for (uint32_t t = tid; t < p.Tp / 2; t += kThreads) {
+            for (uint32_t t = tid; t < m2 / 2; t += kThreads) {
                 const uint32_t lo = 2 * t - (t & (stride - 1));
                 const uint32_t hi = lo + stride;
                 const bool asc = (lo & size) == 0;

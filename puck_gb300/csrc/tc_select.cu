@@ -152,6 +152,8 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
 // value, 32 at a time in index order, to lane 0's MaxHeap(P).
 constexpr uint32_t kSmallP = 16;
 constexpr uint32_t kSmallCap = 64;
+// PMAX: compile-time bound on P (1, 4 or 16) for the per-lane sorted lists.
+template <uint32_t PMAX>
 __global__ __launch_bounds__(256) void k_window_small(
     const float* __restrict__ approx, uint32_t ld, const float* __restrict__ Q, uint32_t d,
     const float* __restrict__ qnorm, const float* __restrict__ cents,
@@ -189,10 +191,10 @@ __global__ __launch_bounds__(256) void k_window_small(
         const float qa = sqrtf(qnorm[row]);
         // P-th smallest (hi, id): each lane keeps its P smallest in ascending order
         // (one pass), then P rounds of warp minima over the lanes' heads
-        float tv[kSmallP];
-        uint32_t ti[kSmallP];
+        float tv[PMAX];
+        uint32_t ti[PMAX];
 #pragma unroll
-        for (uint32_t r = 0; r < kSmallP; ++r) {
+        for (uint32_t r = 0; r < PMAX; ++r) {
             tv[r] = FLT_MAX;
             ti[r] = 0xFFFFFFFFu;
         }
@@ -205,7 +207,7 @@ __global__ __launch_bounds__(256) void k_window_small(
                 float v = hi;
                 uint32_t id = j;
 #pragma unroll
-                for (uint32_t r = 0; r < kSmallP; ++r) {
+                for (uint32_t r = 0; r < PMAX; ++r) {
                     if (r < P && v < tv[r]) {
                         const float t1 = tv[r];
                         const uint32_t t2 = ti[r];
@@ -224,7 +226,7 @@ __global__ __launch_bounds__(256) void k_window_small(
             float hv = FLT_MAX;
             uint32_t hid = 0xFFFFFFFFu;
 #pragma unroll
-            for (uint32_t t = 0; t < kSmallP; ++t)
+            for (uint32_t t = 0; t < PMAX; ++t)
                 if (t == head) {
                     hv = tv[t];
                     hid = ti[t];
@@ -441,7 +443,9 @@ cudaError_t launch_coarse_tc(const DeviceIndex& ix, uint32_t n, Scratch& s, cuda
 cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
                                  cudaStream_t stream) {
     if (s.Pfix <= kSmallP) {
-        k_window_small<<<(n + 7) / 8, 256, 0, stream>>>(
+        auto kern = s.Pfix == 1 ? k_window_small<1> : s.Pfix <= 4 ? k_window_small<4>
+                                                                   : k_window_small<16>;
+        kern<<<(n + 7) / 8, 256, 0, stream>>>(
             s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse, ix.coarse_norms, ix.coarse_abs, ix.C,
             s.Pfix, s.P, n, s.cdist, s.ctag, s.status, s.tc_err, s.counters + kCounterWindowFallbacks,
             s.pconf);
