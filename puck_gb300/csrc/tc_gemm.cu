@@ -189,7 +189,7 @@ __device__ __forceinline__ float epilogue(float acc, uint32_t i, uint32_t j, con
 
 // ASYNC: both operands BF16 with 16-byte aligned rows, staged by cp.async through
 // kAsyncStages buffers so that the loads of the next chunks overlap the MMAs.
-constexpr uint32_t kAsyncStages = 3;
+constexpr uint32_t kAsyncStages = 2;
 
 template <int EPI, bool ASYNC>
 __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B, uint32_t K,
