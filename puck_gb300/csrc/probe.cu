@@ -144,6 +144,7 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     extern __shared__ float sp[];  // [C] probabilities
     __shared__ float red_v[kProbeThreads / 32];
     __shared__ uint32_t red_i[kProbeThreads / 32];
+    __shared__ float sp_top[kProbeThreads / 32];
     __shared__ float bcast;
     __shared__ uint32_t pick[64];
     __shared__ uint32_t npick;
@@ -167,28 +168,59 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     __syncthreads();
     m = bcast;
     float s = 0.0f;
+    float ev = -1.0f;  // the largest exp value, lowest id: the first cluster of the order below
+    uint32_t ei = 0xFFFFFFFFu;
     for (uint32_t c = tid; c < C; c += kProbeThreads) {
         const float e = expf(z[c] - m);
         sp[c] = e;
         s += e;
+        if (e > ev) {  // c ascends within a thread
+            ev = e;
+            ei = c;
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        const float ov = __shfl_xor_sync(0xffffffffu, ev, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, ei, o);
+        if (ov > ev || (ov == ev && oi < ei)) {
+            ev = ov;
+            ei = oi;
+        }
+    }
     __syncthreads();
-    if (lane == 0) red_v[warp] = s;
+    if (lane == 0) {
+        red_v[warp] = s;
+        red_i[warp] = ei;
+        sp_top[warp] = ev;
+    }
     __syncthreads();
     if (tid == 0) {
-        float v = 0.0f;
-        for (int w = 0; w < kProbeThreads / 32; ++w) v += red_v[w];
+        float v = 0.0f, bv = -1.0f;
+        uint32_t bi = 0xFFFFFFFFu;
+        for (int w = 0; w < kProbeThreads / 32; ++w) {
+            v += red_v[w];
+            if (sp_top[w] > bv || (sp_top[w] == bv && red_i[w] < bi)) {
+                bv = sp_top[w];
+                bi = red_i[w];
+            }
+        }
         bcast = v;
         npick = 0;
         confident = 0;
+        // one cluster already holds the mass: no ranking rounds
+        if (bv * (1.0f / v) >= mass && max_probe >= 1) {
+            pick[0] = bi;
+            npick = 1;
+            confident = 1;
+        }
     }
     __syncthreads();
     const float inv = 1.0f / bcast;
     float acc = 0.0f;
     // descending probability, ties to the lower id, until the mass is reached
-    for (uint32_t r = 0; r < max_probe; ++r) {
+    for (uint32_t r = 0; !confident && r < max_probe; ++r) {
         float bv = -1.0f;
         uint32_t bi = 0xFFFFFFFFu;
         for (uint32_t c = tid; c < C; c += kProbeThreads) {
