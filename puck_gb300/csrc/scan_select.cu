@@ -144,8 +144,11 @@ constexpr uint64_t kKeyMax = ~0ull;
 // select with 8-bit digits, stopping as soon as the chosen digit's bucket holds
 // one key (usually after the 2nd or 3rd digit of the float). `hist` has 256
 // slots, `sel` 4. All threads call it.
+// max_digits > 0 stops after that many digit passes and returns the largest key of
+// the bucket reached: then at least K keys are <= the result (a cut-back bound, not
+// the K-th itself).
 __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint32_t K,
-                                     uint32_t* hist, uint64_t* sel) {
+                                     uint32_t* hist, uint64_t* sel, int max_digits = 0) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // the leading bits every key shares need no pass: start at the digit where the
     // smallest and the largest key first differ
@@ -238,6 +241,8 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
         k = (uint32_t)sel[1];
         const bool unique = sel[2] == 1;
         __syncthreads();
+        if (!unique && max_digits > 0 && --max_digits == 0 && shift > 0)
+            return prefix | ~mask;
         if (unique && shift > 0) {
             // the one key under this prefix is the K-th
             for (uint32_t i = tid; i < count; i += kThreads)
@@ -455,12 +460,19 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
             if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
             // cut back when the buffer could not take another round
             if (st.count > kCandCap - kRound) {
-                // cut back to the T best (unordered); tau = the T-th key
+                // cut back to a bound with at least T keys below it (two digit passes;
+                // the final select below is exact); tau = that bound. If the bound's
+                // bucket kept too many to take another round, cut exactly to T.
                 const uint32_t cnt = st.count;
-                const uint64_t kth = block_select_kth(keys, cnt, T, st.hist, st.sel);
+                uint64_t kth = block_select_kth(keys, cnt, T, st.hist, st.sel, 2);
                 block_compact_le<kCandCap / kThreads>(keys, cnt, kth, &st.ccount);
+                const uint32_t kept = st.ccount;
+                if (kept > kCandCap - kRound) {
+                    kth = block_select_kth(keys, kept, T, st.hist, st.sel);
+                    block_compact_le<kCandCap / kThreads>(keys, kept, kth, &st.ccount);
+                }
                 if (tid == 0) {
-                    st.count = T;
+                    st.count = st.ccount;
                     st.tau = kth;
                     st.n_compact += 1;
                     st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
