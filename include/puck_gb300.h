@@ -37,7 +37,7 @@ extern "C" {
 #define PGPU_MODE_SCAN 1       /* every record of the probed coarse clusters is scanned (no pivot
                                   pruning); the filter_topk smallest ADC distances, each bit-identical
                                   to the reference's value for that record, go to the exact rerank.
-                                  filter_topk (+ filter_margin) <= 1024. */
+                                  filter_topk (+ filter_margin) <= 1536. */
 
 /* Arithmetic of the search (pgpu_params.precision).
  * FP32: every distance in FP32 in the reference's operation order (the coarse
@@ -169,7 +169,8 @@ int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
  * 2 fine-order chunks, 3 stationary-order enumerations, 4 coarse clusters walked in
  * fine order, 5 heap inserts, then thread-0 clock cycles: 6 replay, 7 whole walk,
  * 8 prologue (LUT), 9 candidate generation, 10 speculative ADC. Scan mode:
- * 0 records evaluated, 2 records kept, 3 buffer compactions, 5 most records of one
+ * 0 records evaluated, 1 records past the cell-distance test, 2 records kept,
+ * 3 buffer compactions, 5 most records of one
  * query, then cycles: 6 prologue, 7 whole block, 8 record rounds, 9 compactions,
  * 10 final sort. Both modes: 11 queries whose coarse top-P was recomputed in full
  * (exact ties at the cut of the tensor-core window); with a learned probe, 12

@@ -111,6 +111,8 @@ struct Scratch {
     uint16_t* ph2 = nullptr;
     int32_t* pconf = nullptr;  // [B] 1 where the probe chose the clusters (null: no probe)
     float* pz = nullptr;       // [B][C] probe scores
+    uint32_t* order = nullptr; // scan mode: [B] queries in launch order (longest scans first)
+    uint8_t* wbucket = nullptr; // scan mode: [B] work bucket of each query
     uint32_t Pfix = 0;         // fixed coarse count (<= P when a probe widens the slots)
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;

@@ -31,10 +31,25 @@
 namespace pgpu {
 namespace {
 
-constexpr int kThreads = 128;
-constexpr int kRecPerThread = 8;
+// Block shape of the scan (compile-time; -D overrides for tuning sweeps).
+#ifndef PGPU_SCAN_THREADS
+#define PGPU_SCAN_THREADS 128
+#endif
+#ifndef PGPU_SCAN_RECORDS
+#define PGPU_SCAN_RECORDS 4
+#endif
+#ifndef PGPU_SCAN_CAP
+#define PGPU_SCAN_CAP 2048
+#endif
+#ifndef PGPU_SCAN_MIN_BLOCKS
+#define PGPU_SCAN_MIN_BLOCKS 8
+#endif
+constexpr int kThreads = PGPU_SCAN_THREADS;
+constexpr int kRecPerThread = PGPU_SCAN_RECORDS;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
-constexpr uint32_t kCandCap = 2048;               // candidate buffer (keys)
+constexpr uint32_t kCandCap = PGPU_SCAN_CAP;      // candidate buffer (keys)
+static_assert(kCandCap % kThreads == 0 && kCandCap > (uint32_t)kRound,
+              "the buffer holds a round beyond the kept keys");
 
 struct ScanParams {
     const float* q;
@@ -54,6 +69,7 @@ struct ScanParams {
     const float* codebook;
     unsigned long long* counters;
     const unsigned char* luts;  // [B][lut_bytes] tables from k_build_luts
+    const uint32_t* order;      // [B] query of each block
     int* err;                   // set when the table copy did not arrive in time
     uint32_t d, C, F, nsq, lsq, code_stride, P, T, lut_bytes;
     float codebook_max;
@@ -284,10 +300,10 @@ __device__ void block_compact_le(uint64_t* keys, uint32_t count, uint64_t kth, u
 }
 
 // Diagnostic counters (pgpu_walk_counters slots, summed per launch): 0 records
-// evaluated, 2 records kept, 3 compactions, 5 max records of one query, and
+// evaluated, 1 records past the cell-distance test (table lookups), 2 records kept, 3 compactions, 5 max records of one query, and
 // thread-0 clock cycles: 6 prologue (LUT, fine terms), 7 whole block, 8 record
 // rounds, 9 compaction sorts, 10 final sort + output.
-enum { kScRecords = 0, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCycPrologue = 6,
+enum { kScRecords = 0, kScLookups = 1, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCycPrologue = 6,
        kScCycTotal = 7, kScCycRounds = 8, kScCycCompact = 9, kScCycFinal = 10 };
 
 struct ScanState {
@@ -300,16 +316,16 @@ struct ScanState {
     uint32_t c;
     float cdl;
     uint32_t r0, r1;
-    unsigned long long evaluated, passed;
+    unsigned long long evaluated, looked, passed;
     unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
 
 // NW = code words per record (code_stride / 4); HALF = FP16 table.
 template <int NW, bool HALF>
-__global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
+__global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(ScanParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ScanState st;
-    const uint32_t qi = blockIdx.x;
+    const uint32_t qi = p.order[blockIdx.x];
     const int tid = threadIdx.x;
     const uint32_t nsq = p.nsq, F = p.F, T = p.T;
     float* lut = reinterpret_cast<float*>(smem + sizeof(uint64_t) * kCandCap);
@@ -375,12 +391,13 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
         st.tau = kKeyMax;
         st.count = 0;
         st.evaluated = 0;
+        st.looked = 0;
         st.passed = 0;
         st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
     }
     __syncthreads();
     const float inv_scale = HALF ? ldexpf(1.0f, -half_lut_exponent(p.qnorm[qi], p.codebook_max)) : 1.0f;
-    unsigned long long my_eval = 0, my_pass = 0;
+    unsigned long long my_eval = 0, my_look = 0, my_pass = 0;
     __syncthreads();
     const long long t_pro = clock64();
     for (uint32_t l = 0; l < p.P; ++l) {
@@ -401,8 +418,22 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
         const float cdl = st.cdl;
         if (r0 >= r1) continue;
         // per fine id of this cluster: 2 * cell_dist, cell_dist = (cd + stationary) + fd
-        for (uint32_t i = tid; i < F; i += kThreads)
-            srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
+        if ((F & 3u) == 0) {
+            // 16-byte rows (F % 4 == 0): one float4 of each row per step
+            const float4* st4 = reinterpret_cast<const float4*>(p.stationary + (uint64_t)c * F);
+            const float4* fd4 = reinterpret_cast<const float4*>(fdk);
+            float4* s4 = reinterpret_cast<float4*>(srow);
+            for (uint32_t i = tid; i < (F >> 2); i += kThreads) {
+                const float4 a = __ldg(st4 + i), b = __ldg(fd4 + i);
+                s4[i] = make_float4(2.0f * __fadd_rn(__fadd_rn(cdl, a.x), b.x),
+                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.y), b.y),
+                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.z), b.z),
+                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.w), b.w));
+            }
+        } else {
+            for (uint32_t i = tid; i < F; i += kThreads)
+                srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
+        }
         if (!lut_ready) wait_lut();
         __syncthreads();
         if (tid == 0) st.n_records += r1 - r0;
@@ -434,6 +465,7 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
                     const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
                     ++my_eval;
                     if (filter_key(t0, mi) < tau) {  // t can only grow past t0
+                        ++my_look;
                         const float t =
                             HALF ? t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale
                                  : __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
@@ -499,11 +531,23 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
     }
     if (tid == 0) p.hcnt[qi] = out;
     if (p.counters) {
-        // records evaluated / kept (summed over the block's threads)
-        atomicAdd(p.counters + kScRecords, my_eval);
-        atomicAdd(p.counters + kScKept, my_pass);
+        // records evaluated / looked up / kept: summed over the block first, so each
+        // counter takes one global atomic per block (the counters share one sector,
+        // and atomics on it from every thread of the grid serialise in L2)
+        const unsigned we = __reduce_add_sync(0xffffffffu, (unsigned)my_eval);
+        const unsigned wl = __reduce_add_sync(0xffffffffu, (unsigned)my_look);
+        const unsigned wp = __reduce_add_sync(0xffffffffu, (unsigned)my_pass);
+        if ((tid & 31) == 0) {
+            atomicAdd(&st.evaluated, (unsigned long long)we);
+            atomicAdd(&st.looked, (unsigned long long)wl);
+            atomicAdd(&st.passed, (unsigned long long)wp);
+        }
+        __syncthreads();
         if (tid == 0) {
             const long long t_end = clock64();
+            atomicAdd(p.counters + kScRecords, st.evaluated);
+            atomicAdd(p.counters + kScLookups, st.looked);
+            atomicAdd(p.counters + kScKept, st.passed);
             atomicAdd(p.counters + kScCompactions, st.n_compact);
             atomicMax(p.counters + kScMaxRecords, st.n_records);
             atomicAdd(p.counters + kScCycPrologue, (unsigned long long)(t_pro - t_start));
@@ -513,6 +557,59 @@ __global__ __launch_bounds__(kThreads, 6) void k_scan_select(ScanParams p) {
             atomicAdd(p.counters + kScCycFinal, (unsigned long long)(t_end - t_final));
         }
     }
+}
+
+// Launch order of the scan's blocks. A block's time follows the records of the
+// clusters its query probes, and blocks start in index order: queries sorted by
+// descending record count start the longest scans first and end the grid with the
+// shortest, so fewer SMs sit idle at the tail. The sort is by bucket (4 steps per
+// octave of the count), which is all the ordering needs; the results do not depend
+// on it.
+constexpr uint32_t kOrderBuckets = 132;
+constexpr int kOrderThreads = 1024;
+
+__device__ __forceinline__ uint32_t work_bucket(uint32_t w) {
+    if (w == 0) return kOrderBuckets - 1;  // nothing to scan: last
+    const int e = 31 - __clz(w);
+    const uint32_t frac = e >= 2 ? (w >> (e - 2)) & 3u : (w << (2 - e)) & 3u;
+    return (kOrderBuckets - 2) - ((uint32_t)e * 4 + frac);  // more records: earlier
+}
+
+// One thread per query: its record count over the probed clusters, as a bucket.
+__global__ void k_scan_work(const uint32_t* __restrict__ ctag, const int32_t* __restrict__ status,
+                            const uint32_t* __restrict__ cell_start, uint32_t n, uint32_t P,
+                            uint32_t C, uint32_t F, uint8_t* __restrict__ wbucket) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    uint32_t w = 0;
+    if (status[q] == 0) {
+        for (uint32_t l = 0; l < P; ++l) {
+            const uint32_t c = ctag[(uint64_t)q * P + l];
+            if (c < C) w += cell_start[(uint64_t)c * F + F] - cell_start[(uint64_t)c * F];
+        }
+    }
+    wbucket[q] = (uint8_t)work_bucket(w);
+}
+
+// One block: counting sort of the queries by bucket (order within a bucket is free).
+__global__ __launch_bounds__(kOrderThreads) void k_scan_order(const uint8_t* __restrict__ wbucket,
+                                                              uint32_t n, uint32_t* __restrict__ order) {
+    __shared__ uint32_t hist[kOrderBuckets];
+    for (uint32_t i = threadIdx.x; i < kOrderBuckets; i += kOrderThreads) hist[i] = 0;
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < n; q += kOrderThreads) atomicAdd(&hist[wbucket[q]], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t i = 0; i < kOrderBuckets; ++i) {
+            const uint32_t c = hist[i];
+            hist[i] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < n; q += kOrderThreads)
+        order[atomicAdd(&hist[wbucket[q]], 1u)] = q;
 }
 
 }  // namespace
@@ -560,7 +657,11 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.luts = reinterpret_cast<const unsigned char*>(s.luts);
     p.lut_bytes = ix.nsq * 256 * (half_lut ? 2 : 4);
     p.err = s.tc_err;
-    if (s.luts == nullptr) return cudaErrorInvalidValue;
+    if (s.luts == nullptr || s.order == nullptr || s.wbucket == nullptr) return cudaErrorInvalidValue;
+    k_scan_work<<<(n + 255) / 256, 256, 0, stream>>>(s.ctag, s.status, ix.cell_start, n, s.P, ix.C,
+                                                     ix.F, s.wbucket);
+    k_scan_order<<<1, kOrderThreads, 0, stream>>>(s.wbucket, n, s.order);
+    p.order = s.order;
     {
         const dim3 g(n);
         if (half_lut)
