@@ -37,7 +37,7 @@ extern "C" {
 #define PGPU_MODE_SCAN 1       /* every record of the probed coarse clusters is scanned (no pivot
                                   pruning); the filter_topk smallest ADC distances, each bit-identical
                                   to the reference's value for that record, go to the exact rerank.
-                                  filter_topk (+ filter_margin) <= 1536. */
+                                  filter_topk (+ filter_margin) <= 1280. */
 
 /* Arithmetic of the search (pgpu_params.precision).
  * FP32: every distance in FP32 in the reference's operation order (the coarse

@@ -30,8 +30,22 @@
 namespace pgpu {
 namespace {
 
-constexpr int kThreads = 256;
+// Block shapes (compile-time; -D overrides for tuning sweeps). The exact FP32
+// rerank runs 256 threads per query. The screen runs 128 with eight blocks per SM,
+// so one block's select and sort overlap other blocks' row gathers.
+#ifndef PGPU_RERANK_THREADS
+#define PGPU_RERANK_THREADS 256
+#endif
+#ifndef PGPU_RERANK_SCREEN_THREADS
+#define PGPU_RERANK_SCREEN_THREADS 128
+#endif
+#ifndef PGPU_RERANK_SCREEN_MIN_BLOCKS
+#define PGPU_RERANK_SCREEN_MIN_BLOCKS 8
+#endif
+constexpr int kThreads = PGPU_RERANK_THREADS;
 constexpr int kWarps = kThreads / 32;
+constexpr int kScreenThreads = PGPU_RERANK_SCREEN_THREADS;
+constexpr int kScreenWarps = kScreenThreads / 32;
 constexpr int kRows = 8;  // candidate rows per warp in flight
 
 struct RerankParams {
@@ -153,6 +167,12 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
     const uint32_t cnt = p.hcnt[qi];
     const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    {
+        // the candidates' memory ids in shared memory (one coalesced load)
+        uint32_t* stag = reinterpret_cast<uint32_t*>(pq_lut + (p.pq_lsq > 1 ? p.pq_nsq * 256 : 0));
+        for (uint32_t i = tid; i < cnt; i += kThreads) stag[i] = tags[i];
+        tags = stag;
+    }
     __syncthreads();
     if (PQ) {
         const float qn = p.qnorm[qi];
@@ -325,7 +345,7 @@ struct ScreenParams {
     uint32_t d, T, Tp, topk;
 };
 
-__global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
+__global__ __launch_bounds__(kScreenThreads, PGPU_RERANK_SCREEN_MIN_BLOCKS) void k_rerank_screen(ScreenParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);  // [Tp]
     float* qv = reinterpret_cast<float*>(keys + p.Tp);                       // [d]
@@ -345,7 +365,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
     const int32_t stq = p.status[qi];
     if (p.out_status && tid == 0) p.out_status[qi] = stq;
     if (stq != 0) {
-        for (uint32_t i = tid; i < topk; i += kThreads) {
+        for (uint32_t i = tid; i < topk; i += kScreenThreads) {
             od[i] = sentinel_f();
             oi[i] = kNoLabel;
         }
@@ -353,7 +373,12 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
     }
     const uint32_t cnt = p.hcnt[qi];
     const uint32_t* tags = p.htag + (uint64_t)qi * p.T;
-    for (uint32_t i = tid; i < d; i += kThreads) qv[i] = p.q[(uint64_t)qi * d + i];
+    for (uint32_t i = tid; i < d; i += kScreenThreads) qv[i] = p.q[(uint64_t)qi * d + i];
+    // the candidates' memory ids in shared memory: one coalesced load, then every row
+    // gather below starts from a shared-memory read
+    uint32_t* stag = opos + p.Tp;  // [T]
+    for (uint32_t i = tid; i < cnt; i += kScreenThreads) stag[i] = tags[i];
+    tags = stag;
     if (tid == 0) wcount = 0;
     __syncthreads();
     bool full = cnt <= topk;
@@ -368,7 +393,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
             for (int t = 0; t < 8; ++t) qr[t] = active ? qv[hl * 8 + t] : 0.0f;
             // the loop runs the same iterations on both half warps (the shuffles below
             // take the full mask): a warp owns 2 * kRows rows per iteration
-            for (uint32_t jw = warp * 2 * kRows; jw < cnt; jw += kWarps * 2 * kRows) {
+            for (uint32_t jw = warp * 2 * kRows; jw < cnt; jw += kScreenWarps * 2 * kRows) {
                 const uint32_t j0 = jw + half * kRows;
                 uint4 x[kRows];
 #pragma unroll
@@ -412,7 +437,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
             }
         } else {
         // screen: kRows BF16 rows per warp in flight
-        for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
+        for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kScreenWarps * kRows) {
             float acc[kRows];
             const uint16_t* rows[kRows];
 #pragma unroll
@@ -450,13 +475,13 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
         }
         }
         __syncthreads();
-        const float U = key_to_float(block_kth_key<kThreads>(hi, cnt, topk, hist, state));
-        for (uint32_t j = tid; j < cnt; j += kThreads)
+        const float U = key_to_float(block_kth_key<kScreenThreads>(hi, cnt, topk, hist, state));
+        for (uint32_t j = tid; j < cnt; j += kScreenThreads)
             if (approx[j] - bnd[j] <= U) keys[atomicAdd(&wcount, 1u)] = j;
         __syncthreads();
         const uint32_t m = wcount;
         // exact FP32 distances of the window, in the reference's order
-        for (uint32_t i0 = warp * kRows; i0 < m; i0 += kWarps * kRows) {
+        for (uint32_t i0 = warp * kRows; i0 < m; i0 += kScreenWarps * kRows) {
             const float* rows[kRows];
 #pragma unroll
             for (int u = 0; u < kRows; ++u) {
@@ -480,16 +505,16 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
         __syncthreads();
         uint32_t mp = 2;
         while (mp < m) mp <<= 1;
-        for (uint32_t i = m + tid; i < mp; i += kThreads) keys[i] = ~0ull;
+        for (uint32_t i = m + tid; i < mp; i += kScreenThreads) keys[i] = ~0ull;
         __syncthreads();
-        bitonic_sort_u64<kThreads>(keys, mp);
+        bitonic_sort_u64<kScreenThreads>(keys, mp);
         const uint32_t check = m - 1 < topk ? m - 1 : topk;
         int tie = 0;
-        for (uint32_t i = tid; i < check; i += kThreads)
+        for (uint32_t i = tid; i < check; i += kScreenThreads)
             if ((uint32_t)(keys[i] >> 32) == (uint32_t)(keys[i + 1] >> 32)) tie = 1;
         tie = __syncthreads_or(tie);
         if (!tie) {
-            for (uint32_t i = tid; i < topk; i += kThreads) {
+            for (uint32_t i = tid; i < topk; i += kScreenThreads) {
                 od[i] = key_to_float((uint32_t)(keys[i] >> 32));
                 oi[i] = p.mem2local[tags[(uint32_t)keys[i]]];
             }
@@ -498,7 +523,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
         full = true;
     }
     // every candidate exactly, then MaxHeap(topk) in candidate order and reorder()
-    for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kWarps * kRows) {
+    for (uint32_t j0 = warp * kRows; j0 < cnt; j0 += kScreenWarps * kRows) {
         const float* rows[kRows];
 #pragma unroll
         for (int u = 0; u < kRows; ++u) {
@@ -515,7 +540,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_rerank_screen(ScreenParams p) {
     }
     __syncthreads();
     // the heap is fed in the filter's (t, memory id) order
-    order_by_filter_key<kThreads>(p.hdist + (uint64_t)qi * p.T, tags, cnt, p.Tp, keys, opos);
+    order_by_filter_key<kScreenThreads>(p.hdist + (uint64_t)qi * p.T, tags, cnt, p.Tp, keys, opos);
     if (tid == 0) {
         float* h1 = hv;  // 1-based: slots 1..topk
         for (uint32_t i = 1; i <= topk; ++i) h1[i] = sentinel_f();
@@ -546,7 +571,8 @@ size_t rerank_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
     const uint32_t Tp = pow2_at_least(T > topk ? T : topk);
     // the PQ table is only held for subspaces of more than one dimension
     const size_t pq_table = ix.pq_lsq > 1 ? sizeof(float) * ix.pq_nsq * 256 : 0;
-    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp + pq_table;
+    return sizeof(float) * (ix.d + T) + (sizeof(float) + 2 * sizeof(uint32_t) + 8) * Tp + pq_table +
+           sizeof(uint32_t) * T;
 }
 
 cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t n,
@@ -598,7 +624,7 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
 size_t rerank_screen_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk) {
     const uint32_t Tp = pow2_at_least(T);
     return sizeof(unsigned long long) * Tp + sizeof(float) * (ix.d + 3ull * T) +
-           (sizeof(float) + sizeof(uint32_t)) * (topk + 1ull) + sizeof(uint32_t) * Tp;
+           (sizeof(float) + sizeof(uint32_t)) * (topk + 1ull) + sizeof(uint32_t) * (Tp + T);
 }
 
 cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t topk, const Scratch& s,
@@ -629,7 +655,7 @@ cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t top
                              220 * 1024);
         attr_set = true;
     }
-    k_rerank_screen<<<n, kThreads, smem, stream>>>(p);
+    k_rerank_screen<<<n, kScreenThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -39,7 +39,7 @@ namespace {
 #define PGPU_SCAN_RECORDS 4
 #endif
 #ifndef PGPU_SCAN_CAP
-#define PGPU_SCAN_CAP 2048
+#define PGPU_SCAN_CAP 1792
 #endif
 #ifndef PGPU_SCAN_MIN_BLOCKS
 #define PGPU_SCAN_MIN_BLOCKS 8
