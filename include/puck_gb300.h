@@ -26,7 +26,7 @@ extern "C" {
 #define PGPU_E_INVALID (-1)     /* bad argument: topk > configured topk, null feature, ... */
 #define PGPU_E_ZERO_NORM (-2)   /* whether_norm index and a query with norm < 1e-6 */
 #define PGPU_E_IO (-3)          /* index file missing, short or inconsistent */
-#define PGPU_E_UNSUPPORTED (-4) /* index feature outside the supported set (ip2cos, ks != 256) */
+#define PGPU_E_UNSUPPORTED (-4) /* index feature outside the supported set (ip2cos = 2, ks != 256) */
 #define PGPU_E_CUDA (-5)        /* CUDA runtime error, or no usable GPU */
 #define PGPU_E_NOMEM (-6)       /* device allocation failed */
 #define PGPU_E_LIMIT (-7)       /* size beyond a documented limit of a kernel */
@@ -81,6 +81,10 @@ typedef struct {
     uint32_t lsq;
     int32_t whether_norm;
     uint64_t device_bytes; /* HBM held by the resident index */
+    /* floats per query read by the search entry points: feature_dim, or feature_dim - 1
+     * on an ip2cos = 1 index (the caller's vectors; PySearcher::init, py_api_wrapper.cpp:104-106) */
+    uint32_t query_dim;
+    int32_t ip2cos;
 } pgpu_index_info;
 
 /* Host arrays of a Puck-Flat index, in the reference's input ("local") order,
@@ -103,6 +107,10 @@ typedef struct {
     const float* pq_codebook;     /* [pq_nsq][256][feature_dim / pq_nsq] */
     const float* pq_offsets;      /* [total_point_count] */
     const uint8_t* pq_codes;      /* [total_point_count][pq_nsq] */
+    /* ip2cos = 1: the index holds feature_dim = caller dimension + 1 vectors (inner product
+     * recast as L2); each query is the caller's feature_dim - 1 values plus a 0, not
+     * normalised (hierarchical_cluster_index.cpp:1516-1520). 0: off. */
+    int32_t ip2cos;
 } pgpu_index_arrays;
 
 /* Fills the reference's flag defaults (search_coarse_count 200, topk 100,
@@ -127,7 +135,8 @@ int pgpu_open_arrays(const pgpu_index_arrays* arrays, const pgpu_params* params,
 int pgpu_set_search_params(pgpu_index* index, const pgpu_params* params);
 
 /* Replaces PySearcher::search (pyapi_wrapper/py_api_wrapper.cpp:154-170): n queries
- * of feature_dim floats, row-major, HOST memory; writes n*topk distances
+ * of query_dim floats (pgpu_index_info: feature_dim, or feature_dim - 1 on an ip2cos
+ * index), row-major, HOST memory; writes n*topk distances
  * (squared L2 in the searched space, ascending) and labels (input-order ids) per
  * query. Slots past a query's result count hold distance 0x7f7f7f7f (3.3961514e38)
  * and label 0xFFFFFFFF. status (optional, n entries) receives each query's
@@ -223,7 +232,8 @@ typedef struct {
 /* max_batch 1024, scratch budget 1 GiB, 4 slots. */
 void pgpu_server_params_default(pgpu_server_params* params);
 int pgpu_server_create(pgpu_index* index, const pgpu_server_params* params, pgpu_server** out);
-/* Queues n (1..max_batch) host queries with their own topk; returns a ticket. */
+/* Queues n (1..max_batch) host queries (query_dim floats each) with their own topk;
+ * returns a ticket. */
 int pgpu_server_submit(pgpu_server* server, uint32_t n, const float* query, uint32_t topk,
                        float* distance, uint32_t* labels, int32_t* status, uint64_t* ticket);
 /* Waits for a ticket (timeout_ms < 0: no limit); latency_us (optional) receives

@@ -68,6 +68,7 @@ def _load():
         lib.po_load.restype = ctypes.c_void_p
         lib.po_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         lib.po_free.argtypes = [ctypes.c_void_p]
+        lib.po_set_ip2cos.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.po_load_arrays_pq.restype = ctypes.c_void_p
         lib.po_load_arrays_pq.argtypes = [ctypes.c_uint32] * 5 + [ctypes.c_int] + [ctypes.c_void_p] * 7 + [
             ctypes.c_uint32] + [ctypes.c_void_p] * 3 + [ctypes.POINTER(ctypes.c_int)]
@@ -135,11 +136,15 @@ class OracleIndex:
                 a["pq_codes"].ctypes.data if pq else None, ctypes.byref(err))
         if not self._h:
             raise RuntimeError(f"oracle could not load the index (error {err.value})")
+        if index_dir is None and int(arrays.get("ip2cos", 0) or 0):
+            if lib.po_set_ip2cos(self._h, int(arrays["ip2cos"])) != 0:
+                raise RuntimeError("oracle: ip2cos must be 0 or 1")
         vals = [ctypes.c_uint32() for _ in range(6)]
         wn = ctypes.c_int()
         lib.po_info(self._h, *[ctypes.byref(v) for v in vals], ctypes.byref(wn))
         self.d, self.n, self.C, self.F, self.nsq, self.lsq = [v.value for v in vals]
         self.whether_norm = bool(wn.value)
+        self.ip2cos = bool(int(arrays.get("ip2cos", 0) or 0)) if index_dir is None else None
 
     def close(self):
         if self._h:

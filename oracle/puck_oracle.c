@@ -339,7 +339,7 @@ po_index* po_load(const char* dir, int* err) {
     float *pq_cb = NULL, *pq_off = NULL;
     uint8_t *codes = NULL, *pq_rec = NULL, *pq_codes = NULL;
     po_index* ix = NULL;
-    uint32_t d, n, C, F, nsq, pq_nsq = 0;
+    uint32_t d, n, C, F, nsq, pq_nsq = 0, ip2cos = 0;
     int whether_norm;
 
     /* index.dat: size_t length + packed config (hierarchical_cluster_index.cpp:551-567) */
@@ -363,7 +363,10 @@ po_index* po_load(const char* dir, int* err) {
         memcpy(&u, p, 4); p += 4; /* its ks */
         if (whether_pq && u != 256) { e = -4; goto done; }
         memcpy(&u, p, 4); p += 4;
-        if (u != 0) { e = -5; goto done; } /* ip2cos */
+        /* ip2cos: 1 is searchable; 2 is not (PySearcher passes feature_dim - 1 values while
+           normalization widens only for 1, py_api_wrapper.cpp:104-106) */
+        if (u > 1) { e = -5; goto done; }
+        ip2cos = u;
         memcpy(&C, p, 4); p += 4;
         memcpy(&F, p, 4); p += 4;
     }
@@ -410,6 +413,11 @@ po_index* po_load(const char* dir, int* err) {
         }
         ix = po_load_arrays_pq(d, n, C, F, nsq, whether_norm, coarse, fine, feat, cell_assign,
                                codebook, offsets, codes, pq_nsq, pq_cb, pq_off, pq_codes, &e);
+        if (ix != NULL && po_set_ip2cos(ix, (int)ip2cos) != 0) {
+            po_free(ix);
+            ix = NULL;
+            e = -5;
+        }
     }
 done:
     free(raw);
@@ -427,6 +435,12 @@ done:
     free(pq_codes);
     if (err) *err = e;
     return ix;
+}
+
+int po_set_ip2cos(po_index* ix, int ip2cos) {
+    if (ix == NULL || ip2cos < 0 || ip2cos > 1 || (ip2cos == 1 && ix->d < 2)) return -1;
+    ix->ip2cos = ip2cos;
+    return 0;
 }
 
 int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,
@@ -599,6 +613,28 @@ static uint32_t scan_cell(const po_index* ix, uint64_t cell, float cell_dist, co
     return updated;
 }
 
+/* normalization (hierarchical_cluster_index.cpp:1513-1536). ip2cos = 1: the caller's
+ * d - 1 values and a 0, not normalised (:1516-1520; the reference's memset there counts
+ * bytes, so it never clears the last float, which the transform means to be 0).
+ * Returns -2 for a zero-norm query of a whether_norm index (the reference dereferences
+ * nullptr there). */
+static int prep_query(const po_index* ix, po_scratch* s, const float* query) {
+    const uint32_t d = ix->d;
+    if (ix->ip2cos) {
+        memcpy(s->q, query, sizeof(float) * (d - 1));
+        s->q[d - 1] = 0.0f;
+        return 0;
+    }
+    memcpy(s->q, query, sizeof(float) * d);
+    if (ix->whether_norm) {
+        float norm = sqrtf(dotf(s->q, s->q, d));
+        if ((double)norm < 1e-6) return -2;
+        float alpha = (float)(1.0 / (double)norm);
+        for (uint32_t i = 0; i < d; ++i) s->q[i] = alpha * s->q[i];
+    }
+    return 0;
+}
+
 static int search_one(const po_index* ix, const po_params* p, po_scratch* s, const float* query,
                       uint32_t topk, float* dist, uint32_t* ids, uint32_t* result_num,
                       po_trace* trace) {
@@ -608,13 +644,7 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
     if (topk > p->topk || query == NULL || P == 0 || T == 0 || topk == 0) return -1;
 
     /* normalization (hierarchical_cluster_index.cpp:1513-1536) */
-    memcpy(s->q, query, sizeof(float) * d);
-    if (ix->whether_norm) {
-        float norm = sqrtf(dotf(s->q, s->q, d));
-        if ((double)norm < 1e-6) return -2; /* the reference dereferences nullptr here */
-        float alpha = (float)(1.0 / (double)norm);
-        for (uint32_t i = 0; i < d; ++i) s->q[i] = alpha * s->q[i];
-    }
+    if (prep_query(ix, s, query) != 0) return -2;
     const float* q = s->q;
 
     /* search_nearest_coarse_cluster (hierarchical_cluster_index.cpp:700-727) */
@@ -737,13 +767,7 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
     uint32_t P = p->search_coarse_count < C ? p->search_coarse_count : C;
     const uint32_t T = p->filter_topk;
     if (topk > p->topk || query == NULL || P == 0 || T == 0 || topk == 0) return -1;
-    memcpy(s->q, query, sizeof(float) * d);
-    if (ix->whether_norm) {
-        float norm = sqrtf(dotf(s->q, s->q, d));
-        if ((double)norm < 1e-6) return -2;
-        float alpha = (float)(1.0 / (double)norm);
-        for (uint32_t i = 0; i < d; ++i) s->q[i] = alpha * s->q[i];
-    }
+    if (prep_query(ix, s, query) != 0) return -2;
     const float* q = s->q;
     po_heap ch;
     heap_init(&ch, P, s->cd, s->ctag);
@@ -857,10 +881,10 @@ static void* batch_worker(void* arg) {
         if (i >= job->n) break;
         uint32_t rn = 0;
         int rc = job->scan
-                     ? search_scan_one(job->ix, job->p, &s, job->q + i * job->ix->d, job->topk,
+                     ? search_scan_one(job->ix, job->p, &s, job->q + i * (job->ix->d - (uint32_t)job->ix->ip2cos), job->topk,
                                        job->dist + i * job->topk, job->ids + i * job->topk, &rn,
                                        NULL)
-                     : search_one(job->ix, job->p, &s, job->q + i * job->ix->d, job->topk,
+                     : search_one(job->ix, job->p, &s, job->q + i * (job->ix->d - (uint32_t)job->ix->ip2cos), job->topk,
                                   job->dist + i * job->topk, job->ids + i * job->topk, &rn, NULL);
         if (job->status) job->status[i] = rc;
     }

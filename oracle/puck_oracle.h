@@ -58,6 +58,9 @@ po_index* po_load_arrays_pq(uint32_t d, uint32_t n, uint32_t C, uint32_t F, uint
                             const float* pq_offsets_local, const uint8_t* pq_codes_local,
                             int* err);
 void po_free(po_index* ix);
+/* ip2cos = 1: queries carry d - 1 values and get a 0 appended, no normalisation
+ * (hierarchical_cluster_index.cpp:1516-1520). Returns 0, or -1 for other values. */
+int po_set_ip2cos(po_index* ix, int ip2cos);
 int po_info(const po_index* ix, uint32_t* d, uint32_t* n, uint32_t* coarse, uint32_t* fine,
             uint32_t* filter_nsq, uint32_t* lsq, int* whether_norm);
 /* Memory-order arrays built at load (memory_to_local, stationary, cell starts). */

@@ -101,6 +101,26 @@ int ref_probe(void* h, const float* q, uint32_t* coarse_tag, float* coarse_dist,
                                               filter_cnt, lut);
 }
 
+// One query through the reference's Index::search(const Request*, Response*)
+// (puck/index.h:46, puck/puck/puck_index.cpp:559-600) on the probe's index and context
+// pool. On an ip2cos index PySearcher's contexts can hold a stale last query float
+// (normalization's memset counts bytes, hierarchical_cluster_index.cpp:1519); the probe's
+// contexts are only ever written through that same path, so their last float stays as
+// allocated, which the caller checks against the probe's own filter tables.
+int ref_search_one(void* h, const float* q, uint32_t topk, float* dist, uint32_t* labels,
+                   uint32_t* result_num) {
+    puck::Request req;
+    req.topk = topk;
+    req.feature = q;
+    puck::Response resp;
+    resp.distance = dist;
+    resp.local_idx = labels;
+    resp.result_num = 0;
+    const int rc = static_cast<ProbeIndex*>(h)->search(&req, &resp);
+    *result_num = resp.result_num;
+    return rc;
+}
+
 int ref_probe_sizes(void* h, uint32_t* search_coarse_count, uint32_t* filter_topk,
                     uint32_t* total_point_count) {
     auto* p = static_cast<ProbeIndex*>(h);

@@ -285,7 +285,7 @@ int pgpu_search_batch_device(pgpu_index* h, uint32_t n, const float* query, uint
     collect_stage_times(h);
     h->kernels = 0;
     for (float& v : h->stage_ms) v = 0.0f;
-    const uint32_t d = h->ix.d;
+    const uint32_t d = h->ix.qdim;  // floats per caller query
     for (uint32_t off = 0; off < n; off += h->max_batch) {
         const uint32_t m = std::min(h->max_batch, n - off);
         if (int rc = run_pass(h, m, query + (uint64_t)off * d, topk, distance + (uint64_t)off * topk,
@@ -309,7 +309,7 @@ int pgpu_search_batch(pgpu_index* h, uint32_t n, const float* query, uint32_t to
     std::lock_guard<std::mutex> g(h->mu);
     cudaSetDevice(h->device);
     if (int rc = ensure_staging(h, topk)) return rc;
-    const uint32_t d = h->ix.d;
+    const uint32_t d = h->ix.qdim;  // floats per caller query
     cudaStream_t st = h->stream;
     collect_stage_times(h);
     h->kernels = 0;
@@ -366,6 +366,8 @@ int pgpu_search(pgpu_index* h, const float* feature, uint32_t topk, float* dista
 int pgpu_index_info_get(const pgpu_index* h, pgpu_index_info* info) {
     if (h == nullptr || info == nullptr) return fail(PGPU_E_INVALID, "null argument");
     info->feature_dim = h->ix.d;
+    info->query_dim = h->ix.qdim;
+    info->ip2cos = h->ix.ip2cos;
     info->total_point_count = h->ix.n;
     info->coarse_cluster_count = h->ix.C;
     info->fine_cluster_count = h->ix.F;
@@ -460,7 +462,7 @@ int pgpu_filter_candidates(pgpu_index* h, uint32_t n, const float* query, uint32
     if (int rc = ensure_staging(h, topk)) return rc;
     cudaStream_t st = h->stream;
     const uint32_t keep = h->s.T;
-    cudaError_t e = cudaMemcpyAsync(h->d_qin, query, sizeof(float) * n * h->ix.d,
+    cudaError_t e = cudaMemcpyAsync(h->d_qin, query, sizeof(float) * n * h->ix.qdim,
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "query upload");
     if (int rc = run_pass(h, n, h->d_qin, topk, h->d_dist, h->d_ids, h->d_status, st)) return rc;

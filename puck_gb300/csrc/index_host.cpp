@@ -136,8 +136,15 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
         *err = "index_type is not PUCK";
         return PGPU_E_UNSUPPORTED;
     }
-    if (!whether_filter || ks != 256 || ip2cos != 0 || (whether_pq && ks2 != 256)) {
-        *err = "unsupported index (needs whether_filter, ks=256, ip2cos=0)";
+    // ip2cos = 2 is not searchable as the reference has it: PySearcher takes feature_dim - 1
+    // values per query (py_api_wrapper.cpp:104-106) while normalization() widens only for
+    // ip2cos = 1 (hierarchical_cluster_index.cpp:1516), so the search reads past the query
+    if (!whether_filter || ks != 256 || ip2cos > 1 || (whether_pq && ks2 != 256)) {
+        *err = "unsupported index (needs whether_filter, ks=256, ip2cos 0 or 1)";
+        return PGPU_E_UNSUPPORTED;
+    }
+    if (ip2cos == 1 && d < 2) {
+        *err = "ip2cos index needs feature_dim >= 2";
         return PGPU_E_UNSUPPORTED;
     }
     if (whether_pq && (nsq == 0 || nsq > d || d % nsq != 0)) {
@@ -256,6 +263,7 @@ int read_index_files(const char* dir, pgpu_index_arrays* a, std::vector<char>& s
     a->fine_cluster_count = F;
     a->filter_nsq = filter_nsq;
     a->whether_norm = whether_norm ? 1 : 0;
+    a->ip2cos = (int32_t)ip2cos;
     a->coarse = coarse;
     a->fine = fine;
     a->base = whether_pq ? nullptr : basev;
@@ -277,6 +285,11 @@ int build_host_index(const pgpu_index_arrays& a, HostIndex* h, std::string* err)
     h->F = a.fine_cluster_count;
     h->nsq = a.filter_nsq;
     h->whether_norm = a.whether_norm;
+    h->ip2cos = a.ip2cos;
+    if (a.ip2cos < 0 || a.ip2cos > 1 || (a.ip2cos == 1 && h->d < 2)) {
+        *err = "ip2cos must be 0 or 1 (1 needs feature_dim >= 2)";
+        return PGPU_E_UNSUPPORTED;
+    }
     if (h->d == 0 || h->nsq == 0 || h->d % h->nsq != 0 || h->C == 0 || h->F == 0) {
         *err = "inconsistent index shape (feature_dim must be a multiple of filter_nsq)";
         return PGPU_E_UNSUPPORTED;

@@ -74,6 +74,8 @@ int upload_index_with_base(const HostIndex& h, const float* base, DeviceIndex* i
     ix->nsq = h.nsq;
     ix->lsq = h.lsq;
     ix->whether_norm = h.whether_norm;
+    ix->ip2cos = h.ip2cos;
+    ix->qdim = h.d - (uint32_t)h.ip2cos;
     ix->code_stride = h.code_stride;
     {
         // largest codeword norm: bounds every lookup-table entry (precision form)

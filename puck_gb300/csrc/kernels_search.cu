@@ -26,21 +26,28 @@ namespace {
 
 // ---------------------------------------------------------------- kernels
 
+// q_in rows hold qdim floats: d, or d - 1 on an ip2cos index.
 __global__ void k_prep_queries(const float* __restrict__ q_in, float* __restrict__ q_out,
                                uint16_t* __restrict__ q_bf16, float* __restrict__ qnorm,
                                int32_t* __restrict__ status, uint32_t n, uint32_t d,
-                               int whether_norm) {
+                               uint32_t qdim, int whether_norm, int ip2cos) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float* x = q_in + (uint64_t)i * d;
+    const float* x = q_in + (uint64_t)i * qdim;
     float* y = q_out + (uint64_t)i * d;
     int32_t st = 0;
     // Non-finite input has no defined result in the reference; it is rejected so
     // that no NaN reaches the sorts and the walk.
-    for (uint32_t k = 0; k < d; ++k)
+    for (uint32_t k = 0; k < qdim; ++k)
         if (!isfinite(x[k])) st = PGPU_E_INVALID;
     if (st != 0) {
         for (uint32_t k = 0; k < d; ++k) y[k] = 0.0f;
+    } else if (ip2cos) {
+        // the caller's d - 1 values and a 0, not normalised (hierarchical_cluster_index.cpp:
+        // 1516-1520; the reference's memset there counts bytes and leaves the last float
+        // as it was, the transform means it to be 0)
+        for (uint32_t k = 0; k < qdim; ++k) y[k] = x[k];
+        for (uint32_t k = qdim; k < d; ++k) y[k] = 0.0f;
     } else if (whether_norm) {
         // cblas_snrm2 then cblas_sscal(1.0 / norm) (hierarchical_cluster_index.cpp:1524-1531)
         const float norm = __fsqrt_rn(dot_seq(x, x, d));
@@ -435,7 +442,7 @@ __global__ void k_norms_full(const float* __restrict__ X, uint64_t rows, uint32_
 cudaError_t launch_prep_queries(const DeviceIndex& ix, const float* q_in, uint32_t n, Scratch& s,
                                 cudaStream_t stream) {
     k_prep_queries<<<(n + 127) / 128, 128, 0, stream>>>(q_in, s.q, s.qb, s.qnorm, s.status, n,
-                                                       ix.d, ix.whether_norm);
+                                                       ix.d, ix.qdim, ix.whether_norm, ix.ip2cos);
     return cudaGetLastError();
 }
 

@@ -60,6 +60,8 @@ struct ProbeWork {
 struct DeviceIndex {
     uint32_t d = 0, n = 0, C = 0, F = 0, nsq = 0, lsq = 0;
     int whether_norm = 0;
+    int ip2cos = 0;     // 1: the caller's queries have qdim = d - 1 values, a 0 is appended
+    uint32_t qdim = 0;  // floats per caller query
     uint32_t code_stride = 0;     // bytes per code row (nsq rounded up to 4)
     float* coarse = nullptr;      // [C][d]
     float* fine = nullptr;        // [F][d]
@@ -268,6 +270,7 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
 struct HostIndex {
     uint32_t d = 0, n = 0, C = 0, F = 0, nsq = 0, lsq = 0;
     int whether_norm = 0;
+    int ip2cos = 0;  // 1: queries carry d - 1 values and get a 0 appended
     std::vector<float> coarse, fine, codebook;
     std::vector<uint32_t> cell_start, mem2local;
     std::vector<uint16_t> rec_fine;   // memory order

@@ -454,6 +454,21 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
 #pragma unroll
                 for (int i = 0; i < NW; ++i) words[j][i] = __ldg(cw + i);
             }
+            // one shared atomic per warp for the kept records
+            auto insert = [&](bool keep, uint64_t key) {
+                const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+                if (ballot) {
+                    const int lane = tid & 31;
+                    uint32_t base_slot = 0;
+                    if (lane == __ffs(ballot) - 1) base_slot = atomicAdd(&st.count, (uint32_t)__popc(ballot));
+                    base_slot = __shfl_sync(0xffffffffu, base_slot, __ffs(ballot) - 1);
+                    if (keep) {
+                        // capacity is kept >= count + kRound by the compaction below
+                        keys[base_slot + __popc(ballot & ((1u << lane) - 1))] = key;
+                        ++my_pass;
+                    }
+                }
+            };
 #pragma unroll
             for (int j = 0; j < kRecPerThread; ++j) {
                 const uint32_t mi = base + tid + j * kThreads;
@@ -473,19 +488,7 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
                         keep = key < tau;
                     }
                 }
-                // one shared atomic per warp for the kept records
-                const unsigned ballot = __ballot_sync(0xffffffffu, keep);
-                if (ballot) {
-                    const int lane = tid & 31;
-                    uint32_t base_slot = 0;
-                    if (lane == __ffs(ballot) - 1) base_slot = atomicAdd(&st.count, (uint32_t)__popc(ballot));
-                    base_slot = __shfl_sync(0xffffffffu, base_slot, __ffs(ballot) - 1);
-                    if (keep) {
-                        // capacity is kept >= count + kRound by the compaction below
-                        keys[base_slot + __popc(ballot & ((1u << lane) - 1))] = key;
-                        ++my_pass;
-                    }
-                }
+                insert(keep, key);
             }
             __syncthreads();
             const long long t_round_end = clock64();

@@ -329,7 +329,7 @@ int pgpu_server_create(pgpu_index* index, const pgpu_server_params* params, pgpu
     sv->device = pgpu::index_device_ordinal(index);
     sv->cap = p.max_batch;
     sv->topk_max = cfg.topk_max;
-    sv->d = ix.d;
+    sv->d = ix.qdim;  // floats per caller query
     for (uint32_t b = 32; b < sv->cap; b <<= 1) sv->buckets.push_back(b);
     sv->buckets.push_back(sv->cap);
     const uint64_t per_slot = pgpu::scratch_bytes(ix, cfg, sv->cap) +

@@ -112,10 +112,12 @@ def read_filter_data(path, n, filter_nsq):
 
 
 def write_index(dirpath, *, base, coarse, fine, cell_assign, filter_codebook, filter_offsets,
-                filter_codes, whether_norm, pq_codebook=None, pq_offsets=None, pq_codes=None):
+                filter_codes, whether_norm, pq_codebook=None, pq_offsets=None, pq_codes=None,
+                ip2cos=0):
     """Write a complete Puck index directory in the reference's formats: Puck-Flat,
     or with the second-level PQ when pq_codebook/pq_offsets/pq_codes are given
-    (base, the build's input vectors, is then optional)."""
+    (base, the build's input vectors, is then optional). ip2cos=1 marks vectors that
+    carry one dimension more than the caller's queries."""
     os.makedirs(dirpath, exist_ok=True)
     d = np.asarray(coarse).shape[1]
     n = np.asarray(cell_assign).shape[0]
@@ -124,7 +126,7 @@ def write_index(dirpath, *, base, coarse, fine, cell_assign, filter_codebook, fi
     write_index_conf(os.path.join(dirpath, INDEX_FILE), feature_dim=d, total_point_count=n,
                      coarse_cluster_count=coarse.shape[0], fine_cluster_count=fine.shape[0],
                      filter_nsq=nsq, whether_norm=whether_norm, whether_pq=pq,
-                     nsq=pq_codes.shape[1] if pq else None)
+                     nsq=pq_codes.shape[1] if pq else None, ip2cos=ip2cos)
     write_fvecs(os.path.join(dirpath, COARSE_FILE), coarse)
     write_fvecs(os.path.join(dirpath, FINE_FILE), fine)
     if base is not None:
@@ -146,7 +148,7 @@ def read_index(dirpath):
     d, n = conf["feature_dim"], conf["total_point_count"]
     nsq = conf["filter_nsq"]
     lsq = -(-d // nsq)
-    out = dict(conf=conf)
+    out = dict(conf=conf, whether_norm=bool(conf["whether_norm"]), ip2cos=conf["ip2cos"])
     out["coarse"] = read_fvecs(os.path.join(dirpath, COARSE_FILE), d)
     out["fine"] = read_fvecs(os.path.join(dirpath, FINE_FILE), d)
     fp = os.path.join(dirpath, FEATURE_FILE)

@@ -66,7 +66,8 @@ class IndexInfo(ctypes.Structure):
     _fields_ = [("feature_dim", ctypes.c_uint32), ("total_point_count", ctypes.c_uint32),
                 ("coarse_cluster_count", ctypes.c_uint32), ("fine_cluster_count", ctypes.c_uint32),
                 ("filter_nsq", ctypes.c_uint32), ("lsq", ctypes.c_uint32),
-                ("whether_norm", ctypes.c_int32), ("device_bytes", ctypes.c_uint64)]
+                ("whether_norm", ctypes.c_int32), ("device_bytes", ctypes.c_uint64),
+                ("query_dim", ctypes.c_uint32), ("ip2cos", ctypes.c_int32)]
 
 
 class ServerParams(ctypes.Structure):
@@ -91,7 +92,7 @@ class IndexArrays(ctypes.Structure):
                 ("filter_offsets", ctypes.c_void_p), ("filter_codes", ctypes.c_void_p),
                 ("whether_pq", ctypes.c_int32), ("pq_nsq", ctypes.c_uint32),
                 ("pq_codebook", ctypes.c_void_p), ("pq_offsets", ctypes.c_void_p),
-                ("pq_codes", ctypes.c_void_p)]
+                ("pq_codes", ctypes.c_void_p), ("ip2cos", ctypes.c_int32)]
 
 
 _lib = None
@@ -211,7 +212,8 @@ class GpuIndex:
         info = IndexInfo()
         check(lib.pgpu_index_info_get(self._h, ctypes.byref(info)))
         self.info = info
-        self.d = info.feature_dim
+        self.d = info.query_dim  # floats per query (feature_dim - 1 on an ip2cos index)
+        self.feature_dim = info.feature_dim
 
     def set_probe(self, probe, mass=0.9, max_probe=8):
         """Attach a learned Probe (None detaches); scan mode only."""
@@ -321,6 +323,7 @@ def _arrays_struct(arr):
     s.fine_cluster_count = np.asarray(arr["fine"]).shape[0]
     s.filter_nsq = codes.shape[1]
     s.whether_norm = int(bool(arr.get("whether_norm", False)))
+    s.ip2cos = int(arr.get("ip2cos", 0) or 0)
     s.coarse = c("coarse", np.float32)
     s.fine = c("fine", np.float32)
     pq = arr.get("pq_codes") is not None

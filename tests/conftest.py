@@ -10,7 +10,8 @@ if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
 GOLDEN_DIR = os.path.join(REPO, "tests", "golden")
-GOLDEN_CASES = ["l2_int_d32", "cos_d24", "l2_d30_lsq5", "l2_small_heap", "pq_l2_int_d32", "pq_cos_d24"]
+GOLDEN_CASES = ["l2_int_d32", "cos_d24", "l2_d30_lsq5", "l2_small_heap", "pq_l2_int_d32", "pq_cos_d24",
+                "ip2cos_d23"]
 
 
 def pytest_configure(config):

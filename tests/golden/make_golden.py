@@ -10,7 +10,9 @@ For each small case below this script
   3. runs the reference's batch entry point ``PySearcher::search``
      (pyapi_wrapper/py_api_wrapper.cpp:154-170) over the queries, and probes
      the per-query intermediates with the reference's own stage functions
-     (coarse list, filter heap, LUT),
+     (coarse list, filter heap, LUT); for ip2cos cases the final results come
+     from the reference's ``Index::search`` (puck_index.cpp:559-600) on the
+     probe's contexts (see run_case),
   4. stores index files + queries + outputs in ``<case>.npz``.
 
 The reference is the copy compiled from its sources by oracle/ref/Makefile
@@ -60,6 +62,12 @@ CASES = {
                           nq=64, dup=200, pq=True),
     "pq_cos_d24": dict(n=8000, d=24, C=24, F=24, norm=True, mix="gauss", P=12, T=100, topk=20,
                        nq=64, dup=0, pq=True),
+    # ip2cos=1: inner-product data recast as L2. The base file holds d+1 dims,
+    # [x, sqrt(M^2 - |x|^2)] with M the largest |x|; the reference raises feature_dim to
+    # d+1 (index_conf.cpp:34-36) and widens each d-dim query with a 0 (hierarchical_
+    # cluster_index.cpp:1516-1520). filter_nsq = 6 (its ip2cos rule, index_conf.cpp:132-141).
+    "ip2cos_d23": dict(n=6000, d=23, C=16, F=16, norm=False, mix="raw", P=8, T=64, topk=10,
+                       nq=64, dup=0, ip2cos=True),
 }
 
 
@@ -78,7 +86,8 @@ def make_data(case, seed=0):
         def draw(m):
             comp = rng.integers(0, ncomp, size=m)
             x = (centers[comp] + rng.normal(0, 0.3, size=(m, d))).astype(np.float32)
-            x /= np.linalg.norm(x, axis=1, keepdims=True)
+            if case["mix"] != "raw":
+                x /= np.linalg.norm(x, axis=1, keepdims=True)
             return x.astype(np.float32)
     base = draw(n)
     if case["dup"]:
@@ -86,6 +95,10 @@ def make_data(case, seed=0):
         dst = rng.integers(0, n, size=case["dup"])
         base[dst] = base[src]
     queries = draw(case["nq"])
+    if case.get("ip2cos"):
+        sq = (base.astype(np.float64) ** 2).sum(1)
+        extra = np.sqrt(np.maximum(sq.max() - sq, 0.0)).astype(np.float32)
+        base = np.concatenate([base, extra[:, None]], axis=1)
     return base, queries
 
 
@@ -100,6 +113,7 @@ def run_case(name):
                                ctypes.c_void_p, ctypes.c_void_p]
     lib.ref_probe.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
     lib.ref_memory_to_local.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.ref_search_one.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_uint32] + [ctypes.c_void_p] * 3
 
     def flag(k, v):
         assert lib.ref_set_flag(k.encode(), str(v).encode()) == 0, k
@@ -114,6 +128,7 @@ def run_case(name):
         flag("fine_cluster_count", case["F"])
         flag("whether_norm", "true" if case["norm"] else "false")
         flag("whether_pq", "true" if case.get("pq") else "false")
+        flag("ip2cos", 1 if case.get("ip2cos") else 0)
         flag("kmeans_iterations_count", 2)
         flag("train_points_count", case["n"])
         flag("pq_train_points_count", case["n"])
@@ -154,6 +169,15 @@ def run_case(name):
             assert rc == 0, rc
         m2l = np.zeros(case["n"], np.uint32)
         lib.ref_memory_to_local(probe, m2l.ctypes.data)
+        if case.get("ip2cos"):
+            # PySearcher's contexts can carry a stale last query float on an ip2cos index
+            # (normalization's memset counts bytes); the final results come from the
+            # reference's Index::search on the probe's contexts instead, whose filter
+            # tables above were computed with that float at 0.
+            rn = ctypes.c_uint32(0)
+            for i in range(nq):
+                assert lib.ref_search_one(probe, q[i].ctypes.data, k, dist[i].ctypes.data,
+                                          labels[i].ctypes.data, ctypes.byref(rn)) == 0
 
         files = {}
         for fn in sorted(os.listdir(idx)):

@@ -93,7 +93,7 @@ def test_index_io_roundtrip(tmp_path, golden):
                          filter_offsets=ix["filter_offsets"], filter_codes=ix["filter_codes"],
                          whether_norm=ix["conf"]["whether_norm"],
                          pq_codebook=ix.get("pq_codebook"), pq_offsets=ix.get("pq_offsets"),
-                         pq_codes=ix.get("pq_codes"))
+                         pq_codes=ix.get("pq_codes"), ip2cos=ix["ip2cos"])
     for fn in os.listdir(index_dir):
         assert open(os.path.join(index_dir, fn), "rb").read() == \
             open(os.path.join(out, fn), "rb").read(), fn

@@ -188,3 +188,53 @@ def test_nearest_center_matches_oracle():
     torch.cuda.synchronize()
     assert np.array_equal(a.cpu().numpy(), oa)
     assert np.array_equal(_bits(dd.cpu().numpy()), _bits(od))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [native.PGPU_MODE_EXACT, native.PGPU_MODE_SCAN])
+def test_ip2cos_index_equals_oracle(mode):
+    """ip2cos = 1 (inner product recast as L2): the index holds [x, sqrt(M^2 - |x|^2)]
+    rows of d + 1 values; callers pass d-value queries, which get a 0 appended and no
+    normalisation (hierarchical_cluster_index.cpp:1516-1520). Host batch, single-query,
+    device-buffer and serving entry points all read d floats per query."""
+    import torch
+    from puck_gb300 import builder
+    D = 47
+    x = builder.gmm(40000, D, 256, "int", 21).float() / 64.0
+    sq = (x.double() ** 2).sum(1)
+    extra = torch.sqrt(torch.clamp(sq.max() - sq, min=0.0)).float()
+    base = torch.cat([x, extra[:, None]], dim=1).contiguous()
+    arrays = builder.build_index(base, 48, 40, 12, False, train_sample=40000, iters=6,
+                                 pq_sample=32768, seed=21)
+    arrays["ip2cos"] = 1
+    q = (builder.gmm(200, D, 256, "int", 21, row_seed=99).float() / 64.0).cpu().numpy()
+    del x, base
+    torch.cuda.empty_cache()
+    P, T, k = 12, 300, 10
+    ix = native.GpuIndex(arrays=arrays, search_coarse_count=P, filter_topk=T, topk=k,
+                         max_batch=64, mode=mode)
+    assert ix.info.feature_dim == D + 1 and ix.info.query_dim == D and ix.info.ip2cos == 1
+    dist, ids, status = ix.search(q, k, return_status=True)
+    orc = oracle.OracleIndex(arrays=arrays)
+    od, oi, st = orc.search_batch(q, k, P, T, topk_max=k, nthreads=os.cpu_count(),
+                                  scan=(mode == native.PGPU_MODE_SCAN))
+    assert (status == 0).all() and (st == 0).all()
+    assert np.array_equal(_bits(dist), _bits(od))
+    assert np.array_equal(ids, oi)
+    d1, i1, rn = ix.search_one(q[5], k)
+    assert rn == k and np.array_equal(_bits(d1), _bits(dist[5])) and np.array_equal(i1, ids[5])
+    qd = torch.from_numpy(q).cuda()
+    dd = torch.empty((q.shape[0], k), dtype=torch.float32, device="cuda")
+    di = torch.empty((q.shape[0], k), dtype=torch.int32, device="cuda")
+    ix.search_device(q.shape[0], qd, k, dd, di)
+    torch.cuda.synchronize()
+    assert np.array_equal(_bits(dd.cpu().numpy()), _bits(dist))
+    assert np.array_equal(di.cpu().numpy().view(np.uint32), ids)
+    srv = native.Server(ix, max_batch=64, scratch_budget_bytes=64 << 20, max_slots=2)
+    try:
+        t = srv.submit(q[:37], k)
+        sd, si, sst, _ = srv.wait(t, timeout_ms=60000)
+    finally:
+        srv.close()
+    assert (sst == 0).all()
+    assert np.array_equal(_bits(sd), _bits(dist[:37])) and np.array_equal(si, ids[:37])
