@@ -26,46 +26,64 @@ namespace {
 
 // ---------------------------------------------------------------- kernels
 
+// One warp per query (kPrepWarps per block): the row is read coalesced into shared
+// memory; the two sums that fix the result bits (the norm, |q|^2) run sequentially in
+// lane 0 in the reference's order, every other pass is spread over the lanes.
 // q_in rows hold qdim floats: d, or d - 1 on an ip2cos index.
-__global__ void k_prep_queries(const float* __restrict__ q_in, float* __restrict__ q_out,
-                               uint16_t* __restrict__ q_bf16, float* __restrict__ qnorm,
-                               int32_t* __restrict__ status, uint32_t n, uint32_t d,
-                               uint32_t qdim, int whether_norm, int ip2cos) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+constexpr int kPrepWarps = 8;
+__global__ __launch_bounds__(kPrepWarps * 32) void k_prep_queries(
+    const float* __restrict__ q_in, float* __restrict__ q_out, uint16_t* __restrict__ q_bf16,
+    float* __restrict__ qnorm, int32_t* __restrict__ status, uint32_t n, uint32_t d,
+    uint32_t qdim, int whether_norm, int ip2cos) {
+    extern __shared__ float prep_rows[];  // [kPrepWarps][d]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t i = blockIdx.x * kPrepWarps + warp;
+    if (i >= n) return;  // whole warps only; no block barrier follows
+    float* y = prep_rows + (uint64_t)warp * d;
     const float* x = q_in + (uint64_t)i * qdim;
-    float* y = q_out + (uint64_t)i * d;
-    int32_t st = 0;
     // Non-finite input has no defined result in the reference; it is rejected so
     // that no NaN reaches the sorts and the walk.
-    for (uint32_t k = 0; k < qdim; ++k)
-        if (!isfinite(x[k])) st = PGPU_E_INVALID;
-    if (st != 0) {
-        for (uint32_t k = 0; k < d; ++k) y[k] = 0.0f;
-    } else if (ip2cos) {
-        // the caller's d - 1 values and a 0, not normalised (hierarchical_cluster_index.cpp:
-        // 1516-1520; the reference's memset there counts bytes and leaves the last float
-        // as it was, the transform means it to be 0)
-        for (uint32_t k = 0; k < qdim; ++k) y[k] = x[k];
-        for (uint32_t k = qdim; k < d; ++k) y[k] = 0.0f;
-    } else if (whether_norm) {
+    int bad = 0;
+    for (uint32_t k = lane; k < qdim; k += 32) {
+        const float v = x[k];
+        bad |= !isfinite(v);
+        y[k] = v;
+    }
+    // ip2cos: the caller's d - 1 values and a 0, not normalised (hierarchical_cluster_index.cpp:
+    // 1516-1520; the reference's memset there counts bytes and leaves the last float as it
+    // was, the transform means it to be 0)
+    for (uint32_t k = qdim + lane; k < d; k += 32) y[k] = 0.0f;
+    int32_t st = __any_sync(0xffffffffu, bad) ? PGPU_E_INVALID : 0;
+    __syncwarp();
+    bool scale = false;
+    float alpha = 1.0f;
+    if (st == 0 && whether_norm && !ip2cos) {
         // cblas_snrm2 then cblas_sscal(1.0 / norm) (hierarchical_cluster_index.cpp:1524-1531)
-        const float norm = __fsqrt_rn(dot_seq(x, x, d));
+        float s = 0.0f;
+        if (lane == 0) s = dot_seq(y, y, d);
+        const float norm = __fsqrt_rn(__shfl_sync(0xffffffffu, s, 0));
         if ((double)norm < 1e-6) {
             st = PGPU_E_ZERO_NORM;
-            for (uint32_t k = 0; k < d; ++k) y[k] = 0.0f;
         } else {
-            const float alpha = __double2float_rn(1.0 / (double)norm);
-            for (uint32_t k = 0; k < d; ++k) y[k] = __fmul_rn(alpha, x[k]);
+            alpha = __double2float_rn(1.0 / (double)norm);
+            scale = true;
         }
-    } else {
-        for (uint32_t k = 0; k < d; ++k) y[k] = x[k];
     }
-    qnorm[i] = dot_seq(y, y, d);
-    if (st == 0 && !isfinite(qnorm[i])) st = PGPU_E_INVALID;
+    float* yo = q_out + (uint64_t)i * d;
     uint16_t* yb = q_bf16 + (uint64_t)i * d;
-    for (uint32_t k = 0; k < d; ++k) yb[k] = __bfloat16_as_ushort(__float2bfloat16_rn(y[k]));
-    status[i] = st;
+    for (uint32_t k = lane; k < d; k += 32) {
+        const float v = st != 0 ? 0.0f : (scale ? __fmul_rn(alpha, y[k]) : y[k]);
+        y[k] = v;
+        yo[k] = v;
+        yb[k] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const float qn = dot_seq(y, y, d);
+        qnorm[i] = qn;
+        if (st == 0 && !isfinite(qn)) st = PGPU_E_INVALID;
+        status[i] = st;
+    }
 }
 
 // out[i][j] = bias[j] - a_i.b_j (MODE 0), -(a_i.b_j) (MODE 1), bias[j] + a_i.b_j (MODE 2).
@@ -441,8 +459,9 @@ __global__ void k_norms_full(const float* __restrict__ X, uint64_t rows, uint32_
 
 cudaError_t launch_prep_queries(const DeviceIndex& ix, const float* q_in, uint32_t n, Scratch& s,
                                 cudaStream_t stream) {
-    k_prep_queries<<<(n + 127) / 128, 128, 0, stream>>>(q_in, s.q, s.qb, s.qnorm, s.status, n,
-                                                       ix.d, ix.qdim, ix.whether_norm, ix.ip2cos);
+    const size_t smem = sizeof(float) * kPrepWarps * ix.d;  // <= 32 KB (d <= kMaxDim)
+    k_prep_queries<<<(n + kPrepWarps - 1) / kPrepWarps, kPrepWarps * 32, smem, stream>>>(
+        q_in, s.q, s.qb, s.qnorm, s.status, n, ix.d, ix.qdim, ix.whether_norm, ix.ip2cos);
     return cudaGetLastError();
 }
 

@@ -84,24 +84,35 @@ __device__ __forceinline__ int half_lut_exponent(float qnorm, float codebook_max
     return e < -60 ? -60 : (e > 60 ? 60 : e);
 }
 
-// get_dist_table (quantization.cpp:260-270) for a batch: one block per query,
-// thread j computes codeword j of every subspace (coalesced 16-byte codebook
-// loads, 8 subspaces in flight), in the reference's lane order (l2sqr_sse).
+// get_dist_table (quantization.cpp:260-270) for a batch: kLutQueries queries per
+// block, thread j computes codeword j of every subspace for each of them (coalesced
+// 16-byte codebook loads, 8 subspaces in flight, each codeword loaded once for the
+// block's queries), in the reference's lane order (l2sqr_sse).
+constexpr uint32_t kLutQueries = 8;
 template <bool HALF>
 __global__ __launch_bounds__(256) void k_build_luts(const float* __restrict__ q,
                                                     const float* __restrict__ qnorm,
                                                     const int32_t* __restrict__ status,
-                                                    const float* __restrict__ cb, uint32_t d,
-                                                    uint32_t nsq, uint32_t lsq, float codebook_max,
+                                                    const float* __restrict__ cb, uint32_t n,
+                                                    uint32_t d, uint32_t nsq, uint32_t lsq,
+                                                    float codebook_max,
                                                     unsigned char* __restrict__ luts) {
-    __shared__ float qs[kMaxDim];
-    const uint32_t qi = blockIdx.x, j = threadIdx.x;
-    if (status[qi] != 0) return;
-    for (uint32_t k = j; k < d; k += 256) qs[k] = q[(uint64_t)qi * d + k];
+    __shared__ float qs[kLutQueries][kMaxDim];
+    __shared__ float qscale[kLutQueries];
+    __shared__ int qok[kLutQueries];
+    const uint32_t q0 = blockIdx.x * kLutQueries, j = threadIdx.x;
+    const uint32_t nq = n - q0 < kLutQueries ? n - q0 : kLutQueries;
+    for (uint32_t t = j; t < nq * d; t += 256) qs[t / d][t % d] = q[(uint64_t)q0 * d + t];
+    if (j < nq) {
+        qok[j] = status[q0 + j] == 0;
+        qscale[j] = HALF ? ldexpf(1.0f, half_lut_exponent(qnorm[q0 + j], codebook_max)) : 1.0f;
+    }
     __syncthreads();
-    const float scale = HALF ? ldexpf(1.0f, half_lut_exponent(qnorm[qi], codebook_max)) : 1.0f;
-    float* out32 = reinterpret_cast<float*>(luts) + (uint64_t)qi * nsq * 256;
-    __half* out16 = reinterpret_cast<__half*>(luts) + (uint64_t)qi * nsq * 256;
+    auto store = [&](uint32_t u, uint32_t m, float v) {
+        const uint64_t at = (uint64_t)(q0 + u) * nsq * 256 + m * 256 + j;
+        if (HALF) reinterpret_cast<__half*>(luts)[at] = __float2half_rn(v * qscale[u]);
+        else reinterpret_cast<float*>(luts)[at] = v;
+    };
     if (lsq == 4) {
         const float4* cb4 = reinterpret_cast<const float4*>(cb);
         for (uint32_t m0 = 0; m0 < nsq; m0 += 8) {
@@ -109,25 +120,25 @@ __global__ __launch_bounds__(256) void k_build_luts(const float* __restrict__ q,
 #pragma unroll
             for (int u = 0; u < 8; ++u)
                 if (m0 + u < nsq) y[u] = __ldg(cb4 + (uint64_t)(m0 + u) * 256 + j);
+            for (uint32_t qq = 0; qq < nq; ++qq) {
+                if (!qok[qq]) continue;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const uint32_t m = m0 + u;
-                if (m >= nsq) break;
-                const float* x = qs + m * 4;
-                const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
-                const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
-                const float v = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
-                                          __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
-                if (HALF) out16[m * 256 + j] = __float2half_rn(v * scale);
-                else out32[m * 256 + j] = v;
+                for (int u = 0; u < 8; ++u) {
+                    const uint32_t m = m0 + u;
+                    if (m >= nsq) break;
+                    const float* x = qs[qq] + m * 4;
+                    const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
+                    const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
+                    store(qq, m, __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                           __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3))));
+                }
             }
         }
     } else {
-        for (uint32_t m = 0; m < nsq; ++m) {
-            const float v = l2sqr_sse(qs + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq);
-            if (HALF) out16[m * 256 + j] = __float2half_rn(v * scale);
-            else out32[m * 256 + j] = v;
-        }
+        for (uint32_t m = 0; m < nsq; ++m)
+            for (uint32_t qq = 0; qq < nq; ++qq)
+                if (qok[qq])
+                    store(qq, m, l2sqr_sse(qs[qq] + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq));
     }
 }
 
@@ -666,12 +677,12 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     k_scan_order<<<1, kOrderThreads, 0, stream>>>(s.wbucket, n, s.order);
     p.order = s.order;
     {
-        const dim3 g(n);
+        const dim3 g((n + kLutQueries - 1) / kLutQueries);
         if (half_lut)
-            k_build_luts<true><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, ix.d,
+            k_build_luts<true><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, n, ix.d,
                                                       ix.nsq, ix.lsq, ix.codebook_max, s.luts);
         else
-            k_build_luts<false><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, ix.d,
+            k_build_luts<false><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, n, ix.d,
                                                        ix.nsq, ix.lsq, ix.codebook_max, s.luts);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
