@@ -252,6 +252,20 @@ int pgpu_server_destroy(pgpu_server* server);
 int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* points,
                         uint64_t n, int32_t* assign, float* distance, void* stream);
 
+/* Replaces PuckIndex::puck_assign (puck/puck/puck_index.cpp:602-709), the build's
+ * encoder, for n points whose cells are known (cell_assign = coarse * F + fine): the
+ * filter-PQ offset and codes of each point (filter_data.dat records) and, with
+ * pq_nsq > 0, the second-level PQ's (pq_data.dat), bit-identical to the reference.
+ * base [n][d], coarse [C][d], fine [F][d], filter_codebook [filter_nsq][256][d/filter_nsq],
+ * pq_codebook [pq_nsq][256][d/pq_nsq]; outputs offsets [n] and codes [n][nsq]. All
+ * pointers DEVICE; work runs on `stream` and the call returns when it is done.
+ * PGPU_E_INVALID for a cell id >= C * F. */
+int pgpu_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* cell_assign,
+                     const float* coarse, uint32_t C, const float* fine, uint32_t F,
+                     const float* filter_codebook, uint32_t filter_nsq, const float* pq_codebook,
+                     uint32_t pq_nsq, float* filter_offsets, uint8_t* filter_codes,
+                     float* pq_offsets, uint8_t* pq_codes, void* stream);
+
 /* The k-means assignment step of pgpu_nearest_center, allocating no device
  * memory. No counterpart in the reference: it exists for callers that must not
  * allocate GPU memory (a process that hands out device memory from its own pool,

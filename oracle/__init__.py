@@ -91,6 +91,9 @@ def _load():
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.po_search_scan.argtypes = lib.po_search.argtypes
         lib.po_search_scan_batch.argtypes = lib.po_search_batch.argtypes
+        lib.po_puck_assign.argtypes = [ctypes.c_uint32, ctypes.c_uint64] + [ctypes.c_void_p] * 4 + [
+            ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32] + [
+            ctypes.c_void_p] * 4
         lib.po_nearest_center.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                           ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
                                           ctypes.c_void_p]
@@ -240,3 +243,28 @@ def nearest_cell_assign(coarse, fine, x):
                                fine.shape[0], x.ctypes.data, n, cell.ctypes.data,
                                dist.ctypes.data)
     return cell, dist
+
+
+def puck_assign(base, cell_assign, coarse, fine, filter_codebook, pq_codebook=None):
+    """puck_assign (puck/puck/puck_index.cpp:602-709) for points whose cells are known:
+    (filter_offsets [n], filter_codes [n, fnsq]) and, with a second-level PQ codebook,
+    (pq_offsets, pq_codes) as well (else None, None)."""
+    lib = _load()
+    base = np.ascontiguousarray(base, np.float32)
+    n, d = base.shape
+    ca = np.ascontiguousarray(cell_assign, np.uint32)
+    coarse = np.ascontiguousarray(coarse, np.float32)
+    fine = np.ascontiguousarray(fine, np.float32)
+    fcb = np.ascontiguousarray(filter_codebook, np.float32)
+    fnsq = fcb.shape[0]
+    pcb = None if pq_codebook is None else np.ascontiguousarray(pq_codebook, np.float32)
+    pnsq = 0 if pcb is None else pcb.shape[0]
+    f_off = np.zeros(n, np.float32)
+    f_codes = np.zeros((n, fnsq), np.uint8)
+    p_off = np.zeros(n, np.float32) if pnsq else None
+    p_codes = np.zeros((n, pnsq), np.uint8) if pnsq else None
+    lib.po_puck_assign(d, n, base.ctypes.data, ca.ctypes.data, coarse.ctypes.data,
+                       fine.ctypes.data, fine.shape[0], fcb.ctypes.data, fnsq, _ptr(pcb), pnsq,
+                       f_off.ctypes.data, f_codes.ctypes.data, _ptr(p_off), _ptr(p_codes))
+    return f_off, f_codes, p_off, p_codes
+

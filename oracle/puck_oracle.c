@@ -927,6 +927,83 @@ int po_search_scan_batch(const po_index* ix, const po_params* p, uint32_t n, con
 
 /* ------------------------------------------------------------------ assign */
 
+/* One quantizer's pass of puck_assign (puck_index.cpp:644-679): per subspace k, the
+ * nearest codeword of r's slice by nearest_center (kmeans.cpp:221-258) over the ks = 256
+ * codewords, then saxpy(-1) of that codeword from the slice. cbn: codeword norms. */
+static void assign_encode(float* r, const float* cb, const float* cbn, uint32_t nsq, uint32_t lsq,
+                          uint8_t* codes) {
+    for (uint32_t k = 0; k < nsq; ++k) {
+        float* s = r + (uint64_t)k * lsq;
+        const float pn = dotf(s, s, lsq);
+        float best = FLT_MAX;
+        uint32_t bi = 0;
+        for (uint32_t c = 0; c < 256; ++c) {
+            const float* cw = cb + ((uint64_t)k * 256 + c) * lsq;
+            const float t = pn + cbn[(uint64_t)k * 256 + c];
+            const float cur = (float)((double)t - 2.0 * (double)dotf(s, cw, lsq));
+            if (cur < best) {
+                best = cur;
+                bi = c;
+            }
+        }
+        codes[k] = (uint8_t)bi;
+        const float* cw = cb + ((uint64_t)k * 256 + bi) * lsq;
+        for (uint32_t t = 0; t < lsq; ++t) s[t] = s[t] + -1.0f * cw[t];
+    }
+}
+
+/* Quantization::decode (quantization.cpp:228-242) then set_static_value_of_formula
+ * (:244-258): 2 * sdot(decoded residual, vocab), then vocab += decoded residual. */
+static float assign_offset(float* vocab, float* dec, const float* cb, const uint8_t* codes,
+                           uint32_t nsq, uint32_t lsq) {
+    for (uint32_t k = 0; k < nsq; ++k)
+        memcpy(dec + (uint64_t)k * lsq, cb + ((uint64_t)k * 256 + codes[k]) * lsq,
+               sizeof(float) * lsq);
+    const uint32_t d = nsq * lsq;
+    const float off = 2 * dotf(dec, vocab, d);
+    for (uint32_t t = 0; t < d; ++t) vocab[t] += dec[t];
+    return off;
+}
+
+static float* codeword_norms(const float* cb, uint32_t nsq, uint32_t lsq) {
+    float* out = (float*)malloc(sizeof(float) * (uint64_t)nsq * 256);
+    for (uint64_t e = 0; e < (uint64_t)nsq * 256; ++e) out[e] = dotf(cb + e * lsq, cb + e * lsq, lsq);
+    return out;
+}
+
+void po_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* cell_assign,
+                    const float* coarse, const float* fine, uint32_t F, const float* fcb,
+                    uint32_t fnsq, const float* pcb, uint32_t pnsq, float* f_off,
+                    uint8_t* f_codes, float* p_off, uint8_t* p_codes) {
+    const uint32_t flsq = d / fnsq, plsq = pnsq ? d / pnsq : 0;
+    float* fn = codeword_norms(fcb, fnsq, flsq);
+    float* pn = pnsq ? codeword_norms(pcb, pnsq, plsq) : NULL;
+    float* r = (float*)malloc(sizeof(float) * d);
+    float* v = (float*)malloc(sizeof(float) * d);
+    float* dec = (float*)malloc(sizeof(float) * d);
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint32_t cell = cell_assign[i], c = cell / F, f = cell % F;
+        const float* x = base + i * d;
+        /* residual: saxpy(-1, coarse) then saxpy(-1, fine) (puck_index.cpp:638-643) */
+        for (uint32_t t = 0; t < d; ++t) {
+            r[t] = x[t] + -1.0f * coarse[(uint64_t)c * d + t];
+            r[t] = r[t] + -1.0f * fine[(uint64_t)f * d + t];
+        }
+        assign_encode(r, fcb, fn, fnsq, flsq, f_codes + i * fnsq);
+        if (pnsq) assign_encode(r, pcb, pn, pnsq, plsq, p_codes + i * pnsq);
+        /* offsets: vocab = coarse, saxpy(1, fine) (puck_index.cpp:682-694) */
+        for (uint32_t t = 0; t < d; ++t)
+            v[t] = coarse[(uint64_t)c * d + t] + 1.0f * fine[(uint64_t)f * d + t];
+        f_off[i] = assign_offset(v, dec, fcb, f_codes + i * fnsq, fnsq, flsq);
+        if (pnsq) p_off[i] = assign_offset(v, dec, pcb, p_codes + i * pnsq, pnsq, plsq);
+    }
+    free(fn);
+    free(pn);
+    free(r);
+    free(v);
+    free(dec);
+}
+
 void po_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* x,
                        uint64_t n, int32_t* assign, float* dis) {
     float* cn = (float*)malloc(sizeof(float) * (k ? k : 1));

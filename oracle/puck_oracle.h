@@ -84,6 +84,14 @@ int po_search_scan_batch(const po_index* ix, const po_params* p, uint32_t n, con
                          uint32_t topk, float* dist, uint32_t* ids, int32_t* status,
                          int nthreads);
 
+/* puck_assign (puck_index.cpp:602-709) for points whose cells are known: filter-PQ
+ * codes and offsets, and with pnsq > 0 the second-level PQ's, in input order.
+ * fcb [fnsq][256][d/fnsq], pcb [pnsq][256][d/pnsq]; d a multiple of both nsq. */
+void po_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* cell_assign,
+                    const float* coarse, const float* fine, uint32_t F, const float* fcb,
+                    uint32_t fnsq, const float* pcb, uint32_t pnsq, float* f_off,
+                    uint8_t* f_codes, float* p_off, uint8_t* p_codes);
+
 /* k-means assignment step: nearest_center (kmeans.cpp:221-258). */
 void po_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* x,
                        uint64_t n, int32_t* assign, float* dis);

@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "pgpu_contract_bf16", "pgpu_filter_candidates", "pgpu_probe_create", "pgpu_probe_destroy",
     "pgpu_probe_info", "pgpu_probe_train_step", "pgpu_probe_gradients", "pgpu_probe_forward",
     "pgpu_probe_get_params", "pgpu_probe_set_params", "pgpu_set_probe", "pgpu_knn",
+    "pgpu_puck_assign",
 )
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_CENTROIDS = 1 << 16
@@ -131,6 +132,8 @@ def load(build_if_missing=False):
     lib.pgpu_close.argtypes = [vp]
     lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
     lib.pgpu_nearest_center_noalloc.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
+    lib.pgpu_puck_assign.argtypes = [u32, u64, vp, vp, vp, u32, vp, u32, vp, u32, vp, u32, vp, vp,
+                                     vp, vp, vp]
     lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.pgpu_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), u32]
     lib.pgpu_walk_counters.argtypes = [vp, ctypes.POINTER(u64), u32]
@@ -350,6 +353,33 @@ def nearest_center(centroids, points, assign, distance, stream=None):
         s = s.cuda_stream
     return check(load().pgpu_nearest_center(dim, _ptr(centroids), k, _ptr(points), n,
                                             _ptr(assign), _ptr(distance), s))
+
+
+def puck_assign(base, cell_assign, coarse, fine, filter_codebook, pq_codebook=None, stream=None):
+    """The build's encoder (pgpu_puck_assign) on CUDA tensors: base [n, d] float32,
+    cell_assign [n] (int32 or uint32 bits), coarse [C, d], fine [F, d], filter_codebook
+    [fnsq, 256, d/fnsq] and optionally pq_codebook [pnsq, 256, d/pnsq]. Returns
+    (filter_offsets, filter_codes, pq_offsets, pq_codes) as CUDA tensors (the PQ pair
+    None without a PQ codebook)."""
+    import torch
+    n, d = base.shape
+    dev = base.device
+    fnsq = filter_codebook.shape[0]
+    pnsq = 0 if pq_codebook is None else pq_codebook.shape[0]
+    f_off = torch.empty(n, dtype=torch.float32, device=dev)
+    f_codes = torch.empty((n, fnsq), dtype=torch.uint8, device=dev)
+    p_off = torch.empty(n, dtype=torch.float32, device=dev) if pnsq else None
+    p_codes = torch.empty((n, pnsq), dtype=torch.uint8, device=dev) if pnsq else None
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    check(load().pgpu_puck_assign(d, n, _ptr(base.contiguous()), _ptr(cell_assign.contiguous()),
+                                  _ptr(coarse.contiguous()), coarse.shape[0],
+                                  _ptr(fine.contiguous()), fine.shape[0],
+                                  _ptr(filter_codebook.contiguous()), fnsq,
+                                  _ptr(pq_codebook.contiguous()) if pnsq else None, pnsq,
+                                  _ptr(f_off), _ptr(f_codes), _ptr(p_off), _ptr(p_codes), s))
+    return f_off, f_codes, p_off, p_codes
 
 
 CONTRACT_MODES = {"score": 0, "neg": 1, "store": 2, "bias": 3, "bias_gelu": 4, "gelu_bwd": 5}

@@ -105,3 +105,20 @@ def test_scan_mode_distances_agree_with_walk(golden):
         ws = np.sort(tw["filter_dist"][:tw["filter_cnt"]])
         ss = ts["filter_dist"][:ts["filter_cnt"]]
         assert np.all(ss[:len(ws)] <= ws)
+
+
+def test_oracle_puck_assign_matches_reference(golden):
+    """The build's encoder (puck_assign): re-encoding each golden index's vectors from
+    its cell assignment and codebooks gives the reference's filter_data.dat (and
+    pq_data.dat) records byte for byte."""
+    from puck_gb300 import index_io
+    name, z, index_dir = golden
+    a = index_io.read_index(index_dir)
+    f_off, f_codes, p_off, p_codes = oracle.puck_assign(
+        a["base"], a["cell_assign"], a["coarse"], a["fine"], a["filter_codebook"],
+        a.get("pq_codebook"))
+    assert np.array_equal(_bits(f_off), _bits(a["filter_offsets"])), name
+    assert np.array_equal(f_codes, a["filter_codes"]), name
+    if a.get("pq_codebook") is not None:
+        assert np.array_equal(_bits(p_off), _bits(a["pq_offsets"])), name
+        assert np.array_equal(p_codes, a["pq_codes"]), name
