@@ -8,8 +8,9 @@ puck/hierarchical_cluster/hierarchical_cluster_index.cpp:882-1138):
   2. every point assigned to its nearest cell c*F + f (among the `assign_probe`
      nearest coarse clusters, all fine clusters)
   3. filter PQ (filter_nsq subspaces x 256 codewords) trained by k-means on the cell
-     residuals x - c - f, every point encoded, and its offset
-     2 <decoded residual, c + f> stored (quantization.cpp:244-258)
+     residuals x - c - f; every point encoded, with its offset 2 <decoded residual,
+     c + f> (quantization.cpp:244-258), by the library's puck_assign kernel
+     (pgpu_puck_assign): the records the reference writes for these cells and codebooks
 
 The k-means assignment step is the library's own kernel (pgpu_nearest_center,
 kmeans.cpp:221-258). Training is seeded, unlike the reference's time(0) seeds;
@@ -128,27 +129,14 @@ def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters
         sc = _pq_encode(res.contiguous(), books)
         sdec = books[torch.arange(filter_nsq, device=dev)[None, :], sc.long()].reshape(-1, d)
         pq_books = _pq_train((res - sdec).contiguous(), pn, iters=10, seed=seed + 4)
-        pq_codes = torch.empty(n, pn, dtype=torch.uint8, device=dev)
-        pq_offsets = torch.empty(n, dtype=torch.float32, device=dev)
 
-    codes = torch.empty(n, filter_nsq, dtype=torch.uint8, device=dev)
-    offsets = torch.empty(n, dtype=torch.float32, device=dev)
+    # the encode itself: puck_assign's float order on the GPU (pgpu_puck_assign), so
+    # the records are the ones the reference writes for these cells and codebooks
     lsq = d // filter_nsq
-    chunk = 1 << 20
-    for s in range(0, n, chunk):
-        xs = base[s:s + chunk]
-        cs = cell[s:s + chunk]
-        vocab = coarse[cs // F] + fine[cs % F]
-        r = (xs - coarse[cs // F]) - fine[cs % F]
-        cd = _pq_encode(r.contiguous(), books)
-        codes[s:s + chunk] = cd
-        dec = books[torch.arange(filter_nsq, device=dev)[None, :], cd.long()].reshape(-1, d)
-        offsets[s:s + chunk] = 2 * (dec * vocab).sum(1)
-        if whether_pq:
-            cp = _pq_encode((r - dec).contiguous(), pq_books)
-            pq_codes[s:s + chunk] = cp
-            dec2 = pq_books[torch.arange(pn, device=dev)[None, :], cp.long()].reshape(-1, d)
-            pq_offsets[s:s + chunk] = 2 * (dec2 * (vocab + dec)).sum(1)
+    offsets, codes, pq_offsets, pq_codes = native.puck_assign(
+        base.contiguous(), cell.to(torch.int32), coarse.contiguous(), fine.contiguous(),
+        books.reshape(filter_nsq, 256, lsq).contiguous(),
+        pq_books.reshape(pn, 256, d // pn).contiguous() if whether_pq else None)
     out = dict(coarse=coarse.cpu().numpy(), fine=fine.cpu().numpy(),
                base=base.cpu().numpy(), cell_assign=cell.to(torch.int64).cpu().numpy().astype(np.uint32),
                filter_codebook=books.reshape(filter_nsq, 256, lsq).cpu().numpy(),
