@@ -109,3 +109,18 @@ def test_gflag_mirror_defaults():
     assert py_puck_api.current_params()["filter_topk"] == 500
     assert py_puck_api.update_gflag("no_such_flag", "1") == ""
     py_puck_api.reset_gflags()
+
+
+def test_ip2cos_conf_checked_before_device(lib, tmp_path):
+    """ip2cos = 2 is refused from index.dat alone (the reference's search reads past a
+    feature_dim - 1 query there); ip2cos = 1 passes the config check and fails only on
+    the missing vector files."""
+    for ip2cos, want in ((2, native.PGPU_E_UNSUPPORTED), (1, native.PGPU_E_IO)):
+        d = tmp_path / f"ip{ip2cos}"
+        d.mkdir()
+        index_io.write_index_conf(str(d / "index.dat"), feature_dim=8, total_point_count=4,
+                                  coarse_cluster_count=2, fine_cluster_count=2, filter_nsq=2,
+                                  whether_norm=False, ip2cos=ip2cos)
+        h = ctypes.c_void_p()
+        p = native.default_params()
+        assert lib.pgpu_open(str(d).encode(), ctypes.byref(p), ctypes.byref(h)) == want

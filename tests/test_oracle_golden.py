@@ -122,3 +122,24 @@ def test_oracle_puck_assign_matches_reference(golden):
     if a.get("pq_codebook") is not None:
         assert np.array_equal(_bits(p_off), _bits(a["pq_offsets"])), name
         assert np.array_equal(p_codes, a["pq_codes"]), name
+
+
+def test_oracle_ip2cos_arrays_equal_files():
+    """The ip2cos golden index loaded from its files and from arrays (with ip2cos set)
+    searches alike: d - 1 value queries widened by a 0."""
+    import os
+    import tempfile
+    from puck_gb300 import index_io
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ip2cos_d23.npz"))
+    P, T, k = [int(v) for v in z["params"]]
+    with tempfile.TemporaryDirectory() as tmp:
+        index_io.materialize_npz_index(z, tmp)
+        a = index_io.read_index(tmp)
+        assert a["ip2cos"] == 1 and a["coarse"].shape[1] == z["queries"].shape[1] + 1
+        by_file = oracle.OracleIndex(tmp)
+        by_arrays = oracle.OracleIndex(arrays=a)
+        d1, i1, s1 = by_file.search_batch(z["queries"], k, P, T, topk_max=100)
+        d2, i2, s2 = by_arrays.search_batch(z["queries"], k, P, T, topk_max=100)
+    assert (s1 == 0).all() and (s2 == 0).all()
+    assert np.array_equal(_bits(d1), _bits(d2)) and np.array_equal(i1, i2)
+    assert np.array_equal(_bits(d1), _bits(z["dist"])) and np.array_equal(i1, z["labels"])
