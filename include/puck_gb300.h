@@ -258,8 +258,8 @@ int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const 
  * pq_nsq > 0, the second-level PQ's (pq_data.dat), bit-identical to the reference.
  * base [n][d], coarse [C][d], fine [F][d], filter_codebook [filter_nsq][256][d/filter_nsq],
  * pq_codebook [pq_nsq][256][d/pq_nsq]; outputs offsets [n] and codes [n][nsq]. All
- * pointers DEVICE; work runs on `stream` and the call returns when it is done.
- * PGPU_E_INVALID for a cell id >= C * F. */
+ * pointers DEVICE on the calling thread's current device; work runs on `stream` and
+ * the call returns when it is done. PGPU_E_INVALID for a cell id >= C * F. */
 int pgpu_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* cell_assign,
                      const float* coarse, uint32_t C, const float* fine, uint32_t F,
                      const float* filter_codebook, uint32_t filter_nsq, const float* pq_codebook,
