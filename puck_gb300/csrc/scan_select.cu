@@ -12,11 +12,15 @@
 // over all records of the probed clusters, a superset search of the same cells.
 //
 // Selection: a buffer of (t, id) keys in shared memory with a running threshold
-// tau = the key of the current filter_topk-th best; records whose
+// tau, a key with at least filter_topk kept keys at or below it; records whose
 // (2*cell_dist + offset, id) key is not below tau are dropped before the table
-// lookups (t can only grow). When the buffer fills it is bitonic-sorted and cut
-// back to filter_topk keys. The output is the set of the filter_topk smallest
-// (t, id) keys, unordered.
+// lookups (t can only grow). When the buffer could not take another round, an
+// MSB radix select (two digit passes) finds a new bound and the keys above it are
+// dropped. A last exact select leaves the set of the filter_topk smallest (t, id)
+// keys, unordered.
+//
+// Blocks start in launch order longest scan first (k_scan_work, k_scan_order),
+// one block per query.
 //
 // Precision form (HALF): the table is stored in FP16, scaled per query by a
 // power of two 2^e chosen from the bound (|q| + max |codeword|)^2 >= every entry
