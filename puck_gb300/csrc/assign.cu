@@ -195,11 +195,7 @@ extern "C" int pgpu_puck_assign(uint32_t d, uint64_t n, const float* base,
     p.fcb_norm = norms;
     p.pcb_norm = norms + (uint64_t)filter_nsq * 256;
     p.err = err;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_puck_assign, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        attr_set = true;
-    }
+    pgpu::ensure_max_dynamic_smem(k_puck_assign, 100 * 1024);
     e = cudaMemsetAsync(err, 0, sizeof(int), st);
     if (e == cudaSuccess) {
         k_codeword_norms<<<(unsigned)((filter_nsq * 256ull + 255) / 256), 256, 0, st>>>(

@@ -510,23 +510,14 @@ cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L,
                                   uint32_t K, float* out_val, uint32_t* out_idx,
                                   const int32_t* status, cudaStream_t stream) {
     if (K < L && K + 1 <= 32) {
-        static bool sel_attr = false;
-        if (!sel_attr) {
-            cudaFuncSetAttribute(k_topsel_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 220 * 1024);
-            sel_attr = true;
-        }
+        ensure_max_dynamic_smem(k_topsel_small, 220 * 1024);
         k_topsel_small<<<nrows, kSelThreads, (size_t)L * sizeof(float), stream>>>(
             vals, L, ld_vals, K, out_val, out_idx, status);
         return cudaGetLastError();
     }
     const uint32_t Lp = next_pow2(L < 2 ? 2 : L);
     const size_t smem = (size_t)Lp * 8;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_topsort, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr_set = true;
-    }
+    ensure_max_dynamic_smem(k_topsort, 220 * 1024);
     k_topsort<<<nrows, 512, smem, stream>>>(vals, L, Lp, ld_vals, K, out_val, out_idx, status);
     return cudaGetLastError();
 }

@@ -163,6 +163,16 @@ cudaError_t launch_gather_u32(const uint32_t* idx, uint64_t n, const uint32_t* t
                               uint32_t* out, cudaStream_t stream);
 // Records `msg` as the calling thread's last error (pgpu_last_error) and returns `code`.
 int set_last_error(int code, const std::string& msg);
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the calling thread's
+// current device, once per (kernel, device, bytes). Function attributes belong to a
+// device's context, so a process that searches on several GPUs sets them on each one.
+// Thread-safe.
+void ensure_max_dynamic_smem(const void* kernel, int bytes);
+template <class K>
+inline void ensure_max_dynamic_smem(K* kernel, int bytes) {
+    ensure_max_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
+}
 cudaError_t launch_topsort_status(const float* vals, uint32_t nrows, uint32_t L, uint32_t ld_vals,
                                   uint32_t K, float* out_val, uint32_t* out_idx,
                                   const int32_t* status, cudaStream_t stream);

@@ -2,7 +2,10 @@
 // terms (+ full fine order in exact mode), filter stage (exact walk or scan),
 // rerank. Shared by the synchronous entry points and the serving loop.
 #include <algorithm>
+#include <mutex>
+#include <set>
 #include <string>
+#include <tuple>
 
 #include "pgpu_internal.h"
 
@@ -16,6 +19,18 @@ cudaError_t alloc(T** p, uint64_t count, uint64_t* bytes) {
     return e;
 }
 }  // namespace
+
+void ensure_max_dynamic_smem(const void* kernel, int bytes) {
+    static std::mutex mu;
+    static std::set<std::tuple<const void*, int, int>> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(kernel, dev, bytes);
+    std::lock_guard<std::mutex> g(mu);
+    if (done.count(key)) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+        done.insert(key);
+}
 
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qb, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,

@@ -442,12 +442,7 @@ cudaError_t probe_adam(ProbeNet& net, const ProbeNet& grad, ProbeNet& m, ProbeNe
 cudaError_t launch_probe_select(const ProbeNet& net, const DeviceIndex& ix, uint32_t n,
                                 const float* Z, float mass, uint32_t max_probe, Scratch& s,
                                 cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_probe_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        attr = true;
-    }
+    ensure_max_dynamic_smem(k_probe_select, 200 * 1024);
     k_probe_select<<<n, kProbeThreads, sizeof(float) * net.C, st>>>(
         Z, net.C, s.q, ix.d, ix.coarse, ix.coarse_norms, s.status, mass, max_probe, s.P, s.cdist,
         s.ctag, s.pconf, s.counters);

@@ -602,20 +602,11 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
     p.Tp = pow2_at_least(s.T > topk ? s.T : topk);
     p.topk = topk;
     const size_t smem = rerank_smem_bytes(ix, s.T, topk);
-    static bool attr_set[2] = {false, false};
     if (ix.pq_nsq) {
-        if (!attr_set[1]) {
-            cudaFuncSetAttribute(k_rerank<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 220 * 1024);
-            attr_set[1] = true;
-        }
+        ensure_max_dynamic_smem(k_rerank<true>, 220 * 1024);
         k_rerank<true><<<n, kThreads, smem, stream>>>(p);
     } else {
-        if (!attr_set[0]) {
-            cudaFuncSetAttribute(k_rerank<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 220 * 1024);
-            attr_set[0] = true;
-        }
+        ensure_max_dynamic_smem(k_rerank<false>, 220 * 1024);
         k_rerank<false><<<n, kThreads, smem, stream>>>(p);
     }
     return cudaGetLastError();
@@ -649,12 +640,7 @@ cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t top
     p.Tp = pow2_at_least(s.T);
     p.topk = topk;
     const size_t smem = rerank_screen_smem_bytes(ix, s.T, topk);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_rerank_screen, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024);
-        attr_set = true;
-    }
+    ensure_max_dynamic_smem(k_rerank_screen, 220 * 1024);
     k_rerank_screen<<<n, kScreenThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }

@@ -693,12 +693,8 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     }
     const size_t smem = half_lut ? scan_smem_bytes_half(ix) : scan_smem_bytes(ix);
     const uint32_t nw = ix.code_stride / 4;
-    static bool attr_set[10] = {};  // one per instantiation
-    auto launch = [&](void (*kernel)(ScanParams), int slot) {
-        if (!attr_set[slot]) {
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-            attr_set[slot] = true;
-        }
+    auto launch = [&](void (*kernel)(ScanParams), int) {
+        ensure_max_dynamic_smem(kernel, 220 * 1024);
         kernel<<<n, kThreads, smem, stream>>>(p);
     };
     if (half_lut) {

@@ -412,22 +412,13 @@ cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
     const int av = operand_vec(A) ? 1 : 0, bv = operand_vec(B) ? 1 : 0;
     const bool async = A.pb != nullptr && B.pb != nullptr && av && bv;
     const size_t smem = async ? tc_gemm_async_smem_bytes() : tc_gemm_smem_bytes();
-    static bool attr[12] = {};
 #define PGPU_TC_CASE(M)                                                                        \
     case M:                                                                                    \
         if (async) {                                                                           \
-            if (!attr[M + 6]) {                                                                \
-                cudaFuncSetAttribute(k_tc_gemm<M, true>,                                       \
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
-                attr[M + 6] = true;                                                            \
-            }                                                                                  \
+            ensure_max_dynamic_smem(k_tc_gemm<M, true>, (int)smem);                            \
             k_tc_gemm<M, true><<<grid, kTcThreads, smem, stream>>>(A, B, K, av, bv, ep, err); \
         } else {                                                                               \
-            if (!attr[M]) {                                                                    \
-                cudaFuncSetAttribute(k_tc_gemm<M, false>,                                      \
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
-                attr[M] = true;                                                                \
-            }                                                                                  \
+            ensure_max_dynamic_smem(k_tc_gemm<M, false>, (int)smem);                           \
             k_tc_gemm<M, false><<<grid, kTcThreads, smem, stream>>>(A, B, K, av, bv, ep, err);\
         }                                                                                      \
         break;

@@ -452,11 +452,7 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
         return cudaGetLastError();
     }
     const size_t smem = window_smem_bytes(ix.C, ix.d);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_window_topk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
-    }
+    ensure_max_dynamic_smem(k_window_topk, 200 * 1024);
     k_window_topk<<<n, kWinThreads, smem, stream>>>(s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse,
                                                     ix.coarse_norms, ix.coarse_abs, ix.C, s.Pfix,
                                                     s.P, s.cdist, s.ctag, s.status, s.tc_err,

@@ -401,11 +401,7 @@ cudaError_t launch_walk_scan(const DeviceIndex& ix, const SearchConfig& cfg, uin
     p.T = s.T;
     p.rr = cfg.radius_rate;
     const size_t smem = walk_smem_bytes(ix, s.T);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_walk_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr_set = true;
-    }
+    ensure_max_dynamic_smem(k_walk_scan, 220 * 1024);
     k_walk_scan<<<n, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
