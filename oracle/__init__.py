@@ -69,6 +69,11 @@ def _load():
         lib.po_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         lib.po_free.argtypes = [ctypes.c_void_p]
         lib.po_set_ip2cos.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.po_realtime_open.argtypes = [ctypes.c_void_p]
+        lib.po_insert.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.po_insert.restype = ctypes.c_int64
+        lib.po_inserted_records.argtypes = [ctypes.c_void_p] * 6
+        lib.po_inserted_records.restype = ctypes.c_uint32
         lib.po_load_arrays_pq.restype = ctypes.c_void_p
         lib.po_load_arrays_pq.argtypes = [ctypes.c_uint32] * 5 + [ctypes.c_int] + [ctypes.c_void_p] * 7 + [
             ctypes.c_uint32] + [ctypes.c_void_p] * 3 + [ctypes.POINTER(ctypes.c_int)]
@@ -155,6 +160,33 @@ class OracleIndex:
             self._h = None
 
     __del__ = close
+
+    def realtime_open(self):
+        """Switch to RealtimeInsertPuckIndex semantics (realtime_insert_puck_index.cpp)."""
+        if _load().po_realtime_open(self._h) != 0:
+            raise RuntimeError("oracle: realtime open failed")
+        self._inserted = 0
+
+    def insert(self, feature):
+        """Insert one point (d floats); returns its local id (n + insert id)."""
+        x = np.ascontiguousarray(feature, np.float32)
+        lid = _load().po_insert(self._h, x.ctypes.data)
+        if lid < 0:
+            raise RuntimeError("oracle: insert failed")
+        self._inserted += 1
+        return lid
+
+    def inserted_records(self, pq_nsq=0):
+        """(cells, filter offsets, filter codes, pq offsets, pq codes) of the inserts."""
+        m = self._inserted
+        cell = np.zeros(m, np.uint32)
+        off = np.zeros(m, np.float32)
+        codes = np.zeros((m, self.nsq), np.uint8)
+        poff = np.zeros(m, np.float32) if pq_nsq else None
+        pcodes = np.zeros((m, pq_nsq), np.uint8) if pq_nsq else None
+        _load().po_inserted_records(self._h, cell.ctypes.data, off.ctypes.data, codes.ctypes.data,
+                                    _ptr(poff), _ptr(pcodes))
+        return cell, off, codes, poff, pcodes
 
     def memory_to_local(self):
         p = _load().po_memory_to_local(self._h)

@@ -40,6 +40,18 @@ struct po_index {
     float* pq_offsets;      /* n, memory order */
     uint8_t* pq_codes;      /* n*pq_nsq, memory order */
     float* pq_codebook;     /* pq_nsq*256*pq_lsq */
+    /* RealtimeInsertPuckIndex (realtime_insert_puck_index.cpp); realtime = 0: PuckIndex */
+    int realtime;
+    uint32_t ins_n, ins_cap;
+    uint32_t* ins_cell;     /* [ins_n] cell of each inserted point */
+    float* ins_off;         /* [ins_n] filter offsets */
+    uint8_t* ins_codes;     /* [ins_n][nsq] */
+    float* ins_pq_off;      /* [ins_n] (second-level PQ) */
+    uint8_t* ins_pq_codes;  /* [ins_n][pq_nsq] */
+    float* ins_feat;        /* [ins_n][d] (without the second-level PQ) */
+    int32_t* ins_head;      /* [C*F] newest insert of each cell, -1: none */
+    int32_t* ins_next;      /* [ins_n] next older insert of the same cell */
+    uint32_t* cell_cnt;     /* [C*F] base + inserted points (InsertFineCluster::point_cnt) */
 };
 
 /* ---------------------------------------------------------------- BLAS order */
@@ -199,6 +211,15 @@ void po_free(po_index* ix) {
     free(ix->pq_offsets);
     free(ix->pq_codes);
     free(ix->pq_codebook);
+    free(ix->ins_cell);
+    free(ix->ins_off);
+    free(ix->ins_codes);
+    free(ix->ins_pq_off);
+    free(ix->ins_pq_codes);
+    free(ix->ins_feat);
+    free(ix->ins_head);
+    free(ix->ins_next);
+    free(ix->cell_cnt);
     free(ix);
 }
 
@@ -547,6 +568,18 @@ static void rerank_pq(const po_index* ix, const float* q, const uint32_t* tags, 
     for (uint32_t idx = 0; idx < cnt; ++idx) {
         const uint32_t mi = tags[(uint64_t)idx * stride];
         float t = fdist[(uint64_t)idx * stride] - qn;
+        if (ix->realtime) {
+            /* realtime_insert_puck_index.cpp:466-499: inserted records by insert id, and
+               the table summed subspace by subspace while below the top */
+            const int ins = mi >= ix->n;
+            const uint32_t id = mi - ix->n;
+            t = t + (ins ? ix->ins_pq_off[id] : ix->pq_offsets[mi]);
+            const uint8_t* code = ins ? ix->ins_pq_codes + (uint64_t)id * pq_nsq
+                                      : ix->pq_codes + (uint64_t)mi * pq_nsq;
+            for (uint32_t m = 0; m < pq_nsq && t < fin->val[1]; ++m) t = t + lut[m * 256 + code[m]];
+            if (t < fin->val[1]) heap_update(fin, t, ins ? mi : ix->mem2local[mi]);
+            continue;
+        }
         t = t + ix->pq_offsets[mi];
         t = t + lookup_lut(ix->pq_codes + (uint64_t)mi * pq_nsq, lut, pq_nsq);
         if (t < fin->val[1]) heap_update(fin, t, ix->mem2local[mi]);
@@ -593,7 +626,10 @@ static void scratch_free(po_scratch* s) {
     free(s->rtag);
 }
 
-/* compute_quantized_distance (puck_index.cpp:346-390) */
+/* compute_quantized_distance (puck_index.cpp:346-390); on a realtime index then the
+ * cell's inserted points, newest first, none skipped, with memory id n + insert id
+ * (realtime_insert_puck_index.cpp:398-453). The realtime count adds one per inserted
+ * point, which only makes the walk recompute an unchanged pivot. */
 static uint32_t scan_cell(const po_index* ix, uint64_t cell, float cell_dist, const float* lut,
                           po_heap* heap, uint64_t* scanned) {
     uint32_t start = ix->cell_start[cell];
@@ -608,6 +644,15 @@ static uint32_t scan_cell(const po_index* ix, uint64_t cell, float cell_dist, co
         if (t < heap->val[1]) {
             heap_update(heap, t, mi);
             ++updated;
+        }
+    }
+    if (ix->realtime) {
+        for (int32_t id = ix->ins_head[cell]; id >= 0; id = ix->ins_next[id]) {
+            ++updated;
+            ++*scanned;
+            float t = (float)(2.0 * (double)cell_dist + (double)ix->ins_off[id]);
+            t = t + lookup_lut(ix->ins_codes + (uint64_t)id * ix->nsq, lut, ix->nsq);
+            if (t < heap->val[1]) heap_update(heap, t, ix->n + (uint32_t)id);
         }
     }
     return updated;
@@ -726,13 +771,15 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
         return 0;
     }
     for (uint32_t idx = 0; idx < cnt; ++idx) {
-        const float* x = ix->feat + (uint64_t)s->rtag[idx] * d;
+        const uint32_t mi = s->rtag[idx];
+        const int ins = mi >= ix->n;  /* realtime: an inserted point's kept vector */
+        const float* x = ins ? ix->ins_feat + (uint64_t)(mi - ix->n) * d : ix->feat + (uint64_t)mi * d;
         float t = 0.0f;
         uint32_t m = 0;
         for (; m + 16 <= d && t < fin.val[1]; m += 16) t = t + l2sqr16(x + m, q + m);
         if (t < fin.val[1]) {
             if (d - m > 0) t = t + l2sqr_ext(x + m, q + m, d - m);
-            heap_update(&fin, t, ix->mem2local[s->rtag[idx]]);
+            heap_update(&fin, t, ins ? mi : ix->mem2local[mi]);
         }
     }
     heap_reorder(&fin);
@@ -1092,3 +1139,127 @@ void po_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C, const
     free(fip);
     free(list);
 }
+
+/* ------------------------------------------------------------- realtime insert */
+
+/* RealtimeInsertPuckIndex::init (realtime_insert_puck_index.cpp:225-272) over a loaded
+ * index: every cell's insert count starts at its base count, no inserted points. */
+int po_realtime_open(po_index* ix) {
+    if (ix == NULL) return -1;
+    if (ix->realtime) return 0;
+    const uint64_t cells = (uint64_t)ix->C * ix->F;
+    ix->ins_head = (int32_t*)malloc(sizeof(int32_t) * cells);
+    ix->cell_cnt = (uint32_t*)malloc(sizeof(uint32_t) * cells);
+    for (uint64_t i = 0; i < cells; ++i) {
+        ix->ins_head[i] = -1;
+        ix->cell_cnt[i] = ix->cell_start[i + 1] - ix->cell_start[i];
+    }
+    ix->realtime = 1;
+    return 0;
+}
+
+static void ins_reserve(po_index* ix) {
+    if (ix->ins_n < ix->ins_cap) return;
+    const uint32_t cap = ix->ins_cap ? 2 * ix->ins_cap : 64;
+    ix->ins_cell = (uint32_t*)realloc(ix->ins_cell, sizeof(uint32_t) * cap);
+    ix->ins_next = (int32_t*)realloc(ix->ins_next, sizeof(int32_t) * cap);
+    ix->ins_off = (float*)realloc(ix->ins_off, sizeof(float) * cap);
+    ix->ins_codes = (uint8_t*)realloc(ix->ins_codes, (uint64_t)ix->nsq * cap);
+    if (ix->pq_nsq) {
+        ix->ins_pq_off = (float*)realloc(ix->ins_pq_off, sizeof(float) * cap);
+        ix->ins_pq_codes = (uint8_t*)realloc(ix->ins_pq_codes, (uint64_t)ix->pq_nsq * cap);
+    } else {
+        ix->ins_feat = (float*)realloc(ix->ins_feat, sizeof(float) * (uint64_t)ix->d * cap);
+    }
+    ix->ins_cap = cap;
+}
+
+/* RealtimeInsertPuckIndex::insert (realtime_insert_puck_index.cpp:273-337):
+ *   single_build (hierarchical_cluster_index.cpp:1455-1494): normalisation, then
+ *     nearest_cell_assign (:1042-1085) on the index's live stationary terms (a cell
+ *     empty in the base keeps sqrt(FLT_MAX) there, so it is never chosen);
+ *   puck_single_assign (puck_index.cpp:938-988): the encode of puck_assign;
+ *   the point goes to the head of its cell's list; a cell whose count becomes 1 gets
+ *   the stationary term c.f - f.f.
+ * Returns the inserted point's local id (n + insert id), or -1. */
+int64_t po_insert(po_index* ix, const float* feature) {
+    if (ix == NULL || !ix->realtime || feature == NULL) return -1;
+    const uint32_t d = ix->d, C = ix->C, F = ix->F;
+    float* x = (float*)malloc(sizeof(float) * d);
+    memcpy(x, feature, sizeof(float) * d);
+    if (ix->whether_norm) {
+        const float norm = sqrtf(dotf(x, x, d));
+        if (norm < 1e-6) {
+            free(x);
+            return -1;
+        }
+        const float alpha = (float)(1.0 / (double)norm);
+        for (uint32_t i = 0; i < d; ++i) x[i] = alpha * x[i];
+    }
+    pair_fi* list = (pair_fi*)malloc(sizeof(pair_fi) * C);
+    float* fip = (float*)malloc(sizeof(float) * F);
+    const float qn = dotf(x, x, d) / 2;
+    for (uint32_t c = 0; c < C; ++c) {
+        list[c].id = (int32_t)c;
+        list[c].v = (ix->coarse_norms[c] - dotf(ix->coarse + (uint64_t)c * d, x, d)) + qn;
+    }
+    for (uint32_t f = 0; f < F; ++f) fip[f] = dotf(ix->fine + (uint64_t)f * d, x, d);
+    qsort(list, C, sizeof(pair_fi), cmp_pair_fi);
+    float best = FLT_MAX;
+    int32_t best_id = -1;
+    for (uint32_t i = 0; i < C; ++i) {
+        const int32_t cc = list[i].id;
+        const float term = list[i].v;
+        for (uint32_t f = 0; f < F; ++f) {
+            const float* fv = ix->fine + (uint64_t)f * d;
+            const float fneg = 0 - sqrtf(dotf(fv, fv, d) / 2);
+            if (sqrtf(best) - fneg < sqrtf(term)) break;
+            const float score = (term - fip[f]) + ix->stationary[(uint64_t)cc * F + f];
+            if (score < best) {
+                best = score;
+                best_id = cc * (int32_t)F + (int32_t)f;
+            }
+        }
+    }
+    free(list);
+    free(fip);
+    if (best_id < 0) {
+        free(x);
+        return -1;
+    }
+    ins_reserve(ix);
+    const uint32_t id = ix->ins_n;
+    const uint32_t cell = (uint32_t)best_id;
+    po_puck_assign(d, 1, x, &cell, ix->coarse, ix->fine, F, ix->codebook, ix->nsq,
+                   ix->pq_nsq ? ix->pq_codebook : NULL, ix->pq_nsq, ix->ins_off + id,
+                   ix->ins_codes + (uint64_t)id * ix->nsq, ix->pq_nsq ? ix->ins_pq_off + id : NULL,
+                   ix->pq_nsq ? ix->ins_pq_codes + (uint64_t)id * ix->pq_nsq : NULL);
+    if (!ix->pq_nsq) memcpy(ix->ins_feat + (uint64_t)id * d, x, sizeof(float) * d);
+    ix->ins_cell[id] = cell;
+    ix->ins_next[id] = ix->ins_head[cell];
+    ix->ins_head[cell] = (int32_t)id;
+    ix->ins_n = id + 1;
+    if (++ix->cell_cnt[cell] == 1) {
+        const float* cv = ix->coarse + (uint64_t)(cell / F) * d;
+        const float* fv = ix->fine + (uint64_t)(cell % F) * d;
+        float st = dotf(cv, fv, d);
+        st -= dotf(fv, fv, d);
+        ix->stationary[cell] = st;
+    }
+    free(x);
+    return (int64_t)ix->n + id;
+}
+
+/* The inserted points' records: cell, filter offset and codes, second-level PQ offset
+ * and codes (NULL outputs are skipped). Returns the number of inserted points. */
+uint32_t po_inserted_records(const po_index* ix, uint32_t* cell, float* off, uint8_t* codes,
+                             float* pq_off, uint8_t* pq_codes) {
+    const uint32_t m = ix->ins_n;
+    if (cell) memcpy(cell, ix->ins_cell, sizeof(uint32_t) * m);
+    if (off) memcpy(off, ix->ins_off, sizeof(float) * m);
+    if (codes) memcpy(codes, ix->ins_codes, (uint64_t)ix->nsq * m);
+    if (pq_off && ix->pq_nsq) memcpy(pq_off, ix->ins_pq_off, sizeof(float) * m);
+    if (pq_codes && ix->pq_nsq) memcpy(pq_codes, ix->ins_pq_codes, (uint64_t)ix->pq_nsq * m);
+    return m;
+}
+

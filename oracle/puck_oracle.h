@@ -92,6 +92,17 @@ void po_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* c
                     uint32_t fnsq, const float* pcb, uint32_t pnsq, float* f_off,
                     uint8_t* f_codes, float* p_off, uint8_t* p_codes);
 
+/* RealtimeInsertPuckIndex (realtime_insert_puck_index.cpp) on a loaded index:
+ * po_realtime_open switches the index to the realtime index's search (inserted points
+ * scanned per cell after its records; the second-level PQ rerank summed subspace by
+ * subspace), po_insert adds one point of d floats and returns its local id (n + insert
+ * id) or -1, po_inserted_records copies out the inserted records. Not thread-safe
+ * against concurrent searches. */
+int po_realtime_open(po_index* ix);
+int64_t po_insert(po_index* ix, const float* feature);
+uint32_t po_inserted_records(const po_index* ix, uint32_t* cell, float* off, uint8_t* codes,
+                             float* pq_off, uint8_t* pq_codes);
+
 /* k-means assignment step: nearest_center (kmeans.cpp:221-258). */
 void po_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* x,
                        uint64_t n, int32_t* assign, float* dis);

@@ -15,6 +15,7 @@
 #include "gflags/gflags.h"
 #include "puck/gflags/puck_gflags.h"
 #include "puck/puck/puck_index.h"
+#include "puck/puck/realtime_insert_puck_index.h"
 #include "puck/search_context.h"
 #include "pyapi_wrapper/py_api_wrapper.h"
 
@@ -120,6 +121,42 @@ int ref_search_one(void* h, const float* q, uint32_t topk, float* dist, uint32_t
     *result_num = resp.result_num;
     return rc;
 }
+
+// The reference's RealtimeInsertPuckIndex (puck/puck/realtime_insert_puck_index.cpp):
+// init() over an index directory holding the label file, insert() of one point, and
+// Index::search over the base and inserted points.
+void* ref_open_realtime() {
+    auto* p = new puck::RealtimeInsertPuckIndex();
+    if (p->init() != 0) {
+        delete p;
+        return nullptr;
+    }
+    return p;
+}
+
+int ref_realtime_insert(void* h, const float* feature, uint32_t dim, const char* label) {
+    puck::InsertRequest req;
+    req.label = label;
+    req.feature = feature;
+    req.dim = dim;
+    return static_cast<puck::RealtimeInsertPuckIndex*>(h)->insert(&req);
+}
+
+int ref_realtime_search(void* h, const float* q, uint32_t topk, float* dist, uint32_t* labels,
+                        uint32_t* result_num) {
+    puck::Request req;
+    req.topk = topk;
+    req.feature = q;
+    puck::Response resp;
+    resp.distance = dist;
+    resp.local_idx = labels;
+    resp.result_num = 0;
+    const int rc = static_cast<puck::RealtimeInsertPuckIndex*>(h)->search(&req, &resp);
+    *result_num = resp.result_num;
+    return rc;
+}
+
+void ref_close_realtime(void* h) { delete static_cast<puck::RealtimeInsertPuckIndex*>(h); }
 
 int ref_probe_sizes(void* h, uint32_t* search_coarse_count, uint32_t* filter_topk,
                     uint32_t* total_point_count) {

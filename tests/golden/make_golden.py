@@ -68,6 +68,14 @@ CASES = {
     # cluster_index.cpp:1516-1520). filter_nsq = 6 (its ip2cos rule, index_conf.cpp:132-141).
     "ip2cos_d23": dict(n=6000, d=23, C=16, F=16, norm=False, mix="raw", P=8, T=64, topk=10,
                        nq=64, dup=0, ip2cos=True),
+    # RealtimeInsertPuckIndex (realtime_insert_puck_index.cpp): 4000 base points, then 240
+    # inserts (near the data, far from it into cells empty in the base, and repeats into
+    # one cell), then searches through the reference's Index::search. 16 x 16 cells, so
+    # about half the cells are empty in the base.
+    "insert_pq_d16": dict(n=4000, d=16, C=16, F=16, norm=False, mix="int", P=4, T=64, topk=10,
+                          nq=48, dup=0, pq=True, insert=240),
+    "insert_flat_d16": dict(n=4000, d=16, C=16, F=16, norm=False, mix="int", P=4, T=64, topk=10,
+                            nq=48, dup=0, insert=240),
 }
 
 
@@ -102,8 +110,100 @@ def make_data(case, seed=0):
     return base, queries
 
 
+def insert_points(case, base, queries, seed=11):
+    """Points to insert: near the data, far from it, and repeats of a few."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m, d = case["insert"], case["d"]
+    near = base[rng.integers(0, base.shape[0], m // 2)] + rng.normal(0, 4, (m // 2, d))
+    far = rng.uniform(0, 255, (m // 4, d))
+    rep = np.repeat(near[:(m - m // 2 - m // 4) // 2], 2, axis=0)
+    pts = np.concatenate([near, far, rep])[:m]
+    return np.rint(np.clip(pts, 0, 255)).astype(np.float32)
+
+
+def run_insert_case(name):
+    """Base index by train()/build(); its files are kept as they are before any insert.
+    Then RealtimeInsertPuckIndex::init() over them (plus the label file), insert() of
+    every point in order, and Index::search of every query, one at a time."""
+    case = CASES[name]
+    base, queries = make_data(case)
+    ins = insert_points(case, base, queries)
+    # a third of the queries are inserted points, so their own records are found
+    queries = np.concatenate([ins[::max(1, ins.shape[0] // (case["nq"] // 3))][:case["nq"] // 3],
+                              queries[:case["nq"] - case["nq"] // 3]]).astype(np.float32)
+    lib = ctypes.CDLL(REF_LIB)
+    lib.ref_set_flag.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    lib.ref_open_realtime.restype = ctypes.c_void_p
+    lib.ref_realtime_insert.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                        ctypes.c_char_p]
+    lib.ref_realtime_search.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_uint32] + [
+        ctypes.c_void_p] * 3
+    lib.ref_close_realtime.argtypes = [ctypes.c_void_p]
+
+    def flag(k, v):
+        assert lib.ref_set_flag(k.encode(), str(v).encode()) == 0, k
+
+    n, d, m = case["n"], case["d"], case["insert"]
+    with tempfile.TemporaryDirectory() as tmp:
+        idx = os.path.join(tmp, "index")
+        os.makedirs(idx)
+        index_io.write_fvecs(os.path.join(idx, "all_data.feat.bin"), base)
+        flag("index_path", idx)
+        flag("feature_dim", d)
+        flag("coarse_cluster_count", case["C"])
+        flag("fine_cluster_count", case["F"])
+        flag("whether_norm", "true" if case["norm"] else "false")
+        flag("whether_pq", "true" if case.get("pq") else "false")
+        flag("kmeans_iterations_count", 2)
+        flag("train_points_count", n)
+        flag("pq_train_points_count", n)
+        flag("threads_count", 4)
+        flag("train_fea_file_name", os.path.join(tmp, "train_clusters.dat"))
+        flag("train_pq_file_name", os.path.join(tmp, "train_pq.dat"))
+        assert lib.ref_train_build() == 0, "reference train/build failed"
+        flag("search_coarse_count", case["P"])
+        flag("filter_topk", case["T"])
+        flag("topk", case["topk"])
+        flag("context_initial_pool_size", 2)
+        files = {}
+        for fn in sorted(os.listdir(idx)):
+            with open(os.path.join(idx, fn), "rb") as f:
+                files["file:" + fn] = np.frombuffer(f.read(), np.uint8)
+        lengths = {fn: os.path.getsize(os.path.join(idx, fn)) for fn in os.listdir(idx)}
+        with open(os.path.join(idx, "all_data.url"), "w") as f:
+            for i in range(n):
+                f.write(f"p{i}\n")
+        h = lib.ref_open_realtime()
+        assert h, "reference realtime init failed"
+        for i in range(m):
+            x = np.ascontiguousarray(ins[i])
+            assert lib.ref_realtime_insert(h, x.ctypes.data, d, f"i{i}".encode()) == 0, i
+        nq, k = queries.shape[0], case["topk"]
+        dist = np.zeros((nq, k), np.float32)
+        labels = np.full((nq, k), 0xFFFFFFFF, np.uint32)
+        rn = ctypes.c_uint32(0)
+        for i in range(nq):
+            q = np.ascontiguousarray(queries[i])
+            assert lib.ref_realtime_search(h, q.ctypes.data, k, dist[i].ctypes.data,
+                                           labels[i].ctypes.data, ctypes.byref(rn)) == 0, i
+        lib.ref_close_realtime(h)
+
+        def tail(fn):
+            with open(os.path.join(idx, fn), "rb") as f:
+                return np.frombuffer(f.read()[lengths[fn]:], np.uint8)
+        appended = {"appended:" + fn: tail(fn) for fn in lengths
+                    if fn in ("cell_assign.dat", "filter_data.dat", "pq_data.dat")}
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out, queries=queries, inserted=ins, dist=dist, labels=labels,
+                            params=np.array([case["P"], case["T"], case["topk"]], np.int64),
+                            **files, **appended)
+        print(f"{name}: wrote {out} ({os.path.getsize(out)} bytes)")
+
+
 def run_case(name):
     case = CASES[name]
+    if case.get("insert"):
+        return run_insert_case(name)
     base, queries = make_data(case)
     lib = ctypes.CDLL(REF_LIB)
     lib.ref_set_flag.argtypes = [ctypes.c_char_p, ctypes.c_char_p]

@@ -7,6 +7,7 @@ LUT, filter-heap layout (the reference leaves a full heap unsorted and the
 rerank walks it in that order), final distances and ids.
 """
 import numpy as np
+import pytest
 
 import oracle
 
@@ -143,3 +144,41 @@ def test_oracle_ip2cos_arrays_equal_files():
     assert (s1 == 0).all() and (s2 == 0).all()
     assert np.array_equal(_bits(d1), _bits(d2)) and np.array_equal(i1, i2)
     assert np.array_equal(_bits(d1), _bits(z["dist"])) and np.array_equal(i1, z["labels"])
+
+
+@pytest.mark.parametrize("name", ["insert_pq_d16", "insert_flat_d16"])
+def test_oracle_realtime_insert_matches_reference(name):
+    """RealtimeInsertPuckIndex (realtime_insert_puck_index.cpp): after the reference's own
+    base index, 240 inserts. The oracle's inserted records equal what the reference
+    appended to its index files (cell_assign.dat, filter_data.dat, pq_data.dat), and its
+    searches over base and inserted points equal the reference's Index::search, bit for
+    bit."""
+    import os
+    import tempfile
+    from puck_gb300 import index_io
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    P, T, k = [int(v) for v in z["params"]]
+    with tempfile.TemporaryDirectory() as tmp:
+        index_io.materialize_npz_index(z, tmp)
+        conf = index_io.read_index_conf(os.path.join(tmp, "index.dat"))
+        orc = oracle.OracleIndex(tmp)
+    orc.realtime_open()
+    n = conf["total_point_count"]
+    ids = [orc.insert(x) for x in z["inserted"]]
+    assert ids == list(range(n, n + len(ids)))
+    pq_nsq = conf["nsq"] if conf["whether_pq"] else 0
+    cell, off, codes, poff, pcodes = orc.inserted_records(pq_nsq)
+    ac = z["appended:cell_assign.dat"].view(np.uint32)
+    rec = z["appended:filter_data.dat"].reshape(len(ac), -1)
+    assert np.array_equal(cell, ac)
+    assert np.array_equal(_bits(off), rec[:, :4].copy().view(np.uint32).ravel())
+    assert np.array_equal(codes, rec[:, 4:4 + codes.shape[1]])
+    if pq_nsq:
+        prec = z["appended:pq_data.dat"].reshape(len(ac), -1)
+        assert np.array_equal(_bits(poff), prec[:, :4].copy().view(np.uint32).ravel())
+        assert np.array_equal(pcodes, prec[:, 4:4 + pq_nsq])
+    for i, q in enumerate(z["queries"]):
+        rc, d, ids_, rn, _ = orc.search_one(q, k, P, T, topk_max=k)
+        assert rc == 0
+        assert np.array_equal(_bits(d), _bits(z["dist"][i])), (name, i)
+        assert np.array_equal(ids_, z["labels"][i]), (name, i)
