@@ -833,6 +833,11 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
     for (uint32_t l = 0; l < P; ++l) {
         const uint32_t c = s->ctag[l];
         total += ix->cell_start[(uint64_t)c * F + F] - ix->cell_start[(uint64_t)c * F];
+        if (ix->realtime)
+            for (uint32_t f = 0; f < F; ++f) {
+                const uint64_t cell = (uint64_t)c * F + f;
+                total += ix->cell_cnt[cell] - (ix->cell_start[cell + 1] - ix->cell_start[cell]);
+            }
     }
     po_cand* cand = (po_cand*)malloc(sizeof(po_cand) * (total ? total : 1));
     uint64_t nc = 0;
@@ -847,6 +852,14 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
                 t = t + lookup_lut(ix->codes + (uint64_t)mi * nsq, s->lut, nsq);
                 cand[nc].t = t;
                 cand[nc].mi = mi;
+                ++nc;
+            }
+            /* realtime: the cell's inserted points, memory id n + insert id */
+            for (int32_t id = ix->realtime ? ix->ins_head[cell] : -1; id >= 0; id = ix->ins_next[id]) {
+                float t = (float)(2.0 * (double)cell_dist + (double)ix->ins_off[id]);
+                t = t + lookup_lut(ix->ins_codes + (uint64_t)id * nsq, s->lut, nsq);
+                cand[nc].t = t;
+                cand[nc].mi = ix->n + (uint32_t)id;
                 ++nc;
             }
         }
@@ -874,13 +887,15 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
         return 0;
     }
     for (uint32_t idx = 0; idx < cnt; ++idx) {
-        const float* x = ix->feat + (uint64_t)cand[idx].mi * d;
+        const uint32_t mi = cand[idx].mi;
+        const int ins = mi >= ix->n;
+        const float* x = ins ? ix->ins_feat + (uint64_t)(mi - ix->n) * d : ix->feat + (uint64_t)mi * d;
         float t = 0.0f;
         uint32_t m = 0;
         for (; m + 16 <= d && t < fin.val[1]; m += 16) t = t + l2sqr16(x + m, q + m);
         if (t < fin.val[1]) {
             if (d - m > 0) t = t + l2sqr_ext(x + m, q + m, d - m);
-            heap_update(&fin, t, ix->mem2local[cand[idx].mi]);
+            heap_update(&fin, t, ins ? mi : ix->mem2local[mi]);
         }
     }
     heap_reorder(&fin);

@@ -182,3 +182,30 @@ def test_oracle_realtime_insert_matches_reference(name):
         assert rc == 0
         assert np.array_equal(_bits(d), _bits(z["dist"][i])), (name, i)
         assert np.array_equal(ids_, z["labels"][i]), (name, i)
+
+
+def test_oracle_realtime_scan_mode_finds_inserted_points():
+    """The library's scan mode on a realtime index: every inserted point of a probed cell
+    is a candidate, so a query equal to an inserted point (the first third of the
+    golden queries) finds its own id at distance 0, as the exact walk does."""
+    import os
+    import tempfile
+    from puck_gb300 import index_io
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "insert_flat_d16.npz"))
+    P, T, k = [int(v) for v in z["params"]]
+    with tempfile.TemporaryDirectory() as tmp:
+        index_io.materialize_npz_index(z, tmp)
+        n = index_io.read_index_conf(os.path.join(tmp, "index.dat"))["total_point_count"]
+        orc = oracle.OracleIndex(tmp)
+    orc.realtime_open()
+    ins = z["inserted"]
+    for x in ins:
+        orc.insert(x)
+    nq = len(z["queries"]) // 3
+    for scan in (False, True):
+        d, ids, st = orc.search_batch(z["queries"][:nq], k, P, T, topk_max=k, scan=scan)
+        assert (st == 0).all()
+        for i in range(nq):
+            own = [n + j for j in range(len(ins)) if np.array_equal(ins[j], z["queries"][i])]
+            assert own and any(o in ids[i] for o in own), (scan, i)
+            assert d[i][0] == 0.0
