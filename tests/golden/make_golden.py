@@ -76,6 +76,9 @@ CASES = {
                           nq=48, dup=0, pq=True, insert=240),
     "insert_flat_d16": dict(n=4000, d=16, C=16, F=16, norm=False, mix="int", P=4, T=64, topk=10,
                             nq=48, dup=0, insert=240),
+    # the same on L2-normalised data (whether_norm): inserts are normalised by single_build
+    "insert_cos_d16": dict(n=4000, d=16, C=16, F=16, norm=True, mix="gauss", P=4, T=64, topk=10,
+                           nq=48, dup=0, pq=True, insert=240),
 }
 
 
@@ -111,14 +114,19 @@ def make_data(case, seed=0):
 
 
 def insert_points(case, base, queries, seed=11):
-    """Points to insert: near the data, far from it, and repeats of a few."""
+    """Points to insert: near the data, far from it, and repeats of a few (integer
+    data stays integer; other data is left unnormalised, the index normalises it)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     m, d = case["insert"], case["d"]
-    near = base[rng.integers(0, base.shape[0], m // 2)] + rng.normal(0, 4, (m // 2, d))
-    far = rng.uniform(0, 255, (m // 4, d))
+    integer = case["mix"] == "int"
+    scale = 4.0 if integer else 0.2
+    near = base[rng.integers(0, base.shape[0], m // 2)] + rng.normal(0, scale, (m // 2, d))
+    far = rng.uniform(0, 255, (m // 4, d)) if integer else rng.normal(0, 3, (m // 4, d))
     rep = np.repeat(near[:(m - m // 2 - m // 4) // 2], 2, axis=0)
     pts = np.concatenate([near, far, rep])[:m]
-    return np.rint(np.clip(pts, 0, 255)).astype(np.float32)
+    if integer:
+        pts = np.rint(np.clip(pts, 0, 255))
+    return pts.astype(np.float32)
 
 
 def run_insert_case(name):

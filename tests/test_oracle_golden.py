@@ -146,7 +146,7 @@ def test_oracle_ip2cos_arrays_equal_files():
     assert np.array_equal(_bits(d1), _bits(z["dist"])) and np.array_equal(i1, z["labels"])
 
 
-@pytest.mark.parametrize("name", ["insert_pq_d16", "insert_flat_d16"])
+@pytest.mark.parametrize("name", ["insert_pq_d16", "insert_flat_d16", "insert_cos_d16"])
 def test_oracle_realtime_insert_matches_reference(name):
     """RealtimeInsertPuckIndex (realtime_insert_puck_index.cpp): after the reference's own
     base index, 240 inserts. The oracle's inserted records equal what the reference
