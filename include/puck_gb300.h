@@ -167,8 +167,9 @@ int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
 /* Per-stage device timing (CUDA events recorded on the launching stream around
  * each kernel). With profiling enabled, pgpu_stage_times returns, for the last
  * search call, the milliseconds spent in each stage, summed over its passes:
- * 0 query prep, 1 coarse scores, 2 coarse select (+ the learned probe), 3 fine scores, 4 fine order,
- * 5 cell walk + ADC scan, 6 rerank. It waits for the call's work to finish. */
+ * 0 query prep, 1 coarse scores, 2 coarse select (+ the learned probe), 3 fine scores, 4 fine order
+ * (exact mode) or the scan's block launch order (scan mode), 5 cell walk (exact mode) or ADC scan
+ * (scan mode: k_scan_select alone), 6 rerank. It waits for the call's work to finish. */
 #define PGPU_NUM_STAGES 7
 int pgpu_set_profiling(pgpu_index* index, int enable);
 int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);
@@ -267,7 +268,8 @@ int pgpu_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* 
                      float* pq_offsets, uint8_t* pq_codes, void* stream);
 
 /* The k-means assignment step of pgpu_nearest_center, allocating no device
- * memory. No counterpart in the reference: it exists for callers that must not
+ * memory, on the exact SIMT kernel (same results bit for bit as the tensor-core
+ * screen + exact window of pgpu_nearest_center, lower throughput). No counterpart in the reference: it exists for callers that must not
  * allocate GPU memory (a process that hands out device memory from its own pool,
  * or code that must not enter the CUDA allocator). pgpu_nearest_center allocates
  * its norm scratch on every call; this variant keeps it in a fixed array inside
@@ -275,9 +277,10 @@ int pgpu_puck_assign(uint32_t d, uint64_t n, const float* base, const uint32_t* 
  * exit), so it takes at most 1048576 points and 65536 centroids per call
  * (PGPU_E_LIMIT beyond). It runs on the calling thread's current device; its
  * first call on a device looks up the array's device address and should come
- * before any stream capture. All calls on a device share the array: calls whose
- * work overlaps on the GPU race and must be serialised by the caller. Results
- * are identical to pgpu_nearest_center's. */
+ * before any stream capture; the address is kept for the life of the process, so
+ * the library must not be used on a device across cudaDeviceReset. All calls on
+ * a device share the array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller. Results are identical to pgpu_nearest_center's. */
 int pgpu_nearest_center_noalloc(uint32_t dim, const float* centroids, uint64_t k,
                                 const float* points, uint64_t n, int32_t* assign,
                                 float* distance, void* stream);

@@ -34,10 +34,19 @@ def build_oracle(force=False):
     return LIB_PATH
 
 
-def build_reference(native=False):
-    """Compile the reference's own sources from /root/reference (x86 only)."""
-    ref = "/root/reference"
-    if not os.path.isdir(ref):
+def reference_dir():
+    """Where the reference's sources are: the PUCK_REFERENCE_DIR environment
+    variable (None when it is unset or not a directory)."""
+    ref = os.environ.get("PUCK_REFERENCE_DIR", "")
+    return ref if ref and os.path.isdir(ref) else None
+
+
+def build_reference(native=False, ref=None):
+    """Compile the reference's own sources (x86 only) from `ref`, by default the
+    PUCK_REFERENCE_DIR environment variable; returns None when neither names a
+    directory."""
+    ref = ref or reference_dir()
+    if ref is None or not os.path.isdir(ref):
         return None
     target = "native" if native else "all"
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref}", "-j8",

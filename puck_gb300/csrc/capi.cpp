@@ -98,7 +98,8 @@ int check_config(const pgpu_index* h, const pgpu_params* p) {
     if (h != nullptr) {
         const bool bf16 = p->precision == PGPU_PRECISION_BF16;
         if (pgpu::walk_smem_bytes(h->ix, p->filter_topk) > 220 * 1024 ||
-            (bf16 ? pgpu::scan_smem_bytes_half(h->ix) : pgpu::scan_smem_bytes(h->ix)) > 220 * 1024 ||
+            (bf16 ? pgpu::scan_smem_bytes_half(h->ix, (uint32_t)keep)
+                  : pgpu::scan_smem_bytes(h->ix, (uint32_t)keep)) > 220 * 1024 ||
             (bf16 && h->ix.pq_nsq == 0
                  ? pgpu::rerank_screen_smem_bytes(h->ix, (uint32_t)keep, p->topk)
                   : pgpu::rerank_smem_bytes(h->ix, (uint32_t)keep, p->topk)) > 220 * 1024)
@@ -119,9 +120,12 @@ void apply_config(pgpu_index* h, const pgpu_params* p) {
 }
 
 int ensure_precision_data(pgpu_index* h) {
-    // the BF16 screen reranks original vectors; a PQ index reranks by its PQ
-    if (h->cfg.precision != PGPU_PRECISION_BF16 || h->ix.pq_nsq != 0) return PGPU_OK;
+    if (h->cfg.precision != PGPU_PRECISION_BF16) return PGPU_OK;
     std::string err;
+    // the scan's rotated code copy (one table bank per subspace)
+    if (int rc = pgpu::ensure_rotated_codes(&h->ix, &err)) return fail(rc, err);
+    // the BF16 screen reranks original vectors; a PQ index reranks by its PQ
+    if (h->ix.pq_nsq != 0) return PGPU_OK;
     if (int rc = pgpu::ensure_bf16_features(&h->ix, &err)) return fail(rc, err);
     return PGPU_OK;
 }

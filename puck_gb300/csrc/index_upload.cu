@@ -184,4 +184,40 @@ int ensure_bf16_features(DeviceIndex* ix, std::string* err) {
     return PGPU_OK;
 }
 
+// out[r][s] = in[r][(s + r mod nsq) mod nsq] for s < nsq (stride == nsq).
+__global__ void k_rotate_codes(const uint8_t* __restrict__ in, uint64_t n, uint32_t nsq,
+                               uint8_t* __restrict__ out) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const uint32_t rho = (uint32_t)(r % nsq);
+    const uint8_t* src = in + r * nsq;
+    uint8_t* dst = out + r * nsq;
+    for (uint32_t s = 0; s < nsq; ++s) {
+        const uint32_t m = s + rho < nsq ? s + rho : s + rho - nsq;
+        dst[s] = src[m];
+    }
+}
+
+int ensure_rotated_codes(DeviceIndex* ix, std::string* err) {
+    if (ix->codes_rot != nullptr || ix->nsq % 4 != 0 || ix->nsq > 32 ||
+        ix->code_stride != ix->nsq || ix->n == 0)
+        return PGPU_OK;
+    uint64_t bytes = 0;
+    cudaError_t e = dev_alloc(&ix->codes_rot, (uint64_t)ix->n * ix->code_stride, &bytes);
+    if (e == cudaSuccess) {
+        k_rotate_codes<<<(unsigned)((ix->n + 255) / 256), 256>>>(ix->codes, ix->n, ix->nsq,
+                                                                 ix->codes_rot);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        if (ix->codes_rot) cudaFree(ix->codes_rot);
+        ix->codes_rot = nullptr;
+        *err = std::string("rotated code copy: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
+    }
+    ix->bytes += bytes;
+    return PGPU_OK;
+}
+
 }  // namespace pgpu

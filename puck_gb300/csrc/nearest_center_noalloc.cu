@@ -7,8 +7,13 @@
 // own pool and must not be fragmented, code that runs where the CUDA allocator
 // must not be entered, or a tight build loop that should never touch the
 // allocator. This entry point keeps the same scratch in a fixed array that is
-// part of the library image on the GPU instead, and is otherwise the same
-// computation: same kernels, same results bit for bit.
+// part of the library image on the GPU instead. It runs the exact SIMT kernel
+// (k_nearest_center: one sequential FP32 dot per pair, strict-< scan, first
+// index wins ties), not the tensor-core screen + exact window of
+// pgpu_nearest_center. Both compute every candidate distance in the same FP32
+// order with the same tie rule, so the results are the same bit for bit; the
+// throughput is not: at its size limit this variant is a SIMT contraction of
+// 65,536 centroids by 2^20 points, far slower than the tensor-core path.
 //
 // Costs and rules of the fixed array:
 //   * it holds kMaxPoints + kMaxCentroids floats (4.25 MiB), reserved on every
@@ -17,6 +22,10 @@
 //   * the device address of the array is looked up once per device, on the
 //     first call made with that device current (cudaGetSymbolAddress), so that
 //     first call must come before any stream capture on that device;
+//   * the looked-up address is kept for the life of the process: the library
+//     must not be used on a device across cudaDeviceReset (or any other
+//     teardown of the device's primary context), which reloads the module and
+//     moves the array;
 //   * every call on a device shares the array and its contents outlive the call:
 //     calls whose work overlaps on the GPU (different streams, or concurrent
 //     host threads) race on it and must be serialised by the caller. Nothing in

@@ -78,6 +78,8 @@ struct DeviceIndex {
     uint16_t* rec_fine = nullptr;   // [n] fine id of the cell each record belongs to
     float* offsets = nullptr;       // [n] filter offset per point
     uint8_t* codes = nullptr;       // [n][code_stride]
+    uint8_t* codes_rot = nullptr;   // [n][code_stride] precision-form scan copy: record r's
+                                    // codes rotated by r mod nsq (made on first use)
     float* feat = nullptr;          // [n][d] original vectors
     uint16_t* feat_bf16 = nullptr;  // [n][d] BF16 copy (precision form; made on first use)
     float* feat_abs = nullptr;      // [n] |x| rounded up (error bound of the BF16 screen)
@@ -108,7 +110,6 @@ struct Scratch {
     uint32_t* hcnt = nullptr;  // [B]
     unsigned long long* counters = nullptr; // [kNumWalkCounters] walk diagnostics
     int* tc_err = nullptr;     // set by a tensor-core contraction or table copy whose wait expired
-    unsigned char* luts = nullptr; // scan mode: [B][nsq*256] lookup tables (FP32, or FP16)
     uint16_t* ph1 = nullptr;   // probe hidden activations [B][h], BF16 (with a probe attached)
     uint16_t* ph2 = nullptr;
     int32_t* pconf = nullptr;  // [B] 1 where the probe chose the clusters (null: no probe)
@@ -185,13 +186,18 @@ cudaError_t launch_to_bf16(const float* x, uint64_t n, uint16_t* y, cudaStream_t
 cudaError_t launch_cell_constants(float* stationary, const uint32_t* cell_start, float* mdo,
                                   uint32_t C, uint32_t F, float empty_value, cudaStream_t stream);
 size_t walk_smem_bytes(const DeviceIndex& ix, uint32_t T);
-size_t scan_smem_bytes(const DeviceIndex& ix);
+size_t scan_smem_bytes(const DeviceIndex& ix, uint32_t T);
 uint32_t scan_max_filter_topk();
+// Scan mode: the blocks' launch order (longest scans first), then the scan itself.
+cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
 cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                cudaStream_t stream);
-size_t scan_smem_bytes_half(const DeviceIndex& ix);
+size_t scan_smem_bytes_half(const DeviceIndex& ix, uint32_t T);
 // BF16 copy of the vectors and their norms (precision form), synchronous.
 int ensure_bf16_features(DeviceIndex* ix, std::string* err);
+// The precision form's rotated copy of the filter codes (nsq a multiple of 4, at
+// most 32; otherwise nothing is made), synchronous.
+int ensure_rotated_codes(DeviceIndex* ix, std::string* err);
 size_t rerank_screen_smem_bytes(const DeviceIndex& ix, uint32_t T, uint32_t topk);
 cudaError_t launch_rerank_screen(const DeviceIndex& ix, uint32_t n, uint32_t topk, const Scratch& s,
                                  float* out_dist, uint32_t* out_ids, int32_t* out_status,

@@ -34,7 +34,7 @@ void ensure_max_dynamic_smem(const void* kernel, int bytes) {
 
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qb, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
-                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err, s->luts,
+                    s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err,
                     s->ph1, s->ph2, s->pconf, s->pz, s->order, s->wbucket};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -45,7 +45,7 @@ uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t 
     const uint64_t P = cfg.coarse_slots(ix.C), T = cfg.filter_keep();
     const uint64_t probe = cfg.probe ? (uint64_t)B * (cfg.probe->h * 4 + 4 + ix.C * 4ull) : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
-    const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * (ix.nsq * 256 * 4 + 5) : 0;
+    const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * 5 : 0;  // launch order
     return (uint64_t)B * (ix.d * 6 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
            fine_order + tables + probe + kNumWalkCounters * 8 + 4;
 }
@@ -78,7 +78,6 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     PGPU_ALLOC(s.counters, kNumWalkCounters);
     PGPU_ALLOC(s.tc_err, 1);
     if (cfg.mode == PGPU_MODE_SCAN) {
-        PGPU_ALLOC(s.luts, (uint64_t)B * ix.nsq * 256 * 4);
         PGPU_ALLOC(s.order, B);
         PGPU_ALLOC(s.wbucket, B);
     }
@@ -155,6 +154,8 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
         PGPU_STEP(launch_topsort_status(s.dots, n, ix.F, ix.F, ix.F, s.fdist, s.ftag, s.status, st),
                   "fine order");
         k = 7;
+    } else {
+        PGPU_STEP(launch_scan_order(ix, n, s, st), "scan order");
     }
     mark(5);
     if (cfg.mode == PGPU_MODE_EXACT) {
@@ -170,8 +171,8 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     }
     mark(7);
 #undef PGPU_STEP
-    // scan mode adds the tables and the two launch-order kernels
-    if (launched) *launched = k + probe_kernels + (cfg.mode == PGPU_MODE_SCAN ? 3 : 0);
+    // scan mode adds the two launch-order kernels
+    if (launched) *launched = k + probe_kernels + (cfg.mode == PGPU_MODE_SCAN ? 2 : 0);
     return cudaSuccess;
 }
 

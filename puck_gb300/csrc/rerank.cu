@@ -46,7 +46,7 @@ constexpr int kThreads = PGPU_RERANK_THREADS;
 constexpr int kWarps = kThreads / 32;
 constexpr int kScreenThreads = PGPU_RERANK_SCREEN_THREADS;
 constexpr int kScreenWarps = kScreenThreads / 32;
-constexpr int kRows = 8;  // candidate rows per warp in flight
+constexpr int kRows = 8;  // candidate rows per warp in flight (rows8_l2_exact)
 
 struct RerankParams {
     const float* q;
@@ -132,6 +132,93 @@ __device__ __forceinline__ void warp_l2_exact(const float* const* rows, const fl
     }
 #pragma unroll
     for (int u = 0; u < G; ++u) out[u] = t[u];
+}
+
+// The same sums as warp_l2_exact for G = 8 rows, d % 4 == 0 and 16-byte aligned
+// rows and q: each group of 8 lanes measures two rows with 16-byte loads (lane l
+// holds the float4s l, l + 8, ...), so a warp load instruction covers four whole
+// 128-byte row segments. In one 16-dim chunk the four lanes holding float4s
+// 0..3 pair dims i and i + 8 by one exchange (lane u <-> u + 2), lane 0 sums
+// s0..s3 left to right and lane 1 continues with s4..s7 after one more
+// exchange, so each chunk sum keeps the L2Sqr16Ext order; the running total is
+// kept on lane 1 of the group, chunk by chunk in order. Results on every lane.
+__device__ __forceinline__ void warp_l2_exact_vec(const float* const* rows, const float* q,
+                                                  uint32_t d, int lane, float* out) {
+    constexpr int R = 2;  // rows per group of 8 lanes
+    const int g = lane >> 3, l = lane & 7;
+    const uint32_t d16 = d & ~15u;
+    const uint32_t nf4 = d16 >> 2;
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    // this group's rows g and g + 4 (selects on constant indices keep them in registers)
+    const float* mine[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        mine[r] = g == 0 ? rows[4 * r] : g == 1 ? rows[4 * r + 1] : g == 2 ? rows[4 * r + 2] : rows[4 * r + 3];
+    float t[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) t[r] = 0.0f;
+    for (uint32_t f0 = 0; f0 < nf4; f0 += 8) {
+        const uint32_t f = f0 + l;
+        const bool in = f < nf4;
+        float4 x[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            x[r] = in ? __ldg(reinterpret_cast<const float4*>(mine[r]) + f)
+                      : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 qq = in ? q4[f] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool second = f0 + 4 < nf4;  // this step holds two chunks
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float a0 = __fsub_rn(x[r].x, qq.x), a1 = __fsub_rn(x[r].y, qq.y);
+            const float a2 = __fsub_rn(x[r].z, qq.z), a3 = __fsub_rn(x[r].w, qq.w);
+            const float q0 = __fmul_rn(a0, a0), q1 = __fmul_rn(a1, a1);
+            const float q2 = __fmul_rn(a2, a2), q3 = __fmul_rn(a3, a3);
+            // lanes u = 0, 1 of a chunk: d_i^2 + d_{i+8}^2 with the partner u + 2
+            const float s0 = __fadd_rn(q0, __shfl_xor_sync(0xffffffffu, q0, 2));
+            const float s1 = __fadd_rn(q1, __shfl_xor_sync(0xffffffffu, q1, 2));
+            const float s2 = __fadd_rn(q2, __shfl_xor_sync(0xffffffffu, q2, 2));
+            const float s3 = __fadd_rn(q3, __shfl_xor_sync(0xffffffffu, q3, 2));
+            const float a = __fadd_rn(__fadd_rn(__fadd_rn(s0, s1), s2), s3);   // lane u = 0
+            const float b = __shfl_xor_sync(0xffffffffu, a, 1);                 // to lane u = 1
+            const float chunk = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b, s0), s1), s2), s3);
+            const float hi = __shfl_down_sync(0xffffffffu, chunk, 4);           // lane 5 -> 1
+            float tr = __fadd_rn(t[r], chunk);
+            if (second) tr = __fadd_rn(tr, hi);
+            t[r] = tr;
+        }
+    }
+    if (d16 < d && l == 1) {  // L2SqrExt on the last d - d16 (a multiple of 4) dims
+        const uint32_t qty = d - d16;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float* xr = mine[r] + d16;
+            const float* qr = q + d16;
+            float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f, l3 = 0.0f;
+            for (uint32_t i = 0; i + 4 <= qty; i += 4) {
+                const float a0 = __fsub_rn(__ldg(xr + i), qr[i]);
+                const float a1 = __fsub_rn(__ldg(xr + i + 1), qr[i + 1]);
+                const float a2 = __fsub_rn(__ldg(xr + i + 2), qr[i + 2]);
+                const float a3 = __fsub_rn(__ldg(xr + i + 3), qr[i + 3]);
+                l0 = __fadd_rn(l0, __fmul_rn(a0, a0));
+                l1 = __fadd_rn(l1, __fmul_rn(a1, a1));
+                l2 = __fadd_rn(l2, __fmul_rn(a2, a2));
+                l3 = __fadd_rn(l3, __fmul_rn(a3, a3));
+            }
+            t[r] = __fadd_rn(t[r], __fadd_rn(__fadd_rn(__fadd_rn(l0, l1), l2), l3));
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) out[u] = __shfl_sync(0xffffffffu, t[u >> 2], 8 * (u & 3) + 1);
+}
+
+// Dispatch: the vector form when d % 4 == 0 and q is 16-byte aligned (rows then
+// are: the vectors start 256-byte aligned with d * 4 bytes per row).
+__device__ __forceinline__ void rows8_l2_exact(const float* const* rows, const float* q, uint32_t d,
+                                               int lane, float* out) {
+    if ((d & 3u) == 0 && (reinterpret_cast<uintptr_t>(q) & 15u) == 0)
+        warp_l2_exact_vec(rows, q, d, lane, out);
+    else
+        warp_l2_exact<8>(rows, q, d, lane, out);
 }
 
 // PQ: the second-level PQ branch of rank_topN_points (puck_index.cpp:402-427): per
@@ -227,7 +314,7 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
             rows[u] = p.feat + (uint64_t)tags[j < cnt ? j : j0] * p.d;
         }
         float v[kRows];
-        warp_l2_exact<kRows>(rows, qv, p.d, lane, v);
+        rows8_l2_exact(rows, qv, p.d, lane, v);
         if (lane == 0) {
 #pragma unroll
             for (int u = 0; u < kRows; ++u)
@@ -489,7 +576,7 @@ __global__ __launch_bounds__(kScreenThreads, PGPU_RERANK_SCREEN_MIN_BLOCKS) void
                 rows[u] = p.feat + (uint64_t)tags[(uint32_t)keys[i < m ? i : i0]] * d;
             }
             float v[kRows];
-            warp_l2_exact<kRows>(rows, qv, d, lane, v);
+            rows8_l2_exact(rows, qv, d, lane, v);
             __syncwarp();
             if (lane == 0) {
 #pragma unroll
@@ -531,7 +618,7 @@ __global__ __launch_bounds__(kScreenThreads, PGPU_RERANK_SCREEN_MIN_BLOCKS) void
             rows[u] = p.feat + (uint64_t)tags[j < cnt ? j : j0] * d;
         }
         float v[kRows];
-        warp_l2_exact<kRows>(rows, qv, d, lane, v);
+        rows8_l2_exact(rows, qv, d, lane, v);
         if (lane == 0) {
 #pragma unroll
             for (int u = 0; u < kRows; ++u)

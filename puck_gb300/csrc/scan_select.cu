@@ -11,22 +11,41 @@
 // cluster is skipped: the result is the exact top-filter_topk by (t, memory id)
 // over all records of the probed clusters, a superset search of the same cells.
 //
-// Selection: a buffer of (t, id) keys in shared memory with a running threshold
-// tau, a key with at least filter_topk kept keys at or below it; records whose
-// (2*cell_dist + offset, id) key is not below tau are dropped before the table
-// lookups (t can only grow). When the buffer could not take another round, an
-// MSB radix select (two digit passes) finds a new bound and the keys above it are
-// dropped. A last exact select leaves the set of the filter_topk smallest (t, id)
-// keys, unordered.
+// Table: each block builds its query's table in shared memory
+// (get_dist_table, quantization.cpp:260-270, in the reference's lane order):
+// thread j computes codeword j of every subspace from one coalesced 16-byte
+// codebook load per subspace (the codebook stays in L2).
+//
+// Selection: a buffer of (t, id) keys in shared memory, sized from filter_topk,
+// with a running threshold tau, a key with at least filter_topk kept keys below
+// it; records whose (2*cell_dist + offset, id) key is not below tau are dropped
+// before the table lookups (t can only grow). When the buffer could not take
+// another round, one histogram pass over the buffer's float values (1024 linear
+// bins between the smallest and the largest) finds the bin holding the
+// filter_topk-th key; the keys above that bin are dropped and tau becomes the
+// bin's upper edge. A last exact radix select leaves the set of the filter_topk
+// smallest (t, id) keys, unordered.
 //
 // Blocks start in launch order longest scan first (k_scan_work, k_scan_order),
 // one block per query.
 //
-// Precision form (HALF): the table is stored in FP16, scaled per query by a
+// Precision form (FP16 tables): the table is stored in FP16, scaled per query by a
 // power of two 2^e chosen from the bound (|q| + max |codeword|)^2 >= every entry
 // so that all entries stay below 32768; lookups are accumulated in FP32 and the
 // sum is multiplied by 2^-e. Entries are non-negative, so t >= t0 still holds and
 // the threshold test before the lookups stays valid.
+//
+// Rotated layout (precision form, nsq a multiple of 4 and at most 32): the FP32
+// table's lookups are random 4-byte gathers, and all 32 lanes of a warp read the
+// same subspace's 1 KB table at once, so they collide in shared-memory banks
+// (about 3.4 wavefronts per warp-wide lookup). Here subspace m's table lives in
+// bank m alone (FP16 entries c and c+1 share a word: byte address
+// (c >> 1) * 128 + 4m + 2 (c & 1)), and record r's codes are stored rotated by
+// r mod nsq (DeviceIndex::codes_rot), so at lookup step s a lane reads byte s and
+// looks up subspace (s + r mod nsq) mod nsq: consecutive records, on consecutive
+// lanes, hit distinct banks (lanes L and L + nsq share one; two wavefronts per
+// lookup at nsq = 24, one at 32). The precision form sums in FP32 in this
+// rotated order (its error bound does not depend on the order).
 #include <cuda_fp16.h>
 
 #include "device_common.cuh"
@@ -37,23 +56,32 @@ namespace {
 
 // Block shape of the scan (compile-time; -D overrides for tuning sweeps).
 #ifndef PGPU_SCAN_THREADS
-#define PGPU_SCAN_THREADS 128
+#define PGPU_SCAN_THREADS 256
 #endif
 #ifndef PGPU_SCAN_RECORDS
 #define PGPU_SCAN_RECORDS 4
 #endif
-#ifndef PGPU_SCAN_CAP
-#define PGPU_SCAN_CAP 1792
-#endif
 #ifndef PGPU_SCAN_MIN_BLOCKS
-#define PGPU_SCAN_MIN_BLOCKS 8
+#define PGPU_SCAN_MIN_BLOCKS 3
 #endif
 constexpr int kThreads = PGPU_SCAN_THREADS;
 constexpr int kRecPerThread = PGPU_SCAN_RECORDS;
 constexpr int kRound = kThreads * kRecPerThread;  // records per round
-constexpr uint32_t kCandCap = PGPU_SCAN_CAP;      // candidate buffer (keys)
-static_assert(kCandCap % kThreads == 0 && kCandCap > (uint32_t)kRound,
-              "the buffer holds a round beyond the kept keys");
+// Candidate buffer: at most kMaxCap keys (kCapPer per thread in the compaction);
+// sized per launch from filter_topk (scan_cap).
+constexpr int kCapPer = 16;
+constexpr uint32_t kMaxCap = kThreads * kCapPer;
+constexpr uint32_t kHistBins = 1024;  // bins of the cut-back histogram
+static_assert(kHistBins % kThreads == 0, "bins split evenly over the threads");
+
+// Buffer size for filter_topk T: T + a round + room for max(1024, T) more keys
+// before the next cut, in whole multiples of the block, at most kMaxCap.
+__host__ __device__ inline uint32_t scan_cap(uint32_t T) {
+    uint32_t room = T > 1024 ? T : 1024;
+    uint32_t c = T + kRound + room;
+    c = (c + kThreads - 1) / kThreads * kThreads;
+    return c > kMaxCap ? kMaxCap : c;
+}
 
 struct ScanParams {
     const float* q;
@@ -70,12 +98,11 @@ struct ScanParams {
     const uint16_t* rec_fine; // [n] fine id of each record
     const float* offsets;
     const uint8_t* codes;
+    const uint8_t* codes_rot;   // rotated copy (kTabRot)
     const float* codebook;
     unsigned long long* counters;
-    const unsigned char* luts;  // [B][lut_bytes] tables from k_build_luts
     const uint32_t* order;      // [B] query of each block
-    int* err;                   // set when the table copy did not arrive in time
-    uint32_t d, C, F, nsq, lsq, code_stride, P, T, lut_bytes;
+    uint32_t d, C, F, nsq, lsq, code_stride, P, T, cap;
     float codebook_max;
 };
 
@@ -88,61 +115,49 @@ __device__ __forceinline__ int half_lut_exponent(float qnorm, float codebook_max
     return e < -60 ? -60 : (e > 60 ? 60 : e);
 }
 
-// get_dist_table (quantization.cpp:260-270) for a batch: kLutQueries queries per
-// block, thread j computes codeword j of every subspace for each of them (coalesced
-// 16-byte codebook loads, 8 subspaces in flight, each codeword loaded once for the
-// block's queries), in the reference's lane order (l2sqr_sse).
-constexpr uint32_t kLutQueries = 8;
-template <bool HALF>
-__global__ __launch_bounds__(256) void k_build_luts(const float* __restrict__ q,
-                                                    const float* __restrict__ qnorm,
-                                                    const int32_t* __restrict__ status,
-                                                    const float* __restrict__ cb, uint32_t n,
-                                                    uint32_t d, uint32_t nsq, uint32_t lsq,
-                                                    float codebook_max,
-                                                    unsigned char* __restrict__ luts) {
-    __shared__ float qs[kLutQueries][kMaxDim];
-    __shared__ float qscale[kLutQueries];
-    __shared__ int qok[kLutQueries];
-    const uint32_t q0 = blockIdx.x * kLutQueries, j = threadIdx.x;
-    const uint32_t nq = n - q0 < kLutQueries ? n - q0 : kLutQueries;
-    for (uint32_t t = j; t < nq * d; t += 256) qs[t / d][t % d] = q[(uint64_t)q0 * d + t];
-    if (j < nq) {
-        qok[j] = status[q0 + j] == 0;
-        qscale[j] = HALF ? ldexpf(1.0f, half_lut_exponent(qnorm[q0 + j], codebook_max)) : 1.0f;
-    }
-    __syncthreads();
-    auto store = [&](uint32_t u, uint32_t m, float v) {
-        const uint64_t at = (uint64_t)(q0 + u) * nsq * 256 + m * 256 + j;
-        if (HALF) reinterpret_cast<__half*>(luts)[at] = __float2half_rn(v * qscale[u]);
-        else reinterpret_cast<float*>(luts)[at] = v;
-    };
-    if (lsq == 4) {
-        const float4* cb4 = reinterpret_cast<const float4*>(cb);
-        for (uint32_t m0 = 0; m0 < nsq; m0 += 8) {
-            float4 y[8];
+// get_dist_table (quantization.cpp:260-270) for one query into shared memory:
+// thread j computes codeword j of every subspace (one coalesced 16-byte codebook
+// load per subspace when lsq = 4), in the reference's lane order (l2sqr_sse).
+// Table variants: FP32 (the reference's values and order), FP16 in the same
+// layout, FP16 in the rotated one-bank-per-subspace layout.
+enum { kTabF32 = 0, kTabF16 = 1, kTabRot = 2 };
+
+template <int TAB>
+__device__ __forceinline__ void build_table(void* lut, const float* qv,
+                                            const float* __restrict__ cb, uint32_t nsq,
+                                            uint32_t lsq, float scale) {
+    for (uint32_t j = threadIdx.x; j < 256; j += kThreads) {
+        auto store = [&](uint32_t m, float v) {
+            if (TAB == kTabRot)
+                *reinterpret_cast<__half*>(reinterpret_cast<unsigned char*>(lut) + (j >> 1) * 128 +
+                                           4 * m + 2 * (j & 1)) = __float2half_rn(v * scale);
+            else if (TAB == kTabF16)
+                reinterpret_cast<__half*>(lut)[m * 256 + j] = __float2half_rn(v * scale);
+            else
+                reinterpret_cast<float*>(lut)[m * 256 + j] = v;
+        };
+        if (lsq == 4) {
+            const float4* cb4 = reinterpret_cast<const float4*>(cb);
+            for (uint32_t m0 = 0; m0 < nsq; m0 += 8) {
+                float4 y[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (m0 + u < nsq) y[u] = __ldg(cb4 + (uint64_t)(m0 + u) * 256 + j);
-            for (uint32_t qq = 0; qq < nq; ++qq) {
-                if (!qok[qq]) continue;
+                for (int u = 0; u < 8; ++u)
+                    if (m0 + u < nsq) y[u] = __ldg(cb4 + (uint64_t)(m0 + u) * 256 + j);
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     const uint32_t m = m0 + u;
                     if (m >= nsq) break;
-                    const float* x = qs[qq] + m * 4;
+                    const float* x = qv + m * 4;
                     const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
                     const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
-                    store(qq, m, __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
-                                           __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3))));
+                    store(m, __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                       __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3))));
                 }
             }
+        } else {
+            for (uint32_t m = 0; m < nsq; ++m)
+                store(m, l2sqr_sse(qv + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq));
         }
-    } else {
-        for (uint32_t m = 0; m < nsq; ++m)
-            for (uint32_t qq = 0; qq < nq; ++qq)
-                if (qok[qq])
-                    store(qq, m, l2sqr_sse(qs[qq] + m * lsq, cb + ((uint64_t)m * 256 + j) * lsq, lsq));
     }
 }
 
@@ -161,6 +176,29 @@ __device__ __forceinline__ float lut_sum_words_half(const uint32_t (&w)[NW], con
         if (m + 3 < nsq) a3 += __half2float(lut[(m + 3) * 256 + (c >> 24)]);
     }
     return (a0 + a1) + (a2 + a3);
+}
+
+// Sum of the record's table entries in the rotated layout: byte s of the rotated
+// codes is subspace (s + rho) mod nsq, whose entries sit in bank (s + rho) mod nsq.
+// nsq == 4 * NW. FP32 accumulation in the rotated order.
+template <int NW>
+__device__ __forceinline__ float lut_sum_rot(const uint32_t (&w)[NW], const unsigned char* lut,
+                                             uint32_t nsq, uint32_t rho) {
+    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t mb = 4u * rho;  // byte offset of the current subspace's bank
+    const uint32_t wrap = 4u * nsq;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t c = (w[i] >> (8 * j)) & 0xffu;
+            const uint32_t addr = ((c >> 1) << 7) + ((c & 1u) << 1) + mb;
+            a[j] += __half2float(*reinterpret_cast<const __half*>(lut + addr));
+            mb += 4u;
+            mb = mb == wrap ? 0u : mb;
+        }
+    }
+    return (a[0] + a[1]) + (a[2] + a[3]);
 }
 
 __device__ __forceinline__ float key_value(uint64_t k) {
@@ -287,22 +325,94 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
     return prefix;
 }
 
-// Keeps the keys <= kth (exactly K of them, in arbitrary order) at the front;
-// returns nothing, every thread must call it. `cnt` is a shared counter.
-template <int PER>
-__device__ void block_compact_le(uint64_t* keys, uint32_t count, uint64_t kth, uint32_t* cnt) {
-    const int tid = threadIdx.x, lane = tid & 31;
-    uint64_t mine[PER];
+// Cut-back bound of the buffer: keys[0..count) hold at least K keys. One pass
+// of a kHistBins-bin histogram of the keys' float parts, linear between the
+// smallest and the largest, finds the bin holding the K-th smallest; the result
+// is the (exclusive) upper edge of that bin as a key: at least K keys lie below
+// it, and only the keys of that one bin above the K-th are kept in excess.
+// Returns kKeyMax when the float parts are all equal (no cut possible). `hist`
+// has kHistBins slots, `red` 2 * (kThreads / 32) + 2. All threads call it.
+__device__ uint64_t block_cut_bound(const uint64_t* keys, uint32_t count, uint32_t K,
+                                    uint32_t* hist, uint32_t* red) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kW = kThreads / 32;
+    uint32_t lo = 0xFFFFFFFFu, hi = 0;
+    for (uint32_t i = tid; i < count; i += kThreads) {
+        const uint32_t h = (uint32_t)(keys[i] >> 32);
+        lo = h < lo ? h : lo;
+        hi = h > hi ? h : hi;
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0) {
+        red[warp] = lo;
+        red[kW + warp] = hi;
+    }
+    for (uint32_t b = tid; b < kHistBins; b += kThreads) hist[b] = 0;
+    __syncthreads();
+    lo = red[0];
+    hi = red[kW];
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
+    for (int w = 1; w < kW; ++w) {
+        lo = red[w] < lo ? red[w] : lo;
+        hi = red[kW + w] > hi ? red[kW + w] : hi;
+    }
+    if (lo == hi) {
+        __syncthreads();
+        return kKeyMax;
+    }
+    int shift = 0;
+    while (((hi - lo) >> shift) >= kHistBins) ++shift;
+    for (uint32_t i = tid; i < count; i += kThreads)
+        atomicAdd(&hist[((uint32_t)(keys[i] >> 32) - lo) >> shift], 1u);
+    __syncthreads();
+    // thread t owns bins [t * per, (t + 1) * per): the bin where the running count reaches K
+    constexpr uint32_t per = kHistBins / kThreads;
+    uint32_t c[per], run = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < per; ++j) {
+        c[j] = hist[tid * per + j];
+        run += c[j];
+    }
+    uint32_t incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) red[warp] = incl;  // red's min/max were read before the histogram barrier
+    __syncthreads();
+    uint32_t below = incl - run;
+    for (int w = 0; w < warp; ++w) below += red[w];
+    if (below < K && K <= below + run) {
+#pragma unroll
+        for (uint32_t j = 0; j < per; ++j) {
+            if (below < K && K <= below + c[j]) red[2 * kW + 1] = tid * per + j;
+            below += c[j];
+        }
+    }
+    __syncthreads();
+    const uint32_t bin = red[2 * kW + 1];
+    __syncthreads();
+    const uint64_t edge = (uint64_t)lo + ((uint64_t)(bin + 1) << shift);
+    return edge > 0xFFFFFFFFull ? kKeyMax : (edge << 32);
+}
+
+// Keeps the keys < bound at the front (in arbitrary order); returns their count.
+// `cnt` is a shared counter. All threads call it.
+__device__ uint32_t block_compact_lt(uint64_t* keys, uint32_t count, uint64_t bound, uint32_t* cnt) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint64_t mine[kCapPer];
+#pragma unroll
+    for (int j = 0; j < kCapPer; ++j) {
         const uint32_t i = tid + j * kThreads;
         mine[j] = i < count ? keys[i] : ~0ull;
     }
     if (tid == 0) *cnt = 0;
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-        const bool keep = mine[j] <= kth;
+    for (int j = 0; j < kCapPer; ++j) {
+        const bool keep = mine[j] < bound;
         const unsigned b = __ballot_sync(0xffffffffu, keep);
         uint32_t base = 0;
         if (b) {
@@ -312,20 +422,23 @@ __device__ void block_compact_le(uint64_t* keys, uint32_t count, uint64_t kth, u
         if (keep) keys[base + __popc(b & ((1u << lane) - 1))] = mine[j];
     }
     __syncthreads();
+    const uint32_t r = *cnt;
+    __syncthreads();
+    return r;
 }
 
 // Diagnostic counters (pgpu_walk_counters slots, summed per launch): 0 records
 // evaluated, 1 records past the cell-distance test (table lookups), 2 records kept, 3 compactions, 5 max records of one query, and
-// thread-0 clock cycles: 6 prologue (LUT, fine terms), 7 whole block, 8 record
-// rounds, 9 compaction sorts, 10 final sort + output.
+// thread-0 clock cycles: 6 prologue (table, query), 7 whole block, 8 record
+// rounds, 9 compactions, 10 final select + output.
 enum { kScRecords = 0, kScLookups = 1, kScKept = 2, kScCompactions = 3, kScMaxRecords = 5, kScCycPrologue = 6,
        kScCycTotal = 7, kScCycRounds = 8, kScCycCompact = 9, kScCycFinal = 10 };
 
 struct ScanState {
     uint64_t tau;
     uint64_t sel[4];
-    uint64_t lut_bar;
     uint32_t hist[256];
+    uint32_t red[2 * (kThreads / 32) + 2];
     uint32_t ccount;
     uint32_t count;
     uint32_t c;
@@ -335,19 +448,43 @@ struct ScanState {
     unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
 
-// NW = code words per record (code_stride / 4); HALF = FP16 table.
-template <int NW, bool HALF>
+// Loads the NW code words of record `mr` (8-byte loads when the row stride allows).
+template <int NW>
+__device__ __forceinline__ void load_codes(const uint8_t* codes, uint32_t stride, uint32_t mr,
+                                           uint32_t (&w)[NW]) {
+    if ((NW & 1) == 0 && (stride & 7u) == 0) {
+        const uint2* cw = reinterpret_cast<const uint2*>(codes + (uint64_t)mr * stride);
+#pragma unroll
+        for (int i = 0; i < NW / 2; ++i) {
+            const uint2 v = __ldg(cw + i);
+            w[2 * i] = v.x;
+            w[2 * i + 1] = v.y;
+        }
+    } else {
+        const uint32_t* cw = reinterpret_cast<const uint32_t*>(codes + (uint64_t)mr * stride);
+#pragma unroll
+        for (int i = 0; i < NW; ++i) w[i] = __ldg(cw + i);
+    }
+}
+
+// NW = code words per record (code_stride / 4); TAB = table variant.
+template <int NW, int TAB>
 __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(ScanParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ScanState st;
     const uint32_t qi = p.order[blockIdx.x];
     const int tid = threadIdx.x;
-    const uint32_t nsq = p.nsq, F = p.F, T = p.T;
-    float* lut = reinterpret_cast<float*>(smem + sizeof(uint64_t) * kCandCap);
+    const uint32_t nsq = p.nsq, F = p.F, T = p.T, cap = p.cap;
+    uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [cap], first (8-byte aligned)
+    uint32_t* hist = reinterpret_cast<uint32_t*>(keys + cap);  // [kHistBins]
+    float* lut = reinterpret_cast<float*>(hist + kHistBins);
     __half* luth = reinterpret_cast<__half*>(lut);
-    float* srow = HALF ? reinterpret_cast<float*>(luth + nsq * 256)
-                       : lut + nsq * 256;  // [F] 2 * cell_dist of the current cluster's cells
-    uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [kCandCap], first (8-byte aligned)
+    constexpr bool HALF = TAB != kTabF32;
+    // [F] 2 * cell_dist of the current cluster's cells, after the table (the rotated
+    // layout spans 128 rows x 32 banks whatever nsq <= 32 is)
+    float* srow = TAB == kTabRot ? reinterpret_cast<float*>(luth + 32 * 256)
+                  : HALF         ? reinterpret_cast<float*>(luth + nsq * 256)
+                                 : lut + nsq * 256;
     float* qv = srow + F;                  // [d]
 
     if (p.status[qi] != 0) {
@@ -355,51 +492,6 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
         return;
     }
     const long long t_start = clock64();
-    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&st.lut_bar);
-    if (tid == 0) {
-        // the query's table (from k_build_luts): one bulk async copy global -> shared
-        // (TMA), counted in bytes on an mbarrier; it lands while the block sets up
-        // its first cluster
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1u));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                     "r"(p.lut_bytes)
-                     : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-            "[%3];" ::"r"((uint32_t)__cvta_generic_to_shared(lut)),
-            "l"(p.luts + (uint64_t)qi * p.lut_bytes), "r"(p.lut_bytes), "r"(bar)
-            : "memory");
-    }
-    bool lut_ready = false;
-    // Waits (bounded) for the table; on expiry flags the pass and builds the same
-    // table here. Every thread calls it.
-    auto wait_lut = [&]() {
-        uint32_t done = 0;
-        for (uint32_t it = 0; it < (1u << 22) && !done; ++it) {
-            asm volatile(
-                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                "selp.b32 %0, 1, 0, p;\n}"
-                : "=r"(done)
-                : "r"(bar), "r"(0u)
-                : "memory");
-        }
-        if (!__syncthreads_and(done != 0)) {
-            if (tid == 0) atomicExch(p.err, 2);
-            if (HALF) {
-                const float scale =
-                    ldexpf(1.0f, half_lut_exponent(p.qnorm[qi], p.codebook_max));
-                for (uint32_t e = tid; e < nsq * 256; e += kThreads)
-                    luth[e] = __float2half_rn(
-                        l2sqr_sse(qv + (e >> 8) * p.lsq, p.codebook + (uint64_t)e * p.lsq, p.lsq) *
-                        scale);
-            } else {
-                build_lut(lut, qv, p.codebook, nsq, p.lsq, kThreads);
-            }
-            __syncthreads();
-        }
-        lut_ready = true;
-    };
     for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     const float* fdk = p.fd_by_fine + (uint64_t)qi * F;  // fine terms of this query
     if (tid == 0) {
@@ -410,10 +502,11 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
         st.passed = 0;
         st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
     }
+    const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
+    const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
     __syncthreads();
-    const float inv_scale = HALF ? ldexpf(1.0f, -half_lut_exponent(p.qnorm[qi], p.codebook_max)) : 1.0f;
+    build_table<TAB>(lut, qv, p.codebook, nsq, p.lsq, HALF ? ldexpf(1.0f, lut_e) : 1.0f);
     unsigned long long my_eval = 0, my_look = 0, my_pass = 0;
-    __syncthreads();
     const long long t_pro = clock64();
     for (uint32_t l = 0; l < p.P; ++l) {
         __syncthreads();
@@ -449,7 +542,6 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             for (uint32_t i = tid; i < F; i += kThreads)
                 srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
         }
-        if (!lut_ready) wait_lut();
         __syncthreads();
         if (tid == 0) st.n_records += r1 - r0;
         for (uint32_t base = r0; base < r1; base += kRound) {
@@ -465,9 +557,8 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
                 const uint32_t mr = mi < r1 ? mi : r0;
                 fine_id[j] = p.rec_fine[mr];
                 off[j] = p.offsets[mr];
-                const uint32_t* cw = reinterpret_cast<const uint32_t*>(p.codes + (uint64_t)mr * p.code_stride);
-#pragma unroll
-                for (int i = 0; i < NW; ++i) words[j][i] = __ldg(cw + i);
+                load_codes<NW>(TAB == kTabRot ? p.codes_rot : p.codes, p.code_stride, mr,
+                               words[j]);
             }
             // one shared atomic per warp for the kept records
             auto insert = [&](bool keep, uint64_t key) {
@@ -496,9 +587,15 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
                     ++my_eval;
                     if (filter_key(t0, mi) < tau) {  // t can only grow past t0
                         ++my_look;
-                        const float t =
-                            HALF ? t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale
-                                 : __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
+                        float t;
+                        if (TAB == kTabRot)
+                            t = t0 + lut_sum_rot<NW>(words[j],
+                                                     reinterpret_cast<const unsigned char*>(lut),
+                                                     nsq, mi % nsq) * inv_scale;
+                        else if (TAB == kTabF16)
+                            t = t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale;
+                        else
+                            t = __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
                         key = filter_key(t, mi);
                         keep = key < tau;
                     }
@@ -509,21 +606,21 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             const long long t_round_end = clock64();
             if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
             // cut back when the buffer could not take another round
-            if (st.count > kCandCap - kRound) {
-                // cut back to a bound with at least T keys below it (two digit passes;
-                // the final select below is exact); tau = that bound. If the bound's
-                // bucket kept too many to take another round, cut exactly to T.
+            if (st.count > cap - kRound) {
+                // one histogram pass: a bound with at least T keys below it (the final
+                // select below is exact); tau = that bound. If the cut kept too many to
+                // take another round, cut exactly to T.
                 const uint32_t cnt = st.count;
-                uint64_t kth = block_select_kth(keys, cnt, T, st.hist, st.sel, 2);
-                block_compact_le<kCandCap / kThreads>(keys, cnt, kth, &st.ccount);
-                const uint32_t kept = st.ccount;
-                if (kept > kCandCap - kRound) {
-                    kth = block_select_kth(keys, kept, T, st.hist, st.sel);
-                    block_compact_le<kCandCap / kThreads>(keys, kept, kth, &st.ccount);
+                uint64_t bound = block_cut_bound(keys, cnt, T, hist, st.red);
+                uint32_t kept = bound == kKeyMax ? cnt : block_compact_lt(keys, cnt, bound, &st.ccount);
+                if (kept > cap - kRound) {
+                    const uint64_t kth = block_select_kth(keys, kept, T, st.hist, st.sel);
+                    bound = kth + 1;  // kth < kKeyMax: keys are distinct by id
+                    kept = block_compact_lt(keys, kept, bound, &st.ccount);
                 }
                 if (tid == 0) {
-                    st.count = st.ccount;
-                    st.tau = kth;
+                    st.count = kept;
+                    st.tau = bound < tau ? bound : tau;
                     st.n_compact += 1;
                     st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
                 }
@@ -531,13 +628,12 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             }
         }
     }
-    if (!lut_ready) wait_lut();  // no copy may be in flight when the block exits
     __syncthreads();
     const long long t_final = clock64();
     uint32_t count = st.count;
     if (count > T) {
         const uint64_t kth = block_select_kth(keys, count, T, st.hist, st.sel);
-        block_compact_le<kCandCap / kThreads>(keys, count, kth, &st.ccount);
+        block_compact_lt(keys, count, kth + 1, &st.ccount);
         count = T;
     }
     // the T survivors leave unordered: only the rerank's tie path needs their
@@ -632,17 +728,35 @@ __global__ __launch_bounds__(kOrderThreads) void k_scan_order(const uint8_t* __r
 
 }  // namespace
 
-size_t scan_smem_bytes(const DeviceIndex& ix) {
-    return sizeof(uint64_t) * kCandCap + sizeof(float) * ix.nsq * 256 + sizeof(float) * ix.F +
-           sizeof(float) * ix.d;
+size_t scan_smem_bytes(const DeviceIndex& ix, uint32_t T) {
+    return sizeof(uint64_t) * scan_cap(T) + sizeof(uint32_t) * kHistBins +
+           sizeof(float) * ix.nsq * 256 + sizeof(float) * ix.F + sizeof(float) * ix.d;
 }
 
-size_t scan_smem_bytes_half(const DeviceIndex& ix) {
-    return sizeof(uint64_t) * kCandCap + sizeof(__half) * ix.nsq * 256 + sizeof(float) * ix.F +
-           sizeof(float) * ix.d;
+// The rotated table applies when nsq is a multiple of 4, at most 32, and its copy
+// of the codes exists.
+static bool use_rot(const DeviceIndex& ix) {
+    return ix.codes_rot != nullptr && ix.nsq % 4 == 0 && ix.nsq <= 32 && ix.code_stride == ix.nsq;
 }
 
-uint32_t scan_max_filter_topk() { return kCandCap - kRound; }
+size_t scan_smem_bytes_half(const DeviceIndex& ix, uint32_t T) {
+    // the rotated table spans 128 rows x 32 banks (16 KB), enough for nsq <= 32; the
+    // FP16 table of the other layout nsq * 512 bytes
+    const size_t tab = sizeof(__half) * (ix.nsq <= 32 ? 32 : ix.nsq) * 256;
+    return sizeof(uint64_t) * scan_cap(T) + sizeof(uint32_t) * kHistBins + tab +
+           sizeof(float) * ix.F + sizeof(float) * ix.d;
+}
+
+// The buffer takes T + a round + at least 1024 more keys between cuts.
+uint32_t scan_max_filter_topk() { return kMaxCap - kRound - 1024; }
+
+cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream) {
+    if (s.order == nullptr || s.wbucket == nullptr) return cudaErrorInvalidValue;
+    k_scan_work<<<(n + 255) / 256, 256, 0, stream>>>(s.ctag, s.status, ix.cell_start, n, s.P, ix.C,
+                                                     ix.F, s.wbucket);
+    k_scan_order<<<1, kOrderThreads, 0, stream>>>(s.wbucket, n, s.order);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                cudaStream_t stream) {
@@ -661,6 +775,7 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.rec_fine = ix.rec_fine;
     p.offsets = ix.offsets;
     p.codes = ix.codes;
+    p.codes_rot = ix.codes_rot;
     p.codebook = ix.codebook;
     p.counters = s.counters;
     p.d = ix.d;
@@ -671,44 +786,38 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.code_stride = ix.code_stride;
     p.P = s.P;
     p.T = s.T;
+    p.cap = scan_cap(s.T);
     p.codebook_max = ix.codebook_max;
-    p.luts = reinterpret_cast<const unsigned char*>(s.luts);
-    p.lut_bytes = ix.nsq * 256 * (half_lut ? 2 : 4);
-    p.err = s.tc_err;
-    if (s.luts == nullptr || s.order == nullptr || s.wbucket == nullptr) return cudaErrorInvalidValue;
-    k_scan_work<<<(n + 255) / 256, 256, 0, stream>>>(s.ctag, s.status, ix.cell_start, n, s.P, ix.C,
-                                                     ix.F, s.wbucket);
-    k_scan_order<<<1, kOrderThreads, 0, stream>>>(s.wbucket, n, s.order);
+    if (s.order == nullptr || s.T > scan_max_filter_topk()) return cudaErrorInvalidValue;
     p.order = s.order;
-    {
-        const dim3 g((n + kLutQueries - 1) / kLutQueries);
-        if (half_lut)
-            k_build_luts<true><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, n, ix.d,
-                                                      ix.nsq, ix.lsq, ix.codebook_max, s.luts);
-        else
-            k_build_luts<false><<<g, 256, 0, stream>>>(s.q, s.qnorm, s.status, ix.codebook, n, ix.d,
-                                                       ix.nsq, ix.lsq, ix.codebook_max, s.luts);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    const size_t smem = half_lut ? scan_smem_bytes_half(ix) : scan_smem_bytes(ix);
+    const size_t smem = half_lut ? scan_smem_bytes_half(ix, s.T) : scan_smem_bytes(ix, s.T);
     const uint32_t nw = ix.code_stride / 4;
-    auto launch = [&](void (*kernel)(ScanParams), int) {
+    auto launch = [&](void (*kernel)(ScanParams)) {
         ensure_max_dynamic_smem(kernel, 220 * 1024);
         kernel<<<n, kThreads, smem, stream>>>(p);
     };
-    if (half_lut) {
-        if (nw <= 2) launch(k_scan_select<2, true>, 5);
-        else if (nw <= 4) launch(k_scan_select<4, true>, 6);
-        else if (nw <= 6) launch(k_scan_select<6, true>, 7);
-        else if (nw <= 8) launch(k_scan_select<8, true>, 8);
-        else launch(k_scan_select<16, true>, 9);
+    if (half_lut && use_rot(ix)) {
+        // nw == nsq / 4 exactly
+        if (nw == 2) launch(k_scan_select<2, kTabRot>);
+        else if (nw == 4) launch(k_scan_select<4, kTabRot>);
+        else if (nw == 6) launch(k_scan_select<6, kTabRot>);
+        else if (nw == 8) launch(k_scan_select<8, kTabRot>);
+        else if (nw == 1) launch(k_scan_select<1, kTabRot>);
+        else if (nw == 3) launch(k_scan_select<3, kTabRot>);
+        else if (nw == 5) launch(k_scan_select<5, kTabRot>);
+        else launch(k_scan_select<7, kTabRot>);
+    } else if (half_lut) {
+        if (nw <= 2) launch(k_scan_select<2, kTabF16>);
+        else if (nw <= 4) launch(k_scan_select<4, kTabF16>);
+        else if (nw <= 6) launch(k_scan_select<6, kTabF16>);
+        else if (nw <= 8) launch(k_scan_select<8, kTabF16>);
+        else launch(k_scan_select<16, kTabF16>);
     } else {
-        if (nw <= 2) launch(k_scan_select<2, false>, 0);
-        else if (nw <= 4) launch(k_scan_select<4, false>, 1);
-        else if (nw <= 6) launch(k_scan_select<6, false>, 2);
-        else if (nw <= 8) launch(k_scan_select<8, false>, 3);
-        else launch(k_scan_select<16, false>, 4);
+        if (nw <= 2) launch(k_scan_select<2, kTabF32>);
+        else if (nw <= 4) launch(k_scan_select<4, kTabF32>);
+        else if (nw <= 6) launch(k_scan_select<6, kTabF32>);
+        else if (nw <= 8) launch(k_scan_select<8, kTabF32>);
+        else launch(k_scan_select<16, kTabF32>);
     }
     return cudaGetLastError();
 }

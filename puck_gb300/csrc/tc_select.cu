@@ -466,6 +466,8 @@ cudaError_t launch_nearest_center_tc(uint32_t dim, const float* cents, uint64_t 
     // screen buffer of at most 256 MiB: rows per chunk, a multiple of 128
     uint64_t chunk = (256ull << 20) / (4 * (k ? k : 1));
     chunk = chunk < 128 ? 128 : (chunk / 128) * 128;
+    // the contraction's grid.y (row tiles of 128) is at most 65535
+    if (chunk > 65535ull * 128) chunk = 65535ull * 128;
     if (chunk > n) chunk = n;
     float* cnorm = nullptr;
     float* half = nullptr;

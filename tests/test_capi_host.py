@@ -69,9 +69,9 @@ def test_bad_search_params_rejected_before_device(lib, tmp_path):
     p = native.default_params(precision=7, mode=native.PGPU_MODE_SCAN, filter_topk=500)
     assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_INVALID
     p = native.default_params(precision=native.PGPU_PRECISION_BF16, mode=native.PGPU_MODE_SCAN,
-                              filter_topk=1100, filter_margin=200)
+                              filter_topk=1900, filter_margin=200)
     assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_LIMIT
-    p = native.default_params(mode=native.PGPU_MODE_SCAN, filter_topk=1281)
+    p = native.default_params(mode=native.PGPU_MODE_SCAN, filter_topk=2049)
     assert lib.pgpu_open(b"/nonexistent", ctypes.byref(p), ctypes.byref(h)) == native.PGPU_E_LIMIT
 
 

@@ -78,7 +78,7 @@ def test_golden_scan_mode_matches_oracle(golden):
     restatement of the mode (same per-record distances as the reference)."""
     name, z, index_dir = golden
     P, T, k = [int(v) for v in z["params"]]
-    T = min(T, 1280)
+    T = min(T, 2048)
     ix = native.GpuIndex(index_dir, search_coarse_count=P, filter_topk=T, topk=k, max_batch=64,
                          mode=native.PGPU_MODE_SCAN)
     dist, ids, status = ix.search(z["queries"], k, return_status=True)
@@ -124,7 +124,8 @@ def _built_index(tmpdir, n, d, C, F, nsq, kind, seed, norm, pq=False):
     (80000, 96, 96, 80, 24, "unit", True, 24, 500, 100, False),
     (40000, 128, 50, 40, 32, "int", False, 50, 300, 20, False),
     (50000, 96, 64, 64, 24, "unit", True, 8, 300, 10, True),   # second-level PQ rerank
-    (60000, 64, 32, 32, 16, "int", False, 12, 1280, 10, False),  # the scan's largest filter_topk
+    (60000, 64, 32, 32, 16, "int", False, 12, 1280, 10, False),
+    (60000, 64, 32, 32, 16, "int", False, 12, 2048, 10, False),  # the scan's largest filter_topk
 ])
 def test_gpu_equals_oracle_builder_index(n, d, C, F, nsq, kind, norm, P, T, k, pq, mode):
     with tempfile.TemporaryDirectory() as tmp:

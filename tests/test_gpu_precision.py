@@ -101,6 +101,60 @@ def test_filter_distance_error_bound(idx):
     ix.close()
 
 
+def _filter_bound_check(path, host, q, nsq, lsq):
+    """The filter distances of the precision form stay within the stated bound."""
+    ix = native.GpuIndex(path, search_coarse_count=2, filter_topk=200, filter_margin=0, topk=10,
+                         max_batch=512, mode=native.PGPU_MODE_SCAN,
+                         precision=native.PGPU_PRECISION_BF16)
+    labels, fdist, cnt = ix.filter_candidates(q)
+    qn = _qn(q)
+    coarse = host["coarse"].astype(np.float64)
+    fine = host["fine"].astype(np.float64)
+    cb = host["filter_codebook"].astype(np.float64).reshape(nsq, 256, lsq)
+    F = fine.shape[0]
+    for i in range(q.shape[0]):
+        lab = labels[i, :cnt[i]].astype(np.int64)
+        cell = host["cell_assign"][lab].astype(np.int64)
+        c, f = cell // F, cell % F
+        cd = 0.5 * (coarse[c] ** 2).sum(1) - coarse[c] @ qn[i]
+        stat = 0.5 * (fine[f] ** 2).sum(1) + (fine[f] * coarse[c]).sum(1)
+        fd = -(fine[f] @ qn[i])
+        codes = host["filter_codes"][lab].astype(np.int64)
+        sub = qn[i].reshape(nsq, lsq)
+        lut = ((sub[:, None, :] - cb) ** 2).sum(-1)
+        parts = lut[np.arange(nsq)[None, :], codes]
+        t64 = 2.0 * (cd + stat + fd) + host["filter_offsets"][lab] + parts.sum(1)
+        fnorm = np.linalg.norm(fine[f], axis=1)
+        bound = 4 * 2.0 ** -7 * fnorm + 2.0 ** -10 * parts.sum(1) + 1e-5 * (1 + np.abs(t64))
+        err = np.abs(fdist[i, :cnt[i]].astype(np.float64) - t64)
+        assert (err <= bound).all(), float((err / bound).max())
+    ix.close()
+
+
+@pytest.mark.parametrize("d,nsq", [
+    (128, 32),  # rotated one-bank-per-subspace table over all 32 banks
+    (60, 15),   # nsq not a multiple of 4: the FP16 table in the reference's layout
+])
+def test_filter_distance_error_bound_layouts(d, nsq):
+    import torch
+    native.load(build_if_missing=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        base = builder.gmm(60_000, d, 256, "unit", 17)
+        arrays = builder.build_index(base, 48, 48, nsq, True, train_sample=40000, iters=5,
+                                     pq_sample=20000, seed=17)
+        host = {k: (v.cpu().numpy() if hasattr(v, "cpu") else np.asarray(v))
+                for k, v in arrays.items()}
+        index_io.write_index(tmp, base=host["base"], coarse=host["coarse"], fine=host["fine"],
+                             cell_assign=host["cell_assign"],
+                             filter_codebook=host["filter_codebook"],
+                             filter_offsets=host["filter_offsets"],
+                             filter_codes=host["filter_codes"], whether_norm=True)
+        q = builder.gmm(48, d, 256, "unit", 17, row_seed=9).cpu().numpy()
+        del base
+        torch.cuda.empty_cache()
+        _filter_bound_check(tmp, host, q, nsq, d // nsq)
+
+
 def test_bf16_recall_against_fp32_path(idx):
     path, host, q = idx
     fp = native.GpuIndex(path, search_coarse_count=4, filter_topk=300, topk=10, max_batch=512,
