@@ -619,7 +619,8 @@ def run_gpu(args, w, rank, ws):
             ix.set_probe(probe, mass=x, max_probe=w["probe_max"])
 
     def ids_now(kk):
-        return i_dev[:, :kk].cpu().numpy().view(np.uint32)
+        # a search of top-kk writes nq x kk contiguous values
+        return i_dev.view(-1)[:nq * kk].view(nq, kk).cpu().numpy().view(np.uint32)
 
     def measure(form, mode, x, kk):
         topk_now[0] = kk

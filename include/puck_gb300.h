@@ -253,6 +253,19 @@ int pgpu_server_destroy(pgpu_server* server);
 int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const float* points,
                         uint64_t n, int32_t* assign, float* distance, void* stream);
 
+/* The build's cell assignment (hierarchical_cluster_index.cpp:1042-1138,
+ * HierarchicalClusterIndex::nearest_cell_assign driven by assign): for each of n
+ * points (DEVICE pointer, [n][dim]) the cell c * F + f minimising
+ * ((0.5|c|^2 - x.c) + 0.5|x|^2 - x.f) + (0.5|f|^2 + f.c) over the C coarse and F
+ * fine centroids (DEVICE pointers; the fine ones in the index's order, descending
+ * norm), walked like the reference (coarse clusters by ascending term, fine ids in
+ * order, its triangle-inequality break, first minimum wins), in the reference's
+ * FP32 order: the same cells and distances bit for bit. cell: [n] u32, distance:
+ * [n] floats (DEVICE). Enqueued on `stream`; returns after it finished. */
+int pgpu_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C, const float* fine,
+                             uint32_t F, const float* points, uint64_t n, uint32_t* cell,
+                             float* distance, void* stream);
+
 /* Replaces PuckIndex::puck_assign (puck/puck/puck_index.cpp:602-709), the build's
  * encoder, for n points whose cells are known (cell_assign = coarse * F + fine): the
  * filter-PQ offset and codes of each point (filter_data.dat records) and, with

@@ -5,8 +5,8 @@ puck/hierarchical_cluster/hierarchical_cluster_index.cpp:882-1138):
 
   1. coarse k-means on a sample; fine k-means on the coarse residuals;
      fine centroids re-ordered by descending norm (hierarchical_cluster_index.cpp:958-980)
-  2. every point assigned to its nearest cell c*F + f (among the `assign_probe`
-     nearest coarse clusters, all fine clusters)
+  2. every point assigned to its nearest cell c*F + f by the reference's own walk
+     (pgpu_nearest_cell_assign: the same cells as its build for these centroids)
   3. filter PQ (filter_nsq subspaces x 256 codewords) trained by k-means on the cell
      residuals x - c - f; every point encoded, with its offset 2 <decoded residual,
      c + f> (quantization.cpp:244-258), by the library's puck_assign kernel
@@ -75,29 +75,19 @@ def _pq_encode(res, books):
     return codes
 
 
-def assign_cells(x, coarse, fine, probe=8, chunk=32768):
-    """Nearest cell (c, f) of every row of x among the `probe` nearest coarse clusters."""
-    C, F = coarse.shape[0], fine.shape[0]
-    cn = (coarse * coarse).sum(1) / 2
-    fn = (fine * fine).sum(1) / 2
-    stat = fn[None, :] + coarse @ fine.T  # [C, F]
-    out = torch.empty(x.shape[0], dtype=torch.int64, device=x.device)
-    probe = min(probe, C)
-    for s in range(0, x.shape[0], chunk):
-        xs = x[s:s + chunk]
-        xn = (xs * xs).sum(1, keepdim=True) / 2
-        cterm = cn[None, :] - xs @ coarse.T + xn           # 0.5|x-c|^2
-        top = torch.topk(cterm, probe, dim=1, largest=False)
-        fterm = xs @ fine.T                                  # x.f
-        score = top.values[:, :, None] - fterm[:, None, :] + stat[top.indices]  # [b, probe, F]
-        best = score.view(xs.shape[0], -1).argmin(1)
-        pc = best // F
-        out[s:s + chunk] = top.indices.gather(1, pc[:, None])[:, 0] * F + best % F
-    return out
+def assign_cells(x, coarse, fine):
+    """The reference's exact nearest cell of every row of x (pgpu_nearest_cell_assign,
+    hierarchical_cluster_index.cpp:1042-1138); int64 cell ids c * F + f."""
+    n = x.shape[0]
+    cell = torch.empty(n, dtype=torch.int32, device=x.device)
+    dist = torch.empty(n, dtype=torch.float32, device=x.device)
+    native.nearest_cell_assign(coarse.contiguous(), fine.contiguous(), x.contiguous(), cell, dist,
+                               stream=torch.cuda.current_stream())
+    return cell.long()
 
 
 def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters=12,
-                pq_sample=131072, probe=8, seed=0, whether_pq=False, pq_nsq=None):
+                pq_sample=131072, seed=0, whether_pq=False, pq_nsq=None):
     """Trains and builds a Puck index from a device tensor `base` [n, d].
 
     Returns host numpy arrays in input order (the contents of the index files):
@@ -118,7 +108,7 @@ def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters
     order = torch.argsort(-(fine * fine).sum(1), stable=True)
     fine = fine[order].contiguous()
 
-    cell = assign_cells(base, coarse, fine, probe=probe)
+    cell = assign_cells(base, coarse, fine)
     pq_idx = torch.randperm(n, generator=g)[:min(pq_sample, n)].to(dev)
     pcell = cell[pq_idx]
     res = base[pq_idx] - coarse[pcell // F] - fine[pcell % F]

@@ -452,6 +452,22 @@ int pgpu_nearest_center(uint32_t dim, const float* centroids, uint64_t k, const 
     return PGPU_OK;
 }
 
+int pgpu_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C, const float* fine,
+                             uint32_t F, const float* points, uint64_t n, uint32_t* cell,
+                             float* distance, void* stream) {
+    if (dim == 0 || C == 0 || F == 0 || coarse == nullptr || fine == nullptr ||
+        points == nullptr || cell == nullptr || distance == nullptr)
+        return fail(PGPU_E_INVALID, "invalid argument");
+    if ((uint64_t)C * F > 0xFFFFFFFFull) return fail(PGPU_E_LIMIT, "C * F above 2^32 - 1");
+    if (n == 0) return PGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = pgpu::launch_nearest_cell_assign(dim, coarse, C, fine, F, points, n, cell,
+                                                     distance, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "nearest_cell_assign");
+    return PGPU_OK;
+}
+
 int pgpu_filter_candidates(pgpu_index* h, uint32_t n, const float* query, uint32_t* labels,
                            float* distance, uint32_t* count) {
     if (h == nullptr || query == nullptr || labels == nullptr || distance == nullptr ||

@@ -160,6 +160,10 @@ cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, 
 cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint64_t k,
                                           const float* x, uint64_t n, int32_t* assign, float* dis,
                                           float* xnorm, float* cnorm, cudaStream_t stream);
+// The build's exact nearest-cell assignment (cell_assign.cu).
+cudaError_t launch_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C,
+                                       const float* fine, uint32_t F, const float* x, uint64_t n,
+                                       uint32_t* cell, float* dist, cudaStream_t stream);
 cudaError_t launch_gather_u32(const uint32_t* idx, uint64_t n, const uint32_t* table,
                               uint32_t* out, cudaStream_t stream);
 // Records `msg` as the calling thread's last error (pgpu_last_error) and returns `code`.

@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = (
     "pgpu_search_batch", "pgpu_search", "pgpu_search_batch_device", "pgpu_index_info_get",
     "pgpu_last_stats", "pgpu_close", "pgpu_nearest_center", "pgpu_last_error",
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
-    "pgpu_nearest_center_noalloc", "pgpu_server_params_default", "pgpu_server_create",
+    "pgpu_nearest_center_noalloc", "pgpu_nearest_cell_assign", "pgpu_server_params_default", "pgpu_server_create",
     "pgpu_server_submit", "pgpu_server_wait", "pgpu_server_stats_get", "pgpu_server_destroy",
     "pgpu_contract_bf16", "pgpu_filter_candidates", "pgpu_probe_create", "pgpu_probe_destroy",
     "pgpu_probe_info", "pgpu_probe_train_step", "pgpu_probe_gradients", "pgpu_probe_forward",
@@ -132,6 +132,7 @@ def load(build_if_missing=False):
     lib.pgpu_close.argtypes = [vp]
     lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
     lib.pgpu_nearest_center_noalloc.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
+    lib.pgpu_nearest_cell_assign.argtypes = [u32, vp, u32, vp, u32, vp, u64, vp, vp, vp]
     lib.pgpu_puck_assign.argtypes = [u32, u64, vp, vp, vp, u32, vp, u32, vp, u32, vp, u32, vp, vp,
                                      vp, vp, vp]
     lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
@@ -353,6 +354,20 @@ def nearest_center(centroids, points, assign, distance, stream=None):
         s = s.cuda_stream
     return check(load().pgpu_nearest_center(dim, _ptr(centroids), k, _ptr(points), n,
                                             _ptr(assign), _ptr(distance), s))
+
+
+def nearest_cell_assign(coarse, fine, points, cell, distance, stream=None):
+    """The build's exact cell assignment (pgpu_nearest_cell_assign) on CUDA tensors:
+    coarse [C, d], fine [F, d] (index order), points [n, d] float32; cell [n]
+    (int32 or uint32 bits) and distance [n] float32 outputs."""
+    C, dim = coarse.shape
+    F = fine.shape[0]
+    n = points.shape[0]
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    return check(load().pgpu_nearest_cell_assign(dim, _ptr(coarse), C, _ptr(fine), F,
+                                                 _ptr(points), n, _ptr(cell), _ptr(distance), s))
 
 
 def puck_assign(base, cell_assign, coarse, fine, filter_codebook, pq_codebook=None, stream=None):

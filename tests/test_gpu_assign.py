@@ -77,3 +77,45 @@ def test_gpu_puck_assign_rejects_bad_cells():
     with pytest.raises(native.PuckGpuError) as e:
         native.puck_assign(base, cells, coarse, fine, cb)
     assert e.value.code == native.PGPU_E_INVALID
+
+
+def _gpu_cells(coarse, fine, x):
+    import torch
+    xs = _cuda(x, np.float32)
+    cell = torch.empty(x.shape[0], dtype=torch.int32, device="cuda")
+    dist = torch.empty(x.shape[0], dtype=torch.float32, device="cuda")
+    native.nearest_cell_assign(_cuda(coarse, np.float32), _cuda(fine, np.float32), xs, cell, dist)
+    torch.cuda.synchronize()
+    return cell.cpu().numpy().view(np.uint32), dist.cpu().numpy()
+
+
+def test_gpu_nearest_cell_assign_matches_reference(golden):
+    """pgpu_nearest_cell_assign gives the reference's own cell_assign.dat
+    (hierarchical_cluster_index.cpp:1042-1138) and the oracle's distances bit for bit."""
+    name, z, index_dir = golden
+    a = index_io.read_index(index_dir)
+    base = np.ascontiguousarray(a["base"], np.float32)
+    cell, dist = _gpu_cells(a["coarse"], a["fine"], base)
+    assert np.array_equal(cell, np.asarray(a["cell_assign"]).astype(np.uint32)), name
+    ocell, odist = oracle.nearest_cell_assign(a["coarse"], a["fine"], base)
+    assert np.array_equal(cell, ocell)
+    assert np.array_equal(_bits(dist), _bits(odist))
+
+
+def test_gpu_nearest_cell_assign_equals_oracle_many_chunks():
+    """Several point chunks (1024 + 1024 centroids), ties and points with many
+    equally near coarse clusters (the walk's slow path): bit-identical to the oracle."""
+    rng = np.random.default_rng(5)
+    d, C, F = 16, 1024, 1024
+    coarse = rng.normal(size=(C, d)).astype(np.float32)
+    coarse[:200] = coarse[:200] / np.linalg.norm(coarse[:200], axis=1, keepdims=True)  # a shell
+    coarse[300:310] = coarse[200]                                                      # duplicates
+    fine = (0.3 * rng.normal(size=(F, d))).astype(np.float32)
+    fine = fine[np.argsort(-np.linalg.norm(fine, axis=1), kind="stable")]
+    x = rng.normal(size=(140_000, d)).astype(np.float32)
+    x[:64] = 0.0                      # equidistant from the 200 shell centroids
+    x[64:128] = coarse[200] + fine[7]  # exact ties between duplicated cells
+    cell, dist = _gpu_cells(coarse, fine, x)
+    ocell, odist = oracle.nearest_cell_assign(coarse, fine, x)
+    assert np.array_equal(cell, ocell)
+    assert np.array_equal(_bits(dist), _bits(odist))

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
+from puck_gb300 import index_io
 
 
 def _bits(a):
@@ -83,6 +84,16 @@ def test_nearest_cell_assign_is_exact_argmin():
     best = full.min(1)
     # the pruned walk must land on an exact minimiser (up to float rounding)
     assert np.all(full[np.arange(len(x)), cell] <= best + 1e-4)
+
+
+def test_nearest_cell_assign_matches_reference(golden):
+    """The oracle's nearest_cell_assign gives the reference's own cell_assign.dat
+    (hierarchical_cluster_index.cpp:1042-1138) on every golden index."""
+    name, z, index_dir = golden
+    a = index_io.read_index(index_dir)
+    base = np.ascontiguousarray(a["base"], np.float32)
+    cell, _ = oracle.nearest_cell_assign(a["coarse"], a["fine"], base)
+    assert np.array_equal(cell, np.asarray(a["cell_assign"]).astype(np.uint32)), name
 
 
 def test_scan_mode_distances_agree_with_walk(golden):
