@@ -6,7 +6,9 @@ puck/hierarchical_cluster/hierarchical_cluster_index.cpp:882-1138):
   1. coarse k-means on a sample; fine k-means on the coarse residuals;
      fine centroids re-ordered by descending norm (hierarchical_cluster_index.cpp:958-980)
   2. every point assigned to its nearest cell c*F + f by the reference's own walk
-     (pgpu_nearest_cell_assign: the same cells as its build for these centroids)
+     (pgpu_nearest_cell_assign: the same cells as its build for these centroids); above
+     EXACT_ASSIGN_MAX_POINTS points, by the nearest cell within the 8 nearest coarse
+     clusters (assign_cells)
   3. filter PQ (filter_nsq subspaces x 256 codewords) trained by k-means on the cell
      residuals x - c - f; every point encoded, with its offset 2 <decoded residual,
      c + f> (quantization.cpp:244-258), by the library's puck_assign kernel
@@ -15,7 +17,8 @@ puck/hierarchical_cluster/hierarchical_cluster_index.cpp:882-1138):
 The k-means assignment step is the library's own kernel (pgpu_nearest_center,
 kmeans.cpp:221-258). Training is seeded, unlike the reference's time(0) seeds;
 the index it writes is an ordinary Puck index the reference loads unchanged.
-Torch is used for device memory and the k-means update only.
+Torch is used for device memory, the k-means update and the probe assignment of
+large builds.
 """
 import numpy as np
 import torch
@@ -75,19 +78,50 @@ def _pq_encode(res, books):
     return codes
 
 
-def assign_cells(x, coarse, fine):
-    """The reference's exact nearest cell of every row of x (pgpu_nearest_cell_assign,
-    hierarchical_cluster_index.cpp:1042-1138); int64 cell ids c * F + f."""
+# Largest point count the builder assigns with the reference's exact walk. Above it
+# the walk's cost (every near coarse cluster walked per point, exact FP32 dots of
+# every point with every centroid) runs to hours at 100M points, and the builder
+# takes the probe assignment below.
+EXACT_ASSIGN_MAX_POINTS = 4_000_000
+
+
+def assign_cells(x, coarse, fine, exact=None, probe=8, chunk=32768):
+    """Nearest cell c * F + f of every row of x (int64).
+
+    exact (default: n <= EXACT_ASSIGN_MAX_POINTS): the reference's own walk
+    (pgpu_nearest_cell_assign, hierarchical_cluster_index.cpp:1042-1138), the cells
+    its build writes for these centroids. Otherwise the smallest 0.5|x - c - f|^2
+    over the `probe` coarse clusters nearest to x (all fine ids of each): the cell
+    the walk finds whenever it lies in those clusters, at a fraction of the cost."""
     n = x.shape[0]
-    cell = torch.empty(n, dtype=torch.int32, device=x.device)
-    dist = torch.empty(n, dtype=torch.float32, device=x.device)
-    native.nearest_cell_assign(coarse.contiguous(), fine.contiguous(), x.contiguous(), cell, dist,
-                               stream=torch.cuda.current_stream())
-    return cell.long()
+    if exact is None:
+        exact = n <= EXACT_ASSIGN_MAX_POINTS
+    if exact:
+        cell = torch.empty(n, dtype=torch.int32, device=x.device)
+        dist = torch.empty(n, dtype=torch.float32, device=x.device)
+        native.nearest_cell_assign(coarse.contiguous(), fine.contiguous(), x.contiguous(), cell,
+                                   dist, stream=torch.cuda.current_stream())
+        return cell.long()
+    C, F = coarse.shape[0], fine.shape[0]
+    cn = (coarse * coarse).sum(1) / 2
+    fn = (fine * fine).sum(1) / 2
+    stat = fn[None, :] + coarse @ fine.T  # [C, F] stationary terms
+    out = torch.empty(n, dtype=torch.int64, device=x.device)
+    probe = min(probe, C)
+    for s in range(0, n, chunk):
+        xs = x[s:s + chunk]
+        xn = (xs * xs).sum(1, keepdim=True) / 2
+        cterm = cn[None, :] - xs @ coarse.T + xn  # 0.5|x - c|^2
+        top = torch.topk(cterm, probe, dim=1, largest=False)
+        fterm = xs @ fine.T  # x.f
+        score = top.values[:, :, None] - fterm[:, None, :] + stat[top.indices]  # [b, probe, F]
+        best = score.view(xs.shape[0], -1).argmin(1)
+        out[s:s + chunk] = top.indices.gather(1, (best // F)[:, None])[:, 0] * F + best % F
+    return out
 
 
 def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters=12,
-                pq_sample=131072, seed=0, whether_pq=False, pq_nsq=None):
+                pq_sample=131072, seed=0, whether_pq=False, pq_nsq=None, exact_assign=None):
     """Trains and builds a Puck index from a device tensor `base` [n, d].
 
     Returns host numpy arrays in input order (the contents of the index files):
@@ -108,7 +142,7 @@ def build_index(base, C, F, filter_nsq, whether_norm, train_sample=262144, iters
     order = torch.argsort(-(fine * fine).sum(1), stable=True)
     fine = fine[order].contiguous()
 
-    cell = assign_cells(base, coarse, fine)
+    cell = assign_cells(base, coarse, fine, exact=exact_assign)
     pq_idx = torch.randperm(n, generator=g)[:min(pq_sample, n)].to(dev)
     pcell = cell[pq_idx]
     res = base[pq_idx] - coarse[pcell // F] - fine[pcell % F]
