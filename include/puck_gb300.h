@@ -196,6 +196,23 @@ int pgpu_walk_counters(const pgpu_index* index, uint64_t* out, uint32_t n);
 int pgpu_filter_candidates(pgpu_index* index, uint32_t n, const float* query, uint32_t* labels,
                            float* distance, uint32_t* count);
 
+/* ------------------------------------------------------------ realtime insert
+ * RealtimeInsertPuckIndex (puck/puck/realtime_insert_puck_index.h:32-107) on the
+ * device. pgpu_realtime_open replaces its init() (realtime_insert_puck_index.cpp:
+ * 225-272): it reserves room for `capacity` inserted points on the index's GPU
+ * (the per-record arrays are widened once, so call it before any server is created
+ * on the index). pgpu_insert replaces insert(const InsertRequest*) (:273-337) for n
+ * HOST features ([n][query_dim], labels stay with the caller): each is normalised
+ * when the index normalises, assigned to its nearest cell on the index's live
+ * stationary terms, encoded like the build, and then found by every search in both
+ * modes, exactly as the reference scans a cell's inserted points after its base
+ * records. local_idx[i] = the point's local id (point count + insert id), or -1
+ * (a non-finite or zero-norm feature). Inserts take the index's lock; they must not
+ * overlap a server running on the same index. PGPU_E_LIMIT beyond the capacity,
+ * PGPU_E_UNSUPPORTED on an ip2cos index. */
+int pgpu_realtime_open(pgpu_index* index, uint32_t capacity);
+int pgpu_insert(pgpu_index* index, uint32_t n, const float* feature, int64_t* local_idx);
+
 int pgpu_close(pgpu_index* index);
 
 /* ------------------------------------------------------------------ serving

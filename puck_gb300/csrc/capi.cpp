@@ -30,6 +30,7 @@ struct pgpu_index {
     cudaEvent_t ev[PGPU_NUM_STAGES + 1] = {};
     float stage_ms[PGPU_NUM_STAGES] = {};
     bool stage_pending = false;
+    pgpu::RealtimeHost rt;  // host mirrors of the realtime insert lists
 };
 
 namespace {
@@ -394,6 +395,49 @@ int pgpu_last_stats(const pgpu_index* h, uint64_t* kernels_launched, uint64_t* r
 int pgpu_walk_counters(const pgpu_index* h, uint64_t* out, uint32_t n) {
     if (h == nullptr || out == nullptr) return fail(PGPU_E_INVALID, "null argument");
     for (uint32_t i = 0; i < n && i < (uint32_t)pgpu::kNumWalkCounters; ++i) out[i] = h->walk_counters[i];
+    return PGPU_OK;
+}
+
+int pgpu_realtime_open(pgpu_index* h, uint32_t capacity) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    if (h->ix.ip2cos) return fail(PGPU_E_UNSUPPORTED, "inserts into an ip2cos index");
+    std::lock_guard<std::mutex> g(h->mu);
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    std::string err;
+    if (int rc = pgpu::realtime_open(&h->ix, &h->rt, capacity, &err)) return fail(rc, err);
+    return PGPU_OK;
+}
+
+int pgpu_insert(pgpu_index* h, uint32_t n, const float* feature, int64_t* local_idx) {
+    if (h == nullptr) return fail(PGPU_E_INVALID, "null index");
+    if (n == 0) return PGPU_OK;
+    if (feature == nullptr || local_idx == nullptr) return fail(PGPU_E_INVALID, "null argument");
+    if (h->ix.ins_cap == 0) return fail(PGPU_E_INVALID, "pgpu_realtime_open was not called");
+    std::lock_guard<std::mutex> g(h->mu);
+    cudaSetDevice(h->device);
+    if (int rc = ensure_staging(h, 1)) return rc;
+    const uint32_t d = h->ix.qdim;
+    cudaStream_t st = h->stream;
+    std::vector<int32_t> status(h->max_batch);
+    for (uint32_t off = 0; off < n; off += h->max_batch) {
+        const uint32_t m = std::min(h->max_batch, n - off);
+        cudaError_t e = cudaMemcpyAsync(h->d_qin, feature + (uint64_t)off * d,
+                                        sizeof(float) * m * d, cudaMemcpyHostToDevice, st);
+        // single_build's normalisation (hierarchical_cluster_index.cpp:1513-1536); a
+        // non-finite or zero-norm feature is not inserted (local id -1)
+        if (e == cudaSuccess) e = pgpu::launch_prep_queries(h->ix, h->d_qin, m, h->s, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(status.data(), h->s.status, sizeof(int32_t) * m,
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(e, "insert");
+        for (uint32_t i = 0; i < m; ++i) status[i] = status[i] == 0 ? 1 : 0;
+        std::string err;
+        if (int rc = pgpu::realtime_insert(&h->ix, &h->rt, m, h->s.q, status.data(),
+                                           local_idx + off, st, &err))
+            return fail(rc, err);
+    }
     return PGPU_OK;
 }
 

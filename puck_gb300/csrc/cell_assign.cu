@@ -179,7 +179,8 @@ __global__ void k_fneg(const float* __restrict__ fn, uint32_t F, float* __restri
 
 cudaError_t launch_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C,
                                        const float* fine, uint32_t F, const float* x, uint64_t n,
-                                       uint32_t* cell, float* dist, cudaStream_t stream) {
+                                       uint32_t* cell, float* dist, cudaStream_t stream,
+                                       const float* stat_in) {
     if (n == 0) return cudaSuccess;
     // per-chunk scratch of at most 512 MiB for the two term matrices
     uint64_t chunk = (512ull << 20) / (4ull * (C + F) + 4);
@@ -191,7 +192,8 @@ cudaError_t launch_nearest_cell_assign(uint32_t dim, const float* coarse, uint32
     cudaError_t e = cudaMallocAsync(&cn, sizeof(float) * C, stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&fn, sizeof(float) * F, stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&fneg, sizeof(float) * F, stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&stat, sizeof(float) * (uint64_t)C * F, stream);
+    if (e == cudaSuccess && stat_in == nullptr)
+        e = cudaMallocAsync(&stat, sizeof(float) * (uint64_t)C * F, stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&ctm, sizeof(float) * chunk * C, stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&fip, sizeof(float) * chunk * F, stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&qn, sizeof(float) * chunk, stream);
@@ -201,7 +203,9 @@ cudaError_t launch_nearest_cell_assign(uint32_t dim, const float* coarse, uint32
         k_fneg<<<(F + 255) / 256, 256, 0, stream>>>(fn, F, fneg);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = launch_stationary(coarse, C, fine, F, dim, fn, stat, stream);
+    if (e == cudaSuccess && stat_in == nullptr)
+        e = launch_stationary(coarse, C, fine, F, dim, fn, stat, stream);
+    const float* sp = stat_in ? stat_in : stat;
     for (uint64_t r0 = 0; e == cudaSuccess && r0 < n; r0 += chunk) {
         const uint32_t rows = (uint32_t)(n - r0 < chunk ? n - r0 : chunk);
         const float* xr = x + r0 * dim;
@@ -211,7 +215,7 @@ cudaError_t launch_nearest_cell_assign(uint32_t dim, const float* coarse, uint32
         if (e == cudaSuccess) e = launch_half_norms(xr, rows, dim, qn, stream);
         if (e == cudaSuccess) {
             k_cell_walk<<<(rows + kWalkWarps - 1) / kWalkWarps, kWalkWarps * 32, 0, stream>>>(
-                ctm, fip, qn, rows, C, F, fneg, stat, cell + r0, dist + r0);
+                ctm, fip, qn, rows, C, F, fneg, sp, cell + r0, dist + r0);
             e = cudaGetLastError();
         }
     }

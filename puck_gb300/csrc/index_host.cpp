@@ -394,7 +394,8 @@ void free_device_index(DeviceIndex* ix) {
                     ix->feat_abs, ix->stationary, ix->stat_sorted, ix->stat_fine, ix->rec_fine,
                     ix->cell_start,
                     ix->min_dist_offset, ix->mem2local, ix->offsets, ix->codes, ix->codes_rot, ix->feat,
-                    ix->codebook, ix->pq_codebook, ix->pq_offsets, ix->pq_codes};
+                    ix->codebook, ix->pq_codebook, ix->pq_offsets, ix->pq_codes,
+                    ix->ins_head, ix->ins_next, ix->ins_cl_start, ix->ins_cl_ids};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     *ix = DeviceIndex();

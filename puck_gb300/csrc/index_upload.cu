@@ -160,17 +160,22 @@ fail:
     return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
 }
 
+cudaError_t launch_bf16_rows(const float* x, uint64_t rows, uint32_t d, uint16_t* out,
+                             float* absn, cudaStream_t stream) {
+    if (rows == 0) return cudaSuccess;
+    const uint64_t threads = rows * 32;
+    k_bf16_rows<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(x, rows, d, out, absn);
+    return cudaGetLastError();
+}
+
 int ensure_bf16_features(DeviceIndex* ix, std::string* err) {
     if (ix->feat_bf16 != nullptr) return PGPU_OK;
     uint64_t bytes = 0;
-    cudaError_t e = dev_alloc(&ix->feat_bf16, (uint64_t)ix->n * ix->d, &bytes);
-    if (e == cudaSuccess) e = dev_alloc(&ix->feat_abs, ix->n, &bytes);
-    if (e == cudaSuccess && ix->n) {
-        const uint64_t threads = (uint64_t)ix->n * 32;
-        k_bf16_rows<<<(unsigned)((threads + 255) / 256), 256>>>(ix->feat, ix->n, ix->d,
-                                                                ix->feat_bf16, ix->feat_abs);
-        e = cudaGetLastError();
-    }
+    // rows for the inserted points too (realtime: n + ins_cap)
+    const uint64_t rows = (uint64_t)ix->n + ix->ins_cap, used = (uint64_t)ix->n + ix->ins_n;
+    cudaError_t e = dev_alloc(&ix->feat_bf16, rows * ix->d, &bytes);
+    if (e == cudaSuccess) e = dev_alloc(&ix->feat_abs, rows, &bytes);
+    if (e == cudaSuccess) e = launch_bf16_rows(ix->feat, used, ix->d, ix->feat_bf16, ix->feat_abs, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         if (ix->feat_bf16) cudaFree(ix->feat_bf16);
@@ -203,10 +208,11 @@ int ensure_rotated_codes(DeviceIndex* ix, std::string* err) {
         ix->code_stride != ix->nsq || ix->n == 0)
         return PGPU_OK;
     uint64_t bytes = 0;
-    cudaError_t e = dev_alloc(&ix->codes_rot, (uint64_t)ix->n * ix->code_stride, &bytes);
+    const uint64_t rows = (uint64_t)ix->n + ix->ins_cap, used = (uint64_t)ix->n + ix->ins_n;
+    cudaError_t e = dev_alloc(&ix->codes_rot, rows * ix->code_stride, &bytes);
     if (e == cudaSuccess) {
-        k_rotate_codes<<<(unsigned)((ix->n + 255) / 256), 256>>>(ix->codes, ix->n, ix->nsq,
-                                                                 ix->codes_rot);
+        k_rotate_codes<<<(unsigned)((used + 255) / 256), 256>>>(ix->codes, used, ix->nsq,
+                                                                ix->codes_rot);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();

@@ -80,6 +80,13 @@ struct DeviceIndex {
     uint8_t* codes = nullptr;       // [n][code_stride]
     uint8_t* codes_rot = nullptr;   // [n][code_stride] precision-form scan copy: record r's
                                     // codes rotated by r mod nsq (made on first use)
+    // realtime inserts (realtime.cu): per-record arrays hold n + ins_cap rows, inserted
+    // point i at row (memory id) n + i
+    uint32_t ins_cap = 0, ins_n = 0;
+    int32_t* ins_head = nullptr;      // [C*F] newest insert id of each cell, -1: none
+    int32_t* ins_next = nullptr;      // [ins_cap] next older insert id of the same cell, -1
+    uint32_t* ins_cl_start = nullptr; // [C+1] each coarse cluster's range in ins_cl_ids
+    uint32_t* ins_cl_ids = nullptr;   // [ins_cap] inserted memory ids grouped by coarse cluster
     float* feat = nullptr;          // [n][d] original vectors
     uint16_t* feat_bf16 = nullptr;  // [n][d] BF16 copy (precision form; made on first use)
     float* feat_abs = nullptr;      // [n] |x| rounded up (error bound of the BF16 screen)
@@ -160,10 +167,28 @@ cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, 
 cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint64_t k,
                                           const float* x, uint64_t n, int32_t* assign, float* dis,
                                           float* xnorm, float* cnorm, cudaStream_t stream);
-// The build's exact nearest-cell assignment (cell_assign.cu).
+// The build's exact nearest-cell assignment (cell_assign.cu). stat: the [C][F]
+// stationary terms to use (an index's live ones), or null to compute them.
 cudaError_t launch_nearest_cell_assign(uint32_t dim, const float* coarse, uint32_t C,
                                        const float* fine, uint32_t F, const float* x, uint64_t n,
-                                       uint32_t* cell, float* dist, cudaStream_t stream);
+                                       uint32_t* cell, float* dist, cudaStream_t stream,
+                                       const float* stat = nullptr);
+// BF16 copy of rows and |x| rounded up (the precision form's screen operand).
+cudaError_t launch_bf16_rows(const float* x, uint64_t rows, uint32_t d, uint16_t* out,
+                             float* absn, cudaStream_t stream);
+// Host mirrors of the realtime lists (realtime.cu).
+struct RealtimeHost {
+    std::vector<int32_t> head;     // [C*F]
+    std::vector<int32_t> next;     // [ins_n]
+    std::vector<uint32_t> cluster; // [ins_n] coarse cluster of each insert
+    std::vector<uint32_t> cnt;     // [C*F] base + inserted points of each cell
+};
+// RealtimeInsertPuckIndex::init: room for cap inserted points (synchronous).
+int realtime_open(DeviceIndex* ix, RealtimeHost* rh, uint32_t cap, std::string* err);
+// Inserts the rows of x (DEVICE, [m][d], normalised as the index wants) whose ok[i]
+// (host) is set, in order; ids[i] = n + insert id, or -1. Synchronous.
+int realtime_insert(DeviceIndex* ix, RealtimeHost* rh, uint32_t m, const float* x,
+                    const int32_t* ok, int64_t* ids, cudaStream_t st, std::string* err);
 cudaError_t launch_gather_u32(const uint32_t* idx, uint64_t n, const uint32_t* table,
                               uint32_t* out, cudaStream_t stream);
 // Records `msg` as the calling thread's last error (pgpu_last_error) and returns `code`.

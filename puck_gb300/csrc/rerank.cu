@@ -67,6 +67,10 @@ struct RerankParams {
     const float* pq_offsets;
     const uint8_t* pq_codes;
     uint32_t pq_nsq, pq_lsq, pq_code_stride;
+    // a realtime index (RealtimeInsertPuckIndex) sums the PQ table subspace by
+    // subspace in order (realtime_insert_puck_index.cpp:466-499), not in
+    // lookup_dist_table's four partials
+    int pq_sequential;
 };
 
 // Exact-order squared L2 of G rows against q (shared memory), computed by one
@@ -273,6 +277,7 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
                 const uint32_t* w = reinterpret_cast<const uint32_t*>(
                     p.pq_codes + (uint64_t)mi * p.pq_code_stride);
                 float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                float t = __fadd_rn(__fsub_rn(hd[j], qn), p.pq_offsets[mi]);
                 for (uint32_t m0 = 0; m0 < p.pq_nsq; m0 += 4) {
                     const uint32_t c4 = __ldg(w + (m0 >> 2));
 #pragma unroll
@@ -281,13 +286,13 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
                         if (m < p.pq_nsq) {
                             const float y = __ldg(p.pq_codebook + (uint64_t)m * 256 + ((c4 >> (8 * k)) & 255u));
                             const float df = __fsub_rn(qv[m], y);
-                            a[k] = __fadd_rn(a[k], __fmul_rn(df, df));
+                            if (p.pq_sequential) t = __fadd_rn(t, __fmul_rn(df, df));
+                            else a[k] = __fadd_rn(a[k], __fmul_rn(df, df));
                         }
                     }
                 }
-                float t = __fsub_rn(hd[j], qn);
-                t = __fadd_rn(t, p.pq_offsets[mi]);
-                t = __fadd_rn(t, __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3])));
+                if (!p.pq_sequential)
+                    t = __fadd_rn(t, __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3])));
                 dist[j] = t;
             }
         } else {
@@ -299,8 +304,13 @@ __global__ __launch_bounds__(kThreads) void k_rerank(RerankParams p) {
                 const uint32_t mi = tags[j];
                 float t = __fsub_rn(hd[j], qn);
                 t = __fadd_rn(t, p.pq_offsets[mi]);
-                t = __fadd_rn(t,
-                              lut_sum(p.pq_codes + (uint64_t)mi * p.pq_code_stride, pq_lut, p.pq_nsq));
+                const uint8_t* code = p.pq_codes + (uint64_t)mi * p.pq_code_stride;
+                if (p.pq_sequential) {
+                    for (uint32_t m = 0; m < p.pq_nsq; ++m)
+                        t = __fadd_rn(t, pq_lut[m * 256 + code[m]]);
+                } else {
+                    t = __fadd_rn(t, lut_sum(code, pq_lut, p.pq_nsq));
+                }
                 dist[j] = t;
             }
         }
@@ -677,6 +687,7 @@ cudaError_t launch_rerank(const DeviceIndex& ix, const SearchConfig& cfg, uint32
     p.pq_nsq = ix.pq_nsq;
     p.pq_lsq = ix.pq_lsq;
     p.pq_code_stride = ix.pq_code_stride;
+    p.pq_sequential = ix.ins_cap > 0 ? 1 : 0;
     p.htag = s.htag;
     p.hcnt = s.hcnt;
     p.feat = ix.feat;

@@ -102,6 +102,8 @@ struct ScanParams {
     const float* codebook;
     unsigned long long* counters;
     const uint32_t* order;      // [B] query of each block
+    const uint32_t* ins_cl_start;  // realtime: [C+1] inserted records per cluster, or null
+    const uint32_t* ins_cl_ids;    // their memory ids
     uint32_t d, C, F, nsq, lsq, code_stride, P, T, cap;
     float codebook_max;
 };
@@ -443,7 +445,7 @@ struct ScanState {
     uint32_t count;
     uint32_t c;
     float cdl;
-    uint32_t r0, r1;
+    uint32_t r0, r1, i0, i1;
     unsigned long long evaluated, looked, passed;
     unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
@@ -514,17 +516,27 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             const uint32_t c = p.ctag[(uint64_t)qi * p.P + l];
             st.c = c;
             st.cdl = p.cdist[(uint64_t)qi * p.P + l];
+            st.i0 = st.i1 = 0;
             if (c < p.C) {
                 st.r0 = p.cell_start[(uint64_t)c * F];
                 st.r1 = p.cell_start[(uint64_t)c * F + F];
+                if (p.ins_cl_start) {
+                    st.i0 = p.ins_cl_start[c];
+                    st.i1 = p.ins_cl_start[c + 1];
+                }
             } else {
                 st.r0 = st.r1 = 0;  // never taken for finite queries
             }
         }
         __syncthreads();
-        const uint32_t c = st.c, r0 = st.r0, r1 = st.r1;
+        // the probed clusters fill a prefix of the slots (the learned probe leaves the
+        // rest empty): the first empty slot ends the walk
+        if (st.c >= p.C) break;
+        const uint32_t c = st.c, r0 = st.r0, r1 = st.r1, i0 = st.i0;
+        // the cluster's base records [r0, r1), then its inserted ones (realtime)
+        const uint32_t nb = r1 - r0, nall = nb + (st.i1 - st.i0);
         const float cdl = st.cdl;
-        if (r0 >= r1) continue;
+        if (nall == 0) continue;
         // per fine id of this cluster: 2 * cell_dist, cell_dist = (cd + stationary) + fd
         if ((F & 3u) == 0) {
             // 16-byte rows (F % 4 == 0): one float4 of each row per step
@@ -543,18 +555,20 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
                 srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
         }
         __syncthreads();
-        if (tid == 0) st.n_records += r1 - r0;
-        for (uint32_t base = r0; base < r1; base += kRound) {
+        if (tid == 0) st.n_records += nall;
+        for (uint32_t base = 0; base < nall; base += kRound) {
             const long long t_round = clock64();
             const uint64_t tau = st.tau;
             // all loads of the thread's records first, so their latencies overlap
             uint32_t fine_id[kRecPerThread];
             float off[kRecPerThread];
             uint32_t words[kRecPerThread][NW];
+            uint32_t mem[kRecPerThread];
 #pragma unroll
             for (int j = 0; j < kRecPerThread; ++j) {
-                const uint32_t mi = base + tid + j * kThreads;
-                const uint32_t mr = mi < r1 ? mi : r0;
+                const uint32_t v = base + tid + j * kThreads;
+                const uint32_t mr = v < nb ? r0 + v : (v < nall ? p.ins_cl_ids[i0 + v - nb] : r0);
+                mem[j] = mr;
                 fine_id[j] = p.rec_fine[mr];
                 off[j] = p.offsets[mr];
                 load_codes<NW>(TAB == kTabRot ? p.codes_rot : p.codes, p.code_stride, mr,
@@ -577,10 +591,10 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             };
 #pragma unroll
             for (int j = 0; j < kRecPerThread; ++j) {
-                const uint32_t mi = base + tid + j * kThreads;
+                const uint32_t mi = mem[j];
                 bool keep = false;
                 uint64_t key = 0;
-                if (mi < r1) {
+                if (base + tid + j * kThreads < nall) {
                     // (float)(2.0 * cell_dist + offset): one float add of the exact
                     // 2 * cell_dist (see adc_base)
                     const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
@@ -691,7 +705,8 @@ __device__ __forceinline__ uint32_t work_bucket(uint32_t w) {
 
 // One thread per query: its record count over the probed clusters, as a bucket.
 __global__ void k_scan_work(const uint32_t* __restrict__ ctag, const int32_t* __restrict__ status,
-                            const uint32_t* __restrict__ cell_start, uint32_t n, uint32_t P,
+                            const uint32_t* __restrict__ cell_start,
+                            const uint32_t* __restrict__ ins_cl_start, uint32_t n, uint32_t P,
                             uint32_t C, uint32_t F, uint8_t* __restrict__ wbucket) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
@@ -699,7 +714,9 @@ __global__ void k_scan_work(const uint32_t* __restrict__ ctag, const int32_t* __
     if (status[q] == 0) {
         for (uint32_t l = 0; l < P; ++l) {
             const uint32_t c = ctag[(uint64_t)q * P + l];
-            if (c < C) w += cell_start[(uint64_t)c * F + F] - cell_start[(uint64_t)c * F];
+            if (c >= C) break;  // the probed clusters fill a prefix of the slots
+            w += cell_start[(uint64_t)c * F + F] - cell_start[(uint64_t)c * F];
+            if (ins_cl_start) w += ins_cl_start[c + 1] - ins_cl_start[c];
         }
     }
     wbucket[q] = (uint8_t)work_bucket(w);
@@ -752,8 +769,9 @@ uint32_t scan_max_filter_topk() { return kMaxCap - kRound - 1024; }
 
 cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream) {
     if (s.order == nullptr || s.wbucket == nullptr) return cudaErrorInvalidValue;
-    k_scan_work<<<(n + 255) / 256, 256, 0, stream>>>(s.ctag, s.status, ix.cell_start, n, s.P, ix.C,
-                                                     ix.F, s.wbucket);
+    k_scan_work<<<(n + 255) / 256, 256, 0, stream>>>(s.ctag, s.status, ix.cell_start,
+                                                     ix.ins_n ? ix.ins_cl_start : nullptr, n, s.P,
+                                                     ix.C, ix.F, s.wbucket);
     k_scan_order<<<1, kOrderThreads, 0, stream>>>(s.wbucket, n, s.order);
     return cudaGetLastError();
 }
@@ -790,6 +808,8 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.codebook_max = ix.codebook_max;
     if (s.order == nullptr || s.T > scan_max_filter_topk()) return cudaErrorInvalidValue;
     p.order = s.order;
+    p.ins_cl_start = ix.ins_n ? ix.ins_cl_start : nullptr;
+    p.ins_cl_ids = ix.ins_cl_ids;
     const size_t smem = half_lut ? scan_smem_bytes_half(ix, s.T) : scan_smem_bytes(ix, s.T);
     const uint32_t nw = ix.code_stride / 4;
     auto launch = [&](void (*kernel)(ScanParams)) {

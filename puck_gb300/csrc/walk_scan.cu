@@ -51,6 +51,9 @@ struct WalkParams {
     const uint8_t* codes;
     const float* codebook;
     unsigned long long* counters;
+    const int32_t* ins_head;  // realtime: [C*F] newest insert of each cell, or null
+    const int32_t* ins_next;
+    uint32_t n_base;          // memory id of insert 0
     uint32_t d, C, F, nsq, lsq, code_stride, P, T;
     double rr;
 };
@@ -157,6 +160,20 @@ __device__ bool process_candidates(const WalkParams& p, WalkState& st, const Can
                     }
                     ++sp;
                     if (heap_update(hv, ht, p.T, dpc, tf, s0 + pp)) ++upd;
+                }
+                if (p.ins_head) {
+                    // realtime: the cell's inserted points, newest first, none skipped,
+                    // each counted as an update (realtime_insert_puck_index.cpp:398-453)
+                    const uint64_t cell = (uint64_t)st.c * p.F + cd.fine[i];
+                    for (int32_t id = p.ins_head[cell]; id >= 0; id = p.ins_next[id]) {
+                        const uint32_t mi = p.n_base + (uint32_t)id;
+                        const float t0 = adc_base(cd.dist[i], p.offsets[mi]);
+                        const float tf = __fadd_rn(
+                            t0, lut_sum(p.codes + (uint64_t)mi * p.code_stride, lut, p.nsq));
+                        ++sp;
+                        ++upd;
+                        heap_update(hv, ht, p.T, dpc, tf, mi);
+                    }
                 }
                 ins += upd;
                 if (upd > 0) pivot = pivot_of(hv[1], qn, p.rr);
@@ -383,6 +400,9 @@ cudaError_t launch_walk_scan(const DeviceIndex& ix, const SearchConfig& cfg, uin
     p.htag = s.htag;
     p.hcnt = s.hcnt;
     p.stationary = ix.stationary;
+    p.ins_head = ix.ins_n ? ix.ins_head : nullptr;
+    p.ins_next = ix.ins_next;
+    p.n_base = ix.n;
     p.stat_sorted = ix.stat_sorted;
     p.stat_fine = ix.stat_fine;
     p.cell_start = ix.cell_start;

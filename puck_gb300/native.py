@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = (
     "pgpu_contract_bf16", "pgpu_filter_candidates", "pgpu_probe_create", "pgpu_probe_destroy",
     "pgpu_probe_info", "pgpu_probe_train_step", "pgpu_probe_gradients", "pgpu_probe_forward",
     "pgpu_probe_get_params", "pgpu_probe_set_params", "pgpu_set_probe", "pgpu_knn",
-    "pgpu_puck_assign",
+    "pgpu_puck_assign", "pgpu_realtime_open", "pgpu_insert",
 )
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_CENTROIDS = 1 << 16
@@ -133,6 +133,8 @@ def load(build_if_missing=False):
     lib.pgpu_nearest_center.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
     lib.pgpu_nearest_center_noalloc.argtypes = [u32, vp, u64, vp, u64, vp, vp, vp]
     lib.pgpu_nearest_cell_assign.argtypes = [u32, vp, u32, vp, u32, vp, u64, vp, vp, vp]
+    lib.pgpu_realtime_open.argtypes = [vp, u32]
+    lib.pgpu_insert.argtypes = [vp, u32, vp, vp]
     lib.pgpu_puck_assign.argtypes = [u32, u64, vp, vp, vp, u32, vp, u32, vp, u32, vp, u32, vp, vp,
                                      vp, vp, vp]
     lib.pgpu_set_profiling.argtypes = [vp, ctypes.c_int]
@@ -275,6 +277,18 @@ class GpuIndex:
         check(load().pgpu_search(self._h, q.ctypes.data, topk, dist.ctypes.data, ids.ctypes.data,
                                  ctypes.byref(rn)))
         return dist, ids, rn.value
+
+    def realtime_open(self, capacity):
+        """Reserve room for `capacity` inserted points (RealtimeInsertPuckIndex::init)."""
+        check(load().pgpu_realtime_open(self._h, capacity))
+
+    def insert(self, features):
+        """Insert host features [n, query_dim]; returns their local ids (int64, -1 where
+        a feature was not inserted)."""
+        x = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, self.d)
+        ids = np.empty(x.shape[0], np.int64)
+        check(load().pgpu_insert(self._h, x.shape[0], x.ctypes.data, ids.ctypes.data))
+        return ids
 
     def set_profiling(self, enable=True):
         check(load().pgpu_set_profiling(self._h, int(bool(enable))))
