@@ -518,6 +518,23 @@ static float lookup_lut(const uint8_t* code, const float* lut, uint32_t nsq) {
     return h0 + h1;
 }
 
+/* Scan mode's sum for nsq a multiple of 4 up to 32 (the library's interleaved
+ * scan, puck_gb300/csrc/scan_select.cu): step s looks up subspace (s + lane) mod
+ * nsq, lane = memory id & 31, into partial s mod 4; then (p0 + p1) + (p2 + p3). */
+static int scan_rotated(uint32_t nsq) { return nsq > 0 && nsq % 4 == 0 && nsq <= 32; }
+
+static float lookup_lut_rotated(const uint8_t* code, const float* lut, uint32_t nsq, uint32_t mi) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const uint32_t lane = mi & 31u;
+    for (uint32_t s = 0; s < nsq; ++s) {
+        const uint32_t m = (s + lane) % nsq;
+        acc[s & 3] = acc[s & 3] + lut[(uint64_t)m * 256 + code[m]];
+    }
+    float h0 = acc[0] + acc[1];
+    float h1 = acc[2] + acc[3];
+    return h0 + h1;
+}
+
 /* L2Sqr16Ext, AVX build (puck/tinker/method/hnsw_distfunc_opt_impl_inline.h:41-69):
  * lanes i<8 hold d_i^2 + d_{i+8}^2; lanes summed left to right. */
 static float l2sqr16(const float* x, const float* q) {
@@ -792,7 +809,9 @@ static int search_one(const po_index* ix, const po_params* p, po_scratch* s, con
  * normalisation, coarse heap and LUT, then EVERY record of the probed coarse
  * clusters gets the reference's per-point distance
  *   t = (float)(2.0 * ((cd + stationary) + fd) + offset) + lookup_dist_table
- * (puck_index.cpp:360-368, 539-540); the filter_topk smallest by (t, memory id),
+ * (puck_index.cpp:360-368, 539-540), the table sum in the reference's order, or in
+ * the rotated order of lookup_lut_rotated where the library's interleaved scan
+ * applies (nsq a multiple of 4 up to 32); the filter_topk smallest by (t, memory id),
  * ascending, are reranked exactly as rank_topN_points does (puck_index.cpp:428-457). */
 typedef struct {
     float t;
@@ -841,6 +860,7 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
     }
     po_cand* cand = (po_cand*)malloc(sizeof(po_cand) * (total ? total : 1));
     uint64_t nc = 0;
+    const int rot = scan_rotated(nsq);
     for (uint32_t l = 0; l < P; ++l) {
         const uint32_t c = s->ctag[l];
         const float cdl = s->cd[l];
@@ -849,17 +869,20 @@ static int search_scan_one(const po_index* ix, const po_params* p, po_scratch* s
             const float cell_dist = (cdl + ix->stationary[cell]) + s->fd[f];
             for (uint32_t mi = ix->cell_start[cell]; mi < ix->cell_start[cell + 1]; ++mi) {
                 float t = (float)(2.0 * (double)cell_dist + (double)ix->offsets[mi]);
-                t = t + lookup_lut(ix->codes + (uint64_t)mi * nsq, s->lut, nsq);
+                t = t + (rot ? lookup_lut_rotated(ix->codes + (uint64_t)mi * nsq, s->lut, nsq, mi)
+                             : lookup_lut(ix->codes + (uint64_t)mi * nsq, s->lut, nsq));
                 cand[nc].t = t;
                 cand[nc].mi = mi;
                 ++nc;
             }
             /* realtime: the cell's inserted points, memory id n + insert id */
             for (int32_t id = ix->realtime ? ix->ins_head[cell] : -1; id >= 0; id = ix->ins_next[id]) {
+                const uint32_t mi = ix->n + (uint32_t)id;
                 float t = (float)(2.0 * (double)cell_dist + (double)ix->ins_off[id]);
-                t = t + lookup_lut(ix->ins_codes + (uint64_t)id * nsq, s->lut, nsq);
+                const uint8_t* code = ix->ins_codes + (uint64_t)id * nsq;
+                t = t + (rot ? lookup_lut_rotated(code, s->lut, nsq, mi) : lookup_lut(code, s->lut, nsq));
                 cand[nc].t = t;
-                cand[nc].mi = ix->n + (uint32_t)id;
+                cand[nc].mi = mi;
                 ++nc;
             }
         }

@@ -121,10 +121,11 @@ void apply_config(pgpu_index* h, const pgpu_params* p) {
 }
 
 int ensure_precision_data(pgpu_index* h) {
-    if (h->cfg.precision != PGPU_PRECISION_BF16) return PGPU_OK;
     std::string err;
-    // the scan's rotated code copy (one table bank per subspace)
-    if (int rc = pgpu::ensure_rotated_codes(&h->ix, &err)) return fail(rc, err);
+    // the scan's interleaved code copy (both precisions)
+    if (h->cfg.mode == PGPU_MODE_SCAN)
+        if (int rc = pgpu::ensure_interleaved_codes(&h->ix, &err)) return fail(rc, err);
+    if (h->cfg.precision != PGPU_PRECISION_BF16) return PGPU_OK;
     // the BF16 screen reranks original vectors; a PQ index reranks by its PQ
     if (h->ix.pq_nsq != 0) return PGPU_OK;
     if (int rc = pgpu::ensure_bf16_features(&h->ix, &err)) return fail(rc, err);

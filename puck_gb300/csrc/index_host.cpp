@@ -393,7 +393,7 @@ void free_device_index(DeviceIndex* ix) {
                     ix->fine_bf16, ix->feat_bf16,
                     ix->feat_abs, ix->stationary, ix->stat_sorted, ix->stat_fine, ix->rec_fine,
                     ix->cell_start,
-                    ix->min_dist_offset, ix->mem2local, ix->offsets, ix->codes, ix->codes_rot, ix->feat,
+                    ix->min_dist_offset, ix->mem2local, ix->offsets, ix->codes, ix->codes_il, ix->feat,
                     ix->codebook, ix->pq_codebook, ix->pq_offsets, ix->pq_codes,
                     ix->ins_head, ix->ins_next, ix->ins_cl_start, ix->ins_cl_ids};
     for (void* q : ptrs)

@@ -189,37 +189,52 @@ int ensure_bf16_features(DeviceIndex* ix, std::string* err) {
     return PGPU_OK;
 }
 
-// out[r][s] = in[r][(s + r mod nsq) mod nsq] for s < nsq (stride == nsq).
-__global__ void k_rotate_codes(const uint8_t* __restrict__ in, uint64_t n, uint32_t nsq,
-                               uint8_t* __restrict__ out) {
-    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    const uint32_t rho = (uint32_t)(r % nsq);
-    const uint8_t* src = in + r * nsq;
-    uint8_t* dst = out + r * nsq;
-    for (uint32_t s = 0; s < nsq; ++s) {
-        const uint32_t m = s + rho < nsq ? s + rho : s + rho - nsq;
-        dst[s] = src[m];
+// One thread per record: its rotated codes (byte s = code of subspace
+// (s + (r & 31)) mod nsq) written as 8-byte granules of the interleaved layout.
+__global__ void k_interleave_codes(const uint8_t* __restrict__ codes, uint32_t stride,
+                                   uint32_t nsq, uint64_t r0, uint64_t rows,
+                                   uint8_t* __restrict__ il) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const uint64_t r = r0 + i;
+    const uint32_t rho = (uint32_t)(r & 31) % nsq;
+    const uint8_t* src = codes + r * stride;
+    const uint32_t ng = il_record_bytes(nsq) / 8;
+    for (uint32_t g = 0; g < ng; ++g) {
+        unsigned long long v = 0;
+        for (uint32_t b = 0; b < 8; ++b) {
+            const uint32_t s = g * 8 + b;
+            if (s < nsq) {
+                const uint32_t m = s + rho < nsq ? s + rho : s + rho - nsq;
+                v |= (unsigned long long)src[m] << (8 * b);
+            }
+        }
+        *reinterpret_cast<unsigned long long*>(il + il_granule_offset(r, g, nsq)) = v;
     }
 }
 
-int ensure_rotated_codes(DeviceIndex* ix, std::string* err) {
-    if (ix->codes_rot != nullptr || ix->nsq % 4 != 0 || ix->nsq > 32 ||
-        ix->code_stride != ix->nsq || ix->n == 0)
-        return PGPU_OK;
+cudaError_t launch_interleave_codes(const uint8_t* codes, uint32_t code_stride, uint32_t nsq,
+                                    uint64_t r0, uint64_t rows, uint8_t* il, cudaStream_t stream) {
+    if (rows == 0) return cudaSuccess;
+    k_interleave_codes<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(codes, code_stride, nsq,
+                                                                          r0, rows, il);
+    return cudaGetLastError();
+}
+
+int ensure_interleaved_codes(DeviceIndex* ix, std::string* err) {
+    if (ix->codes_il != nullptr || !il_applies(ix->nsq) || ix->n == 0) return PGPU_OK;
     uint64_t bytes = 0;
+    // rows for the inserted points too (realtime: n + ins_cap)
     const uint64_t rows = (uint64_t)ix->n + ix->ins_cap, used = (uint64_t)ix->n + ix->ins_n;
-    cudaError_t e = dev_alloc(&ix->codes_rot, rows * ix->code_stride, &bytes);
-    if (e == cudaSuccess) {
-        k_rotate_codes<<<(unsigned)((used + 255) / 256), 256>>>(ix->codes, used, ix->nsq,
-                                                                ix->codes_rot);
-        e = cudaGetLastError();
-    }
+    cudaError_t e = dev_alloc(&ix->codes_il, il_bytes(rows, ix->nsq), &bytes);
+    if (e == cudaSuccess) e = cudaMemset(ix->codes_il, 0, il_bytes(rows, ix->nsq));
+    if (e == cudaSuccess)
+        e = launch_interleave_codes(ix->codes, ix->code_stride, ix->nsq, 0, used, ix->codes_il, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
-        if (ix->codes_rot) cudaFree(ix->codes_rot);
-        ix->codes_rot = nullptr;
-        *err = std::string("rotated code copy: ") + cudaGetErrorString(e);
+        if (ix->codes_il) cudaFree(ix->codes_il);
+        ix->codes_il = nullptr;
+        *err = std::string("interleaved code copy: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? PGPU_E_NOMEM : PGPU_E_CUDA;
     }
     ix->bytes += bytes;

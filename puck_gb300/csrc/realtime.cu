@@ -5,8 +5,8 @@
 // cell, a list of them newest first (InsertFineCluster, :398-453); its searches
 // scan a cell's base records (with the walk's break) and then every inserted point
 // of the cell, with memory id n + insert id. Here:
-//   * every per-record device array (filter offsets and codes, the rotated code
-//     copy, fine ids, the vectors or the second-level PQ records, the memory ->
+//   * every per-record device array (filter offsets and codes, the scan's
+//     interleaved code copy, fine ids, the vectors or the second-level PQ records, the memory ->
 //     local map, the BF16 copy) is widened once, at open, to n + capacity rows, and
 //     an inserted point's records are written to row n + insert id; nothing that
 //     reads a record by memory id needs to know whether it was inserted;
@@ -51,7 +51,7 @@ cudaError_t grow(T** p, uint64_t old_count, uint64_t new_count, uint64_t* bytes)
 }
 
 // Records of m inserted points into rows base_row + i of the index's arrays: filter
-// offset and codes (packed nsq bytes -> code_stride rows, and the rotated copy),
+// offset and codes (packed nsq bytes -> code_stride rows),
 // fine id, memory -> local id, second-level PQ, vector.
 __global__ void k_ins_records(uint32_t m, uint64_t base_row, const uint32_t* __restrict__ cell,
                               uint32_t F, const float* __restrict__ f_off,
@@ -69,14 +69,8 @@ __global__ void k_ins_records(uint32_t m, uint64_t base_row, const uint32_t* __r
         ix.mem2local[r] = (uint32_t)r;
         if (pnsq) ix.pq_offsets[r] = p_off[i];
     }
-    const uint32_t rho = (uint32_t)(r % nsq);
-    for (uint32_t s = t; s < stride; s += blockDim.x) {
+    for (uint32_t s = t; s < stride; s += blockDim.x)
         ix.codes[r * stride + s] = s < nsq ? f_codes[(uint64_t)i * nsq + s] : 0;
-        if (ix.codes_rot) {
-            const uint32_t mm = s + rho < nsq ? s + rho : s + rho - nsq;
-            ix.codes_rot[r * stride + s] = f_codes[(uint64_t)i * nsq + mm];
-        }
-    }
     for (uint32_t s = t; pnsq && s < pstride; s += blockDim.x)
         ix.pq_codes[r * pstride + s] = s < pnsq ? p_codes[(uint64_t)i * pnsq + s] : 0;
     if (ix.feat) {
@@ -118,7 +112,8 @@ int realtime_open(DeviceIndex* ix, RealtimeHost* rh, uint32_t cap, std::string* 
     if (e == cudaSuccess) e = grow(&(ptr), n * (per), N * (per), &bytes);
     PGPU_GROW(ix->offsets, 1);
     PGPU_GROW(ix->codes, ix->code_stride);
-    PGPU_GROW(ix->codes_rot, ix->code_stride);
+    if (e == cudaSuccess)
+        e = grow(&ix->codes_il, il_bytes(n, ix->nsq), il_bytes(N, ix->nsq), &bytes);
     PGPU_GROW(ix->rec_fine, 1);
     PGPU_GROW(ix->mem2local, 1);
     PGPU_GROW(ix->feat, ix->d);
@@ -242,6 +237,8 @@ int realtime_insert(DeviceIndex* ix, RealtimeHost* rh, uint32_t m, const float* 
         k_ins_records<<<v, 128, 0, st>>>(v, row0, cell, F, f_off, f_codes, fnsq, ix->code_stride,
                                          p_off, p_codes, pnsq, ix->pq_code_stride, xs, d, *ix);
         e = cudaGetLastError();
+        if (e == cudaSuccess && ix->codes_il)
+            e = launch_interleave_codes(ix->codes, ix->code_stride, fnsq, row0, v, ix->codes_il, st);
         if (e == cudaSuccess && ix->feat_bf16)
             e = launch_bf16_rows(ix->feat + row0 * d, v, d, ix->feat_bf16 + row0 * d,
                                  ix->feat_abs + row0, st);

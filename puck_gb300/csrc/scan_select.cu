@@ -35,17 +35,25 @@
 // sum is multiplied by 2^-e. Entries are non-negative, so t >= t0 still holds and
 // the threshold test before the lookups stays valid.
 //
-// Rotated layout (precision form, nsq a multiple of 4 and at most 32): the FP32
-// table's lookups are random 4-byte gathers, and all 32 lanes of a warp read the
-// same subspace's 1 KB table at once, so they collide in shared-memory banks
-// (about 3.4 wavefronts per warp-wide lookup). Here subspace m's table lives in
-// bank m alone (FP16 entries c and c+1 share a word: byte address
-// (c >> 1) * 128 + 4m + 2 (c & 1)), and record r's codes are stored rotated by
-// r mod nsq (DeviceIndex::codes_rot), so at lookup step s a lane reads byte s and
-// looks up subspace (s + r mod nsq) mod nsq: consecutive records, on consecutive
-// lanes, hit distinct banks (lanes L and L + nsq share one; two wavefronts per
-// lookup at nsq = 24, one at 32). The precision form sums in FP32 in this
-// rotated order (its error bound does not depend on the order).
+// Interleaved kernel (k_scan_il; nsq a multiple of 4, at most 32: every index
+// the library builds for its configurations). The codes come from the interleaved
+// copy (DeviceIndex::codes_il, pgpu_internal.h): record r's codes rotated by
+// l = r & 31, its lane in a block of 32 records. Thread t of a round takes the
+// records whose memory id is congruent to t mod 32, so every 8-byte code load of a
+// warp reads one whole 256-byte line, and at lookup step s lane l reads table
+// column s + l. The table holds, for each code c (a row) and each column
+// m' < nsq + 31, the entry of subspace m' mod nsq at word c * 64 + m' (FP32) or
+// half c * 64 + m' (FP16): the 32 lanes of a warp read 32 distinct banks at every
+// lookup, whatever the codes (the reference's [subspace][code] table costs about
+// 3.4 shared-memory wavefronts per warp-wide lookup of random codes). A lookup is
+// one PRMT (the address (c << 8) | 4l from the code word and the lane), one load
+// and one add. The sum runs in the rotated order: lookup step s goes to partial
+// s mod 4, and t = t0 + ((a0 + a1) + (a2 + a3)), FP32 throughout; the oracle's
+// scan mode restates that order (the reference's own order, partial m mod 4 over
+// subspaces m, holds for the other kernel, k_scan_select). This kernel has no
+// threshold test before the lookups: t0 lacks the table's |q|^2 share, so the test
+// passes for almost every record. Loads are double-buffered: a round's records are
+// fetched while the previous round is scored.
 #include <cuda_fp16.h>
 
 #include "device_common.cuh"
@@ -98,7 +106,7 @@ struct ScanParams {
     const uint16_t* rec_fine; // [n] fine id of each record
     const float* offsets;
     const uint8_t* codes;
-    const uint8_t* codes_rot;   // rotated copy (kTabRot)
+    const uint8_t* codes_il;    // interleaved copy (k_scan_il)
     const float* codebook;
     unsigned long long* counters;
     const uint32_t* order;      // [B] query of each block
@@ -122,7 +130,7 @@ __device__ __forceinline__ int half_lut_exponent(float qnorm, float codebook_max
 // load per subspace when lsq = 4), in the reference's lane order (l2sqr_sse).
 // Table variants: FP32 (the reference's values and order), FP16 in the same
 // layout, FP16 in the rotated one-bank-per-subspace layout.
-enum { kTabF32 = 0, kTabF16 = 1, kTabRot = 2 };
+enum { kTabF32 = 0, kTabF16 = 1 };
 
 template <int TAB>
 __device__ __forceinline__ void build_table(void* lut, const float* qv,
@@ -130,10 +138,7 @@ __device__ __forceinline__ void build_table(void* lut, const float* qv,
                                             uint32_t lsq, float scale) {
     for (uint32_t j = threadIdx.x; j < 256; j += kThreads) {
         auto store = [&](uint32_t m, float v) {
-            if (TAB == kTabRot)
-                *reinterpret_cast<__half*>(reinterpret_cast<unsigned char*>(lut) + (j >> 1) * 128 +
-                                           4 * m + 2 * (j & 1)) = __float2half_rn(v * scale);
-            else if (TAB == kTabF16)
+            if (TAB == kTabF16)
                 reinterpret_cast<__half*>(lut)[m * 256 + j] = __float2half_rn(v * scale);
             else
                 reinterpret_cast<float*>(lut)[m * 256 + j] = v;
@@ -178,29 +183,6 @@ __device__ __forceinline__ float lut_sum_words_half(const uint32_t (&w)[NW], con
         if (m + 3 < nsq) a3 += __half2float(lut[(m + 3) * 256 + (c >> 24)]);
     }
     return (a0 + a1) + (a2 + a3);
-}
-
-// Sum of the record's table entries in the rotated layout: byte s of the rotated
-// codes is subspace (s + rho) mod nsq, whose entries sit in bank (s + rho) mod nsq.
-// nsq == 4 * NW. FP32 accumulation in the rotated order.
-template <int NW>
-__device__ __forceinline__ float lut_sum_rot(const uint32_t (&w)[NW], const unsigned char* lut,
-                                             uint32_t nsq, uint32_t rho) {
-    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    uint32_t mb = 4u * rho;  // byte offset of the current subspace's bank
-    const uint32_t wrap = 4u * nsq;
-#pragma unroll
-    for (int i = 0; i < NW; ++i) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t c = (w[i] >> (8 * j)) & 0xffu;
-            const uint32_t addr = ((c >> 1) << 7) + ((c & 1u) << 1) + mb;
-            a[j] += __half2float(*reinterpret_cast<const __half*>(lut + addr));
-            mb += 4u;
-            mb = mb == wrap ? 0u : mb;
-        }
-    }
-    return (a[0] + a[1]) + (a[2] + a[3]);
 }
 
 __device__ __forceinline__ float key_value(uint64_t k) {
@@ -450,198 +432,109 @@ struct ScanState {
     unsigned long long cyc_rounds, cyc_compact, n_compact, n_records;
 };
 
-// Loads the NW code words of record `mr` (8-byte loads when the row stride allows).
-template <int NW>
-__device__ __forceinline__ void load_codes(const uint8_t* codes, uint32_t stride, uint32_t mr,
-                                           uint32_t (&w)[NW]) {
-    if ((NW & 1) == 0 && (stride & 7u) == 0) {
-        const uint2* cw = reinterpret_cast<const uint2*>(codes + (uint64_t)mr * stride);
-#pragma unroll
-        for (int i = 0; i < NW / 2; ++i) {
-            const uint2 v = __ldg(cw + i);
-            w[2 * i] = v.x;
-            w[2 * i + 1] = v.y;
+// Slot l of query qi's probed clusters into st (all threads; barriers on both
+// sides): false when the slot is empty (the probed clusters fill a prefix).
+__device__ __forceinline__ bool scan_cluster_begin(const ScanParams& p, ScanState& st, uint32_t qi,
+                                                   uint32_t l) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t c = p.ctag[(uint64_t)qi * p.P + l];
+        st.c = c;
+        st.cdl = p.cdist[(uint64_t)qi * p.P + l];
+        st.i0 = st.i1 = 0;
+        st.r0 = st.r1 = 0;
+        if (c < p.C) {
+            st.r0 = p.cell_start[(uint64_t)c * p.F];
+            st.r1 = p.cell_start[(uint64_t)c * p.F + p.F];
+            if (p.ins_cl_start) {
+                st.i0 = p.ins_cl_start[c];
+                st.i1 = p.ins_cl_start[c + 1];
+            }
+        }
+    }
+    __syncthreads();
+    return st.c < p.C;
+}
+
+// srow[f] = 2 * cell_dist of cluster c's cell f, cell_dist = (cd + stationary) + fd
+// (puck_index.cpp:539-540); all threads, barrier after.
+__device__ __forceinline__ void scan_fill_srow(const ScanParams& p, float* srow, const float* fdk,
+                                               uint32_t c, float cdl) {
+    const uint32_t F = p.F;
+    if ((F & 3u) == 0) {
+        // 16-byte rows (F % 4 == 0): one float4 of each row per step
+        const float4* st4 = reinterpret_cast<const float4*>(p.stationary + (uint64_t)c * F);
+        const float4* fd4 = reinterpret_cast<const float4*>(fdk);
+        float4* s4 = reinterpret_cast<float4*>(srow);
+        for (uint32_t i = threadIdx.x; i < (F >> 2); i += blockDim.x) {
+            const float4 a = __ldg(st4 + i), b = __ldg(fd4 + i);
+            s4[i] = make_float4(2.0f * __fadd_rn(__fadd_rn(cdl, a.x), b.x),
+                                2.0f * __fadd_rn(__fadd_rn(cdl, a.y), b.y),
+                                2.0f * __fadd_rn(__fadd_rn(cdl, a.z), b.z),
+                                2.0f * __fadd_rn(__fadd_rn(cdl, a.w), b.w));
         }
     } else {
-        const uint32_t* cw = reinterpret_cast<const uint32_t*>(codes + (uint64_t)mr * stride);
-#pragma unroll
-        for (int i = 0; i < NW; ++i) w[i] = __ldg(cw + i);
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
+            srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
+    }
+    __syncthreads();
+}
+
+// Buffer insert of one round slot: the kept keys of the warp take consecutive
+// slots (one shared atomic per warp). The capacity is kept >= count + a round by
+// the cut in scan_after_round.
+__device__ __forceinline__ void scan_insert(ScanState& st, uint64_t* keys, bool keep, uint64_t key,
+                                            unsigned long long& my_pass) {
+    const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    if (ballot) {
+        const int lane = threadIdx.x & 31;
+        uint32_t base_slot = 0;
+        if (lane == __ffs(ballot) - 1) base_slot = atomicAdd(&st.count, (uint32_t)__popc(ballot));
+        base_slot = __shfl_sync(0xffffffffu, base_slot, __ffs(ballot) - 1);
+        if (keep) {
+            keys[base_slot + __popc(ballot & ((1u << lane) - 1))] = key;
+            ++my_pass;
+        }
     }
 }
 
-// NW = code words per record (code_stride / 4); TAB = table variant.
-template <int NW, int TAB>
-__global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(ScanParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ ScanState st;
-    const uint32_t qi = p.order[blockIdx.x];
-    const int tid = threadIdx.x;
-    const uint32_t nsq = p.nsq, F = p.F, T = p.T, cap = p.cap;
-    uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [cap], first (8-byte aligned)
-    uint32_t* hist = reinterpret_cast<uint32_t*>(keys + cap);  // [kHistBins]
-    float* lut = reinterpret_cast<float*>(hist + kHistBins);
-    __half* luth = reinterpret_cast<__half*>(lut);
-    constexpr bool HALF = TAB != kTabF32;
-    // [F] 2 * cell_dist of the current cluster's cells, after the table (the rotated
-    // layout spans 128 rows x 32 banks whatever nsq <= 32 is)
-    float* srow = TAB == kTabRot ? reinterpret_cast<float*>(luth + 32 * 256)
-                  : HALF         ? reinterpret_cast<float*>(luth + nsq * 256)
-                                 : lut + nsq * 256;
-    float* qv = srow + F;                  // [d]
-
-    if (p.status[qi] != 0) {
-        if (tid == 0) p.hcnt[qi] = 0;
-        return;
-    }
-    const long long t_start = clock64();
-    for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
-    const float* fdk = p.fd_by_fine + (uint64_t)qi * F;  // fine terms of this query
-    if (tid == 0) {
-        st.tau = kKeyMax;
-        st.count = 0;
-        st.evaluated = 0;
-        st.looked = 0;
-        st.passed = 0;
-        st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
-    }
-    const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
-    const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
+// After a round (all threads): cut the buffer back when it could not take another
+// round of `round` keys. One histogram pass gives a bound with at least T keys below
+// it (the final select is exact); tau = that bound. If the cut kept too many to take
+// another round, cut exactly to T.
+__device__ __forceinline__ void scan_after_round(ScanState& st, uint64_t* keys, uint32_t* hist,
+                                                 uint32_t cap, uint32_t round, uint32_t T,
+                                                 uint64_t tau, long long t_round) {
     __syncthreads();
-    build_table<TAB>(lut, qv, p.codebook, nsq, p.lsq, HALF ? ldexpf(1.0f, lut_e) : 1.0f);
-    unsigned long long my_eval = 0, my_look = 0, my_pass = 0;
-    const long long t_pro = clock64();
-    for (uint32_t l = 0; l < p.P; ++l) {
-        __syncthreads();
-        if (tid == 0) {
-            const uint32_t c = p.ctag[(uint64_t)qi * p.P + l];
-            st.c = c;
-            st.cdl = p.cdist[(uint64_t)qi * p.P + l];
-            st.i0 = st.i1 = 0;
-            if (c < p.C) {
-                st.r0 = p.cell_start[(uint64_t)c * F];
-                st.r1 = p.cell_start[(uint64_t)c * F + F];
-                if (p.ins_cl_start) {
-                    st.i0 = p.ins_cl_start[c];
-                    st.i1 = p.ins_cl_start[c + 1];
-                }
-            } else {
-                st.r0 = st.r1 = 0;  // never taken for finite queries
-            }
+    const long long t_round_end = clock64();
+    if (threadIdx.x == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
+    if (st.count > cap - round) {
+        const uint32_t cnt = st.count;
+        uint64_t bound = block_cut_bound(keys, cnt, T, hist, st.red);
+        uint32_t kept = bound == kKeyMax ? cnt : block_compact_lt(keys, cnt, bound, &st.ccount);
+        if (kept > cap - round) {
+            const uint64_t kth = block_select_kth(keys, kept, T, st.hist, st.sel);
+            bound = kth + 1;  // kth < kKeyMax: keys are distinct by id
+            kept = block_compact_lt(keys, kept, bound, &st.ccount);
+        }
+        if (threadIdx.x == 0) {
+            st.count = kept;
+            st.tau = bound < tau ? bound : tau;
+            st.n_compact += 1;
+            st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
         }
         __syncthreads();
-        // the probed clusters fill a prefix of the slots (the learned probe leaves the
-        // rest empty): the first empty slot ends the walk
-        if (st.c >= p.C) break;
-        const uint32_t c = st.c, r0 = st.r0, r1 = st.r1, i0 = st.i0;
-        // the cluster's base records [r0, r1), then its inserted ones (realtime)
-        const uint32_t nb = r1 - r0, nall = nb + (st.i1 - st.i0);
-        const float cdl = st.cdl;
-        if (nall == 0) continue;
-        // per fine id of this cluster: 2 * cell_dist, cell_dist = (cd + stationary) + fd
-        if ((F & 3u) == 0) {
-            // 16-byte rows (F % 4 == 0): one float4 of each row per step
-            const float4* st4 = reinterpret_cast<const float4*>(p.stationary + (uint64_t)c * F);
-            const float4* fd4 = reinterpret_cast<const float4*>(fdk);
-            float4* s4 = reinterpret_cast<float4*>(srow);
-            for (uint32_t i = tid; i < (F >> 2); i += kThreads) {
-                const float4 a = __ldg(st4 + i), b = __ldg(fd4 + i);
-                s4[i] = make_float4(2.0f * __fadd_rn(__fadd_rn(cdl, a.x), b.x),
-                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.y), b.y),
-                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.z), b.z),
-                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.w), b.w));
-            }
-        } else {
-            for (uint32_t i = tid; i < F; i += kThreads)
-                srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, p.stationary[(uint64_t)c * F + i]), fdk[i]);
-        }
-        __syncthreads();
-        if (tid == 0) st.n_records += nall;
-        for (uint32_t base = 0; base < nall; base += kRound) {
-            const long long t_round = clock64();
-            const uint64_t tau = st.tau;
-            // all loads of the thread's records first, so their latencies overlap
-            uint32_t fine_id[kRecPerThread];
-            float off[kRecPerThread];
-            uint32_t words[kRecPerThread][NW];
-            uint32_t mem[kRecPerThread];
-#pragma unroll
-            for (int j = 0; j < kRecPerThread; ++j) {
-                const uint32_t v = base + tid + j * kThreads;
-                const uint32_t mr = v < nb ? r0 + v : (v < nall ? p.ins_cl_ids[i0 + v - nb] : r0);
-                mem[j] = mr;
-                fine_id[j] = p.rec_fine[mr];
-                off[j] = p.offsets[mr];
-                load_codes<NW>(TAB == kTabRot ? p.codes_rot : p.codes, p.code_stride, mr,
-                               words[j]);
-            }
-            // one shared atomic per warp for the kept records
-            auto insert = [&](bool keep, uint64_t key) {
-                const unsigned ballot = __ballot_sync(0xffffffffu, keep);
-                if (ballot) {
-                    const int lane = tid & 31;
-                    uint32_t base_slot = 0;
-                    if (lane == __ffs(ballot) - 1) base_slot = atomicAdd(&st.count, (uint32_t)__popc(ballot));
-                    base_slot = __shfl_sync(0xffffffffu, base_slot, __ffs(ballot) - 1);
-                    if (keep) {
-                        // capacity is kept >= count + kRound by the compaction below
-                        keys[base_slot + __popc(ballot & ((1u << lane) - 1))] = key;
-                        ++my_pass;
-                    }
-                }
-            };
-#pragma unroll
-            for (int j = 0; j < kRecPerThread; ++j) {
-                const uint32_t mi = mem[j];
-                bool keep = false;
-                uint64_t key = 0;
-                if (base + tid + j * kThreads < nall) {
-                    // (float)(2.0 * cell_dist + offset): one float add of the exact
-                    // 2 * cell_dist (see adc_base)
-                    const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
-                    ++my_eval;
-                    if (filter_key(t0, mi) < tau) {  // t can only grow past t0
-                        ++my_look;
-                        float t;
-                        if (TAB == kTabRot)
-                            t = t0 + lut_sum_rot<NW>(words[j],
-                                                     reinterpret_cast<const unsigned char*>(lut),
-                                                     nsq, mi % nsq) * inv_scale;
-                        else if (TAB == kTabF16)
-                            t = t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale;
-                        else
-                            t = __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
-                        key = filter_key(t, mi);
-                        keep = key < tau;
-                    }
-                }
-                insert(keep, key);
-            }
-            __syncthreads();
-            const long long t_round_end = clock64();
-            if (tid == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
-            // cut back when the buffer could not take another round
-            if (st.count > cap - kRound) {
-                // one histogram pass: a bound with at least T keys below it (the final
-                // select below is exact); tau = that bound. If the cut kept too many to
-                // take another round, cut exactly to T.
-                const uint32_t cnt = st.count;
-                uint64_t bound = block_cut_bound(keys, cnt, T, hist, st.red);
-                uint32_t kept = bound == kKeyMax ? cnt : block_compact_lt(keys, cnt, bound, &st.ccount);
-                if (kept > cap - kRound) {
-                    const uint64_t kth = block_select_kth(keys, kept, T, st.hist, st.sel);
-                    bound = kth + 1;  // kth < kKeyMax: keys are distinct by id
-                    kept = block_compact_lt(keys, kept, bound, &st.ccount);
-                }
-                if (tid == 0) {
-                    st.count = kept;
-                    st.tau = bound < tau ? bound : tau;
-                    st.n_compact += 1;
-                    st.cyc_compact += (unsigned long long)(clock64() - t_round_end);
-                }
-                __syncthreads();
-            }
-        }
     }
+}
+
+// The block's last steps: the exact T smallest keys of the buffer, written out
+// unordered (only the rerank's tie path needs their (t, id) order, and it sorts
+// them itself), and the diagnostic counters.
+__device__ void scan_finish(const ScanParams& p, ScanState& st, uint64_t* keys, uint32_t qi,
+                            unsigned long long my_eval, unsigned long long my_look,
+                            unsigned long long my_pass, long long t_start, long long t_pro) {
+    const int tid = threadIdx.x;
+    const uint32_t T = p.T;
     __syncthreads();
     const long long t_final = clock64();
     uint32_t count = st.count;
@@ -650,8 +543,6 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
         block_compact_lt(keys, count, kth + 1, &st.ccount);
         count = T;
     }
-    // the T survivors leave unordered: only the rerank's tie path needs their
-    // (t, id) order, and it sorts them itself
     const uint32_t out = count < T ? count : T;
     for (uint32_t i = tid; i < T; i += kThreads) {
         p.hdist[(uint64_t)qi * T + i] = i < out ? key_value(keys[i]) : sentinel_f();
@@ -685,6 +576,309 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             atomicAdd(p.counters + kScCycFinal, (unsigned long long)(t_end - t_final));
         }
     }
+}
+
+// Loads the NW code words of record `mr` (8-byte loads when the row stride allows).
+template <int NW>
+__device__ __forceinline__ void load_codes(const uint8_t* codes, uint32_t stride, uint32_t mr,
+                                           uint32_t (&w)[NW]) {
+    if ((NW & 1) == 0 && (stride & 7u) == 0) {
+        const uint2* cw = reinterpret_cast<const uint2*>(codes + (uint64_t)mr * stride);
+#pragma unroll
+        for (int i = 0; i < NW / 2; ++i) {
+            const uint2 v = __ldg(cw + i);
+            w[2 * i] = v.x;
+            w[2 * i + 1] = v.y;
+        }
+    } else {
+        const uint32_t* cw = reinterpret_cast<const uint32_t*>(codes + (uint64_t)mr * stride);
+#pragma unroll
+        for (int i = 0; i < NW; ++i) w[i] = __ldg(cw + i);
+    }
+}
+
+// NW = code words per record (code_stride / 4); TAB = table variant.
+template <int NW, int TAB>
+__global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(ScanParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ScanState st;
+    const uint32_t qi = p.order[blockIdx.x];
+    const int tid = threadIdx.x;
+    const uint32_t nsq = p.nsq, F = p.F, T = p.T, cap = p.cap;
+    uint64_t* keys = reinterpret_cast<uint64_t*>(smem);  // [cap], first (8-byte aligned)
+    uint32_t* hist = reinterpret_cast<uint32_t*>(keys + cap);  // [kHistBins]
+    float* lut = reinterpret_cast<float*>(hist + kHistBins);
+    __half* luth = reinterpret_cast<__half*>(lut);
+    constexpr bool HALF = TAB != kTabF32;
+    // [F] 2 * cell_dist of the current cluster's cells, after the table
+    float* srow = HALF ? reinterpret_cast<float*>(luth + nsq * 256) : lut + nsq * 256;
+    float* qv = srow + F;                  // [d]
+
+    if (p.status[qi] != 0) {
+        if (tid == 0) p.hcnt[qi] = 0;
+        return;
+    }
+    const long long t_start = clock64();
+    for (uint32_t i = tid; i < p.d; i += kThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    const float* fdk = p.fd_by_fine + (uint64_t)qi * F;  // fine terms of this query
+    if (tid == 0) {
+        st.tau = kKeyMax;
+        st.count = 0;
+        st.evaluated = 0;
+        st.looked = 0;
+        st.passed = 0;
+        st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
+    }
+    const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
+    const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
+    __syncthreads();
+    build_table<TAB>(lut, qv, p.codebook, nsq, p.lsq, HALF ? ldexpf(1.0f, lut_e) : 1.0f);
+    unsigned long long my_eval = 0, my_look = 0, my_pass = 0;
+    const long long t_pro = clock64();
+    for (uint32_t l = 0; l < p.P; ++l) {
+        // the probed clusters fill a prefix of the slots (the learned probe leaves the
+        // rest empty): the first empty slot ends the walk
+        if (!scan_cluster_begin(p, st, qi, l)) break;
+        const uint32_t r0 = st.r0, i0 = st.i0;
+        // the cluster's base records [r0, r1), then its inserted ones (realtime)
+        const uint32_t nb = st.r1 - r0, nall = nb + (st.i1 - st.i0);
+        if (nall == 0) continue;
+        scan_fill_srow(p, srow, fdk, st.c, st.cdl);
+        if (tid == 0) st.n_records += nall;
+        for (uint32_t base = 0; base < nall; base += kRound) {
+            const long long t_round = clock64();
+            const uint64_t tau = st.tau;
+            // all loads of the thread's records first, so their latencies overlap
+            uint32_t fine_id[kRecPerThread];
+            float off[kRecPerThread];
+            uint32_t words[kRecPerThread][NW];
+            uint32_t mem[kRecPerThread];
+#pragma unroll
+            for (int j = 0; j < kRecPerThread; ++j) {
+                const uint32_t v = base + tid + j * kThreads;
+                const uint32_t mr = v < nb ? r0 + v : (v < nall ? p.ins_cl_ids[i0 + v - nb] : r0);
+                mem[j] = mr;
+                fine_id[j] = p.rec_fine[mr];
+                off[j] = p.offsets[mr];
+                load_codes<NW>(p.codes, p.code_stride, mr, words[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < kRecPerThread; ++j) {
+                const uint32_t mi = mem[j];
+                bool keep = false;
+                uint64_t key = 0;
+                if (base + tid + j * kThreads < nall) {
+                    // (float)(2.0 * cell_dist + offset): one float add of the exact
+                    // 2 * cell_dist (see adc_base)
+                    const float t0 = __fadd_rn(srow[fine_id[j]], off[j]);
+                    ++my_eval;
+                    if (filter_key(t0, mi) < tau) {  // t can only grow past t0
+                        ++my_look;
+                        float t;
+                        if (TAB == kTabF16)
+                            t = t0 + lut_sum_words_half<NW>(words[j], luth, nsq) * inv_scale;
+                        else
+                            t = __fadd_rn(t0, lut_sum_words<NW>(words[j], lut, nsq));
+                        key = filter_key(t, mi);
+                        keep = key < tau;
+                    }
+                }
+                scan_insert(st, keys, keep, key, my_pass);
+            }
+            scan_after_round(st, keys, hist, cap, kRound, T, tau, t_round);
+        }
+    }
+    scan_finish(p, st, keys, qi, my_eval, my_look, my_pass, t_start, t_pro);
+}
+
+// ------------------------------------------------------------ interleaved kernel
+constexpr int kIlThreads = kThreads;  // one block per query
+constexpr int kIlRec = 2;             // records per thread and round (double-buffered)
+constexpr int kIlRound = kIlThreads * kIlRec;
+static_assert(kIlThreads % 32 == 0, "rounds of whole warps keep record r on lane r & 31");
+
+// Buffer size of the interleaved kernel for filter_topk T (see scan_cap).
+__host__ __device__ inline uint32_t il_cap(uint32_t T) {
+    uint32_t room = T > 1024 ? T : 1024;
+    uint32_t c = T + kIlRound + room;
+    c = (c + kThreads - 1) / kThreads * kThreads;
+    return c > kMaxCap ? kMaxCap : c;
+}
+__host__ __device__ constexpr uint32_t il_table_bytes(bool half) {
+    return half ? 256u * 64u * 2u : 256u * 64u * 4u;
+}
+// Shared memory after the table: the query, then either the compact table being
+// built ([nsq][257] floats) or the cluster's cell terms, the key buffer and the
+// cut histogram.
+__host__ __device__ inline uint32_t il_query_bytes(uint32_t d) { return (d * 4u + 15u) & ~15u; }
+__host__ __device__ inline uint32_t il_srow_bytes(uint32_t F) { return (F * 4u + 7u) & ~7u; }
+
+template <int NSQ, bool HALF>
+__global__ __launch_bounds__(kIlThreads, 2) void k_scan_il(ScanParams p) {
+    static_assert(NSQ % 4 == 0 && NSQ <= 32, "interleaved layout: nsq a multiple of 4, <= 32");
+    constexpr int NG = (NSQ + 7) / 8;  // 8-byte code granules per record
+    constexpr int NW = 2 * NG;
+    constexpr uint32_t kRecBytes = NG * 8;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ScanState st;
+    const uint32_t qi = p.order[blockIdx.x];
+    const int tid = threadIdx.x;
+    const uint32_t F = p.F, T = p.T, cap = p.cap;
+    unsigned char* tab = smem;  // the rotated table, at offset 0
+    float* qv = reinterpret_cast<float*>(smem + il_table_bytes(HALF));
+    unsigned char* rest = smem + il_table_bytes(HALF) + il_query_bytes(p.d);
+    float* stage = reinterpret_cast<float*>(rest);  // [NSQ][257] while the table is built
+    float* srow = reinterpret_cast<float*>(rest);   // [F] afterwards
+    uint64_t* keys = reinterpret_cast<uint64_t*>(rest + il_srow_bytes(F));  // [cap]
+    uint32_t* hist = reinterpret_cast<uint32_t*>(keys + cap);              // [kHistBins]
+
+    if (p.status[qi] != 0) {
+        if (tid == 0) p.hcnt[qi] = 0;
+        return;
+    }
+    const long long t_start = clock64();
+    for (uint32_t i = tid; i < p.d; i += kIlThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    const float* fdk = p.fd_by_fine + (uint64_t)qi * F;
+    if (tid == 0) {
+        st.tau = kKeyMax;
+        st.count = 0;
+        st.evaluated = st.looked = st.passed = 0;
+        st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
+    }
+    const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
+    const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
+    __syncthreads();
+    // get_dist_table (quantization.cpp:260-270) in the reference's lane order,
+    // stage[m * 257 + j] (row pitch 257: the expansion below reads it without bank
+    // conflicts)
+    for (uint32_t j = tid; j < 256; j += kIlThreads) {
+        if (p.lsq == 4) {
+            const float4* cb4 = reinterpret_cast<const float4*>(p.codebook);
+#pragma unroll
+            for (int m0 = 0; m0 < NSQ; m0 += 4) {
+                float4 y[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) y[u] = __ldg(cb4 + (uint64_t)(m0 + u) * 256 + j);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float* x = qv + (m0 + u) * 4;
+                    const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
+                    const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
+                    stage[(m0 + u) * 257 + j] =
+                        __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                  __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
+                }
+            }
+        } else {
+            for (int m = 0; m < NSQ; ++m)
+                stage[m * 257 + j] = l2sqr_sse(qv + m * p.lsq,
+                                               p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
+        }
+    }
+    __syncthreads();
+    // the rotated table: column m' < NSQ + 31 of row c holds subspace m' mod NSQ
+    if (HALF) {
+        const float scale = ldexpf(1.0f, lut_e);
+        uint32_t* tw = reinterpret_cast<uint32_t*>(tab);
+        for (uint32_t w = tid; w < 256 * 32; w += kIlThreads) {
+            const uint32_t c = w >> 5, m0 = (w & 31) * 2;
+            const float v0 = m0 < NSQ + 31 ? stage[(m0 % NSQ) * 257 + c] : 0.0f;
+            const float v1 = m0 + 1 < NSQ + 31 ? stage[((m0 + 1) % NSQ) * 257 + c] : 0.0f;
+            const __half2 h = __halves2half2(__float2half_rn(v0 * scale), __float2half_rn(v1 * scale));
+            tw[w] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+    } else {
+        float* tf = reinterpret_cast<float*>(tab);
+        for (uint32_t w = tid; w < 256 * 64; w += kIlThreads) {
+            const uint32_t c = w >> 6, m = w & 63;
+            tf[w] = m < NSQ + 31 ? stage[(m % NSQ) * 257 + c] : 0.0f;
+        }
+    }
+    unsigned long long my_eval = 0, my_pass = 0;
+    const long long t_pro = clock64();
+
+    struct Rec {
+        uint32_t w[NW];
+        float off;
+        uint32_t fine, mr;  // mr = ~0: no record in this slot
+    };
+    for (uint32_t l = 0; l < p.P; ++l) {
+        if (!scan_cluster_begin(p, st, qi, l)) break;  // (its first barrier ends the table)
+        const uint32_t r0 = st.r0, i0 = st.i0;
+        const uint32_t nb = st.r1 - r0, nall = nb + (st.i1 - st.i0);
+        if (nall == 0) continue;
+        scan_fill_srow(p, srow, fdk, st.c, st.cdl);
+        if (tid == 0) st.n_records += nall;
+        // slot u of [0, lead + nall) is record u - lead: lead = r0 & 31 puts a base
+        // record with memory id r on lane r & 31 (inserted records come from a list)
+        const uint32_t lead = r0 & 31u, U = lead + nall;
+        auto load = [&](Rec (&b)[kIlRec], uint32_t u0) {
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                const uint32_t v = u0 + tid + j * kIlThreads - lead;  // wraps below lead
+                b[j].mr = ~0u;
+                if (v < nall) {
+                    const uint32_t mr = v < nb ? r0 + v : p.ins_cl_ids[i0 + v - nb];
+                    b[j].mr = mr;
+                    b[j].fine = p.rec_fine[mr];
+                    b[j].off = p.offsets[mr];
+                    const uint2* g = reinterpret_cast<const uint2*>(
+                        p.codes_il + (uint64_t)(mr >> 5) * (32 * kRecBytes) + 8 * (mr & 31));
+#pragma unroll
+                    for (int k = 0; k < NG; ++k) {
+                        const uint2 x = __ldg(g + 32 * k);
+                        b[j].w[2 * k] = x.x;
+                        b[j].w[2 * k + 1] = x.y;
+                    }
+                }
+            }
+        };
+        auto score = [&](const Rec (&b)[kIlRec]) {
+            const long long t_round = clock64();
+            const uint64_t tau = st.tau;
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                bool keep = false;
+                uint64_t key = 0;
+                if (b[j].mr != ~0u) {
+                    // (float)(2.0 * cell_dist + offset): one float add of the exact
+                    // 2 * cell_dist (see adc_base)
+                    const float t0 = __fadd_rn(srow[b[j].fine], b[j].off);
+                    const uint32_t lb = (b[j].mr & 31u) << 2;  // byte 0 of the address
+                    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+                    for (int s2 = 0; s2 < NSQ; ++s2) {
+                        // (code << 8) | 4 * lane: the entry of column s2 + lane
+                        const uint32_t addr =
+                            __byte_perm(b[j].w[s2 >> 2], lb, 0x5504u | ((uint32_t)(s2 & 3) << 4));
+                        if (HALF)
+                            a[s2 & 3] += __half2float(
+                                *reinterpret_cast<const __half*>(tab + (addr >> 1) + 2 * s2));
+                        else
+                            a[s2 & 3] = __fadd_rn(
+                                a[s2 & 3], *reinterpret_cast<const float*>(tab + addr + 4 * s2));
+                    }
+                    const float sum = __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3]));
+                    const float t = HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
+                    ++my_eval;
+                    key = filter_key(t, b[j].mr);
+                    keep = key < tau;
+                }
+                scan_insert(st, keys, keep, key, my_pass);
+            }
+            scan_after_round(st, keys, hist, cap, kIlRound, T, tau, t_round);
+        };
+        Rec ra[kIlRec], rb[kIlRec];
+        load(ra, 0);
+        for (uint32_t u0 = 0; u0 < U; u0 += 2 * kIlRound) {
+            if (u0 + kIlRound < U) load(rb, u0 + kIlRound);
+            score(ra);
+            if (u0 + kIlRound >= U) break;
+            if (u0 + 2 * kIlRound < U) load(ra, u0 + 2 * kIlRound);
+            score(rb);
+        }
+    }
+    scan_finish(p, st, keys, qi, my_eval, my_eval, my_pass, t_start, t_pro);
 }
 
 // Launch order of the scan's blocks. A block's time follows the records of the
@@ -745,23 +939,24 @@ __global__ __launch_bounds__(kOrderThreads) void k_scan_order(const uint8_t* __r
 
 }  // namespace
 
+// Shared memory of the interleaved kernel (il_applies(nsq)) for filter_topk T.
+static size_t il_smem_bytes(const DeviceIndex& ix, uint32_t T, bool half) {
+    const size_t stage = sizeof(float) * ix.nsq * 257;
+    const size_t work = il_srow_bytes(ix.F) + sizeof(uint64_t) * il_cap(T) +
+                        sizeof(uint32_t) * kHistBins;
+    return il_table_bytes(half) + il_query_bytes(ix.d) + (stage > work ? stage : work);
+}
+
 size_t scan_smem_bytes(const DeviceIndex& ix, uint32_t T) {
+    if (il_applies(ix.nsq)) return il_smem_bytes(ix, T, false);
     return sizeof(uint64_t) * scan_cap(T) + sizeof(uint32_t) * kHistBins +
            sizeof(float) * ix.nsq * 256 + sizeof(float) * ix.F + sizeof(float) * ix.d;
 }
 
-// The rotated table applies when nsq is a multiple of 4, at most 32, and its copy
-// of the codes exists.
-static bool use_rot(const DeviceIndex& ix) {
-    return ix.codes_rot != nullptr && ix.nsq % 4 == 0 && ix.nsq <= 32 && ix.code_stride == ix.nsq;
-}
-
 size_t scan_smem_bytes_half(const DeviceIndex& ix, uint32_t T) {
-    // the rotated table spans 128 rows x 32 banks (16 KB), enough for nsq <= 32; the
-    // FP16 table of the other layout nsq * 512 bytes
-    const size_t tab = sizeof(__half) * (ix.nsq <= 32 ? 32 : ix.nsq) * 256;
-    return sizeof(uint64_t) * scan_cap(T) + sizeof(uint32_t) * kHistBins + tab +
-           sizeof(float) * ix.F + sizeof(float) * ix.d;
+    if (il_applies(ix.nsq)) return il_smem_bytes(ix, T, true);
+    return sizeof(uint64_t) * scan_cap(T) + sizeof(uint32_t) * kHistBins +
+           sizeof(__half) * ix.nsq * 256 + sizeof(float) * ix.F + sizeof(float) * ix.d;
 }
 
 // The buffer takes T + a round + at least 1024 more keys between cuts.
@@ -793,7 +988,7 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.rec_fine = ix.rec_fine;
     p.offsets = ix.offsets;
     p.codes = ix.codes;
-    p.codes_rot = ix.codes_rot;
+    p.codes_il = ix.codes_il;
     p.codebook = ix.codebook;
     p.counters = s.counters;
     p.d = ix.d;
@@ -816,16 +1011,17 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
         ensure_max_dynamic_smem(kernel, 220 * 1024);
         kernel<<<n, kThreads, smem, stream>>>(p);
     };
-    if (half_lut && use_rot(ix)) {
-        // nw == nsq / 4 exactly
-        if (nw == 2) launch(k_scan_select<2, kTabRot>);
-        else if (nw == 4) launch(k_scan_select<4, kTabRot>);
-        else if (nw == 6) launch(k_scan_select<6, kTabRot>);
-        else if (nw == 8) launch(k_scan_select<8, kTabRot>);
-        else if (nw == 1) launch(k_scan_select<1, kTabRot>);
-        else if (nw == 3) launch(k_scan_select<3, kTabRot>);
-        else if (nw == 5) launch(k_scan_select<5, kTabRot>);
-        else launch(k_scan_select<7, kTabRot>);
+    if (il_applies(ix.nsq)) {
+        if (ix.codes_il == nullptr) return cudaErrorInvalidValue;
+        p.cap = il_cap(s.T);
+        switch (ix.nsq) {
+#define PGPU_IL(N) \
+    case N: launch(half_lut ? k_scan_il<N, true> : k_scan_il<N, false>); break;
+            PGPU_IL(4) PGPU_IL(8) PGPU_IL(12) PGPU_IL(16) PGPU_IL(20) PGPU_IL(24) PGPU_IL(28)
+            PGPU_IL(32)
+#undef PGPU_IL
+            default: return cudaErrorInvalidValue;
+        }
     } else if (half_lut) {
         if (nw <= 2) launch(k_scan_select<2, kTabF16>);
         else if (nw <= 4) launch(k_scan_select<4, kTabF16>);
