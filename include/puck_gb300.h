@@ -167,7 +167,8 @@ int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
 /* Per-stage device timing (CUDA events recorded on the launching stream around
  * each kernel). With profiling enabled, pgpu_stage_times returns, for the last
  * search call, the milliseconds spent in each stage, summed over its passes:
- * 0 query prep, 1 coarse scores, 2 coarse select (+ the learned probe), 3 fine scores, 4 fine order
+ * 0 query prep, 1 coarse scores (+ the learned probe, which runs first and leaves the coarse
+ * screen only the queries it does not answer), 2 coarse select, 3 fine scores, 4 fine order
  * (exact mode) or the scan's block launch order (scan mode), 5 cell walk (exact mode) or ADC scan
  * (scan mode: k_scan_select alone), 6 rerank. It waits for the call's work to finish. */
 #define PGPU_NUM_STAGES 7

@@ -143,6 +143,8 @@ struct Scratch {
     int32_t* pconf = nullptr;  // [B] 1 where the probe chose the clusters (null: no probe)
     float* pz = nullptr;       // [B][C] probe scores
     uint32_t* order = nullptr; // scan mode: [B] queries in launch order (longest scans first)
+    uint32_t* ulist = nullptr;  // with a probe: [B] queries left to the fixed-count selection
+    uint32_t* ucount = nullptr; // their number (device)
     uint8_t* wbucket = nullptr; // scan mode: [B] work bucket of each query
     uint32_t Pfix = 0;         // fixed coarse count (<= P when a probe widens the slots)
     uint32_t P = 0, T = 0;
@@ -261,6 +263,8 @@ struct TcOperand {
     uint64_t rs, ks;
     uint32_t rows;
     const uint16_t* pb = nullptr;  // BF16 operand instead of p (same strides, in elements)
+    const uint32_t* ridx = nullptr;     // row i reads source row ridx[i] (A only)
+    const uint32_t* rows_dev = nullptr; // device count of rows (<= rows) (A only)
 };
 enum TcEpi {
     TC_EPI_SCORE = 0,     // bias[j] - acc

@@ -35,7 +35,7 @@ void ensure_max_dynamic_smem(const void* kernel, int bytes) {
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qb, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
                     s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err,
-                    s->ph1, s->ph2, s->pconf, s->pz, s->order, s->wbucket};
+                    s->ph1, s->ph2, s->pconf, s->pz, s->order, s->wbucket, s->ulist, s->ucount};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *s = Scratch();
@@ -43,7 +43,7 @@ void free_scratch(Scratch* s) {
 
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
     const uint64_t P = cfg.coarse_slots(ix.C), T = cfg.filter_keep();
-    const uint64_t probe = cfg.probe ? (uint64_t)B * (cfg.probe->h * 4 + 4 + ix.C * 4ull) : 0;
+    const uint64_t probe = cfg.probe ? (uint64_t)B * (cfg.probe->h * 4 + 8 + ix.C * 4ull) + 4 : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * 5 : 0;  // launch order
     return (uint64_t)B * (ix.d * 6 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
@@ -82,6 +82,8 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
         PGPU_ALLOC(s.wbucket, B);
     }
     if (cfg.probe) {
+        PGPU_ALLOC(s.ulist, B);
+        PGPU_ALLOC(s.ucount, 1);
         PGPU_ALLOC(s.ph1, (uint64_t)B * cfg.probe->h);
         PGPU_ALLOC(s.ph2, (uint64_t)B * cfg.probe->h);
         PGPU_ALLOC(s.pconf, B);
@@ -117,13 +119,13 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     mark(0);
     PGPU_STEP(launch_prep_queries(ix, d_q, n, s, st), "prep_queries");
     mark(1);
-    // coarse: BF16 tensor-core screen, then the exact top-P from an FP32 window
-    PGPU_STEP(launch_coarse_tc(ix, n, s, st), "coarse scores");
-    mark(2);
     int probe_kernels = 0;
     if (cfg.probe) {
-        // learned probe: scores of the coarse clusters, then the adaptive choice; the
-        // fixed-count window below only runs for the queries the probe leaves to it
+        // learned probe first: scores of the coarse clusters, then the adaptive choice.
+        // The fixed-count selection (tensor-core screen + exact window) then runs only
+        // for the queries the probe leaves to it (s.ulist, s.ucount on the device): with
+        // a confident probe the coarse screen has nothing to do.
+        PGPU_STEP(cudaMemsetAsync(s.ucount, 0, sizeof(uint32_t), st), "memset");
         float* pz = s.pz;
         PGPU_STEP(probe_infer(*cfg.probe, s.q, s.qb, n, s.ph1, s.ph2, pz, s.tc_err, st),
                   "probe forward");
@@ -131,6 +133,9 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
                   "probe select");
         probe_kernels = 4;
     }
+    // coarse: BF16 tensor-core screen, then the exact top-P from an FP32 window
+    PGPU_STEP(launch_coarse_tc(ix, n, s, st), "coarse scores");
+    mark(2);
     PGPU_STEP(launch_coarse_window(ix, n, s, st), "coarse select");
     mark(3);
     const bool bf16 = cfg.precision == PGPU_PRECISION_BF16;

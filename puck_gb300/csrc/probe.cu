@@ -140,7 +140,8 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     const float* __restrict__ cents, const float* __restrict__ bias, const int32_t* __restrict__ status,
     float mass, uint32_t max_probe, uint32_t Pcap, float* __restrict__ cdist,
     uint32_t* __restrict__ ctag, int32_t* __restrict__ pconf,
-    unsigned long long* __restrict__ counters) {
+    unsigned long long* __restrict__ counters, uint32_t* __restrict__ ulist,
+    uint32_t* __restrict__ ucount) {
     extern __shared__ float sp[];  // [C] probabilities
     __shared__ float red_v[kProbeThreads / 32];
     __shared__ uint32_t red_i[kProbeThreads / 32];
@@ -152,7 +153,14 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     const uint32_t row = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) pconf[row] = 0;
-    if (status[row] != 0) return;
+    // a row the probe does not answer goes to the fixed-count selection's list
+    auto leave = [&]() {
+        if (tid == 0 && ulist != nullptr) ulist[atomicAdd(ucount, 1u)] = row;
+    };
+    if (status[row] != 0) {
+        leave();
+        return;
+    }
     const float* z = Z + (uint64_t)row * C;
     float m = -FLT_MAX;
     for (uint32_t c = tid; c < C; c += kProbeThreads) m = fmaxf(m, z[c]);
@@ -267,6 +275,7 @@ __global__ __launch_bounds__(kProbeThreads) void k_probe_select(
     __syncthreads();
     if (!confident) {
         if (tid == 0) atomicAdd(counters + kCounterProbeFallbacks, 1ull);
+        leave();
         return;  // the fixed-count selection fills this row
     }
     if (tid == 0) pconf[row] = 1;
@@ -445,7 +454,7 @@ cudaError_t launch_probe_select(const ProbeNet& net, const DeviceIndex& ix, uint
     ensure_max_dynamic_smem(k_probe_select, 200 * 1024);
     k_probe_select<<<n, kProbeThreads, sizeof(float) * net.C, st>>>(
         Z, net.C, s.q, ix.d, ix.coarse, ix.coarse_norms, s.status, mass, max_probe, s.P, s.cdist,
-        s.ctag, s.pconf, s.counters);
+        s.ctag, s.pconf, s.counters, s.ulist, s.ucount);
     return cudaGetLastError();
 }
 

@@ -68,6 +68,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// Rows of an operand: op.rows, or fewer when a device count is given; row i of the
+// contraction reads source row ridx[i] when a row index is given.
+__device__ __forceinline__ uint32_t op_rows(const TcOperand& op) {
+    if (op.rows_dev == nullptr) return op.rows;
+    const uint32_t r = *op.rows_dev;
+    return r < op.rows ? r : op.rows;
+}
+__device__ __forceinline__ uint32_t src_row(const TcOperand& op, uint32_t i) {
+    return op.ridx ? op.ridx[i] : i;
+}
+
 // Stages rows [row0, row0+128) x k [k0, k0 + 8*nkg) of an operand into `tile`.
 // Thread t owns row t of the tile and writes one 16-byte core-matrix row per K
 // group, so a quarter warp stores 128 contiguous bytes (no bank conflict). All of
@@ -75,8 +86,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 __device__ __forceinline__ void stage_operand(uint8_t* tile, const TcOperand& op, uint32_t row0,
                                               uint32_t k0, uint32_t K, uint32_t nkg, bool vec) {
     const uint32_t r = threadIdx.x;
-    const uint32_t row = row0 + r;
-    const bool in = row < op.rows;
+    const uint32_t crow = row0 + r;
+    const bool in = crow < op_rows(op);
+    const uint32_t row = in ? src_row(op, crow) : 0u;
     uint8_t* dst = tile + (r >> 3) * 128u + (r & 7u) * 16u;
     if (op.pb != nullptr) {
         const uint16_t* base = op.pb + (uint64_t)row * op.rs;
@@ -145,9 +157,9 @@ __device__ __forceinline__ void stage_operand_async(uint8_t* tile, const TcOpera
                                                     uint32_t row0, uint32_t k0, uint32_t K,
                                                     uint32_t nkg) {
     const uint32_t r = threadIdx.x;
-    const uint32_t row = row0 + r;
-    const bool in = row < op.rows;
-    const uint16_t* base = op.pb + (uint64_t)(in ? row : 0) * op.rs;
+    const uint32_t crow = row0 + r;
+    const bool in = crow < op_rows(op);
+    const uint16_t* base = op.pb + (uint64_t)(in ? src_row(op, crow) : 0u) * op.rs;
     const uint32_t dst = smem_u32(tile) + (r >> 3) * 128u + (r & 7u) * 16u;
     for (uint32_t kg = 0; kg < nkg; ++kg) {
         const uint32_t k = k0 + kg * 8;
@@ -201,6 +213,8 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
     __shared__ int failed;
     const uint32_t m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t a_rows = op_rows(A);
+    if (m0 >= a_rows) return;  // a device row count below the launch's rows: nothing here
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -333,7 +347,7 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
                   "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                 : "r"(lane_addr + c * 16));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row >= A.rows) continue;
+            if (row >= a_rows) continue;
             const uint32_t col0 = n0 + c * 16;
             float v[16];
 #pragma unroll

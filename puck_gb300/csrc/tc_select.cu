@@ -41,7 +41,8 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     uint32_t ld_out, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
     const int32_t* __restrict__ status,
     const int* __restrict__ tc_err, unsigned long long* __restrict__ fallbacks,
-    const int32_t* __restrict__ skip) {
+    const int32_t* __restrict__ skip, const uint32_t* __restrict__ qidx,
+    const uint32_t* __restrict__ nrows_dev) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* shi = reinterpret_cast<float*>(smem);                 // [C]   s^ + E, later exact s
     float* slo = shi + C;                                        // [C+1] s^ - E, later heap values
@@ -52,7 +53,11 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     __shared__ uint32_t hist[256];
     __shared__ uint32_t state[2];
     __shared__ uint32_t ncand;
-    const uint32_t row = blockIdx.x;
+    // screen row rc; the query it belongs to (a compacted list when a probe answered
+    // the others)
+    const uint32_t rc = blockIdx.x;
+    if (nrows_dev != nullptr && rc >= *nrows_dev) return;
+    const uint32_t row = qidx ? qidx[rc] : rc;
     const int tid = threadIdx.x;
     if (skip != nullptr && skip[row]) return;  // the learned probe answered this query
     float* ov = out_val + (uint64_t)row * ld_out;
@@ -76,7 +81,7 @@ __global__ __launch_bounds__(kWinThreads) void k_window_topk(
     if (!exact_all) {
         const float eps = window_eps(d);
         const float qa = sqrtf(qnorm[row]);
-        const float* a = approx + (uint64_t)row * ld;
+        const float* a = approx + (uint64_t)rc * ld;
         for (uint32_t j = tid; j < C; j += kWinThreads) {
             const float s = a[j];
             const float e = eps * qa * cabs[j] + 9.5367431640625e-07f * (fabsf(bias[j]) + fabsf(s)) +
@@ -160,14 +165,16 @@ __global__ __launch_bounds__(256) void k_window_small(
     const float* __restrict__ bias, const float* __restrict__ cabs, uint32_t C, uint32_t P,
     uint32_t ld_out, uint32_t nrows, float* __restrict__ out_val, uint32_t* __restrict__ out_idx,
     const int32_t* __restrict__ status, const int* __restrict__ tc_err,
-    unsigned long long* __restrict__ fallbacks, const int32_t* __restrict__ skip) {
+    unsigned long long* __restrict__ fallbacks, const int32_t* __restrict__ skip,
+    const uint32_t* __restrict__ qidx, const uint32_t* __restrict__ nrows_dev) {
     __shared__ unsigned long long wkey[8][kSmallCap];
     __shared__ float hv_s[8][kSmallP + 1];
     __shared__ uint32_t ht_s[8][kSmallP + 1];
     __shared__ float chunk[8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t row = blockIdx.x * 8 + warp;
-    if (row >= nrows) return;
+    const uint32_t rc = blockIdx.x * 8 + warp;  // screen row; its query below
+    if (rc >= nrows || (nrows_dev != nullptr && rc >= *nrows_dev)) return;
+    const uint32_t row = qidx ? qidx[rc] : rc;
     if (skip != nullptr && skip[row]) return;  // the learned probe answered this query
     float* ov = out_val + (uint64_t)row * ld_out;
     uint32_t* oi = out_idx + (uint64_t)row * ld_out;
@@ -183,7 +190,7 @@ __global__ __launch_bounds__(256) void k_window_small(
         return;
     }
     const float* q = Q + (uint64_t)row * d;
-    const float* a = approx + (uint64_t)row * ld;
+    const float* a = approx + (uint64_t)rc * ld;
     unsigned long long* keys = wkey[warp];
     bool exact_all = (*tc_err != 0);
     if (!exact_all) {
@@ -430,7 +437,8 @@ cudaError_t launch_abs_from_half_norms(const float* half_norms, uint32_t n, floa
 }
 
 cudaError_t launch_coarse_tc(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream) {
-    TcOperand A{nullptr, ix.d, 1, n, s.qb};
+    // with a probe, only the queries it left (s.ulist, their count s.ucount on the device)
+    TcOperand A{nullptr, ix.d, 1, n, s.qb, s.ulist, s.ucount};
     TcOperand B{nullptr, ix.d, 1, ix.C, ix.coarse_bf16};
     TcEpilogue ep{};
     ep.mode = TC_EPI_SCORE;
@@ -448,7 +456,7 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
         kern<<<(n + 7) / 8, 256, 0, stream>>>(
             s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse, ix.coarse_norms, ix.coarse_abs, ix.C,
             s.Pfix, s.P, n, s.cdist, s.ctag, s.status, s.tc_err, s.counters + kCounterWindowFallbacks,
-            s.pconf);
+            s.pconf, s.ulist, s.ucount);
         return cudaGetLastError();
     }
     const size_t smem = window_smem_bytes(ix.C, ix.d);
@@ -456,7 +464,8 @@ cudaError_t launch_coarse_window(const DeviceIndex& ix, uint32_t n, Scratch& s,
     k_window_topk<<<n, kWinThreads, smem, stream>>>(s.dots, ix.C, s.q, ix.d, s.qnorm, ix.coarse,
                                                     ix.coarse_norms, ix.coarse_abs, ix.C, s.Pfix,
                                                     s.P, s.cdist, s.ctag, s.status, s.tc_err,
-                                                    s.counters + kCounterWindowFallbacks, s.pconf);
+                                                    s.counters + kCounterWindowFallbacks, s.pconf,
+                                                    s.ulist, s.ucount);
     return cudaGetLastError();
 }
 

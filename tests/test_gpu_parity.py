@@ -144,9 +144,11 @@ def test_gpu_equals_oracle_builder_index(n, d, C, F, nsq, kind, norm, P, T, k, p
 
 
 def test_properties_large():
-    """Size-independent checks on a 1M-point index: ascending distances, the
-    returned distance equals the exact squared L2 of the returned id, batch
-    search equals one-query searches, and the zero-norm rejection."""
+    """A 1M-point index: exact mode bit-identical to the oracle's restatement of the
+    reference's search and scan mode to its restatement of the mode; size-independent
+    checks: ascending distances, the returned distance equals the exact squared L2
+    of the returned id, batch search equals one-query searches, and the zero-norm
+    rejection."""
     import torch
     with tempfile.TemporaryDirectory() as tmp:
         q = _built_index(tmp, 1_000_000, 96, 512, 512, 24, "unit", 5, True)
@@ -164,6 +166,21 @@ def test_properties_large():
             assert rn == 100
             assert np.array_equal(_bits(d1), _bits(dist[i]))
             assert np.array_equal(i1, ids[i])
+        # the same queries through the oracle's restatement of the reference's search:
+        # exact mode bit for bit at this size, and scan mode against its restatement
+        orc = oracle.OracleIndex(tmp)
+        od, oi, ost = orc.search_batch(q, 100, 64, 500, topk_max=100, nthreads=os.cpu_count())
+        assert (ost == 0).all()
+        assert np.array_equal(_bits(dist), _bits(od))
+        assert np.array_equal(ids, oi)
+        ix.set_search_params(mode=native.PGPU_MODE_SCAN, search_coarse_count=8)
+        sd, si = ix.search(q, 10)
+        od, oi, _ = orc.search_batch(q, 10, 8, 500, topk_max=100, nthreads=os.cpu_count(),
+                                     scan=True)
+        assert np.array_equal(_bits(sd), _bits(od))
+        assert np.array_equal(si, oi)
+        orc.close()
+        ix.set_search_params(mode=native.PGPU_MODE_EXACT, search_coarse_count=64)
         bad = q[:4].copy()
         bad[1] = 0.0
         d2, i2, st2 = ix.search(bad, 10, return_status=True)
