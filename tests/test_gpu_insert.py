@@ -84,19 +84,22 @@ def test_scan_mode_over_inserts_matches_oracle(name):
     assert np.array_equal(_bits(dist), _bits(od)), name
     assert np.array_equal(labels, oi), name
     if "pq" not in name:
-        # the inserted points themselves as queries
+        # the inserted points themselves as queries: found among the results, at
+        # distance 0 on an index that stores them as given
         q = z["inserted"][:16]
         d2, l2 = ix.search(q, k)
         found = [ids[i] in l2[i].astype(np.int64).tolist() for i in range(len(q))]
-        assert np.mean(found) >= 0.9 and np.mean(d2[:, 0] <= 1e-5) >= 0.9
+        assert np.mean(found) >= 0.9
+        if "flat" in name:
+            assert np.mean(d2[:, 0] == 0.0) >= 0.9
     orc.close()
     ix.close()
 
 
 def test_precision_form_over_inserts():
-    """The precision form (BF16 screen, FP16 table) finds the inserted points: its
-    results over the realtime index are exact FP32 distances of returned ids, and
-    agree with the FP32 scan's on nearly every query."""
+    """The precision form (BF16 screen, FP16 table) over the realtime index: its ids
+    agree with the FP32 scan's on nearly every query, and an id both return has the
+    same exact FP32 distance."""
     z, tmp, ix, (P, T, k) = _open("insert_flat_d16", mode=native.PGPU_MODE_SCAN,
                                   precision=native.PGPU_PRECISION_BF16, filter_margin=16)
     ix.realtime_open(1000)
@@ -106,7 +109,11 @@ def test_precision_form_over_inserts():
     od, oi, _ = orc.search_batch(z["queries"], k, P, T, topk_max=max(k, 10), scan=True)
     agree = np.mean([len(set(a.tolist()) & set(b.tolist())) / k for a, b in zip(labels, oi)])
     assert agree >= 0.95, agree
-    np.testing.assert_allclose(dist, od, rtol=1e-5, atol=1e-3)
+    for i in range(len(labels)):
+        mine = dict(zip(labels[i].tolist(), dist[i].tolist()))
+        ref = dict(zip(oi[i].tolist(), od[i].tolist()))
+        for t in set(mine) & set(ref):
+            assert mine[t] == pytest.approx(ref[t], rel=1e-6, abs=1e-6), (i, t)
     orc.close()
     ix.close()
 
