@@ -190,10 +190,12 @@ int ensure_bf16_features(DeviceIndex* ix, std::string* err) {
 }
 
 // One thread per record: its rotated codes (byte s = code of subspace
-// (s + (r & 31)) mod nsq) written as 8-byte granules of the interleaved layout.
+// (s + (r & 31)) mod nsq) as 8-byte granules of the interleaved layout, its filter
+// offset and its fine id.
 __global__ void k_interleave_codes(const uint8_t* __restrict__ codes, uint32_t stride,
-                                   uint32_t nsq, uint64_t r0, uint64_t rows,
-                                   uint8_t* __restrict__ il) {
+                                   const float* __restrict__ offsets,
+                                   const uint16_t* __restrict__ rec_fine, uint32_t nsq,
+                                   uint64_t r0, uint64_t rows, uint8_t* __restrict__ il) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= rows) return;
     const uint64_t r = r0 + i;
@@ -211,13 +213,15 @@ __global__ void k_interleave_codes(const uint8_t* __restrict__ codes, uint32_t s
         }
         *reinterpret_cast<unsigned long long*>(il + il_granule_offset(r, g, nsq)) = v;
     }
+    *reinterpret_cast<float*>(il + il_offset_offset(r, nsq)) = offsets[r];
+    *reinterpret_cast<uint16_t*>(il + il_fine_offset(r, nsq)) = rec_fine[r];
 }
 
-cudaError_t launch_interleave_codes(const uint8_t* codes, uint32_t code_stride, uint32_t nsq,
-                                    uint64_t r0, uint64_t rows, uint8_t* il, cudaStream_t stream) {
+cudaError_t launch_interleave_codes(const DeviceIndex& ix, uint64_t r0, uint64_t rows,
+                                    cudaStream_t stream) {
     if (rows == 0) return cudaSuccess;
-    k_interleave_codes<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(codes, code_stride, nsq,
-                                                                          r0, rows, il);
+    k_interleave_codes<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(
+        ix.codes, ix.code_stride, ix.offsets, ix.rec_fine, ix.nsq, r0, rows, ix.codes_il);
     return cudaGetLastError();
 }
 
@@ -229,7 +233,7 @@ int ensure_interleaved_codes(DeviceIndex* ix, std::string* err) {
     cudaError_t e = dev_alloc(&ix->codes_il, il_bytes(rows, ix->nsq), &bytes);
     if (e == cudaSuccess) e = cudaMemset(ix->codes_il, 0, il_bytes(rows, ix->nsq));
     if (e == cudaSuccess)
-        e = launch_interleave_codes(ix->codes, ix->code_stride, ix->nsq, 0, used, ix->codes_il, 0);
+        e = launch_interleave_codes(*ix, 0, used, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         if (ix->codes_il) cudaFree(ix->codes_il);

@@ -78,9 +78,9 @@ struct DeviceIndex {
     uint16_t* rec_fine = nullptr;   // [n] fine id of the cell each record belongs to
     float* offsets = nullptr;       // [n] filter offset per point
     uint8_t* codes = nullptr;       // [n][code_stride]
-    uint8_t* codes_il = nullptr;    // scan-mode copy of the codes: interleaved by blocks of
-                                    // 32 records, each record's codes rotated by its
-                                    // lane (il_* below; made on first use)
+    uint8_t* codes_il = nullptr;    // scan-mode copy of the records (codes, offset, fine id)
+                                    // interleaved by blocks of 32, each record's codes
+                                    // rotated by its lane (il_* below; made on first use)
     // realtime inserts (realtime.cu): per-record arrays hold n + ins_cap rows, inserted
     // point i at row (memory id) n + i
     uint32_t ins_cap = 0, ins_n = 0;
@@ -102,25 +102,40 @@ struct DeviceIndex {
 };
 
 // Per-pass scratch (sized for max_batch queries).
-// Interleaved, rotated code copy of the scan (DeviceIndex::codes_il), made when
-// nsq is a multiple of 4 and at most 32. Records are grouped in blocks of 32 by
-// memory id (block b = r >> 5, lane l = r & 31); a record takes il_record_bytes
-// bytes, as 8-byte granules: granule g of record r sits at
-//     b * 32 * il_record_bytes + g * 256 + 8 * l,
-// so the 32 records of a block are read by one warp as whole 256-byte lines. Byte
-// s < nsq of a record is the code of subspace (s + l) mod nsq (bytes past nsq are
-// 0): at lookup step s the 32 lanes of a warp read 32 consecutive table columns.
+// Interleaved record copy of the scan (DeviceIndex::codes_il), made when nsq is a
+// multiple of 4 and at most 32. Records are grouped in blocks of 32 by memory id
+// (block b = r >> 5, lane l = r & 31). A block is il_block_bytes long and holds
+//   * the codes, G = il_record_bytes bytes a record as 8-byte granules: granule g
+//     of lane l at g * 256 + 8 * l, so one warp reads a block's granule g as one
+//     256-byte line;
+//   * the 32 filter offsets (float) at 32 * G, and the 32 fine ids (uint16) at
+//     32 * G + 128.
+// Byte s < nsq of a record's codes is the code of subspace (s + l) mod nsq (bytes
+// past nsq are 0): at lookup step s the 32 lanes of a warp read 32 consecutive
+// table columns. A block is a multiple of 16 bytes, so a run of blocks is one bulk
+// copy.
 __host__ __device__ inline bool il_applies(uint32_t nsq) { return nsq % 4 == 0 && nsq <= 32 && nsq > 0; }
 __host__ __device__ inline uint32_t il_record_bytes(uint32_t nsq) { return (nsq + 7u) & ~7u; }
+__host__ __device__ inline uint32_t il_block_bytes(uint32_t nsq) {
+    return 32u * il_record_bytes(nsq) + 128u + 64u;
+}
 __host__ __device__ inline uint64_t il_bytes(uint64_t rows, uint32_t nsq) {
-    return (rows + 31) / 32 * 32 * il_record_bytes(nsq);
+    return (rows + 31) / 32 * il_block_bytes(nsq);
 }
 __host__ __device__ inline uint64_t il_granule_offset(uint64_t r, uint32_t g, uint32_t nsq) {
-    return (r >> 5) * 32 * il_record_bytes(nsq) + g * 256u + 8u * (uint32_t)(r & 31);
+    return (r >> 5) * il_block_bytes(nsq) + g * 256u + 8u * (uint32_t)(r & 31);
 }
-// Interleaved records of rows [r0, r0 + rows) from the row-major codes.
-cudaError_t launch_interleave_codes(const uint8_t* codes, uint32_t code_stride, uint32_t nsq,
-                                    uint64_t r0, uint64_t rows, uint8_t* il, cudaStream_t stream);
+__host__ __device__ inline uint64_t il_offset_offset(uint64_t r, uint32_t nsq) {
+    return (r >> 5) * il_block_bytes(nsq) + 32u * il_record_bytes(nsq) + 4u * (uint32_t)(r & 31);
+}
+__host__ __device__ inline uint64_t il_fine_offset(uint64_t r, uint32_t nsq) {
+    return (r >> 5) * il_block_bytes(nsq) + 32u * il_record_bytes(nsq) + 128u +
+           2u * (uint32_t)(r & 31);
+}
+// Interleaved records of rows [r0, r0 + rows) from the row-major codes, the filter
+// offsets and the fine ids.
+cudaError_t launch_interleave_codes(const DeviceIndex& ix, uint64_t r0, uint64_t rows,
+                                    cudaStream_t stream);
 
 struct Scratch {
     uint32_t cap = 0;

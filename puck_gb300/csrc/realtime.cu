@@ -238,7 +238,7 @@ int realtime_insert(DeviceIndex* ix, RealtimeHost* rh, uint32_t m, const float* 
                                          p_off, p_codes, pnsq, ix->pq_code_stride, xs, d, *ix);
         e = cudaGetLastError();
         if (e == cudaSuccess && ix->codes_il)
-            e = launch_interleave_codes(ix->codes, ix->code_stride, fnsq, row0, v, ix->codes_il, st);
+            e = launch_interleave_codes(*ix, row0, v, st);
         if (e == cudaSuccess && ix->feat_bf16)
             e = launch_bf16_rows(ix->feat + row0 * d, v, d, ix->feat_bf16 + row0 * d,
                                  ix->feat_abs + row0, st);

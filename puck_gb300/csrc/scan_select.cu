@@ -110,6 +110,7 @@ struct ScanParams {
     const float* codebook;
     unsigned long long* counters;
     const uint32_t* order;      // [B] query of each block
+    int* err;                   // set when a bulk copy's wait expired
     const uint32_t* ins_cl_start;  // realtime: [C+1] inserted records per cluster, or null
     const uint32_t* ins_cl_ids;    // their memory ids
     uint32_t d, C, F, nsq, lsq, code_stride, P, T, cap;
@@ -200,13 +201,14 @@ constexpr uint64_t kKeyMax = ~0ull;
 // max_digits > 0 stops after that many digit passes and returns the largest key of
 // the bucket reached: then at least K keys are <= the result (a cut-back bound, not
 // the K-th itself).
+template <int NT>
 __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint32_t K,
                                      uint32_t* hist, uint64_t* sel, int max_digits = 0) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // the leading bits every key shares need no pass: start at the digit where the
     // smallest and the largest key first differ
     uint64_t lo = ~0ull, hi = 0;
-    for (uint32_t i = tid; i < count; i += kThreads) {
+    for (uint32_t i = tid; i < count; i += NT) {
         const uint64_t x = keys[i];
         lo = x < lo ? x : lo;
         hi = x > hi ? x : hi;
@@ -218,7 +220,7 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
         lo = a < lo ? a : lo;
         hi = b > hi ? b : hi;
     }
-    __shared__ uint64_t red_lo[kThreads / 32], red_hi[kThreads / 32];
+    __shared__ uint64_t red_lo[NT / 32], red_hi[NT / 32];
     if (lane == 0) {
         red_lo[warp] = lo;
         red_hi[warp] = hi;
@@ -226,7 +228,7 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
     __syncthreads();
     lo = red_lo[0];
     hi = red_hi[0];
-    for (int w = 1; w < kThreads / 32; ++w) {
+    for (int w = 1; w < NT / 32; ++w) {
         lo = red_lo[w] < lo ? red_lo[w] : lo;
         hi = red_hi[w] > hi ? red_hi[w] : hi;
     }
@@ -242,9 +244,9 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
     uint64_t prefix = lo & mask;
     uint32_t k = K;
     for (int shift = top; shift >= 0; shift -= 8) {
-        for (int i = tid; i < 256; i += kThreads) hist[i] = 0;
+        for (int i = tid; i < 256; i += NT) hist[i] = 0;
         __syncthreads();
-        for (uint32_t i0 = 0; i0 < count; i0 += kThreads) {
+        for (uint32_t i0 = 0; i0 < count; i0 += NT) {
             const uint32_t i = i0 + tid;
             bool in = false;
             uint32_t digit = 0;
@@ -298,7 +300,7 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
             return prefix | ~mask;
         if (unique && shift > 0) {
             // the one key under this prefix is the K-th
-            for (uint32_t i = tid; i < count; i += kThreads)
+            for (uint32_t i = tid; i < count; i += NT)
                 if ((keys[i] & mask) == prefix) sel[3] = keys[i];
             __syncthreads();
             const uint64_t r = sel[3];
@@ -316,12 +318,13 @@ __device__ uint64_t block_select_kth(const uint64_t* keys, uint32_t count, uint3
 // it, and only the keys of that one bin above the K-th are kept in excess.
 // Returns kKeyMax when the float parts are all equal (no cut possible). `hist`
 // has kHistBins slots, `red` 2 * (kThreads / 32) + 2. All threads call it.
+template <int NT>
 __device__ uint64_t block_cut_bound(const uint64_t* keys, uint32_t count, uint32_t K,
                                     uint32_t* hist, uint32_t* red) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int kW = kThreads / 32;
+    constexpr int kW = NT / 32;
     uint32_t lo = 0xFFFFFFFFu, hi = 0;
-    for (uint32_t i = tid; i < count; i += kThreads) {
+    for (uint32_t i = tid; i < count; i += NT) {
         const uint32_t h = (uint32_t)(keys[i] >> 32);
         lo = h < lo ? h : lo;
         hi = h > hi ? h : hi;
@@ -332,7 +335,7 @@ __device__ uint64_t block_cut_bound(const uint64_t* keys, uint32_t count, uint32
         red[warp] = lo;
         red[kW + warp] = hi;
     }
-    for (uint32_t b = tid; b < kHistBins; b += kThreads) hist[b] = 0;
+    for (uint32_t b = tid; b < kHistBins; b += NT) hist[b] = 0;
     __syncthreads();
     lo = red[0];
     hi = red[kW];
@@ -347,11 +350,11 @@ __device__ uint64_t block_cut_bound(const uint64_t* keys, uint32_t count, uint32
     }
     int shift = 0;
     while (((hi - lo) >> shift) >= kHistBins) ++shift;
-    for (uint32_t i = tid; i < count; i += kThreads)
+    for (uint32_t i = tid; i < count; i += NT)
         atomicAdd(&hist[((uint32_t)(keys[i] >> 32) - lo) >> shift], 1u);
     __syncthreads();
     // thread t owns bins [t * per, (t + 1) * per): the bin where the running count reaches K
-    constexpr uint32_t per = kHistBins / kThreads;
+    constexpr uint32_t per = kHistBins / NT;
     uint32_t c[per], run = 0;
 #pragma unroll
     for (uint32_t j = 0; j < per; ++j) {
@@ -384,18 +387,19 @@ __device__ uint64_t block_cut_bound(const uint64_t* keys, uint32_t count, uint32
 
 // Keeps the keys < bound at the front (in arbitrary order); returns their count.
 // `cnt` is a shared counter. All threads call it.
+template <int NT>
 __device__ uint32_t block_compact_lt(uint64_t* keys, uint32_t count, uint64_t bound, uint32_t* cnt) {
     const int tid = threadIdx.x, lane = tid & 31;
-    uint64_t mine[kCapPer];
+    uint64_t mine[(int)(kMaxCap / NT)];
 #pragma unroll
-    for (int j = 0; j < kCapPer; ++j) {
-        const uint32_t i = tid + j * kThreads;
+    for (int j = 0; j < (int)(kMaxCap / NT); ++j) {
+        const uint32_t i = tid + j * NT;
         mine[j] = i < count ? keys[i] : ~0ull;
     }
     if (tid == 0) *cnt = 0;
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kCapPer; ++j) {
+    for (int j = 0; j < (int)(kMaxCap / NT); ++j) {
         const bool keep = mine[j] < bound;
         const unsigned b = __ballot_sync(0xffffffffu, keep);
         uint32_t base = 0;
@@ -422,7 +426,7 @@ struct ScanState {
     uint64_t tau;
     uint64_t sel[4];
     uint32_t hist[256];
-    uint32_t red[2 * (kThreads / 32) + 2];
+    uint32_t red[2 * (512 / 32) + 2];  // for blocks of up to 512 threads
     uint32_t ccount;
     uint32_t count;
     uint32_t c;
@@ -502,6 +506,7 @@ __device__ __forceinline__ void scan_insert(ScanState& st, uint64_t* keys, bool 
 // round of `round` keys. One histogram pass gives a bound with at least T keys below
 // it (the final select is exact); tau = that bound. If the cut kept too many to take
 // another round, cut exactly to T.
+template <int NT>
 __device__ __forceinline__ void scan_after_round(ScanState& st, uint64_t* keys, uint32_t* hist,
                                                  uint32_t cap, uint32_t round, uint32_t T,
                                                  uint64_t tau, long long t_round) {
@@ -510,12 +515,12 @@ __device__ __forceinline__ void scan_after_round(ScanState& st, uint64_t* keys, 
     if (threadIdx.x == 0) st.cyc_rounds += (unsigned long long)(t_round_end - t_round);
     if (st.count > cap - round) {
         const uint32_t cnt = st.count;
-        uint64_t bound = block_cut_bound(keys, cnt, T, hist, st.red);
-        uint32_t kept = bound == kKeyMax ? cnt : block_compact_lt(keys, cnt, bound, &st.ccount);
+        uint64_t bound = block_cut_bound<NT>(keys, cnt, T, hist, st.red);
+        uint32_t kept = bound == kKeyMax ? cnt : block_compact_lt<NT>(keys, cnt, bound, &st.ccount);
         if (kept > cap - round) {
-            const uint64_t kth = block_select_kth(keys, kept, T, st.hist, st.sel);
+            const uint64_t kth = block_select_kth<NT>(keys, kept, T, st.hist, st.sel);
             bound = kth + 1;  // kth < kKeyMax: keys are distinct by id
-            kept = block_compact_lt(keys, kept, bound, &st.ccount);
+            kept = block_compact_lt<NT>(keys, kept, bound, &st.ccount);
         }
         if (threadIdx.x == 0) {
             st.count = kept;
@@ -530,6 +535,7 @@ __device__ __forceinline__ void scan_after_round(ScanState& st, uint64_t* keys, 
 // The block's last steps: the exact T smallest keys of the buffer, written out
 // unordered (only the rerank's tie path needs their (t, id) order, and it sorts
 // them itself), and the diagnostic counters.
+template <int NT>
 __device__ void scan_finish(const ScanParams& p, ScanState& st, uint64_t* keys, uint32_t qi,
                             unsigned long long my_eval, unsigned long long my_look,
                             unsigned long long my_pass, long long t_start, long long t_pro) {
@@ -539,12 +545,12 @@ __device__ void scan_finish(const ScanParams& p, ScanState& st, uint64_t* keys, 
     const long long t_final = clock64();
     uint32_t count = st.count;
     if (count > T) {
-        const uint64_t kth = block_select_kth(keys, count, T, st.hist, st.sel);
-        block_compact_lt(keys, count, kth + 1, &st.ccount);
+        const uint64_t kth = block_select_kth<NT>(keys, count, T, st.hist, st.sel);
+        block_compact_lt<NT>(keys, count, kth + 1, &st.ccount);
         count = T;
     }
     const uint32_t out = count < T ? count : T;
-    for (uint32_t i = tid; i < T; i += kThreads) {
+    for (uint32_t i = tid; i < T; i += NT) {
         p.hdist[(uint64_t)qi * T + i] = i < out ? key_value(keys[i]) : sentinel_f();
         p.htag[(uint64_t)qi * T + i] = i < out ? (uint32_t)keys[i] : kNoLabel;
     }
@@ -600,7 +606,7 @@ __device__ __forceinline__ void load_codes(const uint8_t* codes, uint32_t stride
 // NW = code words per record (code_stride / 4); TAB = table variant.
 template <int NW, int TAB>
 __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(ScanParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ ScanState st;
     const uint32_t qi = p.order[blockIdx.x];
     const int tid = threadIdx.x;
@@ -685,48 +691,79 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
                 }
                 scan_insert(st, keys, keep, key, my_pass);
             }
-            scan_after_round(st, keys, hist, cap, kRound, T, tau, t_round);
+            scan_after_round<kThreads>(st, keys, hist, cap, kRound, T, tau, t_round);
         }
     }
-    scan_finish(p, st, keys, qi, my_eval, my_look, my_pass, t_start, t_pro);
+    scan_finish<kThreads>(p, st, keys, qi, my_eval, my_look, my_pass, t_start, t_pro);
 }
 
 // ------------------------------------------------------------ interleaved kernel
-constexpr int kIlThreads = kThreads;  // one block per query
-constexpr int kIlRec = 2;             // records per thread and round (double-buffered)
-constexpr int kIlRound = kIlThreads * kIlRec;
-static_assert(kIlThreads % 32 == 0, "rounds of whole warps keep record r on lane r & 31");
+// One 512-thread block per query (one block per SM by shared memory). A round is
+// 16 interleaved record blocks, 512 records: thread t takes lane t & 31 of block
+// t >> 5. Rounds arrive in a ring of kIlStages shared-memory slots by one bulk copy
+// each (cp.async.bulk, completion on the slot's mbarrier), issued by thread 0 up to
+// kIlStages rounds ahead; the first copies go out before the table is built.
+#ifndef PGPU_SCAN_IL_STAGES
+#define PGPU_SCAN_IL_STAGES 4
+#endif
+constexpr int kIlThreads = 512;
+constexpr int kIlStages = PGPU_SCAN_IL_STAGES;
+constexpr uint32_t kIlBlocksPerRound = kIlThreads / 32;
+constexpr int kIlRound = kIlThreads;  // records per round
+constexpr uint32_t kIlWaitLimit = 1u << 22;
+static_assert(kMaxCap % kIlThreads == 0 && kHistBins % kIlThreads == 0, "512-thread helpers");
 
 // Buffer size of the interleaved kernel for filter_topk T (see scan_cap).
 __host__ __device__ inline uint32_t il_cap(uint32_t T) {
     uint32_t room = T > 1024 ? T : 1024;
     uint32_t c = T + kIlRound + room;
-    c = (c + kThreads - 1) / kThreads * kThreads;
+    c = (c + kIlThreads - 1) / kIlThreads * kIlThreads;
     return c > kMaxCap ? kMaxCap : c;
 }
 __host__ __device__ constexpr uint32_t il_table_bytes(bool half) {
     return half ? 256u * 64u * 2u : 256u * 64u * 4u;
 }
-// Shared memory after the table: the query, then either the compact table being
-// built ([nsq][257] floats) or the cluster's cell terms, the key buffer and the
+// Shared memory after the table: the query, the ring, then either the compact table
+// being built ([nsq][257] floats) or the cluster's cell terms, the key buffer and the
 // cut histogram.
 __host__ __device__ inline uint32_t il_query_bytes(uint32_t d) { return (d * 4u + 15u) & ~15u; }
 __host__ __device__ inline uint32_t il_srow_bytes(uint32_t F) { return (F * 4u + 7u) & ~7u; }
+__host__ __device__ inline uint32_t il_slot_bytes(uint32_t nsq) {
+    return kIlBlocksPerRound * il_block_bytes(nsq);
+}
+
+__device__ __forceinline__ bool il_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kIlWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.b32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
 
 template <int NSQ, bool HALF>
-__global__ __launch_bounds__(kIlThreads, 2) void k_scan_il(ScanParams p) {
+__global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
     static_assert(NSQ % 4 == 0 && NSQ <= 32, "interleaved layout: nsq a multiple of 4, <= 32");
     constexpr int NG = (NSQ + 7) / 8;  // 8-byte code granules per record
-    constexpr int NW = 2 * NG;
-    constexpr uint32_t kRecBytes = NG * 8;
-    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr uint32_t kG = NG * 8;
+    constexpr uint32_t kBlk = 32 * kG + 192;  // il_block_bytes
+    constexpr uint32_t kSlot = kIlBlocksPerRound * kBlk;
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ ScanState st;
+    __shared__ __align__(8) uint64_t full[kIlStages];
+    __shared__ int il_failed;
     const uint32_t qi = p.order[blockIdx.x];
     const int tid = threadIdx.x;
     const uint32_t F = p.F, T = p.T, cap = p.cap;
     unsigned char* tab = smem;  // the rotated table, at offset 0
     float* qv = reinterpret_cast<float*>(smem + il_table_bytes(HALF));
-    unsigned char* rest = smem + il_table_bytes(HALF) + il_query_bytes(p.d);
+    unsigned char* ring = smem + il_table_bytes(HALF) + il_query_bytes(p.d);  // [kIlStages][kSlot]
+    unsigned char* rest = ring + kIlStages * kSlot;
     float* stage = reinterpret_cast<float*>(rest);  // [NSQ][257] while the table is built
     float* srow = reinterpret_cast<float*>(rest);   // [F] afterwards
     uint64_t* keys = reinterpret_cast<uint64_t*>(rest + il_srow_bytes(F));  // [cap]
@@ -737,40 +774,80 @@ __global__ __launch_bounds__(kIlThreads, 2) void k_scan_il(ScanParams p) {
         return;
     }
     const long long t_start = clock64();
-    for (uint32_t i = tid; i < p.d; i += kIlThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
-    const float* fdk = p.fd_by_fine + (uint64_t)qi * F;
+    // rounds issued and consumed over the whole block (slot g % S, parity (g / S) & 1)
+    uint32_t g_issued = 0, g_done = 0;
+    auto bar_of = [&](uint32_t g) { return (uint32_t)__cvta_generic_to_shared(&full[g % kIlStages]); };
+    // thread 0: bulk copy of record blocks [blk0, blk0 + nblk) into round g's slot
+    auto issue = [&](uint32_t g, uint64_t blk0, uint32_t nblk) {
+        const uint32_t bar = bar_of(g);
+        const uint32_t bytes = nblk * kBlk;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(ring + (g % kIlStages) * kSlot);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(dst),
+            "l"(p.codes_il + blk0 * kBlk), "r"(bytes), "r"(bar)
+            : "memory");
+    };
     if (tid == 0) {
+        for (int i = 0; i < kIlStages; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar_of(i)), "r"(1u));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         st.tau = kKeyMax;
         st.count = 0;
         st.evaluated = st.looked = st.passed = 0;
         st.cyc_rounds = st.cyc_compact = st.n_compact = st.n_records = 0;
+        il_failed = 0;
     }
+    // the first cluster's first rounds go out before the table is built
+    uint32_t primed_blk0 = 0, primed_blocks = 0;
+    if (tid == 0) {
+        const uint32_t c = p.ctag[(uint64_t)qi * p.P];
+        if (c < p.C) {
+            const uint32_t r0 = p.cell_start[(uint64_t)c * F], r1 = p.cell_start[(uint64_t)c * F + F];
+            if (r1 > r0) {
+                const uint32_t b0 = r0 >> 5, nblk = ((r1 - 1) >> 5) - b0 + 1;
+                primed_blk0 = b0;
+                for (uint32_t k = 0; k < (uint32_t)kIlStages && k * kIlBlocksPerRound < nblk; ++k) {
+                    const uint32_t m = min(kIlBlocksPerRound, nblk - k * kIlBlocksPerRound);
+                    issue(g_issued++, (uint64_t)b0 + k * kIlBlocksPerRound, m);
+                    primed_blocks += m;
+                }
+            }
+        }
+    }
+    for (uint32_t i = tid; i < p.d; i += kIlThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
+    const float* fdk = p.fd_by_fine + (uint64_t)qi * F;
     const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
     const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
     __syncthreads();
     // get_dist_table (quantization.cpp:260-270) in the reference's lane order,
     // stage[m * 257 + j] (row pitch 257: the expansion below reads it without bank
-    // conflicts)
-    for (uint32_t j = tid; j < 256; j += kIlThreads) {
+    // conflicts); two threads per codeword, each half of the subspaces
+    {
+        const uint32_t j = tid & 255u;
+        const int mh = (tid >> 8) * (NSQ / 2);
         if (p.lsq == 4) {
             const float4* cb4 = reinterpret_cast<const float4*>(p.codebook);
 #pragma unroll
-            for (int m0 = 0; m0 < NSQ; m0 += 4) {
-                float4 y[4];
+            for (int m0 = 0; m0 < NSQ / 2; m0 += 2) {
+                float4 y[2];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) y[u] = __ldg(cb4 + (uint64_t)(m0 + u) * 256 + j);
+                for (int u = 0; u < 2; ++u) y[u] = __ldg(cb4 + (uint64_t)(mh + m0 + u) * 256 + j);
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const float* x = qv + (m0 + u) * 4;
+                for (int u = 0; u < 2; ++u) {
+                    const int m = mh + m0 + u;
+                    const float* x = qv + m * 4;
                     const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
                     const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
-                    stage[(m0 + u) * 257 + j] =
-                        __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
-                                  __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
+                    stage[m * 257 + j] = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                                   __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
                 }
             }
         } else {
-            for (int m = 0; m < NSQ; ++m)
+            for (int m = mh; m < mh + NSQ / 2; ++m)
                 stage[m * 257 + j] = l2sqr_sse(qv + m * p.lsq,
                                                p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
         }
@@ -797,88 +874,127 @@ __global__ __launch_bounds__(kIlThreads, 2) void k_scan_il(ScanParams p) {
     unsigned long long my_eval = 0, my_pass = 0;
     const long long t_pro = clock64();
 
-    struct Rec {
-        uint32_t w[NW];
-        float off;
-        uint32_t fine, mr;  // mr = ~0: no record in this slot
-    };
-    for (uint32_t l = 0; l < p.P; ++l) {
-        if (!scan_cluster_begin(p, st, qi, l)) break;  // (its first barrier ends the table)
-        const uint32_t r0 = st.r0, i0 = st.i0;
-        const uint32_t nb = st.r1 - r0, nall = nb + (st.i1 - st.i0);
-        if (nall == 0) continue;
-        scan_fill_srow(p, srow, fdk, st.c, st.cdl);
-        if (tid == 0) st.n_records += nall;
-        // slot u of [0, lead + nall) is record u - lead: lead = r0 & 31 puts a base
-        // record with memory id r on lane r & 31 (inserted records come from a list)
-        const uint32_t lead = r0 & 31u, U = lead + nall;
-        auto load = [&](Rec (&b)[kIlRec], uint32_t u0) {
+    // t of one record from its codes (8-byte granules), offset and fine id
+    auto score_record = [&](const uint2 (&gr)[NG], float off, uint32_t fine, uint32_t mr) {
+        const float t0 = __fadd_rn(srow[fine], off);  // (float)(2.0 * cell_dist + offset)
+        const uint32_t lb = (mr & 31u) << 2;           // byte 0 of the table address
+        float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-            for (int j = 0; j < kIlRec; ++j) {
-                const uint32_t v = u0 + tid + j * kIlThreads - lead;  // wraps below lead
-                b[j].mr = ~0u;
-                if (v < nall) {
-                    const uint32_t mr = v < nb ? r0 + v : p.ins_cl_ids[i0 + v - nb];
-                    b[j].mr = mr;
-                    b[j].fine = p.rec_fine[mr];
-                    b[j].off = p.offsets[mr];
-                    const uint2* g = reinterpret_cast<const uint2*>(
-                        p.codes_il + (uint64_t)(mr >> 5) * (32 * kRecBytes) + 8 * (mr & 31));
-#pragma unroll
-                    for (int k = 0; k < NG; ++k) {
-                        const uint2 x = __ldg(g + 32 * k);
-                        b[j].w[2 * k] = x.x;
-                        b[j].w[2 * k + 1] = x.y;
-                    }
-                }
+        for (int s2 = 0; s2 < NSQ; ++s2) {
+            const uint32_t w = (s2 & 4) ? gr[s2 >> 3].y : gr[s2 >> 3].x;
+            // (code << 8) | 4 * lane: the entry of column s2 + lane
+            const uint32_t addr = __byte_perm(w, lb, 0x5504u | ((uint32_t)(s2 & 3) << 4));
+            if (HALF) {
+                const unsigned short h =
+                    *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
+                asm("add.f32.f16 %0, %1, %0;" : "+f"(a[s2 & 3]) : "h"(h));
+            } else {
+                a[s2 & 3] = __fadd_rn(a[s2 & 3], *reinterpret_cast<const float*>(tab + addr + 4 * s2));
             }
-        };
-        auto score = [&](const Rec (&b)[kIlRec]) {
+        }
+        const float sum = __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3]));
+        return HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
+    };
+
+    for (uint32_t l = 0; l < p.P && !il_failed; ++l) {
+        if (!scan_cluster_begin(p, st, qi, l)) break;  // (its first barrier ends the table)
+        const uint32_t r0 = st.r0, r1 = st.r1, i0 = st.i0, ni = st.i1 - st.i0;
+        if (r1 - r0 + ni == 0) continue;
+        if (tid == 0) st.n_records += r1 - r0 + ni;
+        uint32_t b0 = 0, nblk = 0, rounds = 0;
+        if (r1 > r0) {
+            b0 = r0 >> 5;
+            nblk = ((r1 - 1) >> 5) - b0 + 1;
+            rounds = (nblk + kIlBlocksPerRound - 1) / kIlBlocksPerRound;
+        }
+        // rounds of this cluster already in flight (the first cluster's, primed)
+        uint32_t sent = (l == 0 && primed_blocks > 0 && primed_blk0 == b0)
+                            ? (primed_blocks + kIlBlocksPerRound - 1) / kIlBlocksPerRound
+                            : 0;
+        if (tid == 0) {
+            for (; sent < rounds && sent < (uint32_t)kIlStages; ++sent)
+                issue(g_issued++, (uint64_t)b0 + sent * kIlBlocksPerRound,
+                      min(kIlBlocksPerRound, nblk - sent * kIlBlocksPerRound));
+        }
+        sent = rounds < (uint32_t)kIlStages ? rounds : (uint32_t)kIlStages;
+        g_issued = g_done + sent;  // every thread tracks the count thread 0 issued
+        scan_fill_srow(p, srow, fdk, st.c, st.cdl);
+        const uint32_t blk = tid >> 5, lane = tid & 31;
+        for (uint32_t k = 0; k < rounds; ++k) {
             const long long t_round = clock64();
             const uint64_t tau = st.tau;
-#pragma unroll
-            for (int j = 0; j < kIlRec; ++j) {
-                bool keep = false;
-                uint64_t key = 0;
-                if (b[j].mr != ~0u) {
-                    // (float)(2.0 * cell_dist + offset): one float add of the exact
-                    // 2 * cell_dist (see adc_base)
-                    const float t0 = __fadd_rn(srow[b[j].fine], b[j].off);
-                    const uint32_t lb = (b[j].mr & 31u) << 2;  // byte 0 of the address
-                    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-                    for (int s2 = 0; s2 < NSQ; ++s2) {
-                        // (code << 8) | 4 * lane: the entry of column s2 + lane
-                        const uint32_t addr =
-                            __byte_perm(b[j].w[s2 >> 2], lb, 0x5504u | ((uint32_t)(s2 & 3) << 4));
-                        if (HALF)
-                            a[s2 & 3] += __half2float(
-                                *reinterpret_cast<const __half*>(tab + (addr >> 1) + 2 * s2));
-                        else
-                            a[s2 & 3] = __fadd_rn(
-                                a[s2 & 3], *reinterpret_cast<const float*>(tab + addr + 4 * s2));
-                    }
-                    const float sum = __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3]));
-                    const float t = HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
-                    ++my_eval;
-                    key = filter_key(t, b[j].mr);
-                    keep = key < tau;
-                }
-                scan_insert(st, keys, keep, key, my_pass);
+            const uint32_t g = g_done;
+            if (!il_wait(bar_of(g), (g / kIlStages) & 1u)) {
+                if (lane == 0) atomicExch(&il_failed, 1);
             }
-            scan_after_round(st, keys, hist, cap, kIlRound, T, tau, t_round);
-        };
-        Rec ra[kIlRec], rb[kIlRec];
-        load(ra, 0);
-        for (uint32_t u0 = 0; u0 < U; u0 += 2 * kIlRound) {
-            if (u0 + kIlRound < U) load(rb, u0 + kIlRound);
-            score(ra);
-            if (u0 + kIlRound >= U) break;
-            if (u0 + 2 * kIlRound < U) load(ra, u0 + 2 * kIlRound);
-            score(rb);
+            const uint64_t bk = (uint64_t)b0 + k * kIlBlocksPerRound + blk;
+            const uint32_t r = (uint32_t)(bk * 32 + lane);
+            bool keep = false;
+            uint64_t key = 0;
+            if (bk < (uint64_t)b0 + nblk && r >= r0 && r < r1 && !il_failed) {
+                const unsigned char* rec = ring + (g % kIlStages) * kSlot + blk * kBlk;
+                uint2 gr[NG];
+#pragma unroll
+                for (int q2 = 0; q2 < NG; ++q2)
+                    gr[q2] = *reinterpret_cast<const uint2*>(rec + q2 * 256 + 8 * lane);
+                const float off = *reinterpret_cast<const float*>(rec + 32 * kG + 4 * lane);
+                const uint32_t fine = *reinterpret_cast<const uint16_t*>(rec + 32 * kG + 128 + 2 * lane);
+                const float t = score_record(gr, off, fine, r);
+                ++my_eval;
+                key = filter_key(t, r);
+                keep = key < tau;
+            }
+            scan_insert(st, keys, keep, key, my_pass);
+            scan_after_round<kIlThreads>(st, keys, hist, cap, kIlRound, T, tau, t_round);
+            if (il_failed) break;  // read after the barrier: the same on every thread
+            ++g_done;
+            // the slot of round g is free: thread 0 refills it with round k + kIlStages
+            const uint32_t kn = k + kIlStages;
+            if (kn < rounds) {
+                if (tid == 0)
+                    issue(g_issued, (uint64_t)b0 + kn * kIlBlocksPerRound,
+                          min(kIlBlocksPerRound, nblk - kn * kIlBlocksPerRound));
+                ++g_issued;
+            }
+        }
+        // realtime: the cluster's inserted records, read from the interleaved copy
+        for (uint32_t v0 = 0; v0 < ni; v0 += kIlRound) {
+            const long long t_round = clock64();
+            const uint64_t tau = st.tau;
+            bool keep = false;
+            uint64_t key = 0;
+            if (v0 + tid < ni) {
+                const uint32_t mr = p.ins_cl_ids[i0 + v0 + tid];
+                uint2 gr[NG];
+#pragma unroll
+                for (int q2 = 0; q2 < NG; ++q2)
+                    gr[q2] = __ldg(reinterpret_cast<const uint2*>(p.codes_il +
+                                                                  il_granule_offset(mr, q2, NSQ)));
+                const float off = __ldg(reinterpret_cast<const float*>(p.codes_il +
+                                                                       il_offset_offset(mr, NSQ)));
+                const uint32_t fine =
+                    __ldg(reinterpret_cast<const uint16_t*>(p.codes_il + il_fine_offset(mr, NSQ)));
+                const float t = score_record(gr, off, fine, mr);
+                ++my_eval;
+                key = filter_key(t, mr);
+                keep = key < tau;
+            }
+            scan_insert(st, keys, keep, key, my_pass);
+            scan_after_round<kIlThreads>(st, keys, hist, cap, kIlRound, T, tau, t_round);
         }
     }
-    scan_finish(p, st, keys, qi, my_eval, my_eval, my_pass, t_start, t_pro);
+    if (il_failed) {
+        // a copy did not arrive in time: wait (bounded) for every copy issued, so
+        // none lands in shared memory after the block, and report the query as empty
+        for (uint32_t g = g_done; g < g_issued; ++g) il_wait(bar_of(g), (g / kIlStages) & 1u);
+        __syncthreads();
+        if (tid == 0) {
+            p.hcnt[qi] = 0;
+            atomicExch(p.err, 1);
+        }
+        return;
+    }
+    scan_finish<kIlThreads>(p, st, keys, qi, my_eval, my_eval, my_pass, t_start, t_pro);
 }
 
 // Launch order of the scan's blocks. A block's time follows the records of the
@@ -944,7 +1060,8 @@ static size_t il_smem_bytes(const DeviceIndex& ix, uint32_t T, bool half) {
     const size_t stage = sizeof(float) * ix.nsq * 257;
     const size_t work = il_srow_bytes(ix.F) + sizeof(uint64_t) * il_cap(T) +
                         sizeof(uint32_t) * kHistBins;
-    return il_table_bytes(half) + il_query_bytes(ix.d) + (stage > work ? stage : work);
+    return il_table_bytes(half) + il_query_bytes(ix.d) + (size_t)kIlStages * il_slot_bytes(ix.nsq) +
+           (stage > work ? stage : work);
 }
 
 size_t scan_smem_bytes(const DeviceIndex& ix, uint32_t T) {
@@ -1003,37 +1120,38 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.codebook_max = ix.codebook_max;
     if (s.order == nullptr || s.T > scan_max_filter_topk()) return cudaErrorInvalidValue;
     p.order = s.order;
+    p.err = s.tc_err;
     p.ins_cl_start = ix.ins_n ? ix.ins_cl_start : nullptr;
     p.ins_cl_ids = ix.ins_cl_ids;
     const size_t smem = half_lut ? scan_smem_bytes_half(ix, s.T) : scan_smem_bytes(ix, s.T);
     const uint32_t nw = ix.code_stride / 4;
-    auto launch = [&](void (*kernel)(ScanParams)) {
+    auto launch = [&](void (*kernel)(ScanParams), int threads) {
         ensure_max_dynamic_smem(kernel, 220 * 1024);
-        kernel<<<n, kThreads, smem, stream>>>(p);
+        kernel<<<n, threads, smem, stream>>>(p);
     };
     if (il_applies(ix.nsq)) {
         if (ix.codes_il == nullptr) return cudaErrorInvalidValue;
         p.cap = il_cap(s.T);
         switch (ix.nsq) {
 #define PGPU_IL(N) \
-    case N: launch(half_lut ? k_scan_il<N, true> : k_scan_il<N, false>); break;
+    case N: launch(half_lut ? k_scan_il<N, true> : k_scan_il<N, false>, kIlThreads); break;
             PGPU_IL(4) PGPU_IL(8) PGPU_IL(12) PGPU_IL(16) PGPU_IL(20) PGPU_IL(24) PGPU_IL(28)
             PGPU_IL(32)
 #undef PGPU_IL
             default: return cudaErrorInvalidValue;
         }
     } else if (half_lut) {
-        if (nw <= 2) launch(k_scan_select<2, kTabF16>);
-        else if (nw <= 4) launch(k_scan_select<4, kTabF16>);
-        else if (nw <= 6) launch(k_scan_select<6, kTabF16>);
-        else if (nw <= 8) launch(k_scan_select<8, kTabF16>);
-        else launch(k_scan_select<16, kTabF16>);
+        if (nw <= 2) launch(k_scan_select<2, kTabF16>, kThreads);
+        else if (nw <= 4) launch(k_scan_select<4, kTabF16>, kThreads);
+        else if (nw <= 6) launch(k_scan_select<6, kTabF16>, kThreads);
+        else if (nw <= 8) launch(k_scan_select<8, kTabF16>, kThreads);
+        else launch(k_scan_select<16, kTabF16>, kThreads);
     } else {
-        if (nw <= 2) launch(k_scan_select<2, kTabF32>);
-        else if (nw <= 4) launch(k_scan_select<4, kTabF32>);
-        else if (nw <= 6) launch(k_scan_select<6, kTabF32>);
-        else if (nw <= 8) launch(k_scan_select<8, kTabF32>);
-        else launch(k_scan_select<16, kTabF32>);
+        if (nw <= 2) launch(k_scan_select<2, kTabF32>, kThreads);
+        else if (nw <= 4) launch(k_scan_select<4, kTabF32>, kThreads);
+        else if (nw <= 6) launch(k_scan_select<6, kTabF32>, kThreads);
+        else if (nw <= 8) launch(k_scan_select<8, kTabF32>, kThreads);
+        else launch(k_scan_select<16, kTabF32>, kThreads);
     }
     return cudaGetLastError();
 }
