@@ -546,6 +546,14 @@ def run_profile(args, w):
     for _ in range(args.steps):
         ix.search_device(w["nq"], q, w["k"], d, i)
     torch.cuda.synchronize()
+    # one more pass with the library's per-stage events
+    ix.set_profiling(True)
+    ix.search_device(w["nq"], q, w["k"], d, i)
+    stages = ix.stage_times()
+    ix.set_profiling(False)
+    ix.search(queries.cpu().numpy(), w["k"])
+    log(f"[bench] stage ms: {json.dumps({k: round(v, 4) for k, v in stages.items()})}")
+    log(f"[bench] counters: {json.dumps(ix.walk_counters())}")
     ix.close()
     log(f"[bench] profile {form}:{x} on {args.workload}: {args.steps} passes")
 
