@@ -699,17 +699,19 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
 
 // ------------------------------------------------------------ interleaved kernel
 // One 512-thread block per query (one block per SM by shared memory). A round is
-// 16 interleaved record blocks, 512 records: thread t takes lane t & 31 of block
-// t >> 5. Rounds arrive in a ring of kIlStages shared-memory slots by one bulk copy
-// each (cp.async.bulk, completion on the slot's mbarrier), issued by thread 0 up to
-// kIlStages rounds ahead; the first copies go out before the table is built.
+// 32 interleaved record blocks, 1024 records: thread t takes lane t & 31 of blocks
+// t >> 5 and (t >> 5) + 16, and scores the two records together. Rounds arrive in a
+// ring of kIlStages shared-memory slots by one bulk copy each (cp.async.bulk,
+// completion on the slot's mbarrier), issued by thread 0 up to kIlStages rounds
+// ahead; the first copies go out before the table is built.
 #ifndef PGPU_SCAN_IL_STAGES
-#define PGPU_SCAN_IL_STAGES 4
+#define PGPU_SCAN_IL_STAGES 3
 #endif
 constexpr int kIlThreads = 512;
 constexpr int kIlStages = PGPU_SCAN_IL_STAGES;
-constexpr uint32_t kIlBlocksPerRound = kIlThreads / 32;
-constexpr int kIlRound = kIlThreads;  // records per round
+constexpr int kIlRec = 2;  // records per thread and round
+constexpr uint32_t kIlBlocksPerRound = kIlThreads / 32 * kIlRec;
+constexpr int kIlRound = kIlThreads * kIlRec;  // records per round
 constexpr uint32_t kIlWaitLimit = 1u << 22;
 static_assert(kMaxCap % kIlThreads == 0 && kHistBins % kIlThreads == 0, "512-thread helpers");
 
@@ -874,26 +876,41 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
     unsigned long long my_eval = 0, my_pass = 0;
     const long long t_pro = clock64();
 
-    // t of one record from its codes (8-byte granules), offset and fine id
-    auto score_record = [&](const uint2 (&gr)[NG], float off, uint32_t fine, uint32_t mr) {
-        const float t0 = __fadd_rn(srow[fine], off);  // (float)(2.0 * cell_dist + offset)
-        const uint32_t lb = (mr & 31u) << 2;           // byte 0 of the table address
-        float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    // t of R records from their codes (8-byte granules), offsets and fine ids; the
+    // R lookup chains are interleaved
+    auto score_records = [&](const uint2 (&gr)[kIlRec][NG], const float (&off)[kIlRec],
+                             const uint32_t (&fine)[kIlRec], const uint32_t (&mr)[kIlRec],
+                             float (&t)[kIlRec]) {
+        float a[kIlRec][4];
+        uint32_t lb[kIlRec];
+#pragma unroll
+        for (int j = 0; j < kIlRec; ++j) {
+            lb[j] = (mr[j] & 31u) << 2;  // byte 0 of the table address
+            a[j][0] = a[j][1] = a[j][2] = a[j][3] = 0.0f;
+        }
 #pragma unroll
         for (int s2 = 0; s2 < NSQ; ++s2) {
-            const uint32_t w = (s2 & 4) ? gr[s2 >> 3].y : gr[s2 >> 3].x;
-            // (code << 8) | 4 * lane: the entry of column s2 + lane
-            const uint32_t addr = __byte_perm(w, lb, 0x5504u | ((uint32_t)(s2 & 3) << 4));
-            if (HALF) {
-                const unsigned short h =
-                    *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
-                asm("add.f32.f16 %0, %1, %0;" : "+f"(a[s2 & 3]) : "h"(h));
-            } else {
-                a[s2 & 3] = __fadd_rn(a[s2 & 3], *reinterpret_cast<const float*>(tab + addr + 4 * s2));
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                const uint32_t w = (s2 & 4) ? gr[j][s2 >> 3].y : gr[j][s2 >> 3].x;
+                // (code << 8) | 4 * lane: the entry of column s2 + lane
+                const uint32_t addr = __byte_perm(w, lb[j], 0x5504u | ((uint32_t)(s2 & 3) << 4));
+                if (HALF) {
+                    const unsigned short h =
+                        *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
+                    asm("add.f32.f16 %0, %1, %0;" : "+f"(a[j][s2 & 3]) : "h"(h));
+                } else {
+                    a[j][s2 & 3] = __fadd_rn(a[j][s2 & 3],
+                                             *reinterpret_cast<const float*>(tab + addr + 4 * s2));
+                }
             }
         }
-        const float sum = __fadd_rn(__fadd_rn(a[0], a[1]), __fadd_rn(a[2], a[3]));
-        return HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
+#pragma unroll
+        for (int j = 0; j < kIlRec; ++j) {
+            const float t0 = __fadd_rn(srow[fine[j]], off[j]);  // (float)(2.0 * cell_dist + offset)
+            const float sum = __fadd_rn(__fadd_rn(a[j][0], a[j][1]), __fadd_rn(a[j][2], a[j][3]));
+            t[j] = HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
+        }
     };
 
     for (uint32_t l = 0; l < p.P && !il_failed; ++l) {
@@ -927,24 +944,33 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
             if (!il_wait(bar_of(g), (g / kIlStages) & 1u)) {
                 if (lane == 0) atomicExch(&il_failed, 1);
             }
-            const uint64_t bk = (uint64_t)b0 + k * kIlBlocksPerRound + blk;
-            const uint32_t r = (uint32_t)(bk * 32 + lane);
-            bool keep = false;
-            uint64_t key = 0;
-            if (bk < (uint64_t)b0 + nblk && r >= r0 && r < r1 && !il_failed) {
-                const unsigned char* rec = ring + (g % kIlStages) * kSlot + blk * kBlk;
-                uint2 gr[NG];
+            uint2 gr[kIlRec][NG];
+            float off[kIlRec], t[kIlRec];
+            uint32_t fine[kIlRec], rr[kIlRec];
+            bool valid[kIlRec];
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                const uint32_t bl = blk + j * (kIlThreads / 32);  // block of the round
+                const uint64_t bk = (uint64_t)b0 + k * kIlBlocksPerRound + bl;
+                rr[j] = (uint32_t)(bk * 32 + lane);
+                valid[j] = bk < (uint64_t)b0 + nblk && rr[j] >= r0 && rr[j] < r1 && !il_failed;
+                // out-of-range slots read stale bytes of the slot and are dropped below
+                const unsigned char* rec = ring + (g % kIlStages) * kSlot + bl * kBlk;
 #pragma unroll
                 for (int q2 = 0; q2 < NG; ++q2)
-                    gr[q2] = *reinterpret_cast<const uint2*>(rec + q2 * 256 + 8 * lane);
-                const float off = *reinterpret_cast<const float*>(rec + 32 * kG + 4 * lane);
-                const uint32_t fine = *reinterpret_cast<const uint16_t*>(rec + 32 * kG + 128 + 2 * lane);
-                const float t = score_record(gr, off, fine, r);
-                ++my_eval;
-                key = filter_key(t, r);
-                keep = key < tau;
+                    gr[j][q2] = *reinterpret_cast<const uint2*>(rec + q2 * 256 + 8 * lane);
+                off[j] = *reinterpret_cast<const float*>(rec + 32 * kG + 4 * lane);
+                fine[j] = valid[j] ? *reinterpret_cast<const uint16_t*>(rec + 32 * kG + 128 + 2 * lane)
+                                   : 0u;
             }
-            scan_insert(st, keys, keep, key, my_pass);
+            score_records(gr, off, fine, rr, t);
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                const uint64_t key = filter_key(t[j], rr[j]);
+                const bool keep = valid[j] && key < tau;
+                my_eval += valid[j] ? 1 : 0;
+                scan_insert(st, keys, keep, key, my_pass);
+            }
             scan_after_round<kIlThreads>(st, keys, hist, cap, kIlRound, T, tau, t_round);
             if (il_failed) break;  // read after the barrier: the same on every thread
             ++g_done;
@@ -961,25 +987,30 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
         for (uint32_t v0 = 0; v0 < ni; v0 += kIlRound) {
             const long long t_round = clock64();
             const uint64_t tau = st.tau;
-            bool keep = false;
-            uint64_t key = 0;
-            if (v0 + tid < ni) {
-                const uint32_t mr = p.ins_cl_ids[i0 + v0 + tid];
-                uint2 gr[NG];
+            uint2 gr[kIlRec][NG];
+            float off[kIlRec], t[kIlRec];
+            uint32_t fine[kIlRec], mr[kIlRec];
+            bool valid[kIlRec];
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                const uint32_t v = v0 + tid + j * kIlThreads;
+                valid[j] = v < ni;
+                mr[j] = valid[j] ? p.ins_cl_ids[i0 + v] : 0u;
 #pragma unroll
                 for (int q2 = 0; q2 < NG; ++q2)
-                    gr[q2] = __ldg(reinterpret_cast<const uint2*>(p.codes_il +
-                                                                  il_granule_offset(mr, q2, NSQ)));
-                const float off = __ldg(reinterpret_cast<const float*>(p.codes_il +
-                                                                       il_offset_offset(mr, NSQ)));
-                const uint32_t fine =
-                    __ldg(reinterpret_cast<const uint16_t*>(p.codes_il + il_fine_offset(mr, NSQ)));
-                const float t = score_record(gr, off, fine, mr);
-                ++my_eval;
-                key = filter_key(t, mr);
-                keep = key < tau;
+                    gr[j][q2] = __ldg(reinterpret_cast<const uint2*>(
+                        p.codes_il + il_granule_offset(mr[j], q2, NSQ)));
+                off[j] = __ldg(reinterpret_cast<const float*>(p.codes_il + il_offset_offset(mr[j], NSQ)));
+                fine[j] = __ldg(reinterpret_cast<const uint16_t*>(p.codes_il + il_fine_offset(mr[j], NSQ)));
             }
-            scan_insert(st, keys, keep, key, my_pass);
+            score_records(gr, off, fine, mr, t);
+#pragma unroll
+            for (int j = 0; j < kIlRec; ++j) {
+                const uint64_t key = filter_key(t[j], mr[j]);
+                const bool keep = valid[j] && key < tau;
+                my_eval += valid[j] ? 1 : 0;
+                scan_insert(st, keys, keep, key, my_pass);
+            }
             scan_after_round<kIlThreads>(st, keys, hist, cap, kIlRound, T, tau, t_round);
         }
     }
