@@ -87,51 +87,53 @@ __global__ __launch_bounds__(kPrepWarps * 32) void k_prep_queries(
 }
 
 // out[i][j] = bias[j] - a_i.b_j (MODE 0), -(a_i.b_j) (MODE 1), bias[j] + a_i.b_j (MODE 2).
-// 64x64 output tile per block, 4x4 per thread; the k loop runs in order for
-// every output, so each dot product is summed sequentially.
-constexpr int kTile = 64, kTileK = 32;
+// 128x128 output tile per block, 8x8 per thread (rows ty + 16i, columns tx + 16j);
+// the k loop runs in order for every output, so each dot product is summed
+// sequentially (a product, then an add, no contraction).
+constexpr int kTile = 128, kTileK = 16;
 template <int MODE>
 __global__ __launch_bounds__(256) void k_centroid_scores(const float* __restrict__ A, uint32_t na,
                                                          const float* __restrict__ B, uint32_t nb,
                                                          uint32_t d, const float* __restrict__ bias,
                                                          float* __restrict__ out, uint32_t ld_out) {
-    __shared__ float As[kTileK][kTile + 1];
-    __shared__ float Bs[kTileK][kTile + 1];
+    __shared__ float As[kTileK][kTile + 4];
+    __shared__ float Bs[kTileK][kTile + 4];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const uint32_t a0 = blockIdx.y * kTile, b0 = blockIdx.x * kTile;
-    float acc[4][4];
+    float acc[8][8];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
     for (uint32_t k0 = 0; k0 < d; k0 += kTileK) {
+        // 16 consecutive threads read 16 consecutive k of one row
         for (int e = threadIdx.x; e < kTile * kTileK; e += 256) {
             const int r = e / kTileK, kk = e % kTileK;
             const uint32_t k = k0 + kk;
-            As[kk][r] = (a0 + r < na && k < d) ? A[(uint64_t)(a0 + r) * d + k] : 0.0f;
-            Bs[kk][r] = (b0 + r < nb && k < d) ? B[(uint64_t)(b0 + r) * d + k] : 0.0f;
+            As[kk][r] = (a0 + r < na && k < d) ? __ldg(A + (uint64_t)(a0 + r) * d + k) : 0.0f;
+            Bs[kk][r] = (b0 + r < nb && k < d) ? __ldg(B + (uint64_t)(b0 + r) * d + k) : 0.0f;
         }
         __syncthreads();
         const uint32_t kmax = min((uint32_t)kTileK, d - k0);
         for (uint32_t kk = 0; kk < kmax; ++kk) {
-            float av[4], bv[4];
+            float av[8], bv[8];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < 8; ++i) av[i] = As[kk][ty + 16 * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < 8; ++j) bv[j] = Bs[kk][tx + 16 * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 8; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(av[i], bv[j]));
+                for (int j = 0; j < 8; ++j) acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(av[i], bv[j]));
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 8; ++i) {
         const uint32_t a = a0 + ty + 16 * i;
         if (a >= na) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < 8; ++j) {
             const uint32_t b = b0 + tx + 16 * j;
             if (b >= nb) continue;
             float v;
