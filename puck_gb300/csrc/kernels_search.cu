@@ -341,6 +341,8 @@ __global__ __launch_bounds__(kSelThreads) void k_topsel_small(
     }
 }
 
+// Tile of k_nearest_center: 64 points x 64 centroids per step, 4x4 per thread.
+constexpr int kNcTile = 64, kNcTileK = 32;
 // nearest_center (kmeans.cpp:221-258): argmin_c (|x|^2 + |c|^2) - 2 x.c, with the
 // double-precision subtraction of the reference done as one float subtraction
 // (exact 2*dot, innocuous double rounding), first centroid wins ties.
@@ -350,12 +352,12 @@ __global__ __launch_bounds__(256) void k_nearest_center(const float* __restrict_
                                                         const float* __restrict__ cnorm,
                                                         int32_t* __restrict__ assign,
                                                         float* __restrict__ dis) {
-    __shared__ float As[kTileK][kTile + 1];
-    __shared__ float Bs[kTileK][kTile + 1];
-    __shared__ float red_v[16][kTile];
-    __shared__ uint32_t red_i[16][kTile];
+    __shared__ float As[kNcTileK][kNcTile + 1];
+    __shared__ float Bs[kNcTileK][kNcTile + 1];
+    __shared__ float red_v[16][kNcTile];
+    __shared__ uint32_t red_i[16][kNcTile];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const uint64_t a0 = (uint64_t)blockIdx.x * kTile;
+    const uint64_t a0 = (uint64_t)blockIdx.x * kNcTile;
     float best[4];
     uint32_t bidx[4];
 #pragma unroll
@@ -363,21 +365,21 @@ __global__ __launch_bounds__(256) void k_nearest_center(const float* __restrict_
         best[i] = FLT_MAX;
         bidx[i] = 0;
     }
-    for (uint64_t b0 = 0; b0 < k; b0 += kTile) {
+    for (uint64_t b0 = 0; b0 < k; b0 += kNcTile) {
         float acc[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
-        for (uint32_t k0 = 0; k0 < d; k0 += kTileK) {
-            for (int e = threadIdx.x; e < kTile * kTileK; e += 256) {
-                const int r = e / kTileK, kk = e % kTileK;
+        for (uint32_t k0 = 0; k0 < d; k0 += kNcTileK) {
+            for (int e = threadIdx.x; e < kNcTile * kNcTileK; e += 256) {
+                const int r = e / kNcTileK, kk = e % kNcTileK;
                 const uint32_t kd = k0 + kk;
                 As[kk][r] = (a0 + r < n && kd < d) ? X[(a0 + r) * d + kd] : 0.0f;
                 Bs[kk][r] = (b0 + r < k && kd < d) ? Cn[(b0 + r) * d + kd] : 0.0f;
             }
             __syncthreads();
-            const uint32_t kmax = min((uint32_t)kTileK, d - k0);
+            const uint32_t kmax = min((uint32_t)kNcTileK, d - k0);
             for (uint32_t kk = 0; kk < kmax; ++kk) {
                 float av[4], bv[4];
 #pragma unroll
@@ -415,7 +417,7 @@ __global__ __launch_bounds__(256) void k_nearest_center(const float* __restrict_
         red_i[tx][ty + 16 * i] = bidx[i];
     }
     __syncthreads();
-    if (threadIdx.x < kTile) {
+    if (threadIdx.x < kNcTile) {
         const int r = threadIdx.x;
         // Per-thread results are either a strict improvement on FLT_MAX or
         // (FLT_MAX, 0) for "none"; merge to the smallest value, lowest id.
@@ -542,7 +544,7 @@ cudaError_t launch_nearest_center(uint32_t dim, const float* cents, uint64_t k, 
     }
     k_norms_full<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(x, n, dim, xnorm);
     k_norms_full<<<(unsigned)((k + 255) / 256), 256, 0, stream>>>(cents, k, dim, cnorm);
-    k_nearest_center<<<(unsigned)((n + kTile - 1) / kTile), 256, 0, stream>>>(x, n, cents, k, dim,
+    k_nearest_center<<<(unsigned)((n + kNcTile - 1) / kNcTile), 256, 0, stream>>>(x, n, cents, k, dim,
                                                                              xnorm, cnorm, assign,
                                                                              dis);
     e = cudaGetLastError();
@@ -556,7 +558,7 @@ cudaError_t launch_nearest_center_scratch(uint32_t dim, const float* cents, uint
                                           float* xnorm, float* cnorm, cudaStream_t stream) {
     k_norms_full<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(x, n, dim, xnorm);
     k_norms_full<<<(unsigned)((k + 255) / 256), 256, 0, stream>>>(cents, k, dim, cnorm);
-    k_nearest_center<<<(unsigned)((n + kTile - 1) / kTile), 256, 0, stream>>>(x, n, cents, k, dim,
+    k_nearest_center<<<(unsigned)((n + kNcTile - 1) / kNcTile), 256, 0, stream>>>(x, n, cents, k, dim,
                                                                              xnorm, cnorm, assign,
                                                                              dis);
     return cudaGetLastError();
