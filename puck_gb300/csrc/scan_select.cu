@@ -385,6 +385,103 @@ __device__ uint64_t block_cut_bound(const uint64_t* keys, uint32_t count, uint32
     return edge > 0xFFFFFFFFull ? kKeyMax : (edge << 32);
 }
 
+// The K-th smallest (1-based) of keys[0..count), all distinct, K <= count: one
+// histogram pass of kHistBins linear bins over the keys' float parts (as
+// block_cut_bound) finds the bin holding the K-th; the keys of that bin (at most
+// kHistBins / 2 of them: `hist` then holds them as 64-bit keys) are ranked by
+// counting, and the one of rank K - (keys below the bin) is the result. A bin
+// holding more keys, or all float parts equal, goes to block_select_kth. `red` has
+// 2 * (NT / 32) + 2 slots, `cnt` is a shared counter. All threads call it.
+template <int NT>
+__device__ uint64_t block_kth_hist(const uint64_t* keys, uint32_t count, uint32_t K, uint32_t* hist,
+                                   uint32_t* red, uint32_t* cnt, uint32_t* hist256, uint64_t* sel) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kW = NT / 32;
+    uint32_t lo = 0xFFFFFFFFu, hi = 0;
+    for (uint32_t i = tid; i < count; i += NT) {
+        const uint32_t h = (uint32_t)(keys[i] >> 32);
+        lo = h < lo ? h : lo;
+        hi = h > hi ? h : hi;
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0) {
+        red[warp] = lo;
+        red[kW + warp] = hi;
+    }
+    for (uint32_t b = tid; b < kHistBins; b += NT) hist[b] = 0;
+    if (tid == 0) *cnt = 0;
+    __syncthreads();
+    lo = red[0];
+    hi = red[kW];
+#pragma unroll
+    for (int w = 1; w < kW; ++w) {
+        lo = red[w] < lo ? red[w] : lo;
+        hi = red[kW + w] > hi ? red[kW + w] : hi;
+    }
+    if (lo == hi) {
+        __syncthreads();
+        return block_select_kth<NT>(keys, count, K, hist256, sel);
+    }
+    int shift = 0;
+    while (((hi - lo) >> shift) >= kHistBins) ++shift;
+    for (uint32_t i = tid; i < count; i += NT)
+        atomicAdd(&hist[((uint32_t)(keys[i] >> 32) - lo) >> shift], 1u);
+    __syncthreads();
+    constexpr uint32_t per = kHistBins / NT;
+    uint32_t c[per], run = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < per; ++j) {
+        c[j] = hist[tid * per + j];
+        run += c[j];
+    }
+    uint32_t incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) red[warp] = incl;
+    __syncthreads();
+    uint32_t below = incl - run;
+    for (int w = 0; w < warp; ++w) below += red[w];
+    if (below < K && K <= below + run) {
+#pragma unroll
+        for (uint32_t j = 0; j < per; ++j) {
+            if (below < K && K <= below + c[j]) {
+                red[2 * kW] = tid * per + j;  // the bin
+                red[2 * kW + 1] = below;      // keys below it
+                sel[0] = c[j];                // keys in it
+            }
+            below += c[j];
+        }
+    }
+    __syncthreads();
+    const uint32_t bin = red[2 * kW], nbelow = red[2 * kW + 1], m = (uint32_t)sel[0];
+    if (m > kHistBins / 2) {
+        __syncthreads();
+        return block_select_kth<NT>(keys, count, K, hist256, sel);
+    }
+    // the bin's keys into hist (as 64-bit keys), then the one of rank K - nbelow
+    uint64_t* bk = reinterpret_cast<uint64_t*>(hist);
+    for (uint32_t i = tid; i < count; i += NT) {
+        const uint64_t k = keys[i];
+        if ((((uint32_t)(k >> 32) - lo) >> shift) == bin) bk[atomicAdd(cnt, 1u)] = k;
+    }
+    __syncthreads();
+    const uint32_t want = K - nbelow - 1;  // 0-based rank in the bin
+    for (uint32_t i = tid; i < m; i += NT) {
+        const uint64_t k = bk[i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < m; ++j) rank += bk[j] < k ? 1u : 0u;
+        if (rank == want) sel[1] = k;
+    }
+    __syncthreads();
+    const uint64_t r = sel[1];
+    __syncthreads();
+    return r;
+}
+
 // Keeps the keys < bound at the front (in arbitrary order); returns their count.
 // `cnt` is a shared counter. All threads call it.
 template <int NT>
@@ -536,7 +633,8 @@ __device__ __forceinline__ void scan_after_round(ScanState& st, uint64_t* keys, 
 // unordered (only the rerank's tie path needs their (t, id) order, and it sorts
 // them itself), and the diagnostic counters.
 template <int NT>
-__device__ void scan_finish(const ScanParams& p, ScanState& st, uint64_t* keys, uint32_t qi,
+__device__ void scan_finish(const ScanParams& p, ScanState& st, uint64_t* keys, uint32_t* hist,
+                            uint32_t qi,
                             unsigned long long my_eval, unsigned long long my_look,
                             unsigned long long my_pass, long long t_start, long long t_pro) {
     const int tid = threadIdx.x;
@@ -545,7 +643,8 @@ __device__ void scan_finish(const ScanParams& p, ScanState& st, uint64_t* keys, 
     const long long t_final = clock64();
     uint32_t count = st.count;
     if (count > T) {
-        const uint64_t kth = block_select_kth<NT>(keys, count, T, st.hist, st.sel);
+        const uint64_t kth =
+            block_kth_hist<NT>(keys, count, T, hist, st.red, &st.ccount, st.hist, st.sel);
         block_compact_lt<NT>(keys, count, kth + 1, &st.ccount);
         count = T;
     }
@@ -694,7 +793,7 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
             scan_after_round<kThreads>(st, keys, hist, cap, kRound, T, tau, t_round);
         }
     }
-    scan_finish<kThreads>(p, st, keys, qi, my_eval, my_look, my_pass, t_start, t_pro);
+    scan_finish<kThreads>(p, st, keys, hist, qi, my_eval, my_look, my_pass, t_start, t_pro);
 }
 
 // ------------------------------------------------------------ interleaved kernel
@@ -822,6 +921,20 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
     }
     for (uint32_t i = tid; i < p.d; i += kIlThreads) qv[i] = p.q[(uint64_t)qi * p.d + i];
     const float* fdk = p.fd_by_fine + (uint64_t)qi * F;
+    // the first cluster's stationary row and this query's fine terms are loaded now,
+    // so their latency overlaps the table build (srow is written after it)
+    constexpr int kPre = 2;  // float4 per thread and row (F <= kPre * 4 * kIlThreads)
+    const uint32_t c_first = p.ctag[(uint64_t)qi * p.P];
+    const bool pre = c_first < p.C && (F & 3u) == 0 && F <= kPre * 4 * kIlThreads;
+    float4 pre_st[kPre], pre_fd[kPre];
+#pragma unroll
+    for (int u = 0; u < kPre; ++u) {
+        const uint32_t i = tid + u * kIlThreads;
+        if (pre && i < (F >> 2)) {
+            pre_st[u] = __ldg(reinterpret_cast<const float4*>(p.stationary + (uint64_t)c_first * F) + i);
+            pre_fd[u] = __ldg(reinterpret_cast<const float4*>(fdk) + i);
+        }
+    }
     const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
     const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
     __syncthreads();
@@ -918,6 +1031,25 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
         const uint32_t r0 = st.r0, r1 = st.r1, i0 = st.i0, ni = st.i1 - st.i0;
         if (r1 - r0 + ni == 0) continue;
         if (tid == 0) st.n_records += r1 - r0 + ni;
+        if (l == 0 && pre) {
+            // srow from the rows loaded before the table build
+            const float cdl = st.cdl;
+            float4* s4 = reinterpret_cast<float4*>(srow);
+#pragma unroll
+            for (int u = 0; u < kPre; ++u) {
+                const uint32_t i = tid + u * kIlThreads;
+                if (i < (F >> 2)) {
+                    const float4 a = pre_st[u], b = pre_fd[u];
+                    s4[i] = make_float4(2.0f * __fadd_rn(__fadd_rn(cdl, a.x), b.x),
+                                        2.0f * __fadd_rn(__fadd_rn(cdl, a.y), b.y),
+                                        2.0f * __fadd_rn(__fadd_rn(cdl, a.z), b.z),
+                                        2.0f * __fadd_rn(__fadd_rn(cdl, a.w), b.w));
+                }
+            }
+            __syncthreads();
+        } else {
+            scan_fill_srow(p, srow, fdk, st.c, st.cdl);
+        }
         uint32_t b0 = 0, nblk = 0, rounds = 0;
         if (r1 > r0) {
             b0 = r0 >> 5;
@@ -935,7 +1067,6 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
         }
         sent = rounds < (uint32_t)kIlStages ? rounds : (uint32_t)kIlStages;
         g_issued = g_done + sent;  // every thread tracks the count thread 0 issued
-        scan_fill_srow(p, srow, fdk, st.c, st.cdl);
         const uint32_t blk = tid >> 5, lane = tid & 31;
         for (uint32_t k = 0; k < rounds; ++k) {
             const long long t_round = clock64();
@@ -1025,7 +1156,7 @@ __global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
         }
         return;
     }
-    scan_finish<kIlThreads>(p, st, keys, qi, my_eval, my_eval, my_pass, t_start, t_pro);
+    scan_finish<kIlThreads>(p, st, keys, hist, qi, my_eval, my_eval, my_pass, t_start, t_pro);
 }
 
 // Launch order of the scan's blocks. A block's time follows the records of the
