@@ -797,28 +797,34 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
 }
 
 // ------------------------------------------------------------ interleaved kernel
-// One 512-thread block per query (one block per SM by shared memory). A round is
-// 32 interleaved record blocks, 1024 records: thread t takes lane t & 31 of blocks
-// t >> 5 and (t >> 5) + 16, and scores the two records together. Rounds arrive in a
-// ring of kIlStages shared-memory slots by one bulk copy each (cp.async.bulk,
-// completion on the slot's mbarrier), issued by thread 0 up to kIlStages rounds
-// ahead; the first copies go out before the table is built.
-#ifndef PGPU_SCAN_IL_STAGES
-#define PGPU_SCAN_IL_STAGES 3
-#endif
-constexpr int kIlThreads = 512;
-constexpr int kIlStages = PGPU_SCAN_IL_STAGES;
+// One block per query. A round is 2 * NT / 32 interleaved record blocks, 2 * NT
+// records: thread t takes lane t & 31 of blocks t >> 5 and (t >> 5) + NT / 32, and
+// scores the two records together. Rounds arrive in a ring of shared-memory slots
+// by one bulk copy each (cp.async.bulk, completion on the slot's mbarrier), issued
+// by thread 0 up to a ring's length ahead; the first copies go out before the
+// table is built.
+//   FP32 table (64 KB): 512 threads, 3 slots, one block per SM.
+//   FP16 table (32 KB): 256 threads, 2 slots, two blocks per SM, so one block's
+//   table build, cuts and final select overlap the other's rounds.
 constexpr int kIlRec = 2;  // records per thread and round
-constexpr uint32_t kIlBlocksPerRound = kIlThreads / 32 * kIlRec;
-constexpr int kIlRound = kIlThreads * kIlRec;  // records per round
+template <bool HALF>
+struct IlShape {
+    static constexpr int kThreads = HALF ? 256 : 512;
+    static constexpr int kStages = HALF ? 2 : 3;
+    static constexpr int kMinBlocks = HALF ? 2 : 1;
+    static constexpr uint32_t kBlocksPerRound = kThreads / 32 * kIlRec;
+    static constexpr int kRound = kThreads * kIlRec;  // records per round
+    static_assert(kMaxCap % kThreads == 0 && kHistBins % kThreads == 0, "helper shapes");
+};
 constexpr uint32_t kIlWaitLimit = 1u << 22;
-static_assert(kMaxCap % kIlThreads == 0 && kHistBins % kIlThreads == 0, "512-thread helpers");
 
 // Buffer size of the interleaved kernel for filter_topk T (see scan_cap).
+template <bool HALF>
 __host__ __device__ inline uint32_t il_cap(uint32_t T) {
+    constexpr uint32_t NT = IlShape<HALF>::kThreads;
     uint32_t room = T > 1024 ? T : 1024;
-    uint32_t c = T + kIlRound + room;
-    c = (c + kIlThreads - 1) / kIlThreads * kIlThreads;
+    uint32_t c = T + IlShape<HALF>::kRound + room;
+    c = (c + NT - 1) / NT * NT;
     return c > kMaxCap ? kMaxCap : c;
 }
 __host__ __device__ constexpr uint32_t il_table_bytes(bool half) {
@@ -829,8 +835,9 @@ __host__ __device__ constexpr uint32_t il_table_bytes(bool half) {
 // cut histogram.
 __host__ __device__ inline uint32_t il_query_bytes(uint32_t d) { return (d * 4u + 15u) & ~15u; }
 __host__ __device__ inline uint32_t il_srow_bytes(uint32_t F) { return (F * 4u + 7u) & ~7u; }
+template <bool HALF>
 __host__ __device__ inline uint32_t il_slot_bytes(uint32_t nsq) {
-    return kIlBlocksPerRound * il_block_bytes(nsq);
+    return IlShape<HALF>::kBlocksPerRound * il_block_bytes(nsq);
 }
 
 __device__ __forceinline__ bool il_wait(uint32_t bar, uint32_t parity) {
@@ -848,7 +855,12 @@ __device__ __forceinline__ bool il_wait(uint32_t bar, uint32_t parity) {
 }
 
 template <int NSQ, bool HALF>
-__global__ __launch_bounds__(kIlThreads, 1) void k_scan_il(ScanParams p) {
+__global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks) void k_scan_il(
+    ScanParams p) {
+    constexpr int kIlThreads = IlShape<HALF>::kThreads;
+    constexpr int kIlStages = IlShape<HALF>::kStages;
+    constexpr uint32_t kIlBlocksPerRound = IlShape<HALF>::kBlocksPerRound;
+    constexpr int kIlRound = IlShape<HALF>::kRound;
     static_assert(NSQ % 4 == 0 && NSQ <= 32, "interleaved layout: nsq a multiple of 4, <= 32");
     constexpr int NG = (NSQ + 7) / 8;  // 8-byte code granules per record
     constexpr uint32_t kG = NG * 8;
@@ -1220,9 +1232,12 @@ __global__ __launch_bounds__(kOrderThreads) void k_scan_order(const uint8_t* __r
 // Shared memory of the interleaved kernel (il_applies(nsq)) for filter_topk T.
 static size_t il_smem_bytes(const DeviceIndex& ix, uint32_t T, bool half) {
     const size_t stage = sizeof(float) * ix.nsq * 257;
-    const size_t work = il_srow_bytes(ix.F) + sizeof(uint64_t) * il_cap(T) +
+    const size_t work = il_srow_bytes(ix.F) +
+                        sizeof(uint64_t) * (half ? il_cap<true>(T) : il_cap<false>(T)) +
                         sizeof(uint32_t) * kHistBins;
-    return il_table_bytes(half) + il_query_bytes(ix.d) + (size_t)kIlStages * il_slot_bytes(ix.nsq) +
+    const size_t ring = half ? (size_t)IlShape<true>::kStages * il_slot_bytes<true>(ix.nsq)
+                             : (size_t)IlShape<false>::kStages * il_slot_bytes<false>(ix.nsq);
+    return il_table_bytes(half) + il_query_bytes(ix.d) + ring +
            (stage > work ? stage : work);
 }
 
@@ -1293,10 +1308,13 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     };
     if (il_applies(ix.nsq)) {
         if (ix.codes_il == nullptr) return cudaErrorInvalidValue;
-        p.cap = il_cap(s.T);
+        p.cap = half_lut ? il_cap<true>(s.T) : il_cap<false>(s.T);
         switch (ix.nsq) {
 #define PGPU_IL(N) \
-    case N: launch(half_lut ? k_scan_il<N, true> : k_scan_il<N, false>, kIlThreads); break;
+    case N:                                                                                \
+        if (half_lut) launch(k_scan_il<N, true>, IlShape<true>::kThreads);                   \
+        else launch(k_scan_il<N, false>, IlShape<false>::kThreads);                          \
+        break;
             PGPU_IL(4) PGPU_IL(8) PGPU_IL(12) PGPU_IL(16) PGPU_IL(20) PGPU_IL(24) PGPU_IL(28)
             PGPU_IL(32)
 #undef PGPU_IL
