@@ -952,10 +952,11 @@ __global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks)
     __syncthreads();
     // get_dist_table (quantization.cpp:260-270) in the reference's lane order,
     // stage[m * 257 + j] (row pitch 257: the expansion below reads it without bank
-    // conflicts); two threads per codeword, each half of the subspaces
-    {
+    // conflicts); each codeword's subspaces in two halves, a thread per half
+    // (512 threads) or both halves by one thread (256 threads)
+    for (uint32_t h2 = tid >> 8; h2 < 2; h2 += kIlThreads / 256) {
         const uint32_t j = tid & 255u;
-        const int mh = (tid >> 8) * (NSQ / 2);
+        const int mh = (int)h2 * (NSQ / 2);
         if (p.lsq == 4) {
             const float4* cb4 = reinterpret_cast<const float4*>(p.codebook);
 #pragma unroll
