@@ -1084,6 +1084,15 @@ __global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks)
         for (uint32_t k = 0; k < rounds; ++k) {
             const long long t_round = clock64();
             const uint64_t tau = st.tau;
+            // tau as (float, id): key(t, id) < tau iff t < tau_f, or t == tau_f and
+            // id < tau_id (float compares treat -0 as +0, as the keys do; a bound
+            // whose float part is the key of -0 keeps exactly the t < 0)
+            float tau_f = tau == kKeyMax ? __int_as_float(0x7f800000) : key_value(tau);
+            uint32_t tau_id = tau == kKeyMax ? 0xFFFFFFFFu : (uint32_t)tau;
+            if ((uint32_t)(tau >> 32) == 0x7FFFFFFFu) {
+                tau_f = 0.0f;
+                tau_id = 0;
+            }
             const uint32_t g = g_done;
             if (!il_wait(bar_of(g), (g / kIlStages) & 1u)) {
                 if (lane == 0) atomicExch(&il_failed, 1);
@@ -1110,10 +1119,11 @@ __global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks)
             score_records(gr, off, fine, rr, t);
 #pragma unroll
             for (int j = 0; j < kIlRec; ++j) {
-                const uint64_t key = filter_key(t[j], rr[j]);
-                const bool keep = valid[j] && key < tau;
+                // key(t, id) < tau by float compares; the key only for kept records
+                const bool keep =
+                    valid[j] && (t[j] < tau_f || (t[j] == tau_f && rr[j] < tau_id));
                 my_eval += valid[j] ? 1 : 0;
-                scan_insert(st, keys, keep, key, my_pass);
+                scan_insert(st, keys, keep, keep ? filter_key(t[j], rr[j]) : 0ull, my_pass);
             }
             scan_after_round<kIlThreads>(st, keys, hist, cap, kIlRound, T, tau, t_round);
             if (il_failed) break;  // read after the barrier: the same on every thread
