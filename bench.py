@@ -702,6 +702,8 @@ def run_gpu(args, w, rank, ws):
             torch.distributed.barrier()
         torch.cuda.synchronize()
         with ClockSampler(dev.index) as clk:
+            # the timed region is an NVTX range ("timed") for launch-list captures
+            torch.cuda.nvtx.range_push("timed")
             start = torch.cuda.Event(enable_timing=True)
             end = torch.cuda.Event(enable_timing=True)
             start.record(stream)
@@ -711,6 +713,7 @@ def run_gpu(args, w, rank, ws):
                 evs[i][1].record(stream)
             end.record(stream)
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
         total = start.elapsed_time(end)
         per_step = np.array([a.elapsed_time(b) for a, b in evs])
         total = max_over_ranks(total, ws, dev)
