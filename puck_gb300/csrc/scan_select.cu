@@ -806,11 +806,20 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
 //   FP32 table (64 KB): 512 threads, 3 slots, one block per SM.
 //   FP16 table (32 KB): 256 threads, 2 slots, two blocks per SM, so one block's
 //   table build, cuts and final select overlap the other's rounds.
-constexpr int kIlRec = 2;  // records per thread and round
+#ifndef PGPU_SCAN_IL_REC
+#define PGPU_SCAN_IL_REC 2
+#endif
+#ifndef PGPU_SCAN_IL_STAGES32
+#define PGPU_SCAN_IL_STAGES32 3
+#endif
+#ifndef PGPU_SCAN_IL_STAGES16
+#define PGPU_SCAN_IL_STAGES16 2
+#endif
+constexpr int kIlRec = PGPU_SCAN_IL_REC;  // records per thread and round
 template <bool HALF>
 struct IlShape {
     static constexpr int kThreads = HALF ? 256 : 512;
-    static constexpr int kStages = HALF ? 2 : 3;
+    static constexpr int kStages = HALF ? PGPU_SCAN_IL_STAGES16 : PGPU_SCAN_IL_STAGES32;
     static constexpr int kMinBlocks = HALF ? 2 : 1;
     static constexpr uint32_t kBlocksPerRound = kThreads / 32 * kIlRec;
     static constexpr int kRound = kThreads * kIlRec;  // records per round
@@ -840,15 +849,28 @@ __host__ __device__ inline uint32_t il_slot_bytes(uint32_t nsq) {
     return IlShape<HALF>::kBlocksPerRound * il_block_bytes(nsq);
 }
 
+// Bounded wait on a slot's mbarrier phase. A try_wait may suspend the thread for up
+// to PGPU_SCAN_WAIT_HINT ns (0: no hint) while the copy is outstanding.
+#ifndef PGPU_SCAN_WAIT_HINT
+#define PGPU_SCAN_WAIT_HINT 0
+#endif
 __device__ __forceinline__ bool il_wait(uint32_t bar, uint32_t parity) {
     for (uint32_t it = 0; it < kIlWaitLimit; ++it) {
         uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            "selp.b32 %0, 1, 0, p;\n}"
-            : "=r"(ok)
-            : "r"(bar), "r"(parity)
-            : "memory");
+        if (PGPU_SCAN_WAIT_HINT > 0)
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+                "selp.b32 %0, 1, 0, p;\n}"
+                : "=r"(ok)
+                : "r"(bar), "r"(parity), "n"(PGPU_SCAN_WAIT_HINT)
+                : "memory");
+        else
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                "selp.b32 %0, 1, 0, p;\n}"
+                : "=r"(ok)
+                : "r"(bar), "r"(parity)
+                : "memory");
         if (ok) return true;
     }
     return false;
