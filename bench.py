@@ -94,6 +94,14 @@ WORKLOADS = {
                         train_sample=400_000, iters=8, pq_sample=131_072,
                         probe_train=50_000, probe_mass=(0.9,), probe_max=8, probe_fallback=200,
                         probe_epochs=4, top100=False, cpu_sweep=(1,)),
+    # smaller profiling case with the same per-query scan (25k records per coarse cluster,
+    # 4000 fine clusters, filter_topk 1100): 5M points, interleaved records (150 MB) larger
+    # than L2, ~3 GB on the device
+    "scan25k_5m": dict(n=5_000_000, d=96, ncomp=819, kind="unit", C=200, F=4000, nsq=24,
+                       T=1100, k=10, exact_sweep=(1,), scan_sweep=(1,), nq=10000, norm=True,
+                       train_sample=400_000, iters=8, pq_sample=131_072,
+                       probe_train=50_000, probe_mass=(0.9,), probe_max=8, probe_fallback=200,
+                       probe_epochs=4, top100=False, cpu_sweep=(1,)),
     # profiling case for ncu: codes + offsets (150 MB) larger than L2, ~5 GB on the device
     "cosine_5m": dict(n=5_000_000, d=96, ncomp=4096, kind="unit", C=1414, F=1414, nsq=24,
                       T=500, k=10, exact_sweep=(50,), scan_sweep=(1,), nq=10000, norm=True,
@@ -763,9 +771,12 @@ def run_gpu(args, w, rank, ws):
         else:
             clusters = entry["mean_clusters"] * nq
             # every record of the probed clusters (offset + codes + fine id), the probed
-            # clusters' stationary rows, the query's fine terms and the query
+            # clusters' stationary rows, the query's fine terms and the query; the split
+            # scan's kernel also writes each record's distance (4 B, not counted here:
+            # an intermediate of this design, reported as t_write_bytes)
             byts = recs * (R + 2) + clusters * w["F"] * 4 + nq * w["F"] * 4 + nq * w["d"] * 4
-            kern = "k_scan_select"
+            kern = "k_scan_score"
+        # stage 5: the walk, or the scan's record kernel alone
         ms = stage_ms["walk_scan"]
         peak, peak_kind = measured_peaks()
         ach = byts / (ms / 1e3) / 1e9
@@ -782,7 +793,8 @@ def run_gpu(args, w, rank, ws):
         return {"bound": "hbm", "kernel": kern, "achieved": round(ach, 2), "peak": peak,
                 "unit": "GB/s", "frac": round(ach / peak, 5), "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(byts),
-                "kernel_ms": round(ms, 4), "records": int(recs)}
+                "kernel_ms": round(ms, 4), "records": int(recs),
+                "t_write_bytes": int(recs * 4) if entry["mode"] == "scan" else 0}
 
     roof = roofline(best, stage, stats, walk_counters)
     plain_roof = roofline(plain_best, plain_stage, plain_stats, plain_counters)

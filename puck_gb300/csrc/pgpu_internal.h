@@ -137,6 +137,13 @@ __host__ __device__ inline uint64_t il_fine_offset(uint64_t r, uint32_t nsq) {
 cudaError_t launch_interleave_codes(const DeviceIndex& ix, uint64_t r0, uint64_t rows,
                                     cudaStream_t stream);
 
+// Split scan: per query, the histogram cut of its records' distances (k_scan_score).
+struct SplitCut {
+    float lo, scale;  // bin(t) = clamp(trunc((t - lo) * scale), 0, 4095)
+    uint32_t bin;     // the highest bin kept: at least filter_topk records lie at or below it
+    uint32_t n;       // records written to tbuf
+};
+
 struct Scratch {
     uint32_t cap = 0;
     float* q = nullptr;        // [B][d] normalised queries
@@ -161,6 +168,14 @@ struct Scratch {
     uint32_t* ulist = nullptr;  // with a probe: [B] queries left to the fixed-count selection
     uint32_t* ucount = nullptr; // their number (device)
     uint8_t* wbucket = nullptr; // scan mode: [B] work bucket of each query
+    // split scan (interleaved layout): every scanned record's distance, per query at
+    // qoff; qflag 1 where the split scan answers the query
+    float* tbuf = nullptr;      // [tcap]
+    uint64_t tcap = 0;
+    uint32_t* qcnt = nullptr;   // [B] records of each query
+    uint32_t* qoff = nullptr;   // [B]
+    uint32_t* qflag = nullptr;  // [B]
+    SplitCut* cut = nullptr;    // [B]
     uint32_t Pfix = 0;         // fixed coarse count (<= P when a probe widens the slots)
     uint32_t P = 0, T = 0;
     uint64_t bytes = 0;
@@ -257,9 +272,22 @@ size_t scan_smem_bytes(const DeviceIndex& ix, uint32_t T);
 uint32_t scan_max_filter_topk();
 // Scan mode: the blocks' launch order (longest scans first), then the scan itself.
 cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cudaStream_t stream);
-cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+// The scan (scan mode), in three parts timed as stages 4-6: launch_scan_prepare
+// (the split scan's record counts and buffer offsets; nothing otherwise),
+// launch_scan_records (k_scan_score, or the fused kernel when the split scan does
+// not apply), launch_scan_finish (k_scan_pick, then the fused kernel for the queries
+// the split scan left).
+cudaError_t launch_scan_prepare(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                                cudaStream_t stream);
+cudaError_t launch_scan_records(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                                cudaStream_t stream);
+cudaError_t launch_scan_finish(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                cudaStream_t stream);
 size_t scan_smem_bytes_half(const DeviceIndex& ix, uint32_t T);
+// The split scan runs (k_split_counts, k_split_offsets, k_scan_score, k_scan_pick
+// before the fused kernel) when the index has the interleaved layout and the scratch
+// its distance buffer.
+bool scan_split_applies(const DeviceIndex& ix, const Scratch& s);
 // BF16 copy of the vectors and their norms (precision form), synchronous.
 int ensure_bf16_features(DeviceIndex* ix, std::string* err);
 // The precision form's rotated copy of the filter codes (nsq a multiple of 4, at

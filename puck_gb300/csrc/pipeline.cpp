@@ -35,10 +35,23 @@ void ensure_max_dynamic_smem(const void* kernel, int bytes) {
 void free_scratch(Scratch* s) {
     void* ptrs[] = {s->q, s->qb, s->qnorm, s->status, s->dots, s->cdist, s->ctag, s->fdist,
                     s->ftag, s->hdist, s->htag, s->hcnt, s->counters, s->tc_err,
-                    s->ph1, s->ph2, s->pconf, s->pz, s->order, s->wbucket, s->ulist, s->ucount};
+                    s->ph1, s->ph2, s->pconf, s->pz, s->order, s->wbucket, s->ulist, s->ucount,
+                    s->tbuf, s->qcnt, s->qoff, s->qflag, s->cut};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     *s = Scratch();
+}
+
+// Split scan buffer: room for 40960 record distances per query of the batch (about
+// 1.6 times the mean record count of a coarse cluster at 100M points and 4000
+// clusters), at least 2^20 and at most 2^30. A query whose records do not fit runs
+// the fused scan kernel instead.
+uint64_t split_capacity(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
+    if (cfg.mode != PGPU_MODE_SCAN || !il_applies(ix.nsq)) return 0;
+    uint64_t c = (uint64_t)B * 40960ull;
+    if (c < (1ull << 20)) c = 1ull << 20;
+    if (c > (1ull << 30)) c = 1ull << 30;
+    return c;
 }
 
 uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
@@ -46,8 +59,10 @@ uint64_t scratch_bytes(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t 
     const uint64_t probe = cfg.probe ? (uint64_t)B * (cfg.probe->h * 4 + 8 + ix.C * 4ull) + 4 : 0;
     const uint64_t fine_order = cfg.mode == PGPU_MODE_EXACT ? (uint64_t)B * ix.F * 8 : 8;
     const uint64_t tables = cfg.mode == PGPU_MODE_SCAN ? (uint64_t)B * 5 : 0;  // launch order
+    const uint64_t tcap = split_capacity(ix, cfg, B);
+    const uint64_t split = tcap ? tcap * 4 + (uint64_t)B * (12 + sizeof(SplitCut)) : 0;
     return (uint64_t)B * (ix.d * 6 + 4 + 4 + std::max(ix.C, ix.F) * 4ull + P * 8 + T * 8 + 4) +
-           fine_order + tables + probe + kNumWalkCounters * 8 + 4;
+           fine_order + tables + split + probe + kNumWalkCounters * 8 + 4;
 }
 
 int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Scratch* out,
@@ -80,6 +95,15 @@ int alloc_scratch(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B, Sc
     if (cfg.mode == PGPU_MODE_SCAN) {
         PGPU_ALLOC(s.order, B);
         PGPU_ALLOC(s.wbucket, B);
+        const uint64_t tcap = split_capacity(ix, cfg, B);
+        if (tcap) {
+            PGPU_ALLOC(s.tbuf, tcap);
+            PGPU_ALLOC(s.qcnt, B);
+            PGPU_ALLOC(s.qoff, B);
+            PGPU_ALLOC(s.qflag, B);
+            PGPU_ALLOC(s.cut, B);
+            s.tcap = tcap;
+        }
     }
     if (cfg.probe) {
         PGPU_ALLOC(s.ulist, B);
@@ -161,23 +185,28 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
         k = 7;
     } else {
         PGPU_STEP(launch_scan_order(ix, n, s, st), "scan order");
+        PGPU_STEP(launch_scan_prepare(ix, n, s, bf16, st), "scan prepare");
     }
     mark(5);
     if (cfg.mode == PGPU_MODE_EXACT) {
         PGPU_STEP(launch_walk_scan(ix, cfg, n, s, st), "walk_scan");
     } else {
-        PGPU_STEP(launch_scan_select(ix, n, s, bf16, st), "scan_select");
+        PGPU_STEP(launch_scan_records(ix, n, s, bf16, st), "scan records");
     }
     mark(6);
+    if (cfg.mode == PGPU_MODE_SCAN) PGPU_STEP(launch_scan_finish(ix, n, s, bf16, st), "scan finish");
+    mark(7);
     if (bf16 && ix.pq_nsq == 0) {
         PGPU_STEP(launch_rerank_screen(ix, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
     } else {  // the original vectors, or the second-level PQ
         PGPU_STEP(launch_rerank(ix, cfg, n, topk, s, d_dist, d_ids, d_status, st), "rerank");
     }
-    mark(7);
+    mark(8);
 #undef PGPU_STEP
-    // scan mode adds the two launch-order kernels
-    if (launched) *launched = k + probe_kernels + (cfg.mode == PGPU_MODE_SCAN ? 2 : 0);
+    // scan mode adds the two launch-order kernels, and the split scan four more
+    if (launched)
+        *launched = k + probe_kernels +
+                    (cfg.mode == PGPU_MODE_SCAN ? 2 + (scan_split_applies(ix, s) ? 4 : 0) : 0);
     return cudaSuccess;
 }
 

@@ -113,6 +113,7 @@ struct ScanParams {
     int* err;                   // set when a bulk copy's wait expired
     const uint32_t* ins_cl_start;  // realtime: [C+1] inserted records per cluster, or null
     const uint32_t* ins_cl_ids;    // their memory ids
+    const uint32_t* done;          // [B] 1: the split scan has answered the query, or null
     uint32_t d, C, F, nsq, lsq, code_stride, P, T, cap;
     float codebook_max;
 };
@@ -484,19 +485,19 @@ __device__ uint64_t block_kth_hist(const uint64_t* keys, uint32_t count, uint32_
 
 // Keeps the keys < bound at the front (in arbitrary order); returns their count.
 // `cnt` is a shared counter. All threads call it.
-template <int NT>
+template <int NT, int PER = (int)(kMaxCap / NT)>
 __device__ uint32_t block_compact_lt(uint64_t* keys, uint32_t count, uint64_t bound, uint32_t* cnt) {
     const int tid = threadIdx.x, lane = tid & 31;
-    uint64_t mine[(int)(kMaxCap / NT)];
+    uint64_t mine[PER];
 #pragma unroll
-    for (int j = 0; j < (int)(kMaxCap / NT); ++j) {
+    for (int j = 0; j < PER; ++j) {
         const uint32_t i = tid + j * NT;
         mine[j] = i < count ? keys[i] : ~0ull;
     }
     if (tid == 0) *cnt = 0;
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < (int)(kMaxCap / NT); ++j) {
+    for (int j = 0; j < PER; ++j) {
         const bool keep = mine[j] < bound;
         const unsigned b = __ballot_sync(0xffffffffu, keep);
         uint32_t base = 0;
@@ -719,6 +720,7 @@ __global__ __launch_bounds__(kThreads, PGPU_SCAN_MIN_BLOCKS) void k_scan_select(
     float* srow = HALF ? reinterpret_cast<float*>(luth + nsq * 256) : lut + nsq * 256;
     float* qv = srow + F;                  // [d]
 
+    if (p.done && p.done[qi]) return;  // answered by the split scan
     if (p.status[qi] != 0) {
         if (tid == 0) p.hcnt[qi] = 0;
         return;
@@ -876,6 +878,107 @@ __device__ __forceinline__ bool il_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// get_dist_table (quantization.cpp:260-270) of the query qv in the reference's lane
+// order, staged as stage[m * 257 + j] (row pitch 257: the expansion reads it without
+// bank conflicts), then expanded into the rotated table: column m' < NSQ + 31 of row
+// c holds subspace m' mod NSQ (FP32), or the same scaled by 2^lut_e in FP16. Each
+// codeword's subspaces go in two halves, a thread per half (NT = 512) or both halves
+// by one thread (NT = 256). All NT threads; one barrier inside (after the staging),
+// none after the expansion.
+template <int NSQ, bool HALF, int NT>
+__device__ __forceinline__ void il_build_table(unsigned char* tab, float* stage, const float* qv,
+                                               const float* __restrict__ codebook, uint32_t lsq,
+                                               int lut_e) {
+    static_assert(NT % 256 == 0, "a thread per codeword and half");
+    const int tid = threadIdx.x;
+    for (uint32_t h2 = tid >> 8; h2 < 2; h2 += NT / 256) {
+        const uint32_t j = tid & 255u;
+        const int mh = (int)h2 * (NSQ / 2);
+        if (lsq == 4) {
+            const float4* cb4 = reinterpret_cast<const float4*>(codebook);
+#pragma unroll
+            for (int m0 = 0; m0 < NSQ / 2; m0 += 2) {
+                float4 y[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) y[u] = __ldg(cb4 + (uint64_t)(mh + m0 + u) * 256 + j);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int m = mh + m0 + u;
+                    const float* x = qv + m * 4;
+                    const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
+                    const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
+                    stage[m * 257 + j] = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
+                                                   __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
+                }
+            }
+        } else {
+            for (int m = mh; m < mh + NSQ / 2; ++m)
+                stage[m * 257 + j] =
+                    l2sqr_sse(qv + m * lsq, codebook + ((uint64_t)m * 256 + j) * lsq, lsq);
+        }
+    }
+    __syncthreads();
+    if (HALF) {
+        const float scale = ldexpf(1.0f, lut_e);
+        uint32_t* tw = reinterpret_cast<uint32_t*>(tab);
+        for (uint32_t w = tid; w < 256 * 32; w += NT) {
+            const uint32_t c = w >> 5, m0 = (w & 31) * 2;
+            const float v0 = m0 < NSQ + 31 ? stage[(m0 % NSQ) * 257 + c] : 0.0f;
+            const float v1 = m0 + 1 < NSQ + 31 ? stage[((m0 + 1) % NSQ) * 257 + c] : 0.0f;
+            const __half2 h = __halves2half2(__float2half_rn(v0 * scale), __float2half_rn(v1 * scale));
+            tw[w] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+    } else {
+        float* tf = reinterpret_cast<float*>(tab);
+        for (uint32_t w = tid; w < 256 * 64; w += NT) {
+            const uint32_t c = w >> 6, m = w & 63;
+            tf[w] = m < NSQ + 31 ? stage[(m % NSQ) * 257 + c] : 0.0f;
+        }
+    }
+}
+
+// t of R records (memory ids mr, lanes mr & 31) from their codes (8-byte granules
+// of the rotated layout), offsets and fine ids, with srow[f] = 2 * cell_dist of the
+// record's cell; the R lookup chains are interleaved. Lookup step s goes to partial
+// s mod 4 in FP32; t = (srow[f] + offset) + ((a0 + a1) + (a2 + a3)) (the FP16 table's
+// sum scaled back by inv_scale).
+template <int NSQ, bool HALF, int R>
+__device__ __forceinline__ void il_score(const unsigned char* tab, const float* srow,
+                                         const uint2 (&gr)[R][(NSQ + 7) / 8], const float (&off)[R],
+                                         const uint32_t (&fine)[R], const uint32_t (&mr)[R],
+                                         float inv_scale, float (&t)[R]) {
+    float a[R][4];
+    uint32_t lb[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        lb[j] = (mr[j] & 31u) << 2;  // byte 0 of the table address
+        a[j][0] = a[j][1] = a[j][2] = a[j][3] = 0.0f;
+    }
+#pragma unroll
+    for (int s2 = 0; s2 < NSQ; ++s2) {
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const uint32_t w = (s2 & 4) ? gr[j][s2 >> 3].y : gr[j][s2 >> 3].x;
+            // (code << 8) | 4 * lane: the entry of column s2 + lane
+            const uint32_t addr = __byte_perm(w, lb[j], 0x5504u | ((uint32_t)(s2 & 3) << 4));
+            if (HALF) {
+                const unsigned short h =
+                    *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
+                asm("add.f32.f16 %0, %1, %0;" : "+f"(a[j][s2 & 3]) : "h"(h));
+            } else {
+                a[j][s2 & 3] =
+                    __fadd_rn(a[j][s2 & 3], *reinterpret_cast<const float*>(tab + addr + 4 * s2));
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const float t0 = __fadd_rn(srow[fine[j]], off[j]);  // (float)(2.0 * cell_dist + offset)
+        const float sum = __fadd_rn(__fadd_rn(a[j][0], a[j][1]), __fadd_rn(a[j][2], a[j][3]));
+        t[j] = HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
+    }
+}
+
 template <int NSQ, bool HALF>
 __global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks) void k_scan_il(
     ScanParams p) {
@@ -904,6 +1007,7 @@ __global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks)
     uint64_t* keys = reinterpret_cast<uint64_t*>(rest + il_srow_bytes(F));  // [cap]
     uint32_t* hist = reinterpret_cast<uint32_t*>(keys + cap);              // [kHistBins]
 
+    if (p.done && p.done[qi]) return;  // answered by the split scan
     if (p.status[qi] != 0) {
         if (tid == 0) p.hcnt[qi] = 0;
         return;
@@ -972,93 +1076,14 @@ __global__ __launch_bounds__(IlShape<HALF>::kThreads, IlShape<HALF>::kMinBlocks)
     const int lut_e = HALF ? half_lut_exponent(p.qnorm[qi], p.codebook_max) : 0;
     const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
     __syncthreads();
-    // get_dist_table (quantization.cpp:260-270) in the reference's lane order,
-    // stage[m * 257 + j] (row pitch 257: the expansion below reads it without bank
-    // conflicts); each codeword's subspaces in two halves, a thread per half
-    // (512 threads) or both halves by one thread (256 threads)
-    for (uint32_t h2 = tid >> 8; h2 < 2; h2 += kIlThreads / 256) {
-        const uint32_t j = tid & 255u;
-        const int mh = (int)h2 * (NSQ / 2);
-        if (p.lsq == 4) {
-            const float4* cb4 = reinterpret_cast<const float4*>(p.codebook);
-#pragma unroll
-            for (int m0 = 0; m0 < NSQ / 2; m0 += 2) {
-                float4 y[2];
-#pragma unroll
-                for (int u = 0; u < 2; ++u) y[u] = __ldg(cb4 + (uint64_t)(mh + m0 + u) * 256 + j);
-#pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const int m = mh + m0 + u;
-                    const float* x = qv + m * 4;
-                    const float t0 = __fsub_rn(x[0], y[u].x), t1 = __fsub_rn(x[1], y[u].y);
-                    const float t2 = __fsub_rn(x[2], y[u].z), t3 = __fsub_rn(x[3], y[u].w);
-                    stage[m * 257 + j] = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)),
-                                                   __fadd_rn(__fmul_rn(t2, t2), __fmul_rn(t3, t3)));
-                }
-            }
-        } else {
-            for (int m = mh; m < mh + NSQ / 2; ++m)
-                stage[m * 257 + j] = l2sqr_sse(qv + m * p.lsq,
-                                               p.codebook + ((uint64_t)m * 256 + j) * p.lsq, p.lsq);
-        }
-    }
-    __syncthreads();
-    // the rotated table: column m' < NSQ + 31 of row c holds subspace m' mod NSQ
-    if (HALF) {
-        const float scale = ldexpf(1.0f, lut_e);
-        uint32_t* tw = reinterpret_cast<uint32_t*>(tab);
-        for (uint32_t w = tid; w < 256 * 32; w += kIlThreads) {
-            const uint32_t c = w >> 5, m0 = (w & 31) * 2;
-            const float v0 = m0 < NSQ + 31 ? stage[(m0 % NSQ) * 257 + c] : 0.0f;
-            const float v1 = m0 + 1 < NSQ + 31 ? stage[((m0 + 1) % NSQ) * 257 + c] : 0.0f;
-            const __half2 h = __halves2half2(__float2half_rn(v0 * scale), __float2half_rn(v1 * scale));
-            tw[w] = *reinterpret_cast<const uint32_t*>(&h);
-        }
-    } else {
-        float* tf = reinterpret_cast<float*>(tab);
-        for (uint32_t w = tid; w < 256 * 64; w += kIlThreads) {
-            const uint32_t c = w >> 6, m = w & 63;
-            tf[w] = m < NSQ + 31 ? stage[(m % NSQ) * 257 + c] : 0.0f;
-        }
-    }
+    il_build_table<NSQ, HALF, kIlThreads>(tab, stage, qv, p.codebook, p.lsq, lut_e);
     unsigned long long my_eval = 0, my_pass = 0;
     const long long t_pro = clock64();
 
-    // t of R records from their codes (8-byte granules), offsets and fine ids; the
-    // R lookup chains are interleaved
     auto score_records = [&](const uint2 (&gr)[kIlRec][NG], const float (&off)[kIlRec],
                              const uint32_t (&fine)[kIlRec], const uint32_t (&mr)[kIlRec],
                              float (&t)[kIlRec]) {
-        float a[kIlRec][4];
-        uint32_t lb[kIlRec];
-#pragma unroll
-        for (int j = 0; j < kIlRec; ++j) {
-            lb[j] = (mr[j] & 31u) << 2;  // byte 0 of the table address
-            a[j][0] = a[j][1] = a[j][2] = a[j][3] = 0.0f;
-        }
-#pragma unroll
-        for (int s2 = 0; s2 < NSQ; ++s2) {
-#pragma unroll
-            for (int j = 0; j < kIlRec; ++j) {
-                const uint32_t w = (s2 & 4) ? gr[j][s2 >> 3].y : gr[j][s2 >> 3].x;
-                // (code << 8) | 4 * lane: the entry of column s2 + lane
-                const uint32_t addr = __byte_perm(w, lb[j], 0x5504u | ((uint32_t)(s2 & 3) << 4));
-                if (HALF) {
-                    const unsigned short h =
-                        *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
-                    asm("add.f32.f16 %0, %1, %0;" : "+f"(a[j][s2 & 3]) : "h"(h));
-                } else {
-                    a[j][s2 & 3] = __fadd_rn(a[j][s2 & 3],
-                                             *reinterpret_cast<const float*>(tab + addr + 4 * s2));
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < kIlRec; ++j) {
-            const float t0 = __fadd_rn(srow[fine[j]], off[j]);  // (float)(2.0 * cell_dist + offset)
-            const float sum = __fadd_rn(__fadd_rn(a[j][0], a[j][1]), __fadd_rn(a[j][2], a[j][3]));
-            t[j] = HALF ? t0 + sum * inv_scale : __fadd_rn(t0, sum);
-        }
+        il_score<NSQ, HALF, kIlRec>(tab, srow, gr, off, fine, mr, inv_scale, t);
     };
 
     for (uint32_t l = 0; l < p.P && !il_failed; ++l) {
@@ -1260,6 +1285,593 @@ __global__ __launch_bounds__(kOrderThreads) void k_scan_order(const uint8_t* __r
         order[atomicAdd(&hist[wbucket[q]], 1u)] = q;
 }
 
+// ------------------------------------------------------------ split scan
+// The interleaved layout's scan when the per-pass scratch holds the distance of every
+// record the batch scans (Scratch::tbuf); queries that do not fit, or whose cut bin
+// holds too many records, stay with k_scan_il. One block per query (k_scan_score):
+//   1. the table (il_build_table), then, per probed cluster, the cell terms;
+//   2. the histogram's range from one record per thread at evenly spaced positions of
+//      the first probed cluster;
+//   3. records, with no barrier: each warp streams its own record blocks straight
+//      from the interleaved copy (coalesced 8-byte loads, the next step's loads in
+//      flight while the current one is scored), writes each record's t (the same
+//      il_score arithmetic as k_scan_il) to tbuf, query q's records at qoff[q] cluster
+//      by cluster (base records, then inserted ones), and counts it in a
+//      kSplitBins-bin histogram linear in t;
+//   4. the cut: the bin where the running count reaches T; every record of a higher
+//      bin has T records strictly below it;
+//   5. the pick: the block reads its own distances back (mostly from L2), keeps those
+//      at or below the cut bin as (t, position) keys in the table's place, maps
+//      positions to memory ids and writes the exact T smallest (t, id), unordered:
+//      the same set as k_scan_il's.
+// Without k_scan_il's key buffer and its cut-backs, a block holds the table, the cell
+// terms and the histogram: two blocks per SM (FP32 table) or three (FP16), so one
+// block's table build and pick overlap the others' records.
+// record blocks per warp and step (FP32 table, FP16 table)
+#ifndef PGPU_SPLIT_RB32
+#define PGPU_SPLIT_RB32 4
+#endif
+#ifndef PGPU_SPLIT_RB16
+#define PGPU_SPLIT_RB16 2
+#endif
+constexpr int kSplitThreads = 256;
+constexpr int kSplitWarps = kSplitThreads / 32;
+constexpr uint32_t kSplitBins = 4096;
+constexpr uint32_t kSplitMaxSlots = 512;   // probed clusters a split query may have
+constexpr uint32_t kSplitNo = 0xFFFFFFFFu; // count of a query left to k_scan_il
+#ifndef PGPU_SPLIT_AHEAD
+#define PGPU_SPLIT_AHEAD 2
+#endif
+constexpr int kSplitAhead = PGPU_SPLIT_AHEAD;  // L2 prefetch distance in record steps (-1: none)
+// candidates the pick phase holds (in the table's place): 8192 (FP32), 4096 (FP16)
+__host__ __device__ constexpr uint32_t split_max_keys(bool half) { return il_table_bytes(half) / 8; }
+
+struct SplitParams {
+    const uint32_t* ctag;
+    const float* cdist;
+    const int32_t* status;
+    const uint32_t* cell_start;
+    const uint32_t* ins_cl_start;  // realtime: [C+1], or null
+    const uint32_t* ins_cl_ids;
+    const float* stationary;
+    const float* fd_by_fine;
+    const float* q;
+    const float* qnorm;
+    const float* codebook;
+    const uint8_t* codes_il;
+    const uint32_t* order;
+    uint32_t* qcnt;
+    uint32_t* qoff;
+    uint32_t* qflag;
+    SplitCut* cut;
+    float* tbuf;
+    float* hdist;
+    uint32_t* htag;
+    uint32_t* hcnt;
+    unsigned long long* counters;
+    uint64_t tcap;  // floats tbuf holds
+    uint32_t n, d, C, F, lsq, P, T;
+    float codebook_max;
+};
+
+// bin(t) = clamp(trunc((t - lo) * scale), 0, kSplitBins - 1): non-decreasing in t
+// (each step rounds monotonically; a NaN product, 0 * inf at t = lo, converts to 0).
+__device__ __forceinline__ uint32_t split_bin(float t, float lo, float scale) {
+    const int b = __float2int_rz(__fmul_rn(__fsub_rn(t, lo), scale));
+    return (uint32_t)min(max(b, 0), (int)kSplitBins - 1);
+}
+
+// One thread per query: records over its probed clusters (kSplitNo: not split).
+__global__ void k_split_counts(SplitParams sp) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= sp.n) return;
+    uint32_t w = kSplitNo;
+    if (sp.status[q] == 0) {
+        w = 0;
+        for (uint32_t l = 0; l < sp.P; ++l) {
+            const uint32_t c = sp.ctag[(uint64_t)q * sp.P + l];
+            if (c >= sp.C) break;  // the probed clusters fill a prefix of the slots
+            if (l >= kSplitMaxSlots) {
+                w = kSplitNo;
+                break;
+            }
+            w += sp.cell_start[(uint64_t)c * sp.F + sp.F] - sp.cell_start[(uint64_t)c * sp.F];
+            if (sp.ins_cl_start) w += sp.ins_cl_start[c + 1] - sp.ins_cl_start[c];
+        }
+    }
+    sp.qcnt[q] = w;
+}
+
+// One block: each query's place in tbuf (its records rounded up to 4 floats, so
+// every query starts 16-byte aligned), in query order; a query fits when its records
+// end within tcap, and only fitting queries are flagged for the split scan.
+__global__ __launch_bounds__(1024) void k_split_offsets(SplitParams sp) {
+    __shared__ unsigned long long wsum[32];
+    __shared__ unsigned long long base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (uint32_t q0 = 0; q0 < sp.n; q0 += 1024) {
+        const uint32_t q = q0 + threadIdx.x;
+        const uint32_t w = q < sp.n ? sp.qcnt[q] : kSplitNo;
+        const unsigned long long v = w == kSplitNo ? 0ull : ((unsigned long long)w + 3) & ~3ull;
+        const unsigned long long b0 = base;
+        unsigned long long x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long z = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            wsum[lane] = z;
+        }
+        __syncthreads();
+        const unsigned long long excl = b0 + (warp ? wsum[warp - 1] : 0ull) + x - v;
+        if (q < sp.n) {
+            const bool fits = w != kSplitNo && excl + v <= sp.tcap;
+            sp.qoff[q] = fits ? (uint32_t)excl : 0u;
+            sp.qflag[q] = fits ? 1u : 0u;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) base = b0 + wsum[31];
+        __syncthreads();
+    }
+}
+
+template <int NSQ, bool HALF>
+#ifndef PGPU_SPLIT_MINB16
+#define PGPU_SPLIT_MINB16 3
+#endif
+__global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k_scan_score(SplitParams sp) {
+    constexpr int NG = (NSQ + 7) / 8;  // 8-byte code granules per record
+    constexpr uint32_t kG = NG * 8;
+    constexpr uint32_t kBlk = 32 * kG + 192;  // il_block_bytes
+    constexpr int NW = kSplitWarps, RB = HALF ? PGPU_SPLIT_RB16 : PGPU_SPLIT_RB32;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint32_t s_c, s_r0, s_r1, s_i0, s_i1;
+    __shared__ float s_cdl;
+    __shared__ float s_lo[NW], s_hi[NW];
+    __shared__ uint32_t s_red[NW], s_bin;
+    // the pick phase's select scratch (block_kth_hist) and counters
+    __shared__ uint32_t k_red[2 * NW + 2], k_hist256[256], k_cnt, k_count, k_slots, k_out;
+    __shared__ uint64_t k_sel[4];
+    const uint32_t qi = sp.order[blockIdx.x];
+    if (!sp.qflag[qi]) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t F = sp.F, T = sp.T;
+    unsigned char* tab = smem;
+    float* qv = reinterpret_cast<float*>(smem + il_table_bytes(HALF));
+    unsigned char* rest = smem + il_table_bytes(HALF) + il_query_bytes(sp.d);
+    float* stage = reinterpret_cast<float*>(rest);  // [NSQ][257] while the table is built
+    float* srow = reinterpret_cast<float*>(rest);   // [F] afterwards
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rest + il_srow_bytes(F));  // [kSplitBins]
+    // the probed clusters' record positions: start, base records, first memory id,
+    // first inserted slot
+    uint32_t* sl_start = hist + kSplitBins;  // [kSplitMaxSlots + 1]
+    uint32_t* sl_nb = sl_start + kSplitMaxSlots + 1;
+    uint32_t* sl_r0 = sl_nb + kSplitMaxSlots;
+    uint32_t* sl_i0 = sl_r0 + kSplitMaxSlots;
+    for (uint32_t i = tid; i < sp.d; i += kSplitThreads) qv[i] = sp.q[(uint64_t)qi * sp.d + i];
+    const int lut_e = HALF ? half_lut_exponent(sp.qnorm[qi], sp.codebook_max) : 0;
+    const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
+    __syncthreads();
+    il_build_table<NSQ, HALF, kSplitThreads>(tab, stage, qv, sp.codebook, sp.lsq, lut_e);
+    __syncthreads();  // stage (under srow and hist) is read to the end of the expansion
+    for (uint32_t b = tid; b < kSplitBins; b += kSplitThreads) hist[b] = 0;
+    // slot table: records per probed cluster, then an exclusive scan (PS slots per thread)
+    const uint32_t maxl = sp.P < kSplitMaxSlots ? sp.P : kSplitMaxSlots;
+    if (tid == 0) {
+        k_count = 0;
+        k_out = 0;
+        k_slots = maxl;
+    }
+    __syncthreads();
+    for (uint32_t l = tid; l < maxl; l += kSplitThreads)
+        if (sp.ctag[(uint64_t)qi * sp.P + l] >= sp.C) atomicMin(&k_slots, l);
+    __syncthreads();
+    const uint32_t L = k_slots;
+    {
+        constexpr int PS = kSplitMaxSlots / kSplitThreads;
+        uint32_t len[PS], run = 0;
+#pragma unroll
+        for (int j = 0; j < PS; ++j) {
+            const uint32_t l = tid * PS + j;
+            len[j] = 0;
+            if (l < L) {
+                const uint32_t c = sp.ctag[(uint64_t)qi * sp.P + l];
+                const uint32_t r0 = sp.cell_start[(uint64_t)c * F], r1 = sp.cell_start[(uint64_t)c * F + F];
+                uint32_t i0 = 0, i1 = 0;
+                if (sp.ins_cl_start) {
+                    i0 = sp.ins_cl_start[c];
+                    i1 = sp.ins_cl_start[c + 1];
+                }
+                sl_nb[l] = r1 - r0;
+                sl_r0[l] = r0;
+                sl_i0[l] = i0;
+                len[j] = (r1 - r0) + (i1 - i0);
+            }
+            run += len[j];
+        }
+        uint32_t incl = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_red[warp] = incl;
+        __syncthreads();
+        uint32_t st0 = incl - run;
+        for (int w = 0; w < warp; ++w) st0 += s_red[w];
+#pragma unroll
+        for (int j = 0; j < PS; ++j) {
+            const uint32_t l = tid * PS + j;
+            if (l < L) sl_start[l] = st0;
+            st0 += len[j];
+        }
+        if (tid == kSplitThreads - 1) sl_start[L] = st0;  // the total
+    }
+    __syncthreads();
+    const uint32_t N = sl_start[L];  // records of all probed clusters
+    // slot of record position ps (the last slot starting at or before it)
+    auto slot_of = [&](uint32_t ps) {
+        uint32_t a = 0, b = L;
+        while (b - a > 1) {
+            const uint32_t mid = (a + b) >> 1;
+            if (sl_start[mid] <= ps) a = mid;
+            else b = mid;
+        }
+        return a;
+    };
+    float* out = sp.tbuf + sp.qoff[qi];
+    const float* fdk = sp.fd_by_fine + (uint64_t)qi * F;
+    uint32_t pos = 0;  // records written (the same on every thread)
+    float lo = 0.0f, scale = 0.0f;
+    // the histogram's range: the smallest and largest of one t per thread (ok: the
+    // thread has one). All threads; barrier inside.
+    auto set_range = [&](float t1, bool ok) {
+        float mn = ok ? t1 : __int_as_float(0x7f800000), mx = ok ? t1 : __int_as_float(0xff800000);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) {
+            s_lo[warp] = mn;
+            s_hi[warp] = mx;
+        }
+        __syncthreads();
+        mn = s_lo[0];
+        mx = s_hi[0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) {
+            mn = fminf(mn, s_lo[w]);
+            mx = fmaxf(mx, s_hi[w]);
+        }
+        if (mx > mn) {
+            lo = mn;
+            scale = __fdiv_rn((float)(kSplitBins - 1), __fsub_rn(mx, mn));
+        } else {
+            lo = mn > -3.0e38f && mn < 3.0e38f ? mn : 0.0f;
+            scale = 0.0f;
+        }
+    };
+    {
+        // the histogram's range: t of one record per thread at evenly spaced positions
+        // of all probed clusters (its cell term read from global memory; the range only
+        // has to be the same for every record, not exact)
+        const bool ok = N > 0;
+        const uint32_t ps = ok ? (uint32_t)(((uint64_t)tid * N) / kSplitThreads) : 0u;
+        const uint32_t a = ok ? slot_of(ps) : 0u;
+        const uint32_t local = ps - sl_start[a];
+        uint32_t m1[1];
+        m1[0] = !ok ? 0u : local < sl_nb[a] ? sl_r0[a] + local : sp.ins_cl_ids[sl_i0[a] + (local - sl_nb[a])];
+        uint2 g1[1][NG];
+        float o1[1], t1[1];
+        uint32_t f1[1] = {0u};
+#pragma unroll
+        for (int q2 = 0; q2 < NG; ++q2)
+            g1[0][q2] = __ldg(reinterpret_cast<const uint2*>(sp.codes_il + il_granule_offset(m1[0], q2, NSQ)));
+        o1[0] = __ldg(reinterpret_cast<const float*>(sp.codes_il + il_offset_offset(m1[0], NSQ)));
+        const uint32_t fi = __ldg(reinterpret_cast<const uint16_t*>(sp.codes_il + il_fine_offset(m1[0], NSQ)));
+        float cterm[1] = {0.0f};
+        if (ok) {
+            const uint32_t c = sp.ctag[(uint64_t)qi * sp.P + a];
+            const float cd = sp.cdist[(uint64_t)qi * sp.P + a];
+            cterm[0] = 2.0f * __fadd_rn(__fadd_rn(cd, __ldg(sp.stationary + (uint64_t)c * F + fi)), __ldg(fdk + fi));
+        }
+        il_score<NSQ, HALF, 1>(tab, cterm, g1, o1, f1, m1, inv_scale, t1);
+        set_range(t1[0], ok);
+    }
+    for (uint32_t l = 0; l < L; ++l) {
+        __syncthreads();  // the previous cluster's cell terms are no longer read
+        if (tid == 0) {
+            const uint32_t c = sp.ctag[(uint64_t)qi * sp.P + l];
+            s_c = c;
+            s_cdl = sp.cdist[(uint64_t)qi * sp.P + l];
+            s_r0 = s_r1 = s_i0 = s_i1 = 0;
+            if (c < sp.C) {
+                s_r0 = sp.cell_start[(uint64_t)c * F];
+                s_r1 = sp.cell_start[(uint64_t)c * F + F];
+                if (sp.ins_cl_start) {
+                    s_i0 = sp.ins_cl_start[c];
+                    s_i1 = sp.ins_cl_start[c + 1];
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t c = s_c;
+        if (c >= sp.C) break;  // the probed clusters fill a prefix of the slots
+        const uint32_t r0 = s_r0, r1 = s_r1, i0 = s_i0, ni = s_i1 - s_i0, nrec = r1 - r0;
+        if (nrec + ni == 0) continue;
+        // srow[f] = 2 * cell_dist of cell f, cell_dist = (cd + stationary) + fd
+        // (puck_index.cpp:539-540)
+        const float cdl = s_cdl;
+        if ((F & 3u) == 0) {
+            const float4* st4 = reinterpret_cast<const float4*>(sp.stationary + (uint64_t)c * F);
+            const float4* fd4 = reinterpret_cast<const float4*>(fdk);
+            float4* s4 = reinterpret_cast<float4*>(srow);
+            for (uint32_t i = tid; i < (F >> 2); i += kSplitThreads) {
+                const float4 a = __ldg(st4 + i), b = __ldg(fd4 + i);
+                s4[i] = make_float4(2.0f * __fadd_rn(__fadd_rn(cdl, a.x), b.x),
+                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.y), b.y),
+                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.z), b.z),
+                                    2.0f * __fadd_rn(__fadd_rn(cdl, a.w), b.w));
+            }
+        } else {
+            for (uint32_t i = tid; i < F; i += kSplitThreads)
+                srow[i] = 2.0f * __fadd_rn(__fadd_rn(cdl, sp.stationary[(uint64_t)c * F + i]), fdk[i]);
+        }
+        __syncthreads();
+        if (nrec > 0) {
+            const uint32_t b0 = r0 >> 5, nblk = ((r1 - 1) >> 5) - b0 + 1;
+            const uint32_t steps = (nblk + NW * RB - 1) / (NW * RB);
+            // step j: warp w takes record blocks j * NW * RB + r * NW + w of the cluster
+            auto load = [&](uint32_t j, uint2 (&g)[RB][NG], float (&o)[RB], uint32_t (&f)[RB],
+                            uint32_t (&m)[RB], bool (&v)[RB]) {
+#pragma unroll
+                for (int r = 0; r < RB; ++r) {
+                    const uint32_t bi = j * (NW * RB) + r * NW + warp;
+                    m[r] = (b0 + bi) * 32u + lane;
+                    v[r] = bi < nblk && m[r] - r0 < nrec;
+                    if (bi < nblk) {
+                        const unsigned char* rec = sp.codes_il + (uint64_t)(b0 + bi) * kBlk;
+#pragma unroll
+                        for (int q2 = 0; q2 < NG; ++q2)
+                            g[r][q2] = __ldg(reinterpret_cast<const uint2*>(rec + q2 * 256 + 8 * lane));
+                        o[r] = __ldg(reinterpret_cast<const float*>(rec + 32 * kG + 4 * lane));
+                        f[r] = v[r] ? __ldg(reinterpret_cast<const uint16_t*>(rec + 32 * kG + 128 + 2 * lane))
+                                    : 0u;
+                    } else {
+#pragma unroll
+                        for (int q2 = 0; q2 < NG; ++q2) g[r][q2] = make_uint2(0u, 0u);
+                        o[r] = 0.0f;
+                        f[r] = 0u;
+                    }
+                }
+            };
+            // bulk L2 prefetch of step j's record blocks (one copy engine request by
+            // thread 0), kSplitAhead + 1 steps before their loads are issued
+            auto prefetch = [&](uint32_t j) {
+                if (kSplitAhead >= 0 && tid == 0 && j < steps) {
+                    const uint32_t first = j * (NW * RB);
+                    const uint32_t cnt = min((uint32_t)(NW * RB), nblk - first);
+                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                                     sp.codes_il + (uint64_t)(b0 + first) * kBlk),
+                                 "r"(cnt * kBlk)
+                                 : "memory");
+                }
+            };
+            for (int j = 1; j <= kSplitAhead; ++j) prefetch((uint32_t)j);
+            uint2 gr[RB][NG];
+            float off[RB];
+            uint32_t fine[RB], rr[RB];
+            bool valid[RB];
+            load(0, gr, off, fine, rr, valid);
+            for (uint32_t j = 0; j < steps; ++j) {
+                prefetch(j + kSplitAhead + 1);
+                uint2 ngr[RB][NG];
+                float noff[RB];
+                uint32_t nfine[RB], nrr[RB];
+                bool nvalid[RB];
+                const bool more = j + 1 < steps;
+                if (more) load(j + 1, ngr, noff, nfine, nrr, nvalid);
+                float t[RB];
+                il_score<NSQ, HALF, RB>(tab, srow, gr, off, fine, rr, inv_scale, t);
+#pragma unroll
+                for (int r = 0; r < RB; ++r)
+                    if (valid[r]) {
+                        out[pos + (rr[r] - r0)] = t[r];
+                        atomicAdd(&hist[split_bin(t[r], lo, scale)], 1u);
+                    }
+                if (more) {
+#pragma unroll
+                    for (int r = 0; r < RB; ++r) {
+#pragma unroll
+                        for (int q2 = 0; q2 < NG; ++q2) gr[r][q2] = ngr[r][q2];
+                        off[r] = noff[r];
+                        fine[r] = nfine[r];
+                        rr[r] = nrr[r];
+                        valid[r] = nvalid[r];
+                    }
+                }
+            }
+            pos += nrec;
+        }
+        // realtime: the cluster's inserted records (gathered from the interleaved copy)
+        for (uint32_t v0 = 0; v0 < ni; v0 += kSplitThreads * RB) {
+            uint2 g[RB][NG];
+            float o[RB], t[RB];
+            uint32_t f[RB], m[RB];
+            bool v[RB];
+#pragma unroll
+            for (int r = 0; r < RB; ++r) {
+                const uint32_t vi = v0 + r * kSplitThreads + tid;
+                v[r] = vi < ni;
+                m[r] = v[r] ? sp.ins_cl_ids[i0 + vi] : 0u;
+#pragma unroll
+                for (int q2 = 0; q2 < NG; ++q2)
+                    g[r][q2] = __ldg(reinterpret_cast<const uint2*>(sp.codes_il + il_granule_offset(m[r], q2, NSQ)));
+                o[r] = __ldg(reinterpret_cast<const float*>(sp.codes_il + il_offset_offset(m[r], NSQ)));
+                f[r] = v[r] ? __ldg(reinterpret_cast<const uint16_t*>(sp.codes_il + il_fine_offset(m[r], NSQ)))
+                            : 0u;
+            }
+            il_score<NSQ, HALF, RB>(tab, srow, g, o, f, m, inv_scale, t);
+#pragma unroll
+            for (int r = 0; r < RB; ++r)
+                if (v[r]) {
+                    out[pos + v0 + r * kSplitThreads + tid] = t[r];
+                    atomicAdd(&hist[split_bin(t[r], lo, scale)], 1u);
+                }
+        }
+        pos += ni;
+    }
+    __syncthreads();
+    // the cut: the first bin at which the running count reaches T (every bin when
+    // the query has no more than T records)
+    uint32_t bstar = kSplitBins - 1;
+    if (pos > T) {
+        constexpr int PB = kSplitBins / kSplitThreads;
+        uint32_t cb[PB], run = 0;
+#pragma unroll
+        for (int j = 0; j < PB; ++j) {
+            cb[j] = hist[tid * PB + j];
+            run += cb[j];
+        }
+        uint32_t incl = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_red[warp] = incl;
+        __syncthreads();
+        uint32_t below = incl - run;
+        for (int w = 0; w < warp; ++w) below += s_red[w];
+        if (below < T && T <= below + run) {
+#pragma unroll
+            for (int j = 0; j < PB; ++j) {
+                if (below < T && T <= below + cb[j]) s_bin = tid * PB + j;
+                below += cb[j];
+            }
+        }
+        __syncthreads();
+        bstar = s_bin;
+    }
+    // ---- pick: the records at or below the cut bin, read back from this block's own
+    // distances (recently written, mostly still in L2), as (t bits, position) keys in
+    // the table's place; positions to memory ids; the exact T smallest (t, id) out.
+    __syncthreads();  // the table, the cell terms and the histogram are no longer read
+    constexpr uint32_t kKeys = split_max_keys(HALF);
+    uint64_t* keys = reinterpret_cast<uint64_t*>(tab);
+    uint32_t* khist = hist;  // [kHistBins] block_kth_hist scratch
+    // candidates: each thread marks its 16 values of a step, a warp scan of the marks
+    // gives each thread its first slot (one shared atomic per warp and step)
+    const float4* tb4 = reinterpret_cast<const float4*>(out);  // out is 16-byte aligned
+    const uint32_t n4 = (N + 3) / 4;
+    for (uint32_t i0 = 0; i0 < n4; i0 += kSplitThreads * 4) {
+        float4 x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t i = i0 + u * kSplitThreads + tid;
+            x[u] = i < n4 ? __ldcg(tb4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        uint32_t mask = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t i = i0 + u * kSplitThreads + tid;
+            const float tv[4] = {x[u].x, x[u].y, x[u].z, x[u].w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const bool keep = i < n4 && i * 4 + e < N && split_bin(tv[e], lo, scale) <= bstar;
+                mask |= keep ? 1u << (u * 4 + e) : 0u;
+            }
+        }
+        const uint32_t c = __popc(mask);
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        uint32_t base = 0;
+        if (lane == 31 && incl) base = atomicAdd(&k_count, incl);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        uint32_t slot = base + incl - c;
+        while (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int u = b >> 2, e = b & 3;
+            const uint32_t ps = (i0 + u * kSplitThreads + tid) * 4 + e;
+            float tv = 0.0f;  // x[u] element e, by selects (no local-memory array)
+#pragma unroll
+            for (int uu = 0; uu < 4; ++uu)
+                if (uu == u) tv = e == 0 ? x[uu].x : e == 1 ? x[uu].y : e == 2 ? x[uu].z : x[uu].w;
+            if (slot < kKeys) keys[slot] = ((uint64_t)__float_as_uint(tv) << 32) | ps;
+            ++slot;
+        }
+    }
+    __syncthreads();
+    const uint32_t m = k_count;
+    if (m > kKeys) {  // too many records in the cut bin: k_scan_il takes the query
+        if (tid == 0) sp.qflag[qi] = 0;
+        return;
+    }
+    // positions to memory ids: the slot holding the position (binary search), then the
+    // base record or the inserted one
+    for (uint32_t i = tid; i < m; i += kSplitThreads) {
+        const uint64_t k = keys[i];
+        const uint32_t ps = (uint32_t)k;
+        const uint32_t a = slot_of(ps);
+        const uint32_t local = ps - sl_start[a];
+        const uint32_t id =
+            local < sl_nb[a] ? sl_r0[a] + local : sp.ins_cl_ids[sl_i0[a] + (local - sl_nb[a])];
+        keys[i] = filter_key(__uint_as_float((uint32_t)(k >> 32)), id);
+    }
+    __syncthreads();
+    // the exact T smallest: the keys up to the T-th (all of them when m <= T), written
+    // unordered like k_scan_il's
+    const uint64_t bound =
+        m > T ? block_kth_hist<kSplitThreads>(keys, m, T, khist, k_red, &k_cnt, k_hist256, k_sel) + 1
+              : kKeyMax;
+    for (uint32_t i0 = 0; i0 < m; i0 += kSplitThreads) {
+        const uint32_t i = i0 + tid;
+        const uint64_t k = i < m ? keys[i] : kKeyMax;
+        const bool keep = k < bound;
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if (b) {
+            uint32_t base = 0;
+            if (lane == __ffs(b) - 1) base = atomicAdd(&k_out, (uint32_t)__popc(b));
+            base = __shfl_sync(0xffffffffu, base, __ffs(b) - 1);
+            if (keep) {
+                const uint32_t slot = base + __popc(b & ((1u << lane) - 1));
+                sp.hdist[(uint64_t)qi * T + slot] = key_value(k);
+                sp.htag[(uint64_t)qi * T + slot] = (uint32_t)k;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t outn = k_out;  // min(m, T)
+    for (uint32_t i = outn + tid; i < T; i += kSplitThreads) {
+        sp.hdist[(uint64_t)qi * T + i] = sentinel_f();
+        sp.htag[(uint64_t)qi * T + i] = kNoLabel;
+    }
+    if (tid == 0) {
+        sp.hcnt[qi] = outn;
+        if (sp.counters) {
+            atomicAdd(sp.counters + kScRecords, (unsigned long long)N);
+            atomicAdd(sp.counters + kScKept, (unsigned long long)m);
+        }
+    }
+}
+
 }  // namespace
 
 // Shared memory of the interleaved kernel (il_applies(nsq)) for filter_topk T.
@@ -1298,8 +1910,56 @@ cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cud
     return cudaGetLastError();
 }
 
-cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
-                               cudaStream_t stream) {
+bool scan_split_applies(const DeviceIndex& ix, const Scratch& s) {
+    return il_applies(ix.nsq) && ix.codes_il != nullptr && s.tbuf != nullptr && s.tcap > 0;
+}
+
+// Shared memory of k_scan_score: the table, the query, then the compact table being
+// built or the cell terms and the histogram.
+static size_t split_score_smem(const DeviceIndex& ix, bool half) {
+    const size_t stage = sizeof(float) * ix.nsq * 257;
+    const size_t work = il_srow_bytes(ix.F) + sizeof(uint32_t) * (kSplitBins + 4 * kSplitMaxSlots + 1);
+    return il_table_bytes(half) + il_query_bytes(ix.d) + (stage > work ? stage : work);
+}
+
+static SplitParams split_params(const DeviceIndex& ix, uint32_t n, Scratch& s) {
+    SplitParams sp;
+    sp.ctag = s.ctag;
+    sp.cdist = s.cdist;
+    sp.status = s.status;
+    sp.cell_start = ix.cell_start;
+    sp.ins_cl_start = ix.ins_n ? ix.ins_cl_start : nullptr;
+    sp.ins_cl_ids = ix.ins_cl_ids;
+    sp.stationary = ix.stationary;
+    sp.fd_by_fine = s.dots;
+    sp.q = s.q;
+    sp.qnorm = s.qnorm;
+    sp.codebook = ix.codebook;
+    sp.codes_il = ix.codes_il;
+    sp.order = s.order;
+    sp.qcnt = s.qcnt;
+    sp.qoff = s.qoff;
+    sp.qflag = s.qflag;
+    sp.cut = s.cut;
+    sp.tbuf = s.tbuf;
+    sp.hdist = s.hdist;
+    sp.htag = s.htag;
+    sp.hcnt = s.hcnt;
+    sp.counters = s.counters;
+    sp.tcap = s.tcap;
+    sp.n = n;
+    sp.d = ix.d;
+    sp.C = ix.C;
+    sp.F = ix.F;
+    sp.lsq = ix.lsq;
+    sp.P = s.P;
+    sp.T = s.T;
+    sp.codebook_max = ix.codebook_max;
+    return sp;
+}
+
+static cudaError_t launch_fused(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                                const uint32_t* done, cudaStream_t stream) {
     ScanParams p;
     p.q = s.q;
     p.qnorm = s.qnorm;
@@ -1333,6 +1993,7 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
     p.err = s.tc_err;
     p.ins_cl_start = ix.ins_n ? ix.ins_cl_start : nullptr;
     p.ins_cl_ids = ix.ins_cl_ids;
+    p.done = done;
     const size_t smem = half_lut ? scan_smem_bytes_half(ix, s.T) : scan_smem_bytes(ix, s.T);
     const uint32_t nw = ix.code_stride / 4;
     auto launch = [&](void (*kernel)(ScanParams), int threads) {
@@ -1367,6 +2028,48 @@ cudaError_t launch_scan_select(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
         else launch(k_scan_select<16, kTabF32>, kThreads);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_scan_prepare(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                                cudaStream_t stream) {
+    if (!scan_split_applies(ix, s)) return cudaSuccess;
+    if (split_score_smem(ix, half_lut) > 220 * 1024 || s.T >= split_max_keys(half_lut))
+        return cudaErrorInvalidValue;
+    const SplitParams sp = split_params(ix, n, s);
+    k_split_counts<<<(n + 255) / 256, 256, 0, stream>>>(sp);
+    k_split_offsets<<<1, 1024, 0, stream>>>(sp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_records(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                                cudaStream_t stream) {
+    if (!scan_split_applies(ix, s)) return launch_fused(ix, n, s, half_lut, nullptr, stream);
+    const SplitParams sp = split_params(ix, n, s);
+    const size_t smem = split_score_smem(ix, half_lut);
+    auto score = [&](void (*kernel)(SplitParams)) {
+        ensure_max_dynamic_smem(reinterpret_cast<const void*>(kernel), 220 * 1024);
+        kernel<<<n, kSplitThreads, smem, stream>>>(sp);
+    };
+    switch (ix.nsq) {
+#define PGPU_SPLIT(N)                           \
+    case N:                                     \
+        if (half_lut) score(k_scan_score<N, true>); \
+        else score(k_scan_score<N, false>);     \
+        break;
+        PGPU_SPLIT(4) PGPU_SPLIT(8) PGPU_SPLIT(12) PGPU_SPLIT(16) PGPU_SPLIT(20) PGPU_SPLIT(24)
+        PGPU_SPLIT(28) PGPU_SPLIT(32)
+#undef PGPU_SPLIT
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_finish(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
+                               cudaStream_t stream) {
+    if (!scan_split_applies(ix, s)) return cudaSuccess;
+    // the fused kernel takes the queries the split scan did not answer (its blocks for
+    // answered queries return at once)
+    return launch_fused(ix, n, s, half_lut, s.qflag, stream);
 }
 
 }  // namespace pgpu

@@ -46,7 +46,7 @@ WALK_COUNTERS = ("records", "cells", "fd_order_chunks", "enumerations", "fd_orde
                  "heap_inserts", "cyc_replay", "cyc_total", "cyc_prologue", "cyc_candidates",
                  "cyc_adc", "coarse_window_fallbacks", "probe_fallbacks", "probe_clusters")
 STAGES = ("prep", "coarse_scores", "coarse_select", "fine_scores", "fine_order", "walk_scan",
-          "rerank")
+          "filter_select", "rerank")
 
 
 class PuckGpuError(RuntimeError):
