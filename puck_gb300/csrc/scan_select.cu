@@ -1670,37 +1670,32 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
                 }
             };
             for (int j = 1; j <= kSplitAhead; ++j) prefetch((uint32_t)j);
-            uint2 gr[RB][NG];
-            float off[RB];
-            uint32_t fine[RB], rr[RB];
-            bool valid[RB];
-            load(0, gr, off, fine, rr, valid);
-            for (uint32_t j = 0; j < steps; ++j) {
-                prefetch(j + kSplitAhead + 1);
-                uint2 ngr[RB][NG];
-                float noff[RB];
-                uint32_t nfine[RB], nrr[RB];
-                bool nvalid[RB];
-                const bool more = j + 1 < steps;
-                if (more) load(j + 1, ngr, noff, nfine, nrr, nvalid);
+            // two register sets, A and B, in turn: step j + 1's loads go into one set
+            // while step j is scored from the other (no copies between steps)
+            uint2 ga[RB][NG], gb[RB][NG];
+            float oa[RB], ob[RB];
+            uint32_t fa[RB], fb[RB], ma[RB], mb[RB];
+            bool va[RB], vb[RB];
+            auto emit = [&](const uint2 (&g)[RB][NG], const float (&o)[RB], const uint32_t (&f)[RB],
+                            const uint32_t (&m)[RB], const bool (&v)[RB]) {
                 float t[RB];
-                il_score<NSQ, HALF, RB>(tab, srow, gr, off, fine, rr, inv_scale, t);
+                il_score<NSQ, HALF, RB>(tab, srow, g, o, f, m, inv_scale, t);
 #pragma unroll
                 for (int r = 0; r < RB; ++r)
-                    if (valid[r]) {
-                        out[pos + (rr[r] - r0)] = t[r];
+                    if (v[r]) {
+                        out[pos + (m[r] - r0)] = t[r];
                         atomicAdd(&hist[split_bin(t[r], lo, scale)], 1u);
                     }
-                if (more) {
-#pragma unroll
-                    for (int r = 0; r < RB; ++r) {
-#pragma unroll
-                        for (int q2 = 0; q2 < NG; ++q2) gr[r][q2] = ngr[r][q2];
-                        off[r] = noff[r];
-                        fine[r] = nfine[r];
-                        rr[r] = nrr[r];
-                        valid[r] = nvalid[r];
-                    }
+            };
+            load(0, ga, oa, fa, ma, va);
+            for (uint32_t j = 0; j < steps; j += 2) {
+                prefetch(j + kSplitAhead + 1);
+                if (j + 1 < steps) load(j + 1, gb, ob, fb, mb, vb);
+                emit(ga, oa, fa, ma, va);
+                if (j + 1 < steps) {
+                    prefetch(j + kSplitAhead + 2);
+                    if (j + 2 < steps) load(j + 2, ga, oa, fa, ma, va);
+                    emit(gb, ob, fb, mb, vb);
                 }
             }
             pos += nrec;
