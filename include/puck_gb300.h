@@ -338,6 +338,17 @@ int pgpu_contract_bf16(int32_t mode, uint32_t na, uint32_t nb, uint32_t k, const
                        uint64_t a_rs, uint64_t a_ks, const float* b, uint64_t b_rs, uint64_t b_ks,
                        const float* bias, const float* aux, uint64_t ld_aux, float* out,
                        uint64_t ld_out, float* out2, float alpha, float beta, void* stream);
+/* The same contraction on BF16 operands already in memory, row-major (row i of a at
+ * a + i*a_rs elements, k contiguous values). With 16-byte aligned rows (a_rs and b_rs
+ * multiples of 8, 16-byte aligned pointers) it runs the persistent, warp-specialised
+ * kernel (TMA-loaded, 128-byte swizzled operands, double-buffered TMEM accumulators):
+ * the form the search's screens and the probe's inference use; otherwise the
+ * cp.async kernel. Same modes and outputs as pgpu_contract_bf16. No counterpart in
+ * the reference; exported for tests and tools. */
+int pgpu_contract_bf16_rows(int32_t mode, uint32_t na, uint32_t nb, uint32_t k,
+                            const uint16_t* a, uint64_t a_rs, const uint16_t* b, uint64_t b_rs,
+                            const float* bias, const float* aux, uint64_t ld_aux, float* out,
+                            uint64_t ld_out, float* out2, float alpha, float beta, void* stream);
 
 /* ------------------------------------------------------------ learned probe
  * A small MLP (query -> coarse-cluster scores, GELU, 2 hidden layers) trained and

@@ -629,4 +629,41 @@ int pgpu_contract_bf16(int32_t mode, uint32_t na, uint32_t nb, uint32_t k, const
     return PGPU_OK;
 }
 
+int pgpu_contract_bf16_rows(int32_t mode, uint32_t na, uint32_t nb, uint32_t k,
+                            const uint16_t* a, uint64_t a_rs, const uint16_t* b, uint64_t b_rs,
+                            const float* bias, const float* aux, uint64_t ld_aux, float* out,
+                            uint64_t ld_out, float* out2, float alpha, float beta, void* stream) {
+    if (mode < PGPU_CONTRACT_SCORE || mode > PGPU_CONTRACT_GELU_BWD || k == 0 || a == nullptr ||
+        b == nullptr || out == nullptr || ld_out < nb)
+        return fail(PGPU_E_INVALID, "invalid argument");
+    if ((na + 127u) / 128u > 65535u) return fail(PGPU_E_LIMIT, "na above 8388480");
+    cudaStream_t st = (cudaStream_t)stream;
+    int* err = nullptr;
+    cudaError_t e = cudaMallocAsync(&err, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "contract_bf16_rows");
+    e = cudaMemsetAsync(err, 0, sizeof(int), st);
+    if (a_rs < k || b_rs < k) return fail(PGPU_E_INVALID, "row stride below k");
+    pgpu::TcOperand A{nullptr, a_rs, 1, na, a};
+    pgpu::TcOperand B{nullptr, b_rs, 1, nb, b};
+    pgpu::TcEpilogue ep{};
+    ep.mode = mode;
+    ep.out = out;
+    ep.ld = ld_out;
+    ep.bias = bias;
+    ep.aux = aux;
+    ep.ld_aux = ld_aux;
+    ep.out2 = out2;
+    ep.alpha = alpha;
+    ep.beta = beta;
+    if (e == cudaSuccess) e = pgpu::launch_tc_gemm(A, B, k, ep, err, st);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFreeAsync(err, st);
+    if (e == cudaErrorInvalidValue) return fail(PGPU_E_INVALID, "invalid contraction operands");
+    if (e != cudaSuccess) return cuda_fail(e, "contract_bf16_rows");
+    if (flag) return fail(PGPU_E_TIMEOUT, "tensor-core wait expired");
+    return PGPU_OK;
+}
+
 }  // extern "C"

@@ -17,9 +17,11 @@
 // output rows) with tcgen05.ld and applies the epilogue. Every mbarrier wait is
 // bounded: on expiry the kernel sets *err = 1, waits (bounded) for the
 // last commit, skips the epilogue and releases its TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "pgpu_internal.h"
 
@@ -399,10 +401,370 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
     }
 }
 
+// ------------------------------------------------------------ persistent TMA form
+// For BF16 operands with 16-byte aligned rows and no row gather (the probe's
+// inference layers, the coarse and fine screens): a persistent, warp-specialised
+// kernel, one CTA per SM looping over 128 x NT output tiles (n fastest, so
+// neighbouring CTAs share the A tile in L2):
+//   warp 0 (one lane): TMA producer. Per K chunk of 64 it loads the A box
+//     (64 x 128) and the B box (64 x NT) into a ring of kTmaStages stages, 128-byte
+//     swizzled (cp.async.bulk.tensor, completion on the stage's full mbarrier);
+//     rows and K past the operands' ends arrive as zeros.
+//   warp 1 (one lane): MMA issuer. tcgen05.mma (M = 128, N = NT, K = 16) per 32-byte
+//     step of the swizzle atom, into one of two TMEM accumulators (2 x NT columns);
+//     each chunk's MMAs commit to the stage's empty mbarrier, each tile's to the
+//     accumulator's full mbarrier.
+//   warps 2-5: epilogue. Warp w reads TMEM lanes 32 (w % 4) .. +32 (its rows) with
+//     tcgen05.ld, applies the epilogue, stores, and arrives on the accumulator's
+//     empty mbarrier, so the next tile's MMAs overlap this tile's epilogue.
+// Every wait is bounded: on expiry the kernel sets *err, the roles stop, the
+// producer waits (bounded) for its copies in flight and the TMEM is released.
+constexpr int kTmaThreads = 192;
+constexpr uint32_t kTmaStages = 4;
+constexpr uint32_t kTmaK = 64;  // K per chunk: 64 BF16 = one 128-byte swizzle atom row
+constexpr uint32_t kTmaABytes = 128u * kTmaK * 2u;
+
+__host__ __device__ constexpr uint32_t tma_stage_bytes(int nt) {
+    return kTmaABytes + (uint32_t)nt * kTmaK * 2u;
+}
+
+// K-major, 128-byte swizzled operand tile (8-row x 128-byte atoms, 1024 bytes apart):
+// start address, leading byte offset 16 (unused within one atom), stride byte offset
+// 1024, the fixed 0b001 at bits 46-48, swizzle mode 2 (128 B) at bits 61-63.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) |
+           ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) | (2ull << 61);
+}
+
+__device__ __forceinline__ bool tma_wait(uint32_t bar, uint32_t parity, const volatile int* failed) {
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.b32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((it & 1023u) == 1023u && *failed) return false;
+    }
+    return false;
+}
+
+template <int EPI, int NT>
+__global__ __launch_bounds__(kTmaThreads, 1) void k_tc_gemm_tma(
+    const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
+    uint32_t M, uint32_t N, uint32_t K, TcEpilogue ep, int* __restrict__ err) {
+    constexpr uint32_t kStage = tma_stage_bytes(NT);
+    constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NT >> 3) << 17) |
+                                ((128u >> 4) << 24);
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], tfull[2], tempty[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // 128-byte swizzled stages start on 1024-byte boundaries
+    const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const uint32_t tiles_n = (N + NT - 1) / NT, tiles = ((M + 127) / 128) * tiles_n;
+    const uint32_t nch = (K + kTmaK - 1) / kTmaK;
+    if (threadIdx.x == 0) {
+        failed = 0;
+        for (uint32_t i = 0; i < kTmaStages; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full[i])), "r"(1u));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&empty[i])), "r"(1u));
+        }
+        for (uint32_t i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tfull[i])), "r"(1u));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tempty[i])), "r"(4u));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_base)),
+                     "r"(2u * NT)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    auto fail = [&]() {
+        failed = 1;
+        atomicExch(err, 1);
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer
+            uint32_t it = 0;
+            for (uint32_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+                const int32_t m0 = (int32_t)((t / tiles_n) * 128u), n0 = (int32_t)((t % tiles_n) * NT);
+                for (uint32_t c = 0; c < nch; ++c, ++it) {
+                    const uint32_t st = it % kTmaStages;
+                    if (it >= kTmaStages &&
+                        !tma_wait(smem_u32(&empty[st]), ((it / kTmaStages) & 1u) ^ 1u, &failed)) {
+                        fail();
+                        break;
+                    }
+                    const uint32_t bar = smem_u32(&full[st]);
+                    const uint32_t dst = sbase + st * kStage;
+                    const int32_t k0 = (int32_t)(c * kTmaK);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                                 "r"(kStage)
+                                 : "memory");
+                    asm volatile(
+                        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+                        "l"(reinterpret_cast<uint64_t>(&tma_a)), "r"(k0), "r"(m0), "r"(bar)
+                        : "memory");
+                    asm volatile(
+                        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst + kTmaABytes),
+                        "l"(reinterpret_cast<uint64_t>(&tma_b)), "r"(k0), "r"(n0), "r"(bar)
+                        : "memory");
+                }
+            }
+            // no copy may land after the CTA: wait (bounded) for the last one of each stage
+            for (uint32_t st = 0; st < kTmaStages && st < it; ++st) {
+                const uint32_t last = it - 1 - ((it - 1 - st) % kTmaStages);  // last use of stage st
+                tma_wait(smem_u32(&full[st]), (last / kTmaStages) & 1u, &failed);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            uint32_t it = 0, lt = 0;
+            bool any = false;
+            for (uint32_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x, ++lt) {
+                const uint32_t acc = lt & 1u, use = lt >> 1;
+                if (lt >= 2 && !tma_wait(smem_u32(&tempty[acc]), (use - 1) & 1u, &failed)) {
+                    fail();
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t d_tmem = tmem + acc * NT;
+                bool ok = true;
+                for (uint32_t c = 0; c < nch; ++c, ++it) {
+                    const uint32_t st = it % kTmaStages;
+                    if (!tma_wait(smem_u32(&full[st]), (it / kTmaStages) & 1u, &failed)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t a_addr = sbase + st * kStage, b_addr = a_addr + kTmaABytes;
+#pragma unroll
+                    for (uint32_t k = 0; k < kTmaK / 16; ++k) {
+                        const uint64_t ad = sw128_desc(a_addr + k * 32u);
+                        const uint64_t bd = sw128_desc(b_addr + k * 32u);
+                        const uint32_t accum = (c > 0 || k > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+                            "l"(ad), "l"(bd), "r"(kIdesc), "r"(accum)
+                            : "memory");
+                    }
+                    asm volatile(
+                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                            smem_u32(&empty[st]))
+                        : "memory");
+                }
+                if (!ok) {
+                    fail();
+                    break;
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        smem_u32(&tfull[acc]))
+                    : "memory");
+                any = true;
+            }
+            // the last commit covers every MMA issued before it
+            if (any) {
+                const uint32_t lt_last = lt - 1;
+                tma_wait(smem_u32(&tfull[lt_last & 1u]), (lt_last >> 1) & 1u, &failed);
+            }
+        }
+    } else {
+        // epilogue: warps 2..5 own TMEM lanes 32 * (warp % 4)
+        const uint32_t quarter = (uint32_t)(warp & 3);
+        const bool vec_out = ((ep.ld & 3u) == 0) && ((reinterpret_cast<uintptr_t>(ep.out) & 15u) == 0);
+        const bool vec_out_b = ((ep.ld & 7u) == 0) &&
+                               ((reinterpret_cast<uintptr_t>(ep.out_bf16) & 15u) == 0);
+        uint32_t lt = 0;
+        for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, ++lt) {
+            const uint32_t acc = lt & 1u, use = lt >> 1;
+            if (!tma_wait(smem_u32(&tfull[acc]), use & 1u, &failed)) {
+                if (lane == 0) fail();
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t m0 = (t / tiles_n) * 128u, n0 = (t % tiles_n) * NT;
+            const uint32_t row = m0 + quarter * 32 + lane;
+            const uint32_t taddr = tmem + acc * NT + ((quarter * 32u) << 16);
+#pragma unroll 1
+            for (uint32_t cc = 0; cc < NT / 16; ++cc) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+                    "%13,%14,%15}, [%16];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                      "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                      "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                    : "r"(taddr + cc * 16));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const uint32_t col0 = n0 + cc * 16;
+                if (row >= M || col0 >= N) continue;
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    v[j] = (col0 + j < N) ? epilogue<EPI>(__uint_as_float(r[j]), row, col0 + j, ep) : 0.0f;
+                if (ep.out_bf16 != nullptr) {
+                    uint16_t* orow = ep.out_bf16 + (uint64_t)row * ep.ld;
+                    if (vec_out_b && col0 + 16 <= N) {
+                        uint4 lo, hi;
+                        lo.x = bf16x2(v[0], v[1]);
+                        lo.y = bf16x2(v[2], v[3]);
+                        lo.z = bf16x2(v[4], v[5]);
+                        lo.w = bf16x2(v[6], v[7]);
+                        hi.x = bf16x2(v[8], v[9]);
+                        hi.y = bf16x2(v[10], v[11]);
+                        hi.z = bf16x2(v[12], v[13]);
+                        hi.w = bf16x2(v[14], v[15]);
+                        *reinterpret_cast<uint4*>(orow + col0) = lo;
+                        *reinterpret_cast<uint4*>(orow + col0 + 8) = hi;
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (col0 + j < N) orow[col0 + j] = __bfloat16_as_ushort(__float2bfloat16_rn(v[j]));
+                    }
+                    continue;
+                }
+                float* orow = ep.out + (uint64_t)row * ep.ld;
+                if (vec_out && col0 + 16 <= N) {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 4)
+                        *reinterpret_cast<float4*>(orow + col0 + j) =
+                            make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (col0 + j < N) orow[col0 + j] = v[j];
+                }
+            }
+            // this accumulator may take the next tile's MMAs
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc]))
+                             : "memory");
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2u * NT)
+                     : "memory");
+    }
+}
+
 bool operand_vec(const TcOperand& op) {
     if (op.pb != nullptr)
         return op.ks == 1 && (op.rs & 7u) == 0 && (reinterpret_cast<uintptr_t>(op.pb) & 15u) == 0;
     return op.ks == 1 && (op.rs & 3u) == 0 && (reinterpret_cast<uintptr_t>(op.p) & 15u) == 0;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the
+// driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// 2-D BF16 tensor map of an operand (rows x K, row stride rs elements), box 64 (K)
+// x box_rows, 128-byte swizzle, zero fill past the ends.
+bool encode_operand(CUtensorMap* map, const TcOperand& op, uint32_t K, uint32_t box_rows) {
+    EncodeTiledFn fn = encode_tiled_fn();
+    if (fn == nullptr) return false;
+    const cuuint64_t dims[2] = {K, op.rows};
+    const cuuint64_t strides[1] = {op.rs * 2ull};
+    const cuuint32_t box[2] = {kTmaK, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<uint16_t*>(op.pb), dims, strides,
+              box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int sm_count() {
+    static std::mutex mu;
+    static int counts[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 0 && dev < 64 && counts[dev] == 0)
+        cudaDeviceGetAttribute(&counts[dev], cudaDevAttrMultiProcessorCount, dev);
+    return dev >= 0 && dev < 64 && counts[dev] > 0 ? counts[dev] : 1;
+}
+
+// The persistent TMA form applies: both operands BF16, rows 16-byte aligned, every
+// row read in place (no gather, no device row count).
+bool tma_applies(const TcOperand& A, const TcOperand& B, uint32_t K) {
+    return A.pb != nullptr && B.pb != nullptr && operand_vec(A) && operand_vec(B) &&
+           A.ridx == nullptr && A.rows_dev == nullptr && B.ridx == nullptr &&
+           B.rows_dev == nullptr && K >= 8 && (uint64_t)A.rows < (1ull << 31) &&
+           (uint64_t)B.rows < (1ull << 31);
+}
+
+cudaError_t launch_tc_gemm_tma(const TcOperand& A, const TcOperand& B, uint32_t K,
+                               const TcEpilogue& ep, int* err, cudaStream_t stream, bool* done) {
+    *done = false;
+    const int nt = B.rows >= 256 ? 256 : 128;
+    CUtensorMap ma, mb;
+    if (!encode_operand(&ma, A, K, 128) || !encode_operand(&mb, B, K, (uint32_t)nt))
+        return cudaSuccess;  // not encodable: the cp.async form runs instead
+    const uint64_t tiles = (uint64_t)((A.rows + 127) / 128) * ((B.rows + nt - 1) / nt);
+    const unsigned grid = (unsigned)(tiles < (uint64_t)sm_count() ? tiles : (uint64_t)sm_count());
+    const size_t smem = kTmaStages * (size_t)tma_stage_bytes(nt) + 1024;
+#define PGPU_TMA_CASE(M)                                                                    \
+    case M:                                                                                 \
+        if (nt == 256) {                                                                    \
+            ensure_max_dynamic_smem(k_tc_gemm_tma<M, 256>, (int)smem);                      \
+            k_tc_gemm_tma<M, 256><<<grid, kTmaThreads, smem, stream>>>(ma, mb, A.rows, B.rows, \
+                                                                       K, ep, err);        \
+        } else {                                                                            \
+            ensure_max_dynamic_smem(k_tc_gemm_tma<M, 128>, (int)smem);                      \
+            k_tc_gemm_tma<M, 128><<<grid, kTmaThreads, smem, stream>>>(ma, mb, A.rows, B.rows, \
+                                                                       K, ep, err);        \
+        }                                                                                   \
+        break;
+    switch (ep.mode) {
+        PGPU_TMA_CASE(TC_EPI_SCORE)
+        PGPU_TMA_CASE(TC_EPI_NEG)
+        PGPU_TMA_CASE(TC_EPI_STORE)
+        PGPU_TMA_CASE(TC_EPI_BIAS)
+        PGPU_TMA_CASE(TC_EPI_BIAS_GELU)
+        PGPU_TMA_CASE(TC_EPI_GELU_BWD)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef PGPU_TMA_CASE
+    *done = true;
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -421,6 +783,11 @@ cudaError_t launch_tc_gemm(const TcOperand& A, const TcOperand& B, uint32_t K,
         ep.bias == nullptr)
         return cudaErrorInvalidValue;
     if (ep.mode == TC_EPI_GELU_BWD && ep.aux == nullptr) return cudaErrorInvalidValue;
+    if (tma_applies(A, B, K)) {
+        bool done = false;
+        const cudaError_t e = launch_tc_gemm_tma(A, B, K, ep, err, stream, &done);
+        if (e != cudaSuccess || done) return e;
+    }
     const dim3 grid((B.rows + kTileN - 1) / kTileN, (A.rows + kTileM - 1) / kTileM);
     if (grid.y > 65535) return cudaErrorInvalidValue;
     const int av = operand_vec(A) ? 1 : 0, bv = operand_vec(B) ? 1 : 0;

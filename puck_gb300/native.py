@@ -35,7 +35,8 @@ EXPORTED_SYMBOLS = (
     "pgpu_set_profiling", "pgpu_stage_times", "pgpu_walk_counters",
     "pgpu_nearest_center_noalloc", "pgpu_nearest_cell_assign", "pgpu_server_params_default", "pgpu_server_create",
     "pgpu_server_submit", "pgpu_server_wait", "pgpu_server_stats_get", "pgpu_server_destroy",
-    "pgpu_contract_bf16", "pgpu_filter_candidates", "pgpu_probe_create", "pgpu_probe_destroy",
+    "pgpu_contract_bf16", "pgpu_contract_bf16_rows", "pgpu_filter_candidates", "pgpu_probe_create",
+    "pgpu_probe_destroy",
     "pgpu_probe_info", "pgpu_probe_train_step", "pgpu_probe_gradients", "pgpu_probe_forward",
     "pgpu_probe_get_params", "pgpu_probe_set_params", "pgpu_set_probe", "pgpu_knn",
     "pgpu_puck_assign", "pgpu_realtime_open", "pgpu_insert",
@@ -162,6 +163,8 @@ def load(build_if_missing=False):
     lib.pgpu_knn.argtypes = [vp, u64, u32, vp, u32, u32, vp, vp, vp]
     lib.pgpu_contract_bf16.argtypes = [ctypes.c_int32, u32, u32, u32, vp, u64, u64, vp, u64, u64,
                                        vp, vp, u64, vp, u64, vp, f32, f32, vp]
+    lib.pgpu_contract_bf16_rows.argtypes = [ctypes.c_int32, u32, u32, u32, vp, u64, vp, u64, vp,
+                                            vp, u64, vp, u64, vp, f32, f32, vp]
     lib.pgpu_last_error.restype = ctypes.c_char_p
     lib.pgpu_last_error.argtypes = []
     for name in EXPORTED_SYMBOLS:
@@ -432,6 +435,27 @@ def contract_bf16(mode, a, b, out, bias=None, aux=None, out2=None, alpha=1.0, be
         b.stride(0), b.stride(1), _ptr(bias) if bias is not None else None,
         _ptr(aux) if aux is not None else None, ld_aux, _ptr(out), out.stride(0),
         _ptr(out2) if out2 is not None else None, alpha, beta, s))
+
+
+def contract_bf16_rows(mode, a, b, out, bias=None, aux=None, out2=None, alpha=1.0, beta=0.0,
+                       stream=None):
+    """out = f(a @ b.T) on the tensor cores for BF16 operands already in memory
+    (pgpu_contract_bf16_rows): a [na, k] and b [nb, k] are 2-D torch.bfloat16 CUDA
+    tensors with unit column stride (rows may be padded); out is float32 [na, >= nb]."""
+    import torch
+    na, k = a.shape
+    nb, kb = b.shape
+    assert k == kb and a.dtype == torch.bfloat16 and b.dtype == torch.bfloat16
+    assert a.stride(1) == 1 and b.stride(1) == 1 and out.stride(1) == 1
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream
+    ld_aux = aux.stride(0) if aux is not None else 0
+    return check(load().pgpu_contract_bf16_rows(
+        CONTRACT_MODES[mode], na, nb, k, _ptr(a), a.stride(0), _ptr(b), b.stride(0),
+        _ptr(bias) if bias is not None else None, _ptr(aux) if aux is not None else None,
+        ld_aux, _ptr(out), out.stride(0), _ptr(out2) if out2 is not None else None, alpha, beta,
+        s))
 
 
 def nearest_center_noalloc(centroids, points, assign, distance, stream=None):

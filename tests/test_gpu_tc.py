@@ -4,6 +4,9 @@ selections built on it.
 * pgpu_contract_bf16 against an FP64 product of the BF16-rounded operands, in
   every epilogue and for row-major and transposed operands, with the FP32
   accumulation bound |err| <= k * 2^-23 * sum_t |a_t b_t| written in the test;
+* pgpu_contract_bf16_rows (BF16 rows in memory: the persistent TMA kernel when the
+  rows are 16-byte aligned) against the same bound, over ragged rows and K, many
+  tiles per CTA and every epilogue;
 * nearest_center (tensor-core screen + exact FP32 window) bit-identical to the
   oracle, including exact ties between duplicated centroids;
 * the coarse top-P window: with duplicated coarse centroids (ties at the cut)
@@ -103,6 +106,60 @@ def test_contract_epilogues():
     x = aux.double().requires_grad_(True)
     torch.nn.functional.gelu(x).sum().backward()
     torch.testing.assert_close(out.double(), acc.double() * x.grad, rtol=1e-5, atol=1e-6)
+
+
+def _bf16_rows(rows, k, pad, gen):
+    """A random BF16 operand [rows, k] whose rows are `pad` elements apart."""
+    import torch
+    full = torch.randn(rows, pad, device="cuda", generator=gen).to(torch.bfloat16)
+    return full[:, :k]
+
+
+@pytest.mark.parametrize("na,nb,k,pad", [
+    (1, 1, 16, 16),
+    (300, 200, 96, 96),        # one 128-column tile
+    (129, 257, 100, 104),      # ragged rows and K (zero fill past the ends), 256-column tiles
+    (1000, 4000, 512, 512),    # the probe's output layer shape: many tiles per CTA
+    (4100, 512, 96, 96),       # more row tiles than SMs
+    (5, 300, 40, 40),          # K below one 64-wide chunk
+    (257, 130, 8, 8),
+    (130, 70, 100, 100),       # rows not 16-byte aligned: the cp.async kernel
+])
+def test_contract_rows_store(na, nb, k, pad):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(na * 17 + nb + k)
+    a = _bf16_rows(na, k, pad, g)
+    b = _bf16_rows(nb, k, pad, g)
+    out = torch.full((na, nb), float("nan"), device="cuda")
+    native.contract_bf16_rows("store", a, b, out)
+    _check_acc(out, a.float(), b.float())
+
+
+def test_contract_rows_epilogues():
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(5)
+    na, nb, k = 700, 600, 96
+    a = _bf16_rows(na, k, k, g)
+    b = _bf16_rows(nb, k, k, g)
+    bias = torch.randn(nb, device="cuda", generator=g)
+    acc = torch.empty(na, nb, device="cuda")
+    native.contract_bf16_rows("store", a, b, acc)
+    _check_acc(acc, a.float(), b.float())
+    out = torch.empty_like(acc)
+    native.contract_bf16_rows("score", a, b, out, bias=bias)
+    assert torch.equal(out, bias[None, :] - acc)
+    native.contract_bf16_rows("neg", a, b, out)
+    assert torch.equal(out, -acc)
+    native.contract_bf16_rows("bias", a, b, out, bias=bias)
+    assert torch.equal(out, acc + bias[None, :])
+    pre = torch.empty_like(acc)
+    native.contract_bf16_rows("bias_gelu", a, b, out, bias=bias, out2=pre)
+    assert torch.equal(pre, acc + bias[None, :])
+    torch.testing.assert_close(out, torch.nn.functional.gelu(pre), rtol=1e-5, atol=1e-6)
+    # the same accumulators as the FP32-operand entry point on the same BF16 values
+    ref = torch.empty_like(acc)
+    native.contract_bf16("store", a.float(), b.float(), ref)
+    _check_acc(ref, a.float(), b.float())
 
 
 def test_contract_rejects_bad_arguments():
