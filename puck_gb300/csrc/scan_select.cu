@@ -885,7 +885,7 @@ __device__ __forceinline__ bool il_wait(uint32_t bar, uint32_t parity) {
 // codeword's subspaces go in two halves, a thread per half (NT = 512) or both halves
 // by one thread (NT = 256). All NT threads; one barrier inside (after the staging),
 // none after the expansion.
-template <int NSQ, bool HALF, int NT>
+template <int NSQ, bool HALF, int NT, bool WIDE = false>
 __device__ __forceinline__ void il_build_table(unsigned char* tab, float* stage, const float* qv,
                                                const float* __restrict__ codebook, uint32_t lsq,
                                                int lut_e) {
@@ -918,7 +918,16 @@ __device__ __forceinline__ void il_build_table(unsigned char* tab, float* stage,
         }
     }
     __syncthreads();
-    if (HALF) {
+    if (HALF && WIDE) {
+        // each FP16 entry in its own 4-byte slot (the FP32 table's addresses)
+        const float scale = ldexpf(1.0f, lut_e);
+        uint32_t* tw = reinterpret_cast<uint32_t*>(tab);
+        for (uint32_t w = tid; w < 256 * 64; w += NT) {
+            const uint32_t c = w >> 6, m = w & 63;
+            const float v = m < NSQ + 31 ? stage[(m % NSQ) * 257 + c] : 0.0f;
+            tw[w] = (uint32_t)__half_as_ushort(__float2half_rn(v * scale));
+        }
+    } else if (HALF) {
         const float scale = ldexpf(1.0f, lut_e);
         uint32_t* tw = reinterpret_cast<uint32_t*>(tab);
         for (uint32_t w = tid; w < 256 * 32; w += NT) {
@@ -942,7 +951,7 @@ __device__ __forceinline__ void il_build_table(unsigned char* tab, float* stage,
 // record's cell; the R lookup chains are interleaved. Lookup step s goes to partial
 // s mod 4 in FP32; t = (srow[f] + offset) + ((a0 + a1) + (a2 + a3)) (the FP16 table's
 // sum scaled back by inv_scale).
-template <int NSQ, bool HALF, int R>
+template <int NSQ, bool HALF, int R, bool WIDE = false>
 __device__ __forceinline__ void il_score(const unsigned char* tab, const float* srow,
                                          const uint2 (&gr)[R][(NSQ + 7) / 8], const float (&off)[R],
                                          const uint32_t (&fine)[R], const uint32_t (&mr)[R],
@@ -962,8 +971,10 @@ __device__ __forceinline__ void il_score(const unsigned char* tab, const float* 
             // (code << 8) | 4 * lane: the entry of column s2 + lane
             const uint32_t addr = __byte_perm(w, lb[j], 0x5504u | ((uint32_t)(s2 & 3) << 4));
             if (HALF) {
+                // compact table: 2-byte entries (one shift); WIDE: one entry per 4-byte slot
                 const unsigned short h =
-                    *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
+                    WIDE ? *reinterpret_cast<const unsigned short*>(tab + addr + 4 * s2)
+                         : *reinterpret_cast<const unsigned short*>(tab + (addr >> 1) + 2 * s2);
                 asm("add.f32.f16 %0, %1, %0;" : "+f"(a[j][s2 & 3]) : "h"(h));
             } else {
                 a[j][s2 & 3] =
@@ -1305,14 +1316,17 @@ __global__ __launch_bounds__(kOrderThreads) void k_scan_order(const uint8_t* __r
 //      positions to memory ids and writes the exact T smallest (t, id), unordered:
 //      the same set as k_scan_il's.
 // Without k_scan_il's key buffer and its cut-backs, a block holds the table, the cell
-// terms and the histogram: two blocks per SM (FP32 table) or three (FP16), so one
-// block's table build and pick overlap the others' records.
+// terms and the histogram: two blocks per SM, so one block's table build and pick
+// overlap the other's records. The FP16 table (precision form) keeps one entry per
+// 4-byte slot, the FP32 table's addresses: a lookup is the same PRMT, load and add
+// (the compact 2-byte layout costs a shift per lookup, and its smaller footprint buys
+// nothing here).
 // record blocks per warp and step (FP32 table, FP16 table)
 #ifndef PGPU_SPLIT_RB32
 #define PGPU_SPLIT_RB32 4
 #endif
 #ifndef PGPU_SPLIT_RB16
-#define PGPU_SPLIT_RB16 2
+#define PGPU_SPLIT_RB16 4
 #endif
 constexpr int kSplitThreads = 256;
 constexpr int kSplitWarps = kSplitThreads / 32;
@@ -1323,8 +1337,8 @@ constexpr uint32_t kSplitNo = 0xFFFFFFFFu; // count of a query left to k_scan_il
 #define PGPU_SPLIT_AHEAD 2
 #endif
 constexpr int kSplitAhead = PGPU_SPLIT_AHEAD;  // L2 prefetch distance in record steps (-1: none)
-// candidates the pick phase holds (in the table's place): 8192 (FP32), 4096 (FP16)
-__host__ __device__ constexpr uint32_t split_max_keys(bool half) { return il_table_bytes(half) / 8; }
+// candidates the pick phase holds (in the table's place): 8192
+__host__ __device__ constexpr uint32_t split_max_keys(bool) { return il_table_bytes(false) / 8; }
 
 struct SplitParams {
     const uint32_t* ctag;
@@ -1428,7 +1442,7 @@ __global__ __launch_bounds__(1024) void k_split_offsets(SplitParams sp) {
 
 template <int NSQ, bool HALF>
 #ifndef PGPU_SPLIT_MINB16
-#define PGPU_SPLIT_MINB16 3
+#define PGPU_SPLIT_MINB16 2
 #endif
 __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k_scan_score(SplitParams sp) {
     constexpr int NG = (NSQ + 7) / 8;  // 8-byte code granules per record
@@ -1448,8 +1462,9 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t F = sp.F, T = sp.T;
     unsigned char* tab = smem;
-    float* qv = reinterpret_cast<float*>(smem + il_table_bytes(HALF));
-    unsigned char* rest = smem + il_table_bytes(HALF) + il_query_bytes(sp.d);
+    // the FP16 table takes one 4-byte slot per entry (the FP32 table's addresses and size)
+    float* qv = reinterpret_cast<float*>(smem + il_table_bytes(false));
+    unsigned char* rest = smem + il_table_bytes(false) + il_query_bytes(sp.d);
     float* stage = reinterpret_cast<float*>(rest);  // [NSQ][257] while the table is built
     float* srow = reinterpret_cast<float*>(rest);   // [F] afterwards
     uint32_t* hist = reinterpret_cast<uint32_t*>(rest + il_srow_bytes(F));  // [kSplitBins]
@@ -1463,7 +1478,7 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
     const int lut_e = HALF ? half_lut_exponent(sp.qnorm[qi], sp.codebook_max) : 0;
     const float inv_scale = HALF ? ldexpf(1.0f, -lut_e) : 1.0f;
     __syncthreads();
-    il_build_table<NSQ, HALF, kSplitThreads>(tab, stage, qv, sp.codebook, sp.lsq, lut_e);
+    il_build_table<NSQ, HALF, kSplitThreads, true>(tab, stage, qv, sp.codebook, sp.lsq, lut_e);
     __syncthreads();  // stage (under srow and hist) is read to the end of the expansion
     for (uint32_t b = tid; b < kSplitBins; b += kSplitThreads) hist[b] = 0;
     // slot table: records per probed cluster, then an exclusive scan (PS slots per thread)
@@ -1587,7 +1602,7 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
             const float cd = sp.cdist[(uint64_t)qi * sp.P + a];
             cterm[0] = 2.0f * __fadd_rn(__fadd_rn(cd, __ldg(sp.stationary + (uint64_t)c * F + fi)), __ldg(fdk + fi));
         }
-        il_score<NSQ, HALF, 1>(tab, cterm, g1, o1, f1, m1, inv_scale, t1);
+        il_score<NSQ, HALF, 1, true>(tab, cterm, g1, o1, f1, m1, inv_scale, t1);
         set_range(t1[0], ok);
     }
     for (uint32_t l = 0; l < L; ++l) {
@@ -1679,7 +1694,7 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
             auto emit = [&](const uint2 (&g)[RB][NG], const float (&o)[RB], const uint32_t (&f)[RB],
                             const uint32_t (&m)[RB], const bool (&v)[RB]) {
                 float t[RB];
-                il_score<NSQ, HALF, RB>(tab, srow, g, o, f, m, inv_scale, t);
+                il_score<NSQ, HALF, RB, true>(tab, srow, g, o, f, m, inv_scale, t);
 #pragma unroll
                 for (int r = 0; r < RB; ++r)
                     if (v[r]) {
@@ -1718,7 +1733,7 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
                 f[r] = v[r] ? __ldg(reinterpret_cast<const uint16_t*>(sp.codes_il + il_fine_offset(m[r], NSQ)))
                             : 0u;
             }
-            il_score<NSQ, HALF, RB>(tab, srow, g, o, f, m, inv_scale, t);
+            il_score<NSQ, HALF, RB, true>(tab, srow, g, o, f, m, inv_scale, t);
 #pragma unroll
             for (int r = 0; r < RB; ++r)
                 if (v[r]) {
@@ -1764,7 +1779,7 @@ __global__ __launch_bounds__(kSplitThreads, HALF ? PGPU_SPLIT_MINB16 : 2) void k
     // distances (recently written, mostly still in L2), as (t bits, position) keys in
     // the table's place; positions to memory ids; the exact T smallest (t, id) out.
     __syncthreads();  // the table, the cell terms and the histogram are no longer read
-    constexpr uint32_t kKeys = split_max_keys(HALF);
+    constexpr uint32_t kKeys = split_max_keys(false);
     uint64_t* keys = reinterpret_cast<uint64_t*>(tab);
     uint32_t* khist = hist;  // [kHistBins] block_kth_hist scratch
     // candidates: each thread marks its 16 values of a step, a warp scan of the marks
@@ -1914,7 +1929,7 @@ bool scan_split_applies(const DeviceIndex& ix, const Scratch& s) {
 static size_t split_score_smem(const DeviceIndex& ix, bool half) {
     const size_t stage = sizeof(float) * ix.nsq * 257;
     const size_t work = il_srow_bytes(ix.F) + sizeof(uint32_t) * (kSplitBins + 4 * kSplitMaxSlots + 1);
-    return il_table_bytes(half) + il_query_bytes(ix.d) + (stage > work ? stage : work);
+    return il_table_bytes(false) + il_query_bytes(ix.d) + (stage > work ? stage : work);
 }
 
 static SplitParams split_params(const DeviceIndex& ix, uint32_t n, Scratch& s) {
