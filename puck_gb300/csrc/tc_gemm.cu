@@ -414,9 +414,11 @@ __global__ __launch_bounds__(kTcThreads) void k_tc_gemm(TcOperand A, TcOperand B
 //     step of the swizzle atom, into one of two TMEM accumulators (2 x NT columns);
 //     each chunk's MMAs commit to the stage's empty mbarrier, each tile's to the
 //     accumulator's full mbarrier.
-//   warps 2-5: epilogue. Warp w reads TMEM lanes 32 (w % 4) .. +32 (its rows) with
-//     tcgen05.ld, applies the epilogue, stores, and arrives on the accumulator's
-//     empty mbarrier, so the next tile's MMAs overlap this tile's epilogue.
+//   warps 2-5: epilogue. Warp w reads TMEM lanes 32 (w % 4) .. +32 (its rows), 32
+//     columns at a time, with tcgen05.ld, applies the epilogue, and writes the
+//     32 x 32 block through shared memory so that each store covers one row's 32
+//     columns (128 contiguous bytes); then it arrives on the accumulator's empty
+//     mbarrier, so the next tile's MMAs overlap this tile's epilogue.
 // Every wait is bounded: on expiry the kernel sets *err, the roles stop, the
 // producer waits (bounded) for its copies in flight and the TMEM is released.
 constexpr int kTmaThreads = 192;
@@ -589,9 +591,8 @@ __global__ __launch_bounds__(kTmaThreads, 1) void k_tc_gemm_tma(
     } else {
         // epilogue: warps 2..5 own TMEM lanes 32 * (warp % 4)
         const uint32_t quarter = (uint32_t)(warp & 3);
-        const bool vec_out = ((ep.ld & 3u) == 0) && ((reinterpret_cast<uintptr_t>(ep.out) & 15u) == 0);
-        const bool vec_out_b = ((ep.ld & 7u) == 0) &&
-                               ((reinterpret_cast<uintptr_t>(ep.out_bf16) & 15u) == 0);
+        float* stage_out = reinterpret_cast<float*>(smem_raw + (sbase - smem_u32(smem_raw)) +
+                                                    kTmaStages * kStage);
         uint32_t lt = 0;
         for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, ++lt) {
             const uint32_t acc = lt & 1u, use = lt >> 1;
@@ -601,57 +602,50 @@ __global__ __launch_bounds__(kTmaThreads, 1) void k_tc_gemm_tma(
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t m0 = (t / tiles_n) * 128u, n0 = (t % tiles_n) * NT;
-            const uint32_t row = m0 + quarter * 32 + lane;
+            const uint32_t rbase = m0 + quarter * 32;  // this warp's 32 rows
+            const uint32_t row = rbase + lane;
             const uint32_t taddr = tmem + acc * NT + ((quarter * 32u) << 16);
+            float* buf = stage_out + (warp - 2) * (32 * 33);  // [32 rows][33]
 #pragma unroll 1
-            for (uint32_t cc = 0; cc < NT / 16; ++cc) {
-                uint32_t r[16];
+            for (uint32_t cg = 0; cg < NT / 32; ++cg) {
+                // 32 columns of this warp's rows: lane = row, then through shared memory
+                // so that each store writes one row's 32 columns (128 contiguous bytes)
+                uint32_t r[32];
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
                     "%13,%14,%15}, [%16];"
                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
                       "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
                       "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                    : "r"(taddr + cc * 16));
+                    : "r"(taddr + cg * 32));
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+                    "%13,%14,%15}, [%16];"
+                    : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                      "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                      "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr + cg * 32 + 16));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                const uint32_t col0 = n0 + cc * 16;
-                if (row >= M || col0 >= N) continue;
-                float v[16];
+                const uint32_t col0 = n0 + cg * 32;
+                if (rbase >= M || col0 >= N) continue;  // the whole warp: nothing to store
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    v[j] = (col0 + j < N) ? epilogue<EPI>(__uint_as_float(r[j]), row, col0 + j, ep) : 0.0f;
+                for (int j = 0; j < 32; ++j)
+                    buf[lane * 33 + j] = (row < M && col0 + j < N)
+                                             ? epilogue<EPI>(__uint_as_float(r[j]), row, col0 + j, ep)
+                                             : 0.0f;
+                __syncwarp();
+                const uint32_t col = col0 + lane;
+                const uint32_t nrows = M - rbase < 32 ? M - rbase : 32;
                 if (ep.out_bf16 != nullptr) {
-                    uint16_t* orow = ep.out_bf16 + (uint64_t)row * ep.ld;
-                    if (vec_out_b && col0 + 16 <= N) {
-                        uint4 lo, hi;
-                        lo.x = bf16x2(v[0], v[1]);
-                        lo.y = bf16x2(v[2], v[3]);
-                        lo.z = bf16x2(v[4], v[5]);
-                        lo.w = bf16x2(v[6], v[7]);
-                        hi.x = bf16x2(v[8], v[9]);
-                        hi.y = bf16x2(v[10], v[11]);
-                        hi.z = bf16x2(v[12], v[13]);
-                        hi.w = bf16x2(v[14], v[15]);
-                        *reinterpret_cast<uint4*>(orow + col0) = lo;
-                        *reinterpret_cast<uint4*>(orow + col0 + 8) = hi;
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j)
-                            if (col0 + j < N) orow[col0 + j] = __bfloat16_as_ushort(__float2bfloat16_rn(v[j]));
-                    }
-                    continue;
-                }
-                float* orow = ep.out + (uint64_t)row * ep.ld;
-                if (vec_out && col0 + 16 <= N) {
-#pragma unroll
-                    for (int j = 0; j < 16; j += 4)
-                        *reinterpret_cast<float4*>(orow + col0 + j) =
-                            make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    for (uint32_t rr = 0; rr < nrows; ++rr)
+                        if (col < N)
+                            ep.out_bf16[(uint64_t)(rbase + rr) * ep.ld + col] =
+                                __bfloat16_as_ushort(__float2bfloat16_rn(buf[rr * 33 + lane]));
                 } else {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (col0 + j < N) orow[col0 + j] = v[j];
+                    for (uint32_t rr = 0; rr < nrows; ++rr)
+                        if (col < N) ep.out[(uint64_t)(rbase + rr) * ep.ld + col] = buf[rr * 33 + lane];
                 }
+                __syncwarp();
             }
             // this accumulator may take the next tile's MMAs
             asm volatile("tcgen05.fence::before_thread_sync;");
@@ -739,7 +733,8 @@ cudaError_t launch_tc_gemm_tma(const TcOperand& A, const TcOperand& B, uint32_t 
         return cudaSuccess;  // not encodable: the cp.async form runs instead
     const uint64_t tiles = (uint64_t)((A.rows + 127) / 128) * ((B.rows + nt - 1) / nt);
     const unsigned grid = (unsigned)(tiles < (uint64_t)sm_count() ? tiles : (uint64_t)sm_count());
-    const size_t smem = kTmaStages * (size_t)tma_stage_bytes(nt) + 1024;
+    // stages, the epilogue's 4 x [32][33] staging floats, alignment slack
+    const size_t smem = kTmaStages * (size_t)tma_stage_bytes(nt) + 4 * 32 * 33 * 4 + 1024;
 #define PGPU_TMA_CASE(M)                                                                    \
     case M:                                                                                 \
         if (nt == 256) {                                                                    \
