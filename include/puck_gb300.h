@@ -170,10 +170,10 @@ int pgpu_last_stats(const pgpu_index* index, uint64_t* kernels_launched,
  * 0 query prep, 1 coarse scores (+ the learned probe, which runs first and leaves the coarse
  * screen only the queries it does not answer), 2 coarse select, 3 fine scores, 4 fine order
  * (exact mode) or the scan's block launch order and record offsets (scan mode), 5 cell walk
- * (exact mode) or the ADC distances of the probed records (scan mode: k_scan_score, or the
- * fused k_scan_il when the split scan does not apply), 6 the filter's top-filter_topk
- * selection (scan mode: k_scan_pick + the fused kernel for the queries left to it; nothing
- * in exact mode), 7 rerank. It waits for the call's work to finish. */
+ * (exact mode) or the filter scan (scan mode: k_scan_score, which scores the probed records and
+ * selects the top filter_topk, or the fused k_scan_il when the split scan does not apply), 6 the
+ * fused scan for the queries the split scan left (scan mode; nothing in exact mode), 7 rerank.
+ * It waits for the call's work to finish. */
 #define PGPU_NUM_STAGES 8
 int pgpu_set_profiling(pgpu_index* index, int enable);
 int pgpu_stage_times(pgpu_index* index, float* ms, uint32_t n_stages);

@@ -275,8 +275,8 @@ cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cud
 // The scan (scan mode), in three parts timed as stages 4-6: launch_scan_prepare
 // (the split scan's record counts and buffer offsets; nothing otherwise),
 // launch_scan_records (k_scan_score, or the fused kernel when the split scan does
-// not apply), launch_scan_finish (k_scan_pick, then the fused kernel for the queries
-// the split scan left).
+// not apply), launch_scan_finish (the fused kernel for the queries the split scan
+// left).
 cudaError_t launch_scan_prepare(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                 cudaStream_t stream);
 cudaError_t launch_scan_records(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
@@ -284,9 +284,8 @@ cudaError_t launch_scan_records(const DeviceIndex& ix, uint32_t n, Scratch& s, b
 cudaError_t launch_scan_finish(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                cudaStream_t stream);
 size_t scan_smem_bytes_half(const DeviceIndex& ix, uint32_t T);
-// The split scan runs (k_split_counts, k_split_offsets, k_scan_score, k_scan_pick
-// before the fused kernel) when the index has the interleaved layout and the scratch
-// its distance buffer.
+// The split scan runs (k_split_counts, k_split_offsets, k_scan_score before the fused
+// kernel) when the index has the interleaved layout and the scratch its distance buffer.
 bool scan_split_applies(const DeviceIndex& ix, const Scratch& s);
 // BF16 copy of the vectors and their norms (precision form), synchronous.
 int ensure_bf16_features(DeviceIndex* ix, std::string* err);

@@ -203,10 +203,11 @@ cudaError_t run_pipeline(const DeviceIndex& ix, const SearchConfig& cfg, Scratch
     }
     mark(8);
 #undef PGPU_STEP
-    // scan mode adds the two launch-order kernels, and the split scan four more
+    // scan mode adds the two launch-order kernels, and the split scan three more
+    // (k_split_counts, k_split_offsets, k_scan_score; the fused kernel is counted in k)
     if (launched)
         *launched = k + probe_kernels +
-                    (cfg.mode == PGPU_MODE_SCAN ? 2 + (scan_split_applies(ix, s) ? 4 : 0) : 0);
+                    (cfg.mode == PGPU_MODE_SCAN ? 2 + (scan_split_applies(ix, s) ? 3 : 0) : 0);
     return cudaSuccess;
 }
 
