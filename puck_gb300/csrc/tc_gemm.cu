@@ -727,11 +727,16 @@ bool tma_applies(const TcOperand& A, const TcOperand& B, uint32_t K) {
 cudaError_t launch_tc_gemm_tma(const TcOperand& A, const TcOperand& B, uint32_t K,
                                const TcEpilogue& ep, int* err, cudaStream_t stream, bool* done) {
     *done = false;
-    const int nt = B.rows >= 256 ? 256 : 128;
+    // 256-column tiles when they give every SM two or more (the ring and the second
+    // accumulator then overlap tiles), else 128-column tiles
+    const uint64_t tiles_m = (A.rows + 127) / 128;
+    const int nt = B.rows >= 256 && tiles_m * ((B.rows + 255) / 256) >= 2ull * (uint64_t)sm_count()
+                       ? 256
+                       : 128;
     CUtensorMap ma, mb;
     if (!encode_operand(&ma, A, K, 128) || !encode_operand(&mb, B, K, (uint32_t)nt))
         return cudaSuccess;  // not encodable: the cp.async form runs instead
-    const uint64_t tiles = (uint64_t)((A.rows + 127) / 128) * ((B.rows + nt - 1) / nt);
+    const uint64_t tiles = tiles_m * ((B.rows + nt - 1) / nt);
     const unsigned grid = (unsigned)(tiles < (uint64_t)sm_count() ? tiles : (uint64_t)sm_count());
     // stages, the epilogue's 4 x [32][33] staging floats, alignment slack
     const size_t smem = kTmaStages * (size_t)tma_stage_bytes(nt) + 4 * 32 * 33 * 4 + 1024;

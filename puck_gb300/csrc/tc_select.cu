@@ -269,14 +269,20 @@ __global__ __launch_bounds__(256) void k_window_small(
                 m = kSmallCap + 1;
                 break;
             }
-            if (in) {
-                const float v = __fsub_rn(bias[j], dot_seq(q, cents + (uint64_t)j * d, d));
-                keys[m + __popc(b & ((1u << lane) - 1))] =
-                    ((unsigned long long)ordered_key(v) << 32) | j;
-            }
+            if (in) keys[m + __popc(b & ((1u << lane) - 1))] = j;
             m += __popc(b);
         }
         __syncwarp();
+        if (m <= kSmallCap) {
+            // the members' exact values, one member per lane: every dot's loads in flight
+            // together instead of one chunk of the screen at a time
+            for (uint32_t i = lane; i < m; i += 32) {
+                const uint32_t j = (uint32_t)keys[i];
+                const float v = __fsub_rn(bias[j], dot_seq(q, cents + (uint64_t)j * d, d));
+                keys[i] = ((unsigned long long)ordered_key(v) << 32) | j;
+            }
+            __syncwarp();
+        }
         if (m > kSmallCap) {
             exact_all = true;
         } else {
