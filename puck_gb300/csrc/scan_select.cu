@@ -1,6 +1,9 @@
-// k_scan_select: throughput-mode filter stage. For one query it streams every
+// The throughput-mode filter stage (scan mode). For one query it streams every
 // filter record of its probed coarse clusters (each cluster is one contiguous
-// range in memory order) and keeps the filter_topk smallest ADC distances.
+// range in memory order) and keeps the filter_topk smallest ADC distances. Three
+// kernels: the split scan (k_scan_score, "split scan" below), which answers every
+// query whose records fit the per-pass distance buffer; the fused k_scan_il
+// (interleaved layout) for the rest; k_scan_select for nsq not a multiple of 4.
 //
 // Per record the distance is the reference's own expression for a scanned point
 // (puck/puck/puck_index.cpp:360-368 with cell_dist from :539-540):
