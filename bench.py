@@ -839,8 +839,10 @@ def run_gpu(args, w, rank, ws):
             set_form(entry["form"],
                      native.PGPU_MODE_EXACT if entry["mode"] == "exact" else native.PGPU_MODE_SCAN,
                      entry.get("probe_mass", entry["search_coarse_count"]))
+            # offered loads up to past the loop's saturation (achieved below offered)
             serving[name] = dict(run_serving(native, ix, queries.cpu().numpy(),
-                                             loads_qps=(250_000, 500_000, 1_000_000)),
+                                             loads_qps=(250_000, 500_000, 1_000_000, 2_000_000,
+                                                        4_000_000)),
                                  recall_at_10=entry["recall_at_10"])
             log(f"[bench] serving {name}: {serving[name]}")
 
