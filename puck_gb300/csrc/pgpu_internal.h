@@ -285,7 +285,11 @@ cudaError_t launch_scan_finish(const DeviceIndex& ix, uint32_t n, Scratch& s, bo
                                cudaStream_t stream);
 size_t scan_smem_bytes_half(const DeviceIndex& ix, uint32_t T);
 // The split scan runs (k_split_counts, k_split_offsets, k_scan_score before the fused
-// kernel) when the index has the interleaved layout and the scratch its distance buffer.
+// kernel) when the index has the interleaved layout, its block fits shared memory
+// (scan_split_possible: the cell terms of F fine clusters, filter_topk below the
+// pick's 8192 keys) and the scratch holds its distance buffer; otherwise the fused
+// kernel answers every query.
+bool scan_split_possible(const DeviceIndex& ix, uint32_t T);
 bool scan_split_applies(const DeviceIndex& ix, const Scratch& s);
 // BF16 copy of the vectors and their norms (precision form), synchronous.
 int ensure_bf16_features(DeviceIndex* ix, std::string* err);

@@ -47,7 +47,7 @@ void free_scratch(Scratch* s) {
 // clusters), at least 2^20 and at most 2^30. A query whose records do not fit runs
 // the fused scan kernel instead.
 uint64_t split_capacity(const DeviceIndex& ix, const SearchConfig& cfg, uint32_t B) {
-    if (cfg.mode != PGPU_MODE_SCAN || !il_applies(ix.nsq)) return 0;
+    if (cfg.mode != PGPU_MODE_SCAN || !scan_split_possible(ix, cfg.filter_keep())) return 0;
     uint64_t c = (uint64_t)B * 40960ull;
     if (c < (1ull << 20)) c = 1ull << 20;
     if (c > (1ull << 30)) c = 1ull << 30;

@@ -1923,16 +1923,22 @@ cudaError_t launch_scan_order(const DeviceIndex& ix, uint32_t n, Scratch& s, cud
     return cudaGetLastError();
 }
 
-bool scan_split_applies(const DeviceIndex& ix, const Scratch& s) {
-    return il_applies(ix.nsq) && ix.codes_il != nullptr && s.tbuf != nullptr && s.tcap > 0;
-}
-
 // Shared memory of k_scan_score: the table, the query, then the compact table being
 // built or the cell terms and the histogram.
 static size_t split_score_smem(const DeviceIndex& ix, bool half) {
+    (void)half;  // the FP16 table takes the FP32 table's slots
     const size_t stage = sizeof(float) * ix.nsq * 257;
     const size_t work = il_srow_bytes(ix.F) + sizeof(uint32_t) * (kSplitBins + 4 * kSplitMaxSlots + 1);
     return il_table_bytes(false) + il_query_bytes(ix.d) + (stage > work ? stage : work);
+}
+
+bool scan_split_possible(const DeviceIndex& ix, uint32_t T) {
+    return il_applies(ix.nsq) && split_score_smem(ix, false) <= 220 * 1024 &&
+           T < split_max_keys(false);
+}
+
+bool scan_split_applies(const DeviceIndex& ix, const Scratch& s) {
+    return ix.codes_il != nullptr && s.tbuf != nullptr && s.tcap > 0 && scan_split_possible(ix, s.T);
 }
 
 static SplitParams split_params(const DeviceIndex& ix, uint32_t n, Scratch& s) {
@@ -2046,8 +2052,7 @@ static cudaError_t launch_fused(const DeviceIndex& ix, uint32_t n, Scratch& s, b
 cudaError_t launch_scan_prepare(const DeviceIndex& ix, uint32_t n, Scratch& s, bool half_lut,
                                 cudaStream_t stream) {
     if (!scan_split_applies(ix, s)) return cudaSuccess;
-    if (split_score_smem(ix, half_lut) > 220 * 1024 || s.T >= split_max_keys(half_lut))
-        return cudaErrorInvalidValue;
+    (void)half_lut;
     const SplitParams sp = split_params(ix, n, s);
     k_split_counts<<<(n + 255) / 256, 256, 0, stream>>>(sp);
     k_split_offsets<<<1, 1024, 0, stream>>>(sp);
