@@ -37,7 +37,7 @@ extern "C" {
 #define PGPU_MODE_SCAN 1       /* every record of the probed coarse clusters is scanned (no pivot
                                   pruning); the filter_topk smallest ADC distances, each bit-identical
                                   to the reference's value for that record, go to the exact rerank.
-                                  filter_topk (+ filter_margin) <= 1280. */
+                                  filter_topk (+ filter_margin) <= 2048. */
 
 /* Arithmetic of the search (pgpu_params.precision).
  * FP32: every distance in FP32 in the reference's operation order (the coarse
@@ -64,7 +64,8 @@ typedef struct {
     uint32_t filter_topk;
     double radius_rate;
     int32_t device;     /* CUDA device ordinal */
-    uint32_t max_batch; /* queries per device pass; sizes the per-pass scratch */
+    uint32_t max_batch; /* queries per device pass; sizes the per-pass scratch (scan mode adds a
+                           distance buffer of 40960 floats per query, 4 MiB to 4 GiB in all) */
     int32_t mode;       /* PGPU_MODE_* */
     int32_t precision;  /* PGPU_PRECISION_* (default FP32) */
     uint32_t filter_margin; /* BF16 only: extra filter candidates kept for the rerank */
