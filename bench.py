@@ -57,29 +57,29 @@ TARGET_RECALL = 0.95
 # path's exact and scan modes (the precision form reuses scan_sweep); cpu_sweep:
 # values tried for the CPU port's operating point.
 WORKLOADS = {
-    # BASELINE config 3: the learned-probe configuration
+    # the learned-probe configuration: 100M x 96 cosine, 4000 x 4000 clusters, probe MLP
     "learned_100m": dict(n=100_000_000, d=96, ncomp=16384, kind="unit", C=4000, F=4000, nsq=24,
                          T=1100, k=10, exact_sweep=(1, 8, 64), scan_sweep=(1, 2), nq=10000,
                          norm=True, train_sample=1_000_000, iters=10, pq_sample=262_144,
                          probe_train=200_000, probe_mass=(0.5, 0.9), probe_max=8,
                          probe_fallback=200, probe_epochs=8, top100=True,
                          cpu_sweep=(1, 2, 4, 8, 16, 32, 64)),
-    # BASELINE config 1: the plain GPU path, cosine
+    # the plain GPU path, cosine: 10M x 96, 2000 x 2000 clusters
     "cosine_10m": dict(n=10_000_000, d=96, ncomp=4096, kind="unit", C=2000, F=2000, nsq=24,
                        T=500, k=10, exact_sweep=(50, 100, 200), scan_sweep=(1, 2, 4), nq=10000,
                        norm=True, train_sample=500_000, iters=12, pq_sample=262_144,
                        probe_train=200_000, probe_mass=(0.5, 0.9), probe_max=8,
                        probe_fallback=200, probe_epochs=8, top100=True,
                        cpu_sweep=(1, 2, 4, 8, 16, 50, 100, 200)),
-    # BASELINE config 2: the precision form's configuration (config 1 scaled to d=128
-    # with config 0's mixture; filter PQ 32 x 256 keeps 4 dims per subspace)
+    # the precision form's configuration: 10M x 128 from the integer mixture below, 2000 x 2000
+    # clusters (filter PQ 32 x 256 keeps 4 dims per subspace)
     "precision_10m_d128": dict(n=10_000_000, d=128, ncomp=1024, kind="int", C=2000, F=2000,
                                nsq=32, T=500, k=10, exact_sweep=(50,), scan_sweep=(1, 2, 4, 8),
                                nq=10000, norm=False, train_sample=500_000, iters=12,
                                pq_sample=262_144, probe_train=200_000, probe_mass=(0.5, 0.9),
                                probe_max=8, probe_fallback=200, probe_epochs=8, top100=False,
                                cpu_sweep=(1, 2, 4, 8, 16, 50)),
-    # BASELINE config 0: plain Puck, L2, integer GMM (the reference CPU build's case)
+    # plain Puck, L2: 1M x 128 integer mixture, 1000 x 1000 clusters (the reference CPU build's case)
     "l2int_1m": dict(n=1_000_000, d=128, ncomp=1024, kind="int", C=1000, F=1000, nsq=32, T=200,
                      k=10, exact_sweep=(200,), scan_sweep=(1, 2, 4, 8, 200), nq=10000,
                      norm=False, train_sample=262_144, iters=12, pq_sample=131_072,
